@@ -1,0 +1,43 @@
+"""Configurations of the reference build used to pin the oracle (test infrastructure).
+
+Each variant is the unmodified reference solver compiled with one set of
+compile-time switches (Ark/Constant/ZeroFlip.h), constants
+(Ark/Constant/ZeroReference.h, Ark/Constant/ZeroNamespace.h,
+Ark/Lib/nonidealEoS.h) and velocity model (Ark/Makefile:7), on a mesh written
+by ``mesh_cas.py``.  ``consts`` holds the physical inputs; ``build_ref.py``
+turns them into header substitutions and the tests turn the same numbers into
+a product case, so both sides always run the same physics.
+
+Keys of ``consts`` (all optional; absent = reference default):
+  Mu0 (dynamic viscosity, Rho0 = 1 so also nu), M_Phi (mobility),
+  W (interface width; Cn = W/ChLength), Sigma, RhoL, RhoV, Gy (gravity,
+  enables the commented gravity line of Ark/Cpp/SourceM.cpp:32), radius,
+  PP_RhoL, PP_RhoV, Tr, aCS, Tc_CS.
+"""
+
+REFERENCE_DEFAULTS = dict(Mu0=0.1, M_Phi=0.1, W=5.0, Sigma=1e-2, RhoL=10.0, RhoV=1.0,
+                          Gy=0.0, radius_frac=0.36, Tr=0.85, aCS=1.0, Tc_CS=0.0943,
+                          PP_RhoL=2.4806e-1, PP_RhoV=4.5435e-2, PP_radius_frac=0.25)
+
+VARIANTS = {
+    # The reference exactly as shipped: AC_Drop, D2Q9AC, 128x128 periodic.
+    'ac_default': dict(model='D2Q9AC', nx=128, ny=128, walls=False, init='ac_drop',
+                       consts={}),
+    # Stationary droplet, 128x128 periodic, heavy phase inside (density
+    # ratio 10, nu = 0.01, sigma = 1e-3, W = 4, R = 25).
+    'ac_c1': dict(model='D2Q9AC', nx=128, ny=128, walls=False, init='ac_drop_inside',
+                  consts=dict(Mu0=0.01, W=4.0, Sigma=1e-3, RhoL=1.0, RhoV=0.1, radius=25.0)),
+    # Small non-square droplet for long, fast runs.
+    'ac_small': dict(model='D2Q9AC', nx=24, ny=20, walls=False, init='ac_drop_inside',
+                     consts=dict(Mu0=0.01, W=4.0, Sigma=1e-3, RhoL=1.0, RhoV=0.1, radius=6.0)),
+    # HCZ pressure-based Allen-Cahn model (u != 0), periodic droplet.
+    'hcz_drop': dict(model='D2Q9HCZ', nx=32, ny=32, walls=False, init='ac_drop_inside',
+                     consts=dict(Mu0=0.02, W=4.0, Sigma=1e-2, RhoL=10.0, RhoV=1.0, radius=8.0)),
+    # Rayleigh-Taylor: HCZ, bounce-back walls top/bottom, periodic sides,
+    # gravity; Atwood 0.5 (rho 3:1).  Small box, strong gravity.
+    'hcz_rt': dict(model='D2Q9HCZ', nx=16, ny=64, walls=True, init='ac_rt',
+                   consts=dict(Mu0=0.01, M_Phi=0.05, W=4.0, Sigma=1e-4, RhoL=3.0, RhoV=1.0,
+                               Gy=1e-4)),
+    # Pseudopotential D2Q9 with the reference's own SCMP_Drop init.
+    'pp_drop': dict(model='D2Q9PP', nx=32, ny=32, walls=False, init='scmp_drop', consts={}),
+}
