@@ -1,0 +1,151 @@
+/* dugks_gpu.h -- C ABI of the GB300 DUGKS time-step library (libdugks_gpu.so).
+ *
+ * The library replaces the body of the reference solver's time loop,
+ * DUGKS2DSolver() (Ark/Cpp/DUGKS2DSolver.cpp:148-337), for Cartesian meshes
+ * of unit cells that are periodic in x and either periodic or bounce-back
+ * walls in y.  One handle owns one case: its distributions and macroscopic
+ * fields stay resident in GPU memory between calls.  Every call returns a
+ * dugks_status; no C++ exception crosses this ABI.  A handle is used by one
+ * host thread at a time; kernels run asynchronously on the stream given to
+ * dugks_gpu_step (NULL = the legacy default stream) and every call that
+ * returns host data synchronises that stream first.
+ *
+ * Layouts: cell fields are [ny][nx] row-major doubles, cell (i,j) at
+ * j*nx+i with x = i+0.5, y = j+0.5.  Distributions are [Q][ny][nx], the
+ * discrete-velocity order of the reference model (D2Q9: 0,E,NE,N,NW,W,SW,S,SE,
+ * Ark/Lib/D2Q9.h:86-88; D2V16: Ark/Lib/D2V16.cpp:53-66).
+ */
+#ifndef DUGKS_GPU_H
+#define DUGKS_GPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum dugks_status {
+    DUGKS_OK = 0,
+    DUGKS_EINVAL = 1,   /* bad argument or unsupported combination */
+    DUGKS_ENOMEM = 2,   /* device or host allocation failed */
+    DUGKS_ECUDA = 3,    /* a CUDA call failed; see dugks_gpu_last_error */
+    DUGKS_ETIMEOUT = 4, /* a bounded device wait gave up */
+    DUGKS_ENAN = 5      /* a NaN/Inf was found in the state */
+} dugks_status;
+
+/* Velocity model + multiphase model (Ark/Makefile:7 QModel + ZeroFlip.h flips). */
+typedef enum dugks_model {
+    DUGKS_MODEL_AC = 0,   /* D2Q9AC: Allen-Cahn, u forced to 0 (Ark/Lib/D2Q9AC.cpp) */
+    DUGKS_MODEL_HCZ = 1,  /* D2Q9HCZ: Allen-Cahn, pressure-based f (Ark/Lib/D2Q9HCZ.cpp) */
+    DUGKS_MODEL_PP9 = 2,  /* D2Q9PP: pseudopotential (Ark/Lib/D2Q9PP.cpp, Ark/Cpp/PseudoP.cpp) */
+    DUGKS_MODEL_PP16 = 3  /* D2V16 pseudopotential (Ark/Lib/D2V16.cpp restated) */
+} dugks_model;
+
+typedef enum dugks_precision {
+    DUGKS_FP64 = 0,       /* plain FP64 drop-in */
+    DUGKS_FP32_DEV = 1    /* FP32 storage of deviations from rest equilibrium */
+} dugks_precision;
+
+/* Case parameters: the primary inputs of Ark/Constant/ZeroReference.h and
+ * Ark/Constant/ZeroNamespace.h; every derived constant (dt, tau0, beta,
+ * kappa, ...) is computed inside the library with the reference's formulas.
+ * ChLength = NL = nx, MinL = 1, R0 = 1, T0 = 1/3, Rho0 = 1, p0 = 1, CFL 0.5. */
+typedef struct dugks_case {
+    int model;          /* dugks_model */
+    int precision;      /* dugks_precision */
+    double Mu0;         /* reference dynamic viscosity (nu0 = Mu0 / Rho0) */
+    double M_Phi;       /* phase-field mobility */
+    double W;           /* interface width (Cn = W / ChLength) */
+    double Sigma;       /* surface tension */
+    double RhoL, RhoV;  /* densities of phi = 1 and phi = 0 */
+    double Gy;          /* gravity: Fy -= Gy*(rho - RhoL); 0 = off */
+    double Tr;          /* pseudopotential: T / Tc */
+    double aCS;         /* Carnahan-Starling attraction a (b = 4, R = 1) */
+    double Tc_CS;       /* Carnahan-Starling critical temperature (0.3773 a / b) */
+    double d2v16_c;     /* D2V16 lattice speed c (1.2 in the reference) */
+} dugks_case_t;
+
+typedef struct dugks_grid {
+    int nx, ny;         /* cells; nx, ny >= 3 */
+    int y_walls;        /* 0: periodic in y; 1: bounce-back walls top and bottom */
+} dugks_grid_t;
+
+typedef struct dugks_handle dugks_handle_t;
+
+/* Field ids for dugks_gpu_set_field / dugks_gpu_get_field.  The first group
+ * is the macroscopic state the reference keeps in MacroQuantity
+ * (Ark/Header/Macroscopic.h:32-44): DUGKS_F_PHIX/PHIY hold the phase-field
+ * source vector after MacroSource (Ark/Cpp/SourceM.cpp:47-58). */
+typedef enum dugks_field {
+    DUGKS_F_RHO = 0, DUGKS_F_U, DUGKS_F_V, DUGKS_F_P, DUGKS_F_PHI, DUGKS_F_TAU,
+    DUGKS_F_PHIX, DUGKS_F_PHIY, DUGKS_F_RHOX, DUGKS_F_RHOY, DUGKS_F_FX, DUGKS_F_FY,
+    DUGKS_F_PREVPHIU, DUGKS_F_PREVPHIV, DUGKS_F_PSI, DUGKS_F_SCG,
+    DUGKS_F_NFIELDS
+} dugks_field;
+
+typedef struct dugks_reductions {
+    double sum_rho;     /* sum of rho over cells (Ark/Cpp/DUGKS2DSolver.cpp:793-806) */
+    double sum_phi;     /* sum of phi: phase-field mass */
+    double residual;    /* ||rho - rho_last||2 / ||rho||2 since the previous call
+                           (Ark/Cpp/DUGKS2DSolver.cpp:807-820); 1.0 on the first call */
+    int64_t steps;      /* steps done since upload */
+} dugks_reductions_t;
+
+/* Create a solver; allocates all device memory.  replaces the reference's
+ * mesh construction + AllocateResource (Ark/Cpp/main.cpp:106-131). */
+int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, dugks_handle_t **out);
+
+/* Number of discrete velocities of the handle's model (9 or 16). */
+int dugks_gpu_nq(const dugks_handle_t *h);
+
+/* Upload a full state: f and hdist are [Q][ny][nx] (hdist ignored for the
+ * pseudopotential models, may be NULL); aux is [DUGKS_F_NFIELDS][ny][nx] in
+ * dugks_field order.  The next step uses aux as-is (like the reference's
+ * first step after an initialisation function). */
+int dugks_gpu_upload(dugks_handle_t *h, const double *f, const double *hdist, const double *aux);
+
+/* Initialise on the host like the reference initialisation functions and
+ * upload.  kind: 0 AC_Drop (Ark/Cpp/Preprocess.cpp:705-760, light phase
+ * inside), 1 droplet with the heavy phase inside, 2 Rayleigh-Taylor
+ * interface y = Lx(2 + 0.1 cos(2 pi x/Lx)) (heavy above), 3 SCMP_Drop
+ * (Ark/Cpp/Preprocess.cpp:337-401), 4 seeded density noise
+ * rho = p0 (1 + p1 U(-1,1)) with a 64-bit LCG.  params: kind 0/1: radius
+ * (<0: 0.36 ChLength); kind 3: rho_l, rho_v, radius (<0: 0.25 ChLength);
+ * kind 4: rho0, amplitude; seed used by kind 4. */
+int dugks_gpu_init(dugks_handle_t *h, int kind, const double *params, int nparams, uint64_t seed);
+
+/* Advance nsteps time steps on `stream` (a cudaStream_t, NULL = default). */
+int dugks_gpu_step(dugks_handle_t *h, int nsteps, void *stream);
+
+/* Same as dugks_gpu_step, with CUDA events recorded between the kernels of
+ * every step; ms_per_phase[k] receives the summed device time of phase k
+ * (0 collision, 1 faces (both passes), 2 update) and *nphases = 3.  Used by
+ * the benchmark to time the dominant kernel live; synchronises the stream. */
+int dugks_gpu_step_profiled(dugks_handle_t *h, int nsteps, void *stream, double *ms_per_phase, int *nphases);
+
+/* Sum of rho, sum of phi and the density residual (FP64 device reductions). */
+int dugks_gpu_reduce(dugks_handle_t *h, dugks_reductions_t *r);
+
+/* Download the macroscopic fields (any pointer may be NULL): [ny][nx] each. */
+int dugks_gpu_download(dugks_handle_t *h, double *rho, double *u, double *v, double *phi, double *p);
+
+/* Single field / distribution access.  which: 0 = f, 1 = h. */
+int dugks_gpu_get_field(dugks_handle_t *h, int field, double *out);
+int dugks_gpu_set_field(dugks_handle_t *h, int field, const double *in);
+int dugks_gpu_get_dist(dugks_handle_t *h, int which, double *out);
+
+/* Scan the state for NaN/Inf: DUGKS_OK or DUGKS_ENAN. */
+int dugks_gpu_check_finite(dugks_handle_t *h);
+
+/* Last error message of the handle (or of the last failed create if h is NULL). */
+int dugks_gpu_last_error(const dugks_handle_t *h, char *buf, size_t len);
+
+/* Kernel launches issued by this handle so far (for launch accounting). */
+int64_t dugks_gpu_launch_count(const dugks_handle_t *h);
+
+int dugks_gpu_destroy(dugks_handle_t *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

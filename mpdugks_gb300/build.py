@@ -1,0 +1,69 @@
+"""Build libdugks_gpu.so in-tree for sm_103a (nvcc, one -gencode, parallel TUs)."""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / 'csrc'
+BUILD = PKG / '_build'
+LIB = BUILD / 'libdugks_gpu.so'
+INCLUDE = PKG.parent / 'include'
+
+ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
+# host code: no FMA contraction, so the host-side initial states are the same
+# doubles on x86-64 and aarch64 (and equal the reference's)
+NVFLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompiler', '-O2',
+           '-Xcompiler', '-ffp-contract=off', '--expt-relaxed-constexpr', f'-I{INCLUDE}']
+
+
+def sources() -> list[Path]:
+    return sorted(CSRC.glob('*.cu')) + sorted(CSRC.glob('*.cpp'))
+
+
+def nvcc() -> str:
+    exe = shutil.which('nvcc') or '/usr/local/cuda/bin/nvcc'
+    if not Path(exe).exists():
+        raise RuntimeError('nvcc not found')
+    return exe
+
+
+def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    srcs = sources()
+    deps = srcs + sorted(CSRC.glob('*.cuh')) + sorted(CSRC.glob('*.h')) + sorted(INCLUDE.glob('*.h'))
+    newest = max(p.stat().st_mtime for p in deps)
+    if not force and LIB.exists() and LIB.stat().st_mtime >= newest and not extra:
+        return LIB
+    exe = nvcc()
+    flags = NVFLAGS + (extra or [])
+
+    def compile_one(src: Path) -> Path:
+        obj = BUILD / (src.name + '.o')
+        cmd = [exe] + ARCH + flags + ['-x', 'cu', '-c', str(src), '-o', str(obj)]
+        if verbose:
+            cmd.insert(1, '-Xptxas=-v')
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f'nvcc failed on {src.name}:\n{r.stderr}')
+        if verbose and r.stderr:
+            print(r.stderr)
+        return obj
+
+    with cf.ThreadPoolExecutor(min(8, os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(compile_one, srcs))
+    tmp = LIB.with_suffix('.so.tmp')
+    r = subprocess.run([exe] + ARCH + ['-shared', '-cudart=static', '-o', str(tmp)] + [str(o) for o in objs],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f'nvcc link failed:\n{r.stderr}')
+    tmp.replace(LIB)
+    return LIB
+
+
+if __name__ == '__main__':
+    import sys
+    print(build(force=True, verbose='-v' in sys.argv))

@@ -1,0 +1,180 @@
+"""ctypes binding of libdugks_gpu.so (the C ABI in include/dugks_gpu.h).
+
+The library is built in-tree by ``mpdugks_gb300.build``; loading fails loudly
+when it is missing -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+DUGKS_OK, DUGKS_EINVAL, DUGKS_ENOMEM, DUGKS_ECUDA, DUGKS_ETIMEOUT, DUGKS_ENAN = range(6)
+STATUS_NAMES = {0: 'DUGKS_OK', 1: 'DUGKS_EINVAL', 2: 'DUGKS_ENOMEM', 3: 'DUGKS_ECUDA', 4: 'DUGKS_ETIMEOUT',
+                5: 'DUGKS_ENAN'}
+MODELS = {'AC': 0, 'HCZ': 1, 'PP9': 2, 'PP16': 3}
+PRECISION = {'fp64': 0, 'fp32dev': 1}
+FIELDS = ['rho', 'u', 'v', 'p', 'phi', 'tauf', 'phix', 'phiy', 'rhox', 'rhoy', 'fx', 'fy', 'prevphiu', 'prevphiv',
+          'psi', 'scg']
+INIT_KINDS = {'ac_drop': 0, 'ac_drop_inside': 1, 'ac_rt': 2, 'scmp_drop': 3, 'pp_noise': 4}
+
+
+class DugksError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f'{STATUS_NAMES.get(code, code)}: {msg}')
+        self.code = code
+
+
+class CaseT(C.Structure):
+    _fields_ = [('model', C.c_int), ('precision', C.c_int), ('Mu0', C.c_double), ('M_Phi', C.c_double),
+                ('W', C.c_double), ('Sigma', C.c_double), ('RhoL', C.c_double), ('RhoV', C.c_double),
+                ('Gy', C.c_double), ('Tr', C.c_double), ('aCS', C.c_double), ('Tc_CS', C.c_double),
+                ('d2v16_c', C.c_double)]
+
+
+class GridT(C.Structure):
+    _fields_ = [('nx', C.c_int), ('ny', C.c_int), ('y_walls', C.c_int)]
+
+
+class ReductionsT(C.Structure):
+    _fields_ = [('sum_rho', C.c_double), ('sum_phi', C.c_double), ('residual', C.c_double),
+                ('steps', C.c_int64)]
+
+
+# every symbol declared in include/dugks_gpu.h, with its ctypes signature
+SIGNATURES = {
+    'dugks_gpu_create': (C.c_int, [C.POINTER(CaseT), C.POINTER(GridT), C.POINTER(C.c_void_p)]),
+    'dugks_gpu_nq': (C.c_int, [C.c_void_p]),
+    'dugks_gpu_upload': (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    'dugks_gpu_init': (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_int, C.c_uint64]),
+    'dugks_gpu_step': (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    'dugks_gpu_step_profiled': (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_double),
+                                          C.POINTER(C.c_int)]),
+    'dugks_gpu_reduce': (C.c_int, [C.c_void_p, C.POINTER(ReductionsT)]),
+    'dugks_gpu_download': (C.c_int, [C.c_void_p] + [C.c_void_p] * 5),
+    'dugks_gpu_get_field': (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    'dugks_gpu_set_field': (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    'dugks_gpu_get_dist': (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    'dugks_gpu_check_finite': (C.c_int, [C.c_void_p]),
+    'dugks_gpu_last_error': (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
+    'dugks_gpu_launch_count': (C.c_int64, [C.c_void_p]),
+    'dugks_gpu_destroy': (C.c_int, [C.c_void_p]),
+}
+
+_lib = None
+
+
+def library_path() -> Path:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load libdugks_gpu.so; raise if it is not built (no fallback path exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not path.exists():
+        if not build_if_missing:
+            raise RuntimeError(f'{path} is not built; run `python -m mpdugks_gb300.build` '
+                               '(the DUGKS kernels have no CPU fallback)')
+        _build.build()
+    lib = C.CDLL(str(path))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def make_case(model: str, precision: str = 'fp64', *, Mu0=0.1, M_Phi=0.1, W=5.0, Sigma=1e-2, RhoL=10.0,
+              RhoV=1.0, Gy=0.0, Tr=0.85, aCS=1.0, Tc_CS=0.0943, d2v16_c=1.2) -> CaseT:
+    return CaseT(MODELS[model], PRECISION[precision], Mu0, M_Phi, W, Sigma, RhoL, RhoV, Gy, Tr, aCS, Tc_CS,
+                 d2v16_c)
+
+
+class GpuCase:
+    """One resident case on the GPU, driven through the C ABI."""
+
+    def __init__(self, case: CaseT, nx: int, ny: int, y_walls: bool = False):
+        self.lib = load()
+        self.nx, self.ny = nx, ny
+        self.case = case
+        self.grid = GridT(nx, ny, int(y_walls))
+        h = C.c_void_p()
+        rc = self.lib.dugks_gpu_create(C.byref(case), C.byref(self.grid), C.byref(h))
+        if rc != DUGKS_OK:
+            buf = C.create_string_buffer(512)
+            self.lib.dugks_gpu_last_error(None, buf, 512)
+            raise DugksError(rc, buf.value.decode())
+        self.h = h
+        self.Q = self.lib.dugks_gpu_nq(h)
+
+    def _check(self, rc: int) -> None:
+        if rc != DUGKS_OK:
+            buf = C.create_string_buffer(512)
+            self.lib.dugks_gpu_last_error(self.h, buf, 512)
+            raise DugksError(rc, buf.value.decode())
+
+    def close(self) -> None:
+        if getattr(self, 'h', None):
+            self.lib.dugks_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init(self, kind: str, params=(), seed: int = 12345) -> None:
+        arr = (C.c_double * max(1, len(params)))(*params)
+        self._check(self.lib.dugks_gpu_init(self.h, INIT_KINDS[kind], arr, len(params), seed))
+
+    def upload(self, f: np.ndarray, hdist: np.ndarray | None, aux: np.ndarray) -> None:
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        aux = np.ascontiguousarray(aux, dtype=np.float64)
+        hp = None
+        if hdist is not None:
+            hdist = np.ascontiguousarray(hdist, dtype=np.float64)
+            hp = hdist.ctypes.data
+        self._check(self.lib.dugks_gpu_upload(self.h, f.ctypes.data, hp, aux.ctypes.data))
+
+    def step(self, n: int = 1, stream: int | None = None) -> None:
+        self._check(self.lib.dugks_gpu_step(self.h, n, stream))
+
+    def step_profiled(self, n: int, stream: int | None = None) -> list[float]:
+        ms = (C.c_double * 4)()
+        nph = C.c_int()
+        self._check(self.lib.dugks_gpu_step_profiled(self.h, n, stream, ms, C.byref(nph)))
+        return [ms[k] for k in range(nph.value)]
+
+    def reduce(self) -> ReductionsT:
+        r = ReductionsT()
+        self._check(self.lib.dugks_gpu_reduce(self.h, C.byref(r)))
+        return r
+
+    def get(self, name: str) -> np.ndarray:
+        out = np.empty((self.ny, self.nx), dtype=np.float64)
+        self._check(self.lib.dugks_gpu_get_field(self.h, FIELDS.index(name), out.ctypes.data))
+        return out
+
+    def set(self, name: str, arr: np.ndarray) -> None:
+        a = np.ascontiguousarray(arr, dtype=np.float64).reshape(self.ny, self.nx)
+        self._check(self.lib.dugks_gpu_set_field(self.h, FIELDS.index(name), a.ctypes.data))
+
+    def dist(self, which: str = 'f') -> np.ndarray:
+        out = np.empty((self.Q, self.ny, self.nx), dtype=np.float64)
+        self._check(self.lib.dugks_gpu_get_dist(self.h, 0 if which == 'f' else 1, out.ctypes.data))
+        return out
+
+    def check_finite(self) -> int:
+        return self.lib.dugks_gpu_check_finite(self.h)
+
+    @property
+    def launches(self) -> int:
+        return self.lib.dugks_gpu_launch_count(self.h)

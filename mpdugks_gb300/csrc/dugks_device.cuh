@@ -1,0 +1,70 @@
+// Device-side definitions shared by the DUGKS kernels (sm_103a).
+//
+// Grid: nx*ny unit cells, SoA fields [ny][pitch] (pitch = nx rounded up to 32
+// doubles = 256 B, so every row starts on a 256-byte boundary and a warp's 32
+// consecutive cells are one coalesced 256-B access).  x is periodic; y is
+// periodic or closed by bounce-back walls with one extrapolated ghost row on
+// each side (Ark/Cpp/Boundary.cpp:38-139), evaluated on the fly.
+//
+// Face numbering: x-face (i,j) is the west face of cell (i,j), between
+// (i-1,j) and (i,j), normal +x; y-face (i,j) is the south face of cell
+// (i,j), between (i,j-1) and (i,j), normal +y; with walls y-faces run
+// j = 0..ny (0 and ny are the wall faces).  The reference evaluates each
+// face from its owner's side and each periodic face twice
+// (Ark/Cpp/DUGKS2DSolver.cpp:219-230); its central-difference face formulas
+// are orientation independent, so every physical face is evaluated once here.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+namespace dugks {
+
+enum Model { AC = 0, HCZ = 1, PP9 = 2, PP16 = 3 };
+
+enum Field {
+    F_RHO = 0, F_U, F_V, F_P, F_PHI, F_TAU, F_PHIX, F_PHIY, F_RHOX, F_RHOY, F_FX, F_FY,
+    F_PPU, F_PPV, F_PSI, F_SCG, NFIELDS
+};
+
+// Constants of one case.  Names follow Ark/Constant/ZeroReference.h and
+// Ark/Constant/ZeroNamespace.h; all are derived on the host with the
+// reference's expressions (see host_params.cpp).
+struct Params {
+    int nx, ny, pitch, walls, model, gravity, Q, pad_;
+    double R0, T0, RT, Lambda0, dt, hDt, Tau0, Kp, MinL, dx, dy, _2dx, _2dy;
+    double aPhi, bPhi, Beta, Kappa, wI, PhiL, PhiV, RhoL, RhoV, Gy, NuL, NuV, TauMass;
+    double h_aBP, h_bBP, h_cBP, h_ah, h_bh, h_ch;  // constant phase-field relaxation factors
+    double aTP, bTP, dtV;                          // 4/3, 1/3, dt/volume
+    double T_CS, aCS;                              // Carnahan-Starling EOS
+    double c16;                                    // D2V16 lattice speed
+    double xi_u[16], xi_v[16], omega[16];
+    int bb[16];
+};
+
+// Device pointers of one case.  qs = ny*pitch (stride between velocities).
+struct State {
+    double *f, *h;             // tilde distributions [Q][ny][pitch]
+    double *bf, *bh;           // BarP (collision pre-step) [Q][ny][pitch]
+    double *xff, *xfh;         // x-face fluxes [Q][ny][pitch]
+    double *yff, *yfh;         // y-face fluxes [Q][ny+1][pitch]
+    double *fld[NFIELDS];      // macroscopic cell fields [ny][pitch]
+    double *gphi;              // 2 buffers x (bottom, top) ghost phi rows [2][2][pitch]
+    // pseudopotential face state, x: [ny][pitch], y: [ny][pitch] (periodic only)
+    double *xfFx, *xfFy, *yfFx, *yfFy;
+    double *xpsi, *ypsi, *xscg, *yscg, *xrho, *yrho, *xu, *yu, *xv, *yv;
+    double *xbf, *ybf;         // face BhDt kept between the two pseudopotential face passes [Q][ny][pitch]
+    size_t qs, qsy;            // velocity strides of cell/x-face arrays and of y-face arrays
+};
+
+// D2Q9 velocity set (Ark/Lib/D2Q9.h:86-90), MaSpan = sqrt(3RT) = 1 exactly.
+__host__ __device__ constexpr int d2q9_xu(int q) { return q == 1 || q == 2 || q == 8 ? 1 : (q >= 4 && q <= 6 ? -1 : 0); }
+__host__ __device__ constexpr int d2q9_xv(int q) { return q >= 2 && q <= 4 ? 1 : (q >= 6 ? -1 : 0); }
+__host__ __device__ constexpr double d2q9_w(int q) {
+    return q == 0 ? 4.0 / 9.0 : ((q & 1) ? 1.0 / 9.0 : 1.0 / 36.0);
+}
+__host__ __device__ constexpr int d2q9_bb(int q) { return q == 0 ? 0 : (q <= 4 ? q + 4 : q - 4); }
+
+// x * s for s in {-1, 0, 1}: exact, no multiply issued.
+__device__ __forceinline__ double sx(int s, double x) { return s > 0 ? x : (s < 0 ? -x : 0.0); }
+
+}  // namespace dugks

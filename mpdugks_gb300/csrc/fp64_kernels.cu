@@ -1,0 +1,713 @@
+// FP64 DUGKS step kernels for sm_103a -- the plain drop-in path.
+//
+// One time step = three launches, in the phase order of
+// Ark/Cpp/DUGKS2DSolver.cpp:175-327:
+//   k_collide : [deferred P10 MacroSource of the previous step] + P1 + P2
+//               (equilibria, force source, f-bar-plus; ghost phi rows)
+//   k_faces   : P4 + P6 for every physical face (CD reconstruction, face
+//               moments, face equilibrium/source, flux x xi.n dS, wall BB)
+//   k_update  : P8 + P9 (finite-volume update, cell macros)
+// The pseudopotential models split the face pass in two (face psi, then
+// face force) -- the Jacobi semantics of the face psi gradient.
+//
+// Arithmetic follows the reference expressions term by term (same operand
+// association); the compiler may contract a*b+c into FMA, so results agree
+// with the FP64 reference to rounding, not bit for bit.
+#include <cuda_runtime.h>
+#include "dugks_device.cuh"
+
+namespace dugks {
+
+__constant__ double c_iM16[16][16];  // D2V16 inverse moment matrix (Ark/Lib/D2V16.cpp:34-52)
+
+__device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+__device__ __forceinline__ void SetZero(double &d) { if (d < 1.0E-14 && d > -1.0E-14) d = 0.0; }  // Ark/Header/Mesh_2D.h:196-200
+
+// Cell field at logical row j in -1..ny (ghost rows: 2 a0 - a1 with walls,
+// wrap otherwise), column i already wrapped.
+template <bool WALLS>
+__device__ __forceinline__ double cellv(const double *__restrict__ a, int ny, int pitch, int j, int i) {
+    if (j < 0) {
+        if (WALLS) return 2.0 * a[i] - a[pitch + i];
+        j += ny;
+    } else if (j >= ny) {
+        if (WALLS) return 2.0 * a[(size_t)(ny - 1) * pitch + i] - a[(size_t)(ny - 2) * pitch + i];
+        j -= ny;
+    }
+    return a[(size_t)j * pitch + i];
+}
+
+// ---------------------------------------------------------------------------
+// D2V16 equilibrium: Macro16 (Ark/Lib/D2V16.cpp:125-145) at T = T0, p = rho R0 T0,
+// then the inverse moment matrix.
+__device__ __forceinline__ void d2v16_eq(const Params &P, double rho, double u, double v, double *eq) {
+    const double degrees = 3.0, degPlus2 = degrees + 2.0;
+    const double T = P.T0, p = rho * P.R0 * T;
+    const double u2 = u * u, v2 = v * v, RT = P.R0 * T;
+    double M[16];
+    M[0] = rho;
+    M[1] = rho * u;
+    M[2] = rho * v;
+    M[3] = rho * (degrees * RT + u2 + v2);
+    M[4] = M[1] * v;
+    M[5] = rho * u2 + p;
+    M[6] = rho * v2 + p;
+    M[7] = M[1] * (degPlus2 * RT + u2 + v2);
+    M[8] = M[2] * (degPlus2 * RT + u2 + v2);
+    M[9] = M[1] * (3.0 * RT + u2);
+    M[10] = M[2] * (3.0 * RT + v2);
+    M[11] = M[2] * (RT + u2);
+    M[12] = M[1] * (RT + v2);
+    M[13] = ((degrees + 4.0) * RT + u2 + v2) * M[4];
+    M[14] = degPlus2 * rho * RT * RT + p * ((degrees + 5.0) * u2 + v2) + rho * u2 * (u2 + v2);
+    M[15] = degPlus2 * rho * RT * RT + p * ((degrees + 5.0) * v2 + u2) + rho * v2 * (u2 + v2);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        double s = 0;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) s += c_iM16[j][k] * M[k];
+        eq[j] = s;
+    }
+}
+
+// D2Q9PP equilibrium (Ark/Lib/D2Q9PP.cpp:51-62).
+__device__ __forceinline__ void d2q9pp_eq(const Params &P, double rho, double U, double V, double *eq) {
+    const double uu = U * U + V * V;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const int xu = d2q9_xu(q), xv = d2q9_xv(q);
+        double u1 = (sx(xu, U) + sx(xv, V)) / P.RT;
+        eq[q] = d2q9_w(q) * rho * (1.0 + u1 + 0.5 * u1 * u1 - uu * P.Lambda0);
+    }
+}
+
+template <int MODEL>
+__device__ __forceinline__ void pp_eq(const Params &P, double rho, double U, double V, double *eq) {
+    if (MODEL == PP16) d2v16_eq(P, rho, U, V, eq);
+    else d2q9pp_eq(P, rho, U, V, eq);
+}
+
+// Carnahan-Starling, b = 4 (Ark/Lib/nonidealEoS.h:114-118) and calcPsi
+// (Ark/Header/Macroscopic.h:64-68).
+__device__ __forceinline__ double cs_pressure(const Params &P, double rho) {
+    return rho * P.R0 * P.T_CS * (1.0 + rho + rho * rho - rho * rho * rho) /
+               ((1.0 - rho) * (1.0 - rho) * (1.0 - rho)) -
+           P.aCS * rho * rho;
+}
+__device__ __forceinline__ void calc_psi(const Params &P, double rho, double p, double &scg, double &psi) {
+    double G = (double)((p > rho * P.RT) - (p < rho * P.RT));
+    scg = G;
+    psi = sqrt(2 * (p - rho * P.RT) / G);
+}
+
+// 8-neighbour isotropic gradient (Ark/Lib/GradSchemeBasic.h:153-208).
+__device__ __forceinline__ double iso_gx(double E, double W, double NE, double NW, double SE, double SW, double d2) {
+    return (4 * (E - W) + 1 * (NE - NW + SE - SW)) / (d2 * 6);
+}
+__device__ __forceinline__ double iso_gy(double N, double S, double NE, double NW, double SE, double SW, double d2) {
+    return (4 * (N - S) + 1 * (NE - SE + NW - SW)) / (d2 * 6);
+}
+
+// ---------------------------------------------------------------------------
+// MacroSource (Ark/Cpp/SourceM.cpp:35-62) with Grad_Phi_6points
+// (Ark/Cpp/GradScheme.cpp:347-376).  Ghost phi rows come from the P2
+// extrapolation of the step that produced phi (gphi buffer `gin`).
+template <bool WALLS>
+__device__ __forceinline__ void macro_source(const Params &P, const State &S, int i, int j, int gin, double phi,
+                                             double rho, double U, double V, double ppu_old, double ppv_old,
+                                             double &srcx, double &srcy, double &rhox, double &rhoy, double &fx,
+                                             double &fy) {
+    const int nx = P.nx, ny = P.ny, pitch = P.pitch;
+    const double *__restrict__ PH = S.fld[F_PHI];
+    const int im = wrapi(i - 1, nx), ip = wrapi(i + 1, nx);
+    auto at = [&](int jj, int ii) -> double {
+        if (jj < 0) return WALLS ? S.gphi[(size_t)(gin * 2 + 0) * pitch + ii] : PH[(size_t)(ny - 1) * pitch + ii];
+        if (jj >= ny) return WALLS ? S.gphi[(size_t)(gin * 2 + 1) * pitch + ii] : PH[ii];
+        return PH[(size_t)jj * pitch + ii];
+    };
+    const double E = at(j, ip), W = at(j, im), N = at(j + 1, i), Sd = at(j - 1, i);
+    const double NE = at(j + 1, ip), NW = at(j + 1, im), SW = at(j - 1, im), SE = at(j - 1, ip);
+    double Phi_x = iso_gx(E, W, NE, NW, SE, SW, P._2dx);
+    double Phi_y = iso_gy(N, Sd, NE, NW, SE, SW, P._2dy);
+    const double lap = (4 * (E + N + W + Sd) + (NE + NW + SW + SE) - 20 * phi) / (6 * P.MinL * P.MinL);
+    SetZero(Phi_x);
+    SetZero(Phi_y);
+    const double F = 2 * P.Beta * (phi - P.PhiL) * (phi - P.PhiV) * (2 * phi - P.PhiL - P.PhiV) - P.Kappa * lap;
+    rhox = P.aPhi * Phi_x;
+    rhoy = P.aPhi * Phi_y;
+    fx = F * Phi_x;
+    fy = F * Phi_y;
+    if (P.gravity) fy -= P.Gy * (rho - P.RhoL);
+    const double L = sqrt(Phi_x * Phi_x + Phi_y * Phi_y);
+    const double dU = phi * U - ppu_old, dV = phi * V - ppv_old;
+    if (L != 0) {
+        const double tmp = -4 * (phi - P.PhiL) * (phi - P.PhiV) / (P.wI * (P.PhiL - P.PhiV));
+        srcx = Phi_x * tmp / L + dU / (P.RT * P.dt);
+        srcy = Phi_y * tmp / L + dV / (P.RT * P.dt);
+    } else {
+        srcx = dU / (P.RT * P.dt);
+        srcy = dV / (P.RT * P.dt);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Collision pre-step.  MODEL AC/HCZ: Update_phi_Eq + Update_DVDF_Source +
+// Update_phi_BP (Ark/Lib/D2Q9AC.cpp:69-105,331-344, Ark/Lib/D2Q9HCZ.cpp:54-92,
+// Ark/Cpp/DUGKS2DSolver.cpp:379-401); PP: Ark/Lib/D2Q9PP.cpp:51-62,137-145.
+// do_msrc: run the previous step's MacroSource / pseudopotential cell force
+// (Ark/Cpp/PseudoP.cpp:31-38) first.
+template <int MODEL, bool WALLS>
+__global__ void __launch_bounds__(256) k_collide(Params P, State S, int do_msrc, int gin, int gout) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= P.nx || j >= P.ny) return;
+    const int pitch = P.pitch;
+    const size_t c = (size_t)j * pitch + i;
+    const double rho = S.fld[F_RHO][c], U = S.fld[F_U][c], V = S.fld[F_V][c], tau = S.fld[F_TAU][c];
+    const double aBP = (2.0 * tau - P.hDt) / (2.0 * tau + P.dt), bBP = 1.0 - aBP, cBP = tau * bBP;
+    if (MODEL == AC || MODEL == HCZ) {
+        const double phi = S.fld[F_PHI][c], p = S.fld[F_P][c];
+        double srcx, srcy, rhox, rhoy, fx, fy;
+        if (do_msrc) {
+            const double ppu = S.fld[F_PPU][c], ppv = S.fld[F_PPV][c];
+            macro_source<WALLS>(P, S, i, j, gin, phi, rho, U, V, ppu, ppv, srcx, srcy, rhox, rhoy, fx, fy);
+            S.fld[F_PHIX][c] = srcx;
+            S.fld[F_PHIY][c] = srcy;
+            S.fld[F_RHOX][c] = rhox;
+            S.fld[F_RHOY][c] = rhoy;
+            S.fld[F_FX][c] = fx;
+            S.fld[F_FY][c] = fy;
+            S.fld[F_PPU][c] = phi * U;
+            S.fld[F_PPV][c] = phi * V;
+        } else {
+            srcx = S.fld[F_PHIX][c];
+            srcy = S.fld[F_PHIY][c];
+            rhox = S.fld[F_RHOX][c];
+            rhoy = S.fld[F_RHOY][c];
+            fx = S.fld[F_FX][c];
+            fy = S.fld[F_FY][c];
+        }
+        if (WALLS) {  // P2: ghost phi for the next MacroSource (Ark/Cpp/Boundary.cpp:38-63)
+            if (j == 0) S.gphi[(size_t)(gout * 2 + 0) * pitch + i] = 2.0 * phi - S.fld[F_PHI][c + pitch];
+            if (j == P.ny - 1) S.gphi[(size_t)(gout * 2 + 1) * pitch + i] = 2.0 * phi - S.fld[F_PHI][c - pitch];
+        }
+        const double invRT = 1.0 / P.RT;
+        const double pRT = p * invRT;
+        const double uu = U * U + V * V;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const int xu = d2q9_xu(q), xv = d2q9_xv(q);
+            const double w = d2q9_w(q);
+            double hEq, fEq, fSo;
+            if (MODEL == AC) {  // u = v = 0 (Ark/Lib/D2Q9AC.cpp:197-198): Gamma = 0, u1 = 0
+                hEq = w * phi;
+                fEq = w * pRT;
+                if (q == 0) fEq -= pRT;
+                fSo = w * ((sx(xu, fx) + sx(xv, fy)) * invRT);
+            } else {
+                const double u1 = (sx(xu, U) + sx(xv, V)) * invRT;
+                const double G = u1 + 0.5 * u1 * u1 - uu * P.Lambda0;
+                const double cu = (double)xu - U, cv = (double)xv - V;
+                hEq = w * (1.0 + u1) * phi;
+                fEq = w * (p + rho * G * P.RT);
+                fSo = w * ((1 + G) * (cu * fx + cv * fy) + G * P.RT * (cu * rhox + cv * rhoy));
+            }
+            const double hSo = (sx(xu, srcx) + sx(xv, srcy)) * w;
+            const size_t o = (size_t)q * S.qs + c;
+            S.bh[o] = P.h_aBP * S.h[o] + P.h_bBP * hEq + P.h_cBP * hSo;
+            S.bf[o] = aBP * S.f[o] + bBP * fEq + cBP * fSo;
+        }
+    } else {
+        double fx, fy;
+        if (do_msrc) {
+            const int nx = P.nx, ny = P.ny;
+            const int im = wrapi(i - 1, nx), ip = wrapi(i + 1, nx), jm = wrapi(j - 1, ny), jp = wrapi(j + 1, ny);
+            const double *__restrict__ PS = S.fld[F_PSI];
+            auto at = [&](int jj, int ii) { return PS[(size_t)jj * pitch + ii]; };
+            const double gx = iso_gx(at(j, ip), at(j, im), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dx);
+            const double gy = iso_gy(at(jp, i), at(jm, i), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dy);
+            const double k = -S.fld[F_SCG][c] * at(j, i);
+            fx = gx * k;
+            fy = gy * k;
+            S.fld[F_FX][c] = fx;
+            S.fld[F_FY][c] = fy;
+        } else {
+            fx = S.fld[F_FX][c];
+            fy = S.fld[F_FY][c];
+        }
+        constexpr int Q = MODEL == PP16 ? 16 : 9;
+        double eq[Q];
+        pp_eq<MODEL>(P, rho, U, V, eq);
+        const double inv = 1.0 / (rho * P.RT);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const double So = (fx * (P.xi_u[q] - U) + fy * (P.xi_v[q] - V)) * eq[q] * inv;
+            const size_t o = (size_t)q * S.qs + c;
+            S.bf[o] = aBP * S.f[o] + bBP * eq[q] + cBP * So;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Face reconstruction CD_Interior_phi_Bh (Ark/Cpp/DUGKS2DSolver.cpp:604-687)
+// for velocity q of one face.  XF: x-face between L=(im,j) and R=(i,j);
+// else y-face between B=(i,j-1) and T=(i,j).
+template <bool XF, bool WALLS>
+__device__ __forceinline__ double face_bh(const Params &P, const double *__restrict__ B, int i, int im, int ip,
+                                          int j, double xu, double xv) {
+    const int ny = P.ny, pitch = P.pitch;
+    double o, n, gx, gy;
+    if (XF) {
+        o = cellv<WALLS>(B, ny, pitch, j, im);
+        n = cellv<WALLS>(B, ny, pitch, j, i);
+        const double SL = cellv<WALLS>(B, ny, pitch, j - 1, im), SR = cellv<WALLS>(B, ny, pitch, j - 1, i);
+        const double NL = cellv<WALLS>(B, ny, pitch, j + 1, im), NR = cellv<WALLS>(B, ny, pitch, j + 1, i);
+        gy = (0.5 * (NR - SR) + 0.5 * (NL - SL)) / (2 * P.dy);
+        gx = (o - n) / (-P.dx);
+    } else {
+        o = cellv<WALLS>(B, ny, pitch, j - 1, i);
+        n = cellv<WALLS>(B, ny, pitch, j, i);
+        const double WB = cellv<WALLS>(B, ny, pitch, j - 1, im), EB = cellv<WALLS>(B, ny, pitch, j - 1, ip);
+        const double WT = cellv<WALLS>(B, ny, pitch, j, im), ET = cellv<WALLS>(B, ny, pitch, j, ip);
+        gx = (0.5 * (WT - ET) + 0.5 * (WB - EB)) / (2 * (-P.dx));
+        gy = (o - n) / (-P.dy);
+    }
+    return 0.5 * (o + n) - P.hDt * (gx * xu + gy * xv);
+}
+
+// Allen-Cahn face: Update_MacroVar_h + Update_phi_Eqh + Update_DVDF_Source_h
+// + Update_phi_h + Update_phiFlux_h (+ Wall_3_BB) -- Ark/Lib/D2Q9AC.cpp:106-144,
+// 232-329,345-358; Ark/Lib/D2Q9HCZ.cpp:93-131,183-271;
+// Ark/Cpp/DUGKS2DSolver.cpp:402-441; Ark/Cpp/Boundary.cpp:118-139.
+template <int MODEL, bool WALLS>
+__global__ void __launch_bounds__(256) k_faces_ac(Params P, State S) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    const bool xf = blockIdx.z == 0;
+    const int nrows = xf ? P.ny : (WALLS ? P.ny + 1 : P.ny);
+    if (i >= P.nx || j >= nrows) return;
+    const int nx = P.nx, ny = P.ny, pitch = P.pitch;
+    const int im = wrapi(i - 1, nx), ip = wrapi(i + 1, nx);
+    // owner/neighbour cells of this face and the averaged source fields
+    int jo, io;
+    if (xf) { jo = j; io = im; } else { jo = j - 1; io = i; }
+    double avg[6];
+    const int fid[6] = {F_PHIX, F_PHIY, F_RHOX, F_RHOY, F_FX, F_FY};
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+        avg[k] = 0.5 * (cellv<WALLS>(S.fld[fid[k]], ny, pitch, jo, io) + cellv<WALLS>(S.fld[fid[k]], ny, pitch, j, i));
+    const double Phi_x = avg[0], Phi_y = avg[1], Rho_x = avg[2], Rho_y = avg[3], Fx = avg[4], Fy = avg[5];
+    double bf[9], bh[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const double xu = d2q9_xu(q), xv = d2q9_xv(q);
+        if (xf) {
+            bf[q] = face_bh<true, WALLS>(P, S.bf + (size_t)q * S.qs, i, im, ip, j, xu, xv);
+            bh[q] = face_bh<true, WALLS>(P, S.bh + (size_t)q * S.qs, i, im, ip, j, xu, xv);
+        } else {
+            bf[q] = face_bh<false, WALLS>(P, S.bf + (size_t)q * S.qs, i, im, ip, j, xu, xv);
+            bh[q] = face_bh<false, WALLS>(P, S.bh + (size_t)q * S.qs, i, im, ip, j, xu, xv);
+        }
+    }
+    double Phi = 0, sumf = 0;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) Phi += bh[q];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) sumf += bf[q];
+    const double Rho = P.aPhi * Phi + P.bPhi;
+    const double invRT = 1.0 / P.RT;
+    double U, V, p, Mu;
+    if (MODEL == AC) {
+        U = 0.0;
+        V = 0.0;
+        p = (sumf - bf[0]) * P.Kp;  // the u-dependent terms vanish with u = 0
+        Mu = Rho * P.RT * P.Tau0;
+    } else {
+        double su = 0, sv = 0;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) su += sx(d2q9_xu(q), bf[q]);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) sv += sx(d2q9_xv(q), bf[q]);
+        const double inv = 1.0 / (Rho * P.RT);
+        U = su * inv;
+        V = sv * inv;
+        U += 0.5 * P.hDt * Fx * inv;
+        V += 0.5 * P.hDt * Fy * inv;
+        p = sumf + 0.5 * P.hDt * P.RT * (Rho_x * U + Rho_y * V);
+        Mu = P.NuV + (Phi - P.PhiV) * (P.NuL - P.NuV);
+        Mu *= Rho;
+    }
+    const double tauh = Mu / (Rho * P.RT);
+    const double ah = 2.0 * tauh / (2.0 * tauh + P.hDt), bh_ = 1.0 - ah, ch = tauh * bh_;
+    const double uu = U * U + V * V;
+    const double pRT = p * invRT;
+    double hf[9], hh[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const int xu = d2q9_xu(q), xv = d2q9_xv(q);
+        const double w = d2q9_w(q);
+        double hEq, fEq, fSo;
+        if (MODEL == AC) {
+            hEq = w * Phi;
+            fEq = w * pRT;
+            if (q == 0) fEq -= pRT;
+            fSo = w * ((sx(xu, Fx) + sx(xv, Fy)) * invRT);
+        } else {
+            const double u1 = (sx(xu, U) + sx(xv, V)) * invRT;
+            const double G = u1 + 0.5 * u1 * u1 - uu * P.Lambda0;
+            const double cu = (double)xu - U, cv = (double)xv - V;
+            hEq = w * Phi * (1.0 + u1);
+            fEq = w * (p + Rho * P.RT * G);
+            fSo = w * ((1 + G) * (cu * Fx + cv * Fy) + G * P.RT * (cu * Rho_x + cv * Rho_y));
+        }
+        const double hSo = (sx(xu, Phi_x) + sx(xv, Phi_y)) * w;
+        hh[q] = P.h_ah * bh[q] + P.h_bh * hEq + P.h_ch * hSo;
+        hf[q] = ah * bf[q] + bh_ * fEq + ch * fSo;
+    }
+    if (WALLS && !xf && (j == 0 || j == ny)) {
+        // bounce-back of the directions entering the fluid (xi.n_out < 0)
+        const bool bottom = (j == 0);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const int xv = d2q9_xv(q);
+            if (bottom ? xv > 0 : xv < 0) {
+                hh[q] = hh[d2q9_bb(q)];
+                hf[q] = hf[d2q9_bb(q)];
+            }
+        }
+    }
+    double *outf = xf ? S.xff : S.yff;
+    double *outh = xf ? S.xfh : S.yfh;
+    const size_t qs = xf ? S.qs : S.qsy;
+    const size_t c = (size_t)j * pitch + i;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const int s = xf ? d2q9_xu(q) : d2q9_xv(q);
+        outf[(size_t)q * qs + c] = sx(s, hf[q]);
+        outh[(size_t)q * qs + c] = sx(s, hh[q]);
+    }
+}
+
+// Pseudopotential face pass 1: BhDt, face moments with the previous face
+// force, face pressure and psi (Ark/Lib/D2Q9PP.cpp:110-136, Ark/Cpp/PseudoP.cpp:23-30).
+template <int MODEL>
+__global__ void __launch_bounds__(256) k_faces_pp1(Params P, State S) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    const bool xf = blockIdx.z == 0;
+    if (i >= P.nx || j >= P.ny) return;
+    constexpr int Q = MODEL == PP16 ? 16 : 9;
+    const int im = wrapi(i - 1, P.nx), ip = wrapi(i + 1, P.nx);
+    const size_t c = (size_t)j * P.pitch + i;
+    double R = 0, su = 0, sv = 0, b[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        b[q] = xf ? face_bh<true, false>(P, S.bf + (size_t)q * S.qs, i, im, ip, j, P.xi_u[q], P.xi_v[q])
+                  : face_bh<false, false>(P, S.bf + (size_t)q * S.qs, i, im, ip, j, P.xi_u[q], P.xi_v[q]);
+        (xf ? S.xbf : S.ybf)[(size_t)q * S.qs + c] = b[q];
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) R += b[q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) su += b[q] * P.xi_u[q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) sv += b[q] * P.xi_v[q];
+    double U = su / R, V = sv / R;
+    U += 0.5 * P.hDt * (xf ? S.xfFx : S.yfFx)[c] / R;
+    V += 0.5 * P.hDt * (xf ? S.xfFy : S.yfFy)[c] / R;
+    const double p = 1.0 * cs_pressure(P, R);
+    double scg, psi;
+    calc_psi(P, R, p, scg, psi);
+    (xf ? S.xrho : S.yrho)[c] = R;
+    (xf ? S.xu : S.yu)[c] = U;
+    (xf ? S.xv : S.yv)[c] = V;
+    (xf ? S.xscg : S.yscg)[c] = scg;
+    (xf ? S.xpsi : S.ypsi)[c] = psi;
+}
+
+// Pseudopotential face pass 2: face force from the face-psi stencil
+// (Ark/Cpp/PseudoP.cpp:39-46 over faceFaces, Ark/Lib/GradSchemeBasic.h:181-208),
+// equilibrium, He-Shan-Doolen source and flux (Ark/Lib/D2Q9PP.cpp:97-105).
+template <int MODEL>
+__global__ void __launch_bounds__(256) k_faces_pp2(Params P, State S) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    const bool xf = blockIdx.z == 0;
+    if (i >= P.nx || j >= P.ny) return;
+    constexpr int Q = MODEL == PP16 ? 16 : 9;
+    const int nx = P.nx, ny = P.ny, pitch = P.pitch;
+    const int im = wrapi(i - 1, nx), ip = wrapi(i + 1, nx), jm = wrapi(j - 1, ny), jp = wrapi(j + 1, ny);
+    const size_t c = (size_t)j * pitch + i;
+    const double *__restrict__ PS = xf ? S.xpsi : S.ypsi;
+    auto at = [&](int jj, int ii) { return PS[(size_t)jj * pitch + ii]; };
+    const double gx = iso_gx(at(j, ip), at(j, im), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dx);
+    const double gy = iso_gy(at(jp, i), at(jm, i), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dy);
+    const double k = -(xf ? S.xscg : S.yscg)[c] * at(j, i);
+    const double Fx = gx * k, Fy = gy * k;
+    (xf ? S.xfFx : S.yfFx)[c] = Fx;
+    (xf ? S.xfFy : S.yfFy)[c] = Fy;
+    const double R = (xf ? S.xrho : S.yrho)[c], U = (xf ? S.xu : S.yu)[c], V = (xf ? S.xv : S.yv)[c];
+    double eq[Q];
+    pp_eq<MODEL>(P, R, U, V, eq);
+    const double tauh = P.Tau0;
+    const double ah = 2.0 * tauh / (2.0 * tauh + P.hDt), bh = 1.0 - ah, ch = tauh * bh;
+    const double inv = 1.0 / (R * P.RT);
+    const double *__restrict__ BB = xf ? S.xbf : S.ybf;
+    double *out = xf ? S.xff : S.yff;
+    const size_t qs = xf ? S.qs : S.qsy;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const double So = (Fx * (P.xi_u[q] - U) + Fy * (P.xi_v[q] - V)) * eq[q] * inv;
+        const double t = ah * BB[(size_t)q * S.qs + c] + bh * eq[q] + ch * So;
+        out[(size_t)q * qs + c] = t * (xf ? P.xi_u[q] : P.xi_v[q]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Finite-volume update Update_phi_T (Ark/Cpp/DUGKS2DSolver.cpp:748-792) and
+// cell macros Update_MacroVar (Ark/Lib/D2Q9AC.cpp:146-231,
+// Ark/Lib/D2Q9HCZ.cpp:133-182, Ark/Lib/D2Q9PP.cpp:89-109).
+template <int MODEL, bool WALLS>
+__global__ void __launch_bounds__(256) k_update(Params P, State S) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= P.nx || j >= P.ny) return;
+    constexpr int Q = MODEL == PP16 ? 16 : 9;
+    constexpr bool HASH = (MODEL == AC || MODEL == HCZ);
+    const int pitch = P.pitch;
+    const int ip = wrapi(i + 1, P.nx);
+    const int jn = WALLS ? j + 1 : wrapi(j + 1, P.ny);
+    const size_t c = (size_t)j * pitch + i;
+    const size_t cE = (size_t)j * pitch + ip, cN = (size_t)jn * pitch + i;
+    double sumf = 0, su = 0, sv = 0, Phi = 0, f0 = 0;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const size_t oq = (size_t)q * S.qs, oy = (size_t)q * S.qsy;
+        double s = 0.0;
+        s += -S.xff[oq + cE];
+        s += -S.yff[oy + cN];
+        s += S.xff[oq + c];
+        s += S.yff[oy + c];
+        const double fn = P.aTP * S.bf[oq + c] - P.bTP * S.f[oq + c] + P.dtV * s;
+        S.f[oq + c] = fn;
+        sumf += fn;
+        if (q == 0) f0 = fn;
+        su += (MODEL == PP16) ? fn * P.xi_u[q] : sx(d2q9_xu(q), fn);
+        sv += (MODEL == PP16) ? fn * P.xi_v[q] : sx(d2q9_xv(q), fn);
+        if (HASH) {
+            double t = 0.0;
+            t += -S.xfh[oq + cE];
+            t += -S.yfh[oy + cN];
+            t += S.xfh[oq + c];
+            t += S.yfh[oy + c];
+            const double hn = P.aTP * S.bh[oq + c] - P.bTP * S.h[oq + c] + P.dtV * t;
+            S.h[oq + c] = hn;
+            Phi += hn;
+        }
+    }
+    if (MODEL == AC || MODEL == HCZ) {
+        const double Rho = P.aPhi * Phi + P.bPhi;
+        double U, V, p, Mu;
+        if (MODEL == AC) {
+            U = 0.0;
+            V = 0.0;
+            p = (sumf - f0) * P.Kp;  // (hDt rho_x.u - rho w0 |u|^2 lambda) vanishes with u = 0
+            Mu = Rho * P.RT * P.Tau0;
+        } else {
+            const double inv = 1.0 / (Rho * P.RT);
+            U = su * inv;
+            V = sv * inv;
+            U += P.hDt * S.fld[F_FX][c] * inv;
+            V += P.hDt * S.fld[F_FY][c] * inv;
+            p = sumf + P.hDt * (S.fld[F_RHOX][c] * U + S.fld[F_RHOY][c] * V) * P.RT;
+            Mu = P.NuV + (Phi - P.PhiV) * (P.NuL - P.NuV);
+            Mu *= Rho;
+        }
+        S.fld[F_PHI][c] = Phi;
+        S.fld[F_RHO][c] = Rho;
+        S.fld[F_U][c] = U;
+        S.fld[F_V][c] = V;
+        S.fld[F_P][c] = p;
+        S.fld[F_TAU][c] = Mu / (Rho * P.RT);
+    } else {
+        const double Rho = sumf;
+        double U = su / Rho, V = sv / Rho;
+        U += P.hDt * S.fld[F_FX][c] / Rho;
+        V += P.hDt * S.fld[F_FY][c] / Rho;
+        const double p = 1.0 * cs_pressure(P, Rho);
+        double scg, psi;
+        calc_psi(P, Rho, p, scg, psi);
+        S.fld[F_RHO][c] = Rho;
+        S.fld[F_U][c] = U;
+        S.fld[F_V][c] = V;
+        S.fld[F_P][c] = p;
+        S.fld[F_SCG][c] = scg;
+        S.fld[F_PSI][c] = psi;
+    }
+}
+
+// Deferred MacroSource / pseudopotential cell force on its own (used before
+// handing the fields to the host).
+template <int MODEL, bool WALLS>
+__global__ void __launch_bounds__(256) k_finalize(Params P, State S, int gin) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= P.nx || j >= P.ny) return;
+    const size_t c = (size_t)j * P.pitch + i;
+    if (MODEL == AC || MODEL == HCZ) {
+        const double phi = S.fld[F_PHI][c], U = S.fld[F_U][c], V = S.fld[F_V][c];
+        double srcx, srcy, rhox, rhoy, fx, fy;
+        macro_source<WALLS>(P, S, i, j, gin, phi, S.fld[F_RHO][c], U, V, S.fld[F_PPU][c], S.fld[F_PPV][c], srcx,
+                            srcy, rhox, rhoy, fx, fy);
+        // neighbours read phi only, so in-place writes are race-free
+        S.fld[F_PHIX][c] = srcx;
+        S.fld[F_PHIY][c] = srcy;
+        S.fld[F_RHOX][c] = rhox;
+        S.fld[F_RHOY][c] = rhoy;
+        S.fld[F_FX][c] = fx;
+        S.fld[F_FY][c] = fy;
+        S.fld[F_PPU][c] = phi * U;
+        S.fld[F_PPV][c] = phi * V;
+    } else {
+        const int nx = P.nx, ny = P.ny, pitch = P.pitch;
+        const int im = wrapi(i - 1, nx), ip = wrapi(i + 1, nx), jm = wrapi(j - 1, ny), jp = wrapi(j + 1, ny);
+        const double *__restrict__ PS = S.fld[F_PSI];
+        auto at = [&](int jj, int ii) { return PS[(size_t)jj * pitch + ii]; };
+        const double gx = iso_gx(at(j, ip), at(j, im), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dx);
+        const double gy = iso_gy(at(jp, i), at(jm, i), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dy);
+        const double k = -S.fld[F_SCG][c] * at(j, i);
+        S.fld[F_FX][c] = gx * k;
+        S.fld[F_FY][c] = gy * k;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Reductions: per-block partial sums of rho, phi, (rho-rho_last)^2, rho^2,
+// fixed-order tree (deterministic), then one block sums the partials.
+__global__ void __launch_bounds__(256) k_reduce_partial(Params P, const double *__restrict__ rho,
+                                                        const double *__restrict__ phi, double *rho_last,
+                                                        double *partial, int has_phi) {
+    __shared__ double sh[4][256];
+    const int tid = threadIdx.x;
+    const long n = (long)P.nx * P.ny;
+    double a = 0, b = 0, d = 0, r2 = 0;
+    for (long k = (long)blockIdx.x * blockDim.x + tid; k < n; k += (long)gridDim.x * blockDim.x) {
+        const int j = (int)(k / P.nx), i = (int)(k % P.nx);
+        const size_t c = (size_t)j * P.pitch + i;
+        const double r = rho[c];
+        a += r;
+        if (has_phi) b += phi[c];
+        const double dr = r - rho_last[c];
+        d += dr * dr;
+        r2 += r * r;
+        rho_last[c] = r;
+    }
+    sh[0][tid] = a;
+    sh[1][tid] = b;
+    sh[2][tid] = d;
+    sh[3][tid] = r2;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (tid < s)
+            for (int m = 0; m < 4; ++m) sh[m][tid] += sh[m][tid + s];
+        __syncthreads();
+    }
+    if (tid < 4) partial[(size_t)blockIdx.x * 4 + tid] = sh[tid][0];
+}
+
+__global__ void k_reduce_final(const double *__restrict__ partial, int nblocks, double *out) {
+    __shared__ double sh[4][256];
+    const int tid = threadIdx.x;
+    double v[4] = {0, 0, 0, 0};
+    for (int k = tid; k < nblocks; k += blockDim.x)
+        for (int m = 0; m < 4; ++m) v[m] += partial[(size_t)k * 4 + m];
+    for (int m = 0; m < 4; ++m) sh[m][tid] = v[m];
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (tid < s)
+            for (int m = 0; m < 4; ++m) sh[m][tid] += sh[m][tid + s];
+        __syncthreads();
+    }
+    if (tid < 4) out[tid] = sh[tid][0];
+}
+
+__global__ void k_check_finite(const double *__restrict__ a, size_t n, int *flag) {
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        if (!isfinite(a[k])) {
+            atomicOr(flag, 1);
+            return;
+        }
+}
+
+// ---------------------------------------------------------------------------
+// Host-side launch helpers (called from capi.cu).
+void set_d2v16_matrix(const double *m256, cudaStream_t st) {
+    cudaMemcpyToSymbolAsync(c_iM16, m256, sizeof(double) * 256, 0, cudaMemcpyHostToDevice, st);
+}
+
+template <int MODEL, bool WALLS>
+static void launch_step_t(const Params &P, const State &S, int do_msrc, int gin, int gout, cudaStream_t st,
+                          int64_t *launches, cudaEvent_t *ev) {
+    const dim3 blk(32, 8);
+    const dim3 grd((P.nx + 31) / 32, (P.ny + 7) / 8);
+    if (ev) cudaEventRecord(ev[0], st);
+    k_collide<MODEL, WALLS><<<grd, blk, 0, st>>>(P, S, do_msrc, gin, gout);
+    if (ev) cudaEventRecord(ev[1], st);
+    if constexpr (MODEL == AC || MODEL == HCZ) {
+        const dim3 gf((P.nx + 31) / 32, (P.ny + 1 + 7) / 8, 2);
+        k_faces_ac<MODEL, WALLS><<<gf, blk, 0, st>>>(P, S);
+        *launches += 3;
+    } else {
+        const dim3 gf((P.nx + 31) / 32, (P.ny + 7) / 8, 2);
+        k_faces_pp1<MODEL><<<gf, blk, 0, st>>>(P, S);
+        k_faces_pp2<MODEL><<<gf, blk, 0, st>>>(P, S);
+        *launches += 4;
+    }
+    if (ev) cudaEventRecord(ev[2], st);
+    k_update<MODEL, WALLS><<<grd, blk, 0, st>>>(P, S);
+    if (ev) cudaEventRecord(ev[3], st);
+}
+
+template <int MODEL, bool WALLS>
+static void launch_finalize_t(const Params &P, const State &S, int gin, cudaStream_t st) {
+    const dim3 blk(32, 8);
+    const dim3 grd((P.nx + 31) / 32, (P.ny + 7) / 8);
+    k_finalize<MODEL, WALLS><<<grd, blk, 0, st>>>(P, S, gin);
+}
+
+void launch_fp64_step(const Params &P, const State &S, int do_msrc, int gin, int gout, cudaStream_t st,
+                      int64_t *launches, cudaEvent_t *ev) {
+    switch (P.model * 2 + (P.walls ? 1 : 0)) {
+        case AC * 2 + 0: launch_step_t<AC, false>(P, S, do_msrc, gin, gout, st, launches, ev); break;
+        case AC * 2 + 1: launch_step_t<AC, true>(P, S, do_msrc, gin, gout, st, launches, ev); break;
+        case HCZ * 2 + 0: launch_step_t<HCZ, false>(P, S, do_msrc, gin, gout, st, launches, ev); break;
+        case HCZ * 2 + 1: launch_step_t<HCZ, true>(P, S, do_msrc, gin, gout, st, launches, ev); break;
+        case PP9 * 2 + 0: launch_step_t<PP9, false>(P, S, do_msrc, gin, gout, st, launches, ev); break;
+        case PP16 * 2 + 0: launch_step_t<PP16, false>(P, S, do_msrc, gin, gout, st, launches, ev); break;
+        default: break;
+    }
+}
+
+void launch_fp64_finalize(const Params &P, const State &S, int gin, cudaStream_t st, int64_t *launches) {
+    switch (P.model * 2 + (P.walls ? 1 : 0)) {
+        case AC * 2 + 0: launch_finalize_t<AC, false>(P, S, gin, st); break;
+        case AC * 2 + 1: launch_finalize_t<AC, true>(P, S, gin, st); break;
+        case HCZ * 2 + 0: launch_finalize_t<HCZ, false>(P, S, gin, st); break;
+        case HCZ * 2 + 1: launch_finalize_t<HCZ, true>(P, S, gin, st); break;
+        case PP9 * 2 + 0: launch_finalize_t<PP9, false>(P, S, gin, st); break;
+        case PP16 * 2 + 0: launch_finalize_t<PP16, false>(P, S, gin, st); break;
+        default: return;
+    }
+    *launches += 1;
+}
+
+void launch_reduce(const Params &P, const double *rho, const double *phi, double *rho_last, double *partial,
+                   int nblocks, double *out4, int has_phi, cudaStream_t st, int64_t *launches) {
+    k_reduce_partial<<<nblocks, 256, 0, st>>>(P, rho, phi, rho_last, partial, has_phi);
+    k_reduce_final<<<1, 256, 0, st>>>(partial, nblocks, out4);
+    *launches += 2;
+}
+
+void launch_check_finite(const double *a, size_t n, int *flag, cudaStream_t st, int64_t *launches) {
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    k_check_finite<<<blocks, 256, 0, st>>>(a, n, flag);
+    *launches += 1;
+}
+
+}  // namespace dugks

@@ -1,0 +1,90 @@
+"""The CPU restatement (oracle) against the reference's own outputs.
+
+The fixtures in tests/golden were written by the unmodified reference solver
+(tests/golden/make_golden.py); the oracle must reproduce them bit for bit.
+"""
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from variants import VARIANTS
+
+SMALL = ['ac_small', 'hcz_drop', 'hcz_rt', 'pp_drop']
+
+
+def _fields(o, names):
+    out = {}
+    for k in names:
+        try:
+            out[k] = o.get(k)
+        except KeyError:
+            pass
+    return out
+
+
+@pytest.mark.parametrize('name', SMALL)
+def test_oracle_init_bitexact(golden, name):
+    meta, load = golden
+    g = load(name)[0]
+    o = Oracle.from_variant(VARIANTS[name])
+    got = _fields(o, g.keys())
+    # the init of the pseudopotential psi/scg and of the ghost-only fields is not stored
+    checked = 0
+    for k, ref in g.items():
+        if k in got and k not in ('psi', 'scg'):
+            assert np.array_equal(got[k], ref), f'{name} init field {k} differs'
+            checked += 1
+    assert checked >= 10
+
+
+@pytest.mark.parametrize('name', SMALL)
+def test_oracle_steps_bitexact(golden, name):
+    meta, load = golden
+    steps = meta[name]['steps']
+    g = load(name)[steps]
+    o = Oracle.from_variant(VARIANTS[name])
+    o.step(steps)
+    got = _fields(o, g.keys())
+    checked = 0
+    for k, ref in g.items():
+        if k in got:
+            assert np.array_equal(got[k], ref), f'{name} step {steps} field {k} differs'
+            checked += 1
+    assert checked >= 20
+
+
+@pytest.mark.parametrize('name', ['ac_c1', 'ac_default'])
+def test_oracle_droplet_2000_steps(golden, name):
+    """128x128 droplet, 2000 steps: fields, mass and the step-2000 residual."""
+    meta, load = golden
+    g = load(name)[2000]
+    o = Oracle.from_variant(VARIANTS[name])
+    o.step(1000)
+    rho1k = o.get('rho')
+    o.step(1000)
+    for k in ('rho', 'p', 'phi'):
+        assert np.array_equal(o.get(k), g[k]), k
+    rho = o.get('rho')
+    res = np.sqrt(np.sum((rho - rho1k) ** 2) / (np.sum(rho * rho) + 1e-30))
+    ref = meta[name]['log']['2000']
+    # numpy sums pairwise, the reference sequentially: agree to rounding
+    assert abs(res - ref['residual']) <= 1e-12 * abs(ref['residual'])
+    assert abs(o.sums()[0] - ref['sumrho']) <= 1e-12 * ref['sumrho']
+
+
+def test_reference_default_smoke_values(golden):
+    """Pinned values of the reference default run (AC_Drop, 128x128, 2000 steps)."""
+    meta, _ = golden
+    log = meta['ac_default']['log']['2000']
+    assert log['residual'] == pytest.approx(1.159233983870e-06, rel=1e-12)
+    # sum of rho without the reference's excluded cell [64][65] (rho = 1 there)
+    assert log['sumrho'] - 1.0 == pytest.approx(1.036568881239e+05, rel=1e-12)
+
+
+def test_oracle_mass_conservation_periodic():
+    o = Oracle('AC', 24, 20, False, 'ac_drop_inside', Mu0=0.01, W=4.0, Sigma=1e-3, RhoL=1.0, RhoV=0.1, radius=6.0)
+    m0 = o.sums()
+    o.step(300)
+    m1 = o.sums()
+    assert abs(m1[1] - m0[1]) <= 1e-11 * abs(m0[1])
+    assert abs(m1[0] - m0[0]) <= 1e-11 * abs(m0[0])
