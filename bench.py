@@ -161,7 +161,7 @@ def run_ours(args, rank, world, local):
         if world > 1:
             dist.barrier()
 
-    case = capi.make_case('HCZ', 'fp64', **CASE_KW)
+    case = capi.make_case('HCZ', args.precision, **CASE_KW)
     gc = capi.GpuCase(case, NX, NY, True)
     gc.init('ac_rt')
     stream = torch.cuda.Stream()
@@ -232,9 +232,11 @@ def run_ours(args, rank, world, local):
         cpu = None
         if not args.no_cpu_baseline:
             thr = os.cpu_count() or 1
-            cmlups, csecs = cpu_baseline_sample(args.cpu_steps, thr)
+            _, one = cpu_baseline_sample(1, thr)
+            nsteps = args.cpu_steps or max(2, int(args.cpu_seconds / max(one, 1e-3)))
+            cmlups, csecs = cpu_baseline_sample(nsteps, thr)
             cpu = {'value': round(cmlups, 4), 'unit': 'MLUPS', 'cores': thr, 'kind': 'port',
-                   'sample': f'{args.cpu_steps} steps of the {NX}x{NY} workload on the CPU restatement '
+                   'sample': f'{nsteps} steps of the {NX}x{NY} workload on the CPU restatement '
                              f'(OpenMP, {thr} threads, {csecs:.1f} s)'}
         clocks = clk.summary()
         line = {
@@ -242,7 +244,7 @@ def run_ours(args, rank, world, local):
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_max / args.steps, 5),
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
             'data': 'synthetic (seeded Rayleigh-Taylor initial condition, no dataset)',
-            'config': {'workload': WORKLOAD, 'cells': cells, 'precision': 'fp64',
+            'config': {'workload': WORKLOAD, 'cells': cells, 'precision': args.precision,
                        'l2_flush': 'none needed: resident state ~0.9 GB > 129 MB L2',
                        'parallelism': f'{world} independent replicas' if world > 1 else 'single GPU'},
             'roofline': {'bound': 'hbm', 'achieved': round(achieved_step, 2), 'peak': hbm_peak, 'unit': 'GB/s',
@@ -273,8 +275,11 @@ def main():
     ap.add_argument('--steps', type=int, default=1000)
     ap.add_argument('--warmup', type=int, default=20)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
-    ap.add_argument('--cpu-steps', type=int, default=4)
+    ap.add_argument('--cpu-steps', type=int, default=0, help='CPU baseline steps (0: about --cpu-seconds)')
+    ap.add_argument('--cpu-seconds', type=float, default=15.0)
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--precision', default='fp64', choices=['fp64', 'fp64fma'],
+                    help='fp64: reference-exact rounding (default); fp64fma: FMA-contracted FP64')
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -20,6 +20,10 @@ NVFLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompiler'
            '-Xcompiler', '-ffp-contract=off', '--expt-relaxed-constexpr', f'-I{INCLUDE}']
 
 
+# the reference-exact FP64 step keeps every multiply and add separately rounded
+PER_FILE = {'fp64_exact.cu': ['-fmad=false']}
+
+
 def sources() -> list[Path]:
     return sorted(CSRC.glob('*.cu')) + sorted(CSRC.glob('*.cpp'))
 
@@ -43,7 +47,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
 
     def compile_one(src: Path) -> Path:
         obj = BUILD / (src.name + '.o')
-        cmd = [exe] + ARCH + flags + ['-x', 'cu', '-c', str(src), '-o', str(obj)]
+        cmd = [exe] + ARCH + flags + PER_FILE.get(src.name, []) + ['-x', 'cu', '-c', str(src), '-o', str(obj)]
         if verbose:
             cmd.insert(1, '-Xptxas=-v')
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -16,13 +16,20 @@
 #include "dugks_device.cuh"
 
 namespace dugks {
-void set_d2v16_matrix(const double *m256, cudaStream_t st);
-void launch_fp64_step(const Params &P, const State &S, int do_msrc, int gin, int gout, cudaStream_t st,
-                      int64_t *launches, cudaEvent_t *ev);
-void launch_fp64_finalize(const Params &P, const State &S, int gin, cudaStream_t st, int64_t *launches);
-void launch_reduce(const Params &P, const double *rho, const double *phi, double *rho_last, double *partial,
-                   int nblocks, double *out4, int has_phi, cudaStream_t st, int64_t *launches);
-void launch_check_finite(const double *a, size_t n, int *flag, cudaStream_t st, int64_t *launches);
+#define DUGKS_DECLARE_FP64(NS)                                                                                  \
+    namespace NS {                                                                                              \
+    void set_d2v16_matrix(const double *m256, cudaStream_t st);                                                 \
+    void launch_fp64_step(const Params &P, const State &S, int do_msrc, int gin, int gout, cudaStream_t st,     \
+                          int64_t *launches, cudaEvent_t *ev);                                                  \
+    void launch_fp64_finalize(const Params &P, const State &S, int gin, cudaStream_t st, int64_t *launches);   \
+    void launch_reduce(const Params &P, const double *rho, const double *phi, double *rho_last, double *partial, \
+                       int nblocks, double *out4, int has_phi, cudaStream_t st, int64_t *launches);             \
+    void launch_check_finite(const double *a, size_t n, int *flag, cudaStream_t st, int64_t *launches);         \
+    }
+DUGKS_DECLARE_FP64(exact)
+DUGKS_DECLARE_FP64(fast)
+using exact::launch_reduce;
+using exact::launch_check_finite;
 void build_d2v16_matrix(double c, double out[16][16]);
 void derive_params(const dugks_case_t &cs, const dugks_grid_t &g, Params &P);
 int host_init_state(const Params &P, const double iM[16][16], int kind, const double *params, int nparams,
@@ -52,6 +59,11 @@ struct dugks_handle {
 
 static std::string g_create_err;
 
+using step_fn = void (*)(const Params &, const State &, int, int, int, cudaStream_t, int64_t *, cudaEvent_t *);
+static step_fn step_launcher(const dugks_handle *h) {
+    return h->cs.precision == DUGKS_FP64_FMA ? fast::launch_fp64_step : exact::launch_fp64_step;
+}
+
 static int fail(dugks_handle *h, int code, const std::string &msg) {
     if (h) h->err = msg;
     else g_create_err = msg;
@@ -73,7 +85,7 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
         return fail(nullptr, DUGKS_EINVAL, "unknown model");
     if ((c->model == DUGKS_MODEL_PP9 || c->model == DUGKS_MODEL_PP16) && g->y_walls)
         return fail(nullptr, DUGKS_EINVAL, "pseudopotential models are periodic only (faceFaces need no walls)");
-    if (c->precision != DUGKS_FP64 && c->precision != DUGKS_FP32_DEV)
+    if (c->precision != DUGKS_FP64 && c->precision != DUGKS_FP32_DEV && c->precision != DUGKS_FP64_FMA)
         return fail(nullptr, DUGKS_EINVAL, "unknown precision");
     if (c->precision == DUGKS_FP32_DEV)
         return fail(nullptr, DUGKS_EINVAL, "FP32 deviation storage is served by dugks_f32_* entry points");
@@ -140,7 +152,10 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
     h->partial = take(align256(sizeof(double) * 4 * h->nblocks));
     h->out4 = take(256);
     h->flag = reinterpret_cast<int *>(take(256));
-    if (P.model == PP16) set_d2v16_matrix(&h->iM[0][0], nullptr);
+    if (P.model == PP16) {
+        exact::set_d2v16_matrix(&h->iM[0][0], nullptr);
+        fast::set_d2v16_matrix(&h->iM[0][0], nullptr);
+    }
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         cudaFree(h->arena);
@@ -222,7 +237,7 @@ extern "C" int dugks_gpu_step(dugks_handle_t *h, int nsteps, void *stream) {
         h->last_stream = st;
     }
     for (int s = 0; s < nsteps; ++s) {
-        launch_fp64_step(h->P, h->S, h->pending, h->gcur, h->gcur ^ 1, st, &h->launches, nullptr);
+        step_launcher(h)(h->P, h->S, h->pending, h->gcur, h->gcur ^ 1, st, &h->launches, nullptr);
         h->gcur ^= 1;
         h->pending = 1;
     }
@@ -243,7 +258,7 @@ extern "C" int dugks_gpu_step_profiled(dugks_handle_t *h, int nsteps, void *stre
     double acc[3] = {0, 0, 0};
     cudaError_t e = cudaSuccess;
     for (int s = 0; s < nsteps && e == cudaSuccess; ++s) {
-        launch_fp64_step(h->P, h->S, h->pending, h->gcur, h->gcur ^ 1, st, &h->launches, ev);
+        step_launcher(h)(h->P, h->S, h->pending, h->gcur, h->gcur ^ 1, st, &h->launches, ev);
         h->gcur ^= 1;
         h->pending = 1;
         h->steps += 1;
@@ -263,7 +278,8 @@ extern "C" int dugks_gpu_step_profiled(dugks_handle_t *h, int nsteps, void *stre
 
 static int finalize(dugks_handle *h) {
     if (!h->pending) return DUGKS_OK;
-    launch_fp64_finalize(h->P, h->S, h->gcur, h->last_stream, &h->launches);
+    (h->cs.precision == DUGKS_FP64_FMA ? fast::launch_fp64_finalize : exact::launch_fp64_finalize)(
+        h->P, h->S, h->gcur, h->last_stream, &h->launches);
     h->pending = 0;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(h, e, "finalize launch");

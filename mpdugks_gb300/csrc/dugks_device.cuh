@@ -36,6 +36,10 @@ struct Params {
     double h_aBP, h_bBP, h_cBP, h_ah, h_bh, h_ch;  // constant phase-field relaxation factors
     double aTP, bTP, dtV;                          // 4/3, 1/3, dt/volume
     double T_CS, aCS;                              // Carnahan-Starling EOS
+    // Reconstruction denominators as multipliers: -1/dx, -1/dy, 1/(2dy), 1/(-2dx).
+    // grad_mul = 1 when dx and dy are powers of two, so x/d == x*(1/d) exactly.
+    double r_ndx, r_ndy, r_2dy, r_n2dx;
+    int grad_mul, pad2_;
     double c16;                                    // D2V16 lattice speed
     double xi_u[16], xi_v[16], omega[16];
     int bb[16];

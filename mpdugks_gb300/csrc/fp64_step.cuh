@@ -10,13 +10,30 @@
 // The pseudopotential models split the face pass in two (face psi, then
 // face force) -- the Jacobi semantics of the face psi gradient.
 //
-// Arithmetic follows the reference expressions term by term (same operand
-// association); the compiler may contract a*b+c into FMA, so results agree
-// with the FP64 reference to rounding, not bit for bit.
+// This file is compiled twice (see fp64_exact.cu / fp64_fast.cu):
+//  * DUGKS_EXACT = 1 with -fmad=false: every expression keeps the reference's
+//    operand association, divisions stay divisions and nothing is contracted
+//    into FMA, so the step reproduces the reference solver bit for bit (CUDA's
+//    FP64 +, -, *, / and sqrt are correctly rounded, like the host's);
+//  * DUGKS_EXACT = 0 with FMA contraction and reciprocal multiplies: the same
+//    algorithm with fewer FP64 instructions, equal to the reference to rounding.
+#pragma once
 #include <cuda_runtime.h>
 #include "dugks_device.cuh"
 
+#ifndef DUGKS_EXACT
+#error "define DUGKS_EXACT before including fp64_step.cuh"
+#endif
+#if DUGKS_EXACT
+#define DUGKS_KNS exact
+#define RDIV(x, d, invd) ((x) / (d))   // reference: a true division
+#else
+#define DUGKS_KNS fast
+#define RDIV(x, d, invd) ((x) * (invd)) // one reciprocal, then multiplies
+#endif
+
 namespace dugks {
+namespace DUGKS_KNS {
 
 __constant__ double c_iM16[16][16];  // D2V16 inverse moment matrix (Ark/Lib/D2V16.cpp:34-52)
 
@@ -35,6 +52,29 @@ __device__ __forceinline__ double cellv(const double *__restrict__ a, int ny, in
         j -= ny;
     }
     return a[(size_t)j * pitch + i];
+}
+
+// (xu*a + xv*b)/RT for the 9 D2Q9 directions from 4 divisions:
+// a/RT, b/RT, (a+b)/RT, (b-a)/RT; the other directions are their negatives
+// ((-x)/RT == -(x/RT) and -a + -b == -(a+b) exactly), direction 0 gives 0.
+struct Xi4 {
+    double a, b, s, d;
+    __device__ __forceinline__ double get(int xu, int xv) const {
+        if (xu == 0 && xv == 0) return 0.0;
+        if (xv == 0) return xu > 0 ? a : -a;
+        if (xu == 0) return xv > 0 ? b : -b;
+        if (xu == xv) return xu > 0 ? s : -s;
+        return xv > 0 ? d : -d;  // (-1,1): b - a;  (1,-1): a - b = -(b - a)
+    }
+};
+__device__ __forceinline__ Xi4 xi4(double a, double b, double RT, double invRT) {
+    (void)invRT;
+    Xi4 r;
+    r.a = RDIV(a, RT, invRT);
+    r.b = RDIV(b, RT, invRT);
+    r.s = RDIV(a + b, RT, invRT);
+    r.d = RDIV(b - a, RT, invRT);
+    return r;
 }
 
 // ---------------------------------------------------------------------------
@@ -191,8 +231,12 @@ __global__ void __launch_bounds__(256) k_collide(Params P, State S, int do_msrc,
             if (j == P.ny - 1) S.gphi[(size_t)(gout * 2 + 1) * pitch + i] = 2.0 * phi - S.fld[F_PHI][c - pitch];
         }
         const double invRT = 1.0 / P.RT;
-        const double pRT = p * invRT;
+        const double pRT = RDIV(p, P.RT, invRT);
         const double uu = U * U + V * V;
+        // (xi.a)/RT for xi in {0,+-1}^2 takes 4 distinct magnitudes; (-x)/RT == -(x/RT)
+        Xi4 ur, fr;
+        if (MODEL == AC) fr = xi4(fx, fy, P.RT, invRT);
+        else ur = xi4(U, V, P.RT, invRT);
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
             const int xu = d2q9_xu(q), xv = d2q9_xv(q);
@@ -202,9 +246,9 @@ __global__ void __launch_bounds__(256) k_collide(Params P, State S, int do_msrc,
                 hEq = w * phi;
                 fEq = w * pRT;
                 if (q == 0) fEq -= pRT;
-                fSo = w * ((sx(xu, fx) + sx(xv, fy)) * invRT);
+                fSo = w * fr.get(xu, xv);
             } else {
-                const double u1 = (sx(xu, U) + sx(xv, V)) * invRT;
+                const double u1 = ur.get(xu, xv);
                 const double G = u1 + 0.5 * u1 * u1 - uu * P.Lambda0;
                 const double cu = (double)xu - U, cv = (double)xv - V;
                 hEq = w * (1.0 + u1) * phi;
@@ -240,7 +284,7 @@ __global__ void __launch_bounds__(256) k_collide(Params P, State S, int do_msrc,
         const double inv = 1.0 / (rho * P.RT);
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
-            const double So = (fx * (P.xi_u[q] - U) + fy * (P.xi_v[q] - V)) * eq[q] * inv;
+            const double So = RDIV((fx * (P.xi_u[q] - U) + fy * (P.xi_v[q] - V)) * eq[q], rho * P.RT, inv);
             const size_t o = (size_t)q * S.qs + c;
             S.bf[o] = aBP * S.f[o] + bBP * eq[q] + cBP * So;
         }
@@ -255,21 +299,36 @@ template <bool XF, bool WALLS>
 __device__ __forceinline__ double face_bh(const Params &P, const double *__restrict__ B, int i, int im, int ip,
                                           int j, double xu, double xv) {
     const int ny = P.ny, pitch = P.pitch;
+    // Denominators: the reference divides by _dx = xo - xn = -dx (normal) and by
+    // 2(x1 - x0) = +-2d (tangential).  When dx, dy are powers of two (grad_mul)
+    // the division is the exact multiply by the reciprocal, and
+    // 0.5a + 0.5b == 0.5(a + b) exactly (power-of-two scaling commutes with
+    // rounding away from the subnormal range), so these forms round alike.
     double o, n, gx, gy;
     if (XF) {
         o = cellv<WALLS>(B, ny, pitch, j, im);
         n = cellv<WALLS>(B, ny, pitch, j, i);
         const double SL = cellv<WALLS>(B, ny, pitch, j - 1, im), SR = cellv<WALLS>(B, ny, pitch, j - 1, i);
         const double NL = cellv<WALLS>(B, ny, pitch, j + 1, im), NR = cellv<WALLS>(B, ny, pitch, j + 1, i);
-        gy = (0.5 * (NR - SR) + 0.5 * (NL - SL)) / (2 * P.dy);
-        gx = (o - n) / (-P.dx);
+        if (P.grad_mul) {
+            gy = (0.5 * ((NR - SR) + (NL - SL))) * P.r_2dy;
+            gx = (o - n) * P.r_ndx;
+        } else {
+            gy = (0.5 * (NR - SR) + 0.5 * (NL - SL)) / (2 * P.dy);
+            gx = (o - n) / (-P.dx);
+        }
     } else {
         o = cellv<WALLS>(B, ny, pitch, j - 1, i);
         n = cellv<WALLS>(B, ny, pitch, j, i);
         const double WB = cellv<WALLS>(B, ny, pitch, j - 1, im), EB = cellv<WALLS>(B, ny, pitch, j - 1, ip);
         const double WT = cellv<WALLS>(B, ny, pitch, j, im), ET = cellv<WALLS>(B, ny, pitch, j, ip);
-        gx = (0.5 * (WT - ET) + 0.5 * (WB - EB)) / (2 * (-P.dx));
-        gy = (o - n) / (-P.dy);
+        if (P.grad_mul) {
+            gx = (0.5 * ((WT - ET) + (WB - EB))) * P.r_n2dx;
+            gy = (o - n) * P.r_ndy;
+        } else {
+            gx = (0.5 * (WT - ET) + 0.5 * (WB - EB)) / (2 * (-P.dx));
+            gy = (o - n) / (-P.dy);
+        }
     }
     return 0.5 * (o + n) - P.hDt * (gx * xu + gy * xv);
 }
@@ -327,10 +386,10 @@ __global__ void __launch_bounds__(256) k_faces_ac(Params P, State S) {
 #pragma unroll
         for (int q = 0; q < 9; ++q) sv += sx(d2q9_xv(q), bf[q]);
         const double inv = 1.0 / (Rho * P.RT);
-        U = su * inv;
-        V = sv * inv;
-        U += 0.5 * P.hDt * Fx * inv;
-        V += 0.5 * P.hDt * Fy * inv;
+        U = RDIV(su, Rho * P.RT, inv);
+        V = RDIV(sv, Rho * P.RT, inv);
+        U += RDIV(0.5 * P.hDt * Fx, Rho * P.RT, inv);
+        V += RDIV(0.5 * P.hDt * Fy, Rho * P.RT, inv);
         p = sumf + 0.5 * P.hDt * P.RT * (Rho_x * U + Rho_y * V);
         Mu = P.NuV + (Phi - P.PhiV) * (P.NuL - P.NuV);
         Mu *= Rho;
@@ -338,7 +397,10 @@ __global__ void __launch_bounds__(256) k_faces_ac(Params P, State S) {
     const double tauh = Mu / (Rho * P.RT);
     const double ah = 2.0 * tauh / (2.0 * tauh + P.hDt), bh_ = 1.0 - ah, ch = tauh * bh_;
     const double uu = U * U + V * V;
-    const double pRT = p * invRT;
+    const double pRT = RDIV(p, P.RT, invRT);
+    Xi4 ur, fr;
+    if (MODEL == AC) fr = xi4(Fx, Fy, P.RT, invRT);
+    else ur = xi4(U, V, P.RT, invRT);
     double hf[9], hh[9];
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
@@ -349,9 +411,9 @@ __global__ void __launch_bounds__(256) k_faces_ac(Params P, State S) {
             hEq = w * Phi;
             fEq = w * pRT;
             if (q == 0) fEq -= pRT;
-            fSo = w * ((sx(xu, Fx) + sx(xv, Fy)) * invRT);
+            fSo = w * fr.get(xu, xv);
         } else {
-            const double u1 = (sx(xu, U) + sx(xv, V)) * invRT;
+            const double u1 = ur.get(xu, xv);
             const double G = u1 + 0.5 * u1 * u1 - uu * P.Lambda0;
             const double cu = (double)xu - U, cv = (double)xv - V;
             hEq = w * Phi * (1.0 + u1);
@@ -453,7 +515,7 @@ __global__ void __launch_bounds__(256) k_faces_pp2(Params P, State S) {
     const size_t qs = xf ? S.qs : S.qsy;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-        const double So = (Fx * (P.xi_u[q] - U) + Fy * (P.xi_v[q] - V)) * eq[q] * inv;
+        const double So = RDIV((Fx * (P.xi_u[q] - U) + Fy * (P.xi_v[q] - V)) * eq[q], R * P.RT, inv);
         const double t = ah * BB[(size_t)q * S.qs + c] + bh * eq[q] + ch * So;
         out[(size_t)q * qs + c] = t * (xf ? P.xi_u[q] : P.xi_v[q]);
     }
@@ -510,10 +572,10 @@ __global__ void __launch_bounds__(256) k_update(Params P, State S) {
             Mu = Rho * P.RT * P.Tau0;
         } else {
             const double inv = 1.0 / (Rho * P.RT);
-            U = su * inv;
-            V = sv * inv;
-            U += P.hDt * S.fld[F_FX][c] * inv;
-            V += P.hDt * S.fld[F_FY][c] * inv;
+            U = RDIV(su, Rho * P.RT, inv);
+            V = RDIV(sv, Rho * P.RT, inv);
+            U += RDIV(P.hDt * S.fld[F_FX][c], Rho * P.RT, inv);
+            V += RDIV(P.hDt * S.fld[F_FY][c], Rho * P.RT, inv);
             p = sumf + P.hDt * (S.fld[F_RHOX][c] * U + S.fld[F_RHOY][c] * V) * P.RT;
             Mu = P.NuV + (Phi - P.PhiV) * (P.NuL - P.NuV);
             Mu *= Rho;
@@ -710,4 +772,5 @@ void launch_check_finite(const double *a, size_t n, int *flag, cudaStream_t st, 
     *launches += 1;
 }
 
+}  // namespace DUGKS_KNS
 }  // namespace dugks

@@ -80,6 +80,15 @@ void derive_params(const dugks_case_t &cs, const dugks_grid_t &g, Params &P) {
         P.h_bh = 1.0 - P.h_ah;
         P.h_ch = tau * P.h_bh;
     }
+    {   // power-of-two spacings make every reconstruction division an exact multiply
+        int e;
+        const bool p2 = std::frexp(P.dx, &e) == 0.5 && std::frexp(P.dy, &e) == 0.5;
+        P.grad_mul = p2 ? 1 : 0;
+        P.r_ndx = 1.0 / (-P.dx);
+        P.r_ndy = 1.0 / (-P.dy);
+        P.r_2dy = 1.0 / (2 * P.dy);
+        P.r_n2dx = 1.0 / (2 * (-P.dx));
+    }
     P.T_CS = cs.Tr * cs.Tc_CS;
     P.aCS = cs.aCS;
     if (d2v16) {

@@ -1,10 +1,14 @@
 """FP64 GPU path vs the reference (golden fixtures) and vs the oracle.
 
-Tolerance: the plain FP64 path must match the reference CPU solver to 1e-12
-relative in rho, u and phi after N steps.  "Relative" is the max-norm ratio
-max|gpu - ref| / max|ref| per field (fields such as u cross zero, so a
-per-element ratio is meaningless); the same bound is applied here to every
-macroscopic field and to both distributions.
+Two FP64 variants run through the same C ABI:
+  'fp64'    (DUGKS_FP64)     every operation rounded like the reference:
+            the results must be BIT-IDENTICAL to the reference's;
+  'fp64fma' (DUGKS_FP64_FMA) FMA contraction + reciprocal multiplies: must
+            match to 1e-12 relative in rho, p, phi and the distributions,
+            "relative" being the max-norm ratio max|gpu - ref| / max|ref|
+            per field.  The velocity is a small difference of O(0.1)
+            distribution moments, so its rounding floor is absolute: u and v
+            must agree to 1e-13 in lattice units (|xi| = 1).
 """
 import numpy as np
 import pytest
@@ -15,16 +19,18 @@ from variants import VARIANTS
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-12
+UV_ABS = 1e-13
 SMALL = ['ac_small', 'hcz_drop', 'hcz_rt', 'pp_drop']
+PRECISIONS = ['fp64', 'fp64fma']
 MODEL = {'D2Q9AC': 'AC', 'D2Q9HCZ': 'HCZ', 'D2Q9PP': 'PP9'}
 CASE_KEYS = ('Mu0', 'M_Phi', 'W', 'Sigma', 'RhoL', 'RhoV', 'Gy', 'Tr', 'aCS', 'Tc_CS')
 
 
-def gpu_from_variant(v):
+def gpu_from_variant(v, precision='fp64'):
     from mpdugks_gb300 import capi
     c = v['consts']
     kw = {k: c[k] for k in CASE_KEYS if k in c}
-    gc = capi.GpuCase(capi.make_case(MODEL[v['model']], 'fp64', **kw), v['nx'], v['ny'], v['walls'])
+    gc = capi.GpuCase(capi.make_case(MODEL[v['model']], precision, **kw), v['nx'], v['ny'], v['walls'])
     if v['init'] in ('ac_drop', 'ac_drop_inside'):
         gc.init(v['init'], [c.get('radius', -1.0)])
     elif v['init'] == 'scmp_drop':
@@ -34,7 +40,7 @@ def gpu_from_variant(v):
     return gc
 
 
-def compare_state(gc, ref, tol, what):
+def compare_state(gc, ref, tol, what, exact=False, min_fields=None):
     n = 0
     for k, r in ref.items():
         if k in ('psi', 'scg', 'tauf') and not np.any(r):
@@ -46,61 +52,102 @@ def compare_state(gc, ref, tol, what):
             got = gc.dist(k[0])[q]
         else:
             got = gc.get(k)
-        e = rel_err(got, r)
-        assert e <= tol, f'{what}: field {k} rel err {e:.3e} > {tol:g}'
+        if exact:
+            nbad = int(np.sum(got != r))
+            assert nbad == 0, f'{what}: field {k} differs in {nbad} cells (max rel {rel_err(got, r):.3e})'
+        elif k in ('u', 'v', 'prevphiu', 'prevphiv'):
+            e = float(np.max(np.abs(got - r)))
+            assert e <= UV_ABS, f'{what}: field {k} abs err {e:.3e} > {UV_ABS:g}'
+        elif k in ('phix', 'phiy', 'fx', 'fy', 'rhox', 'rhoy', 'psi'):
+            # gradients/sources of near-uniform regions: rounding floor relative to the largest value
+            e = rel_err(got, r)
+            assert e <= 1e-9, f'{what}: field {k} rel err {e:.3e}'
+        else:
+            e = rel_err(got, r)
+            assert e <= tol, f'{what}: field {k} rel err {e:.3e} > {tol:g}'
         n += 1
-    assert n >= 10
+    assert n >= (min_fields if min_fields is not None else min(10, len(ref)))
 
 
 @pytest.mark.parametrize('name', SMALL)
 def test_init_matches_reference(golden, name):
     _, load = golden
     gc = gpu_from_variant(VARIANTS[name])
-    compare_state(gc, load(name)[0], 1e-15, f'{name} init')
+    compare_state(gc, load(name)[0], 0.0, f'{name} init', exact=True)
 
 
+# The reference normalises grad(phi) after clamping |grad phi| < 1e-14 to zero
+# (Ark/Cpp/GradScheme.cpp:374-375, Ark/Cpp/SourceM.cpp:47-58): a discontinuous
+# branch.  In the small Rayleigh-Taylor box a rounding-level difference flips it
+# after ~150 steps (a 1e-14 perturbation of one distribution grows to 5e-7 in
+# one jump in the CPU restatement), so only the bit-exact variant can follow
+# that case to 300 steps; the FMA variant is checked on it for 100 steps.
+FMA_FLIPS = {'hcz_rt'}
+
+
+@pytest.mark.parametrize('precision', PRECISIONS)
 @pytest.mark.parametrize('name', SMALL)
-def test_steps_match_reference(golden, name):
+def test_steps_match_reference(golden, name, precision):
+    if precision == 'fp64fma' and name in FMA_FLIPS:
+        pytest.skip('branch flip of the reference clamp; covered by test_fma_rayleigh_taylor_short')
     meta, load = golden
     steps = meta[name]['steps']
-    gc = gpu_from_variant(VARIANTS[name])
+    gc = gpu_from_variant(VARIANTS[name], precision)
     gc.step(steps)
-    compare_state(gc, load(name)[steps], TOL, f'{name} after {steps} steps')
+    compare_state(gc, load(name)[steps], TOL, f'{name} {precision} after {steps} steps',
+                  exact=(precision == 'fp64'))
     assert gc.check_finite() == 0
 
 
+def test_fma_rayleigh_taylor_short():
+    from oracle.oracle import Oracle
+    v = VARIANTS['hcz_rt']
+    gc = gpu_from_variant(v, 'fp64fma')
+    o = Oracle.from_variant(v)
+    gc.step(100)
+    o.step(100)
+    ref = {k: o.get(k) for k in ('rho', 'u', 'v', 'p', 'phi', 'phix', 'fy')}
+    compare_state(gc, ref, TOL, 'hcz_rt fp64fma 100 steps')
+
+
+@pytest.mark.parametrize('precision', PRECISIONS)
 @pytest.mark.parametrize('name', ['ac_c1', 'ac_default'])
-def test_droplet_2000_steps_match_reference(golden, name):
+def test_droplet_2000_steps_match_reference(golden, name, precision):
     meta, load = golden
-    gc = gpu_from_variant(VARIANTS[name])
+    gc = gpu_from_variant(VARIANTS[name], precision)
     gc.step(1000)
     r1 = gc.reduce()
     gc.step(1000)
     r2 = gc.reduce()
     ref = load(name)[2000]
     for k in ('rho', 'p', 'phi'):
+        if precision == 'fp64':
+            assert np.array_equal(gc.get(k), ref[k]), f'{name} {k} not bit-identical'
         e = rel_err(gc.get(k), ref[k])
         assert e <= TOL, f'{name} {k} rel err {e:.3e}'
     log = meta[name]['log']['2000']
     assert abs(r2.sum_rho - log['sumrho']) <= 1e-12 * log['sumrho']
-    assert abs(r2.residual - log['residual']) <= 1e-9 * log['residual']
+    # the residual is a difference of fields 1000 steps apart (~1e-6 of rho), so
+    # rounding-level differences of rho show up amplified ~1e6 in it
+    rtol = 1e-12 if precision == 'fp64' else 1e-8
+    assert abs(r2.residual - log['residual']) <= rtol * log['residual']
     assert r1.residual == pytest.approx(1.0, rel=1e-12)
 
 
-def test_rayleigh_taylor_512x2048_matches_oracle():
+@pytest.mark.parametrize('precision', PRECISIONS)
+def test_rayleigh_taylor_512x2048_matches_oracle(precision):
     """The benchmark configuration (512x2048, walls, gravity) against the restatement."""
     from mpdugks_gb300 import capi
     from oracle.oracle import Oracle
     kw = dict(Mu0=0.04 * 512 / 3000, M_Phi=0.02, W=4.0, Sigma=5e-5, RhoL=3.0, RhoV=1.0, Gy=0.0016 / 512)
-    gc = capi.GpuCase(capi.make_case('HCZ', 'fp64', **kw), 512, 2048, True)
+    gc = capi.GpuCase(capi.make_case('HCZ', precision, **kw), 512, 2048, True)
     gc.init('ac_rt')
     o = Oracle('HCZ', 512, 2048, True, 'ac_rt', **kw)
     steps = 12
     gc.step(steps)
     o.step(steps)
-    for k in ('rho', 'u', 'v', 'p', 'phi', 'phix', 'fy'):
-        e = rel_err(gc.get(k), o.get(k))
-        assert e <= TOL, f'{k} rel err {e:.3e}'
+    ref = {k: o.get(k) for k in ('rho', 'u', 'v', 'p', 'phi', 'phix', 'fy')}
+    compare_state(gc, ref, TOL, f'RT 512x2048 {precision}', exact=(precision == 'fp64'))
 
 
 def test_d2v16_pseudopotential_matches_oracle():
@@ -108,16 +155,15 @@ def test_d2v16_pseudopotential_matches_oracle():
     from mpdugks_gb300 import capi
     from oracle.oracle import Oracle
     kw = dict(Mu0=0.1, Tr=0.7, aCS=0.5, Tc_CS=0.3773 * 0.5 / 4)
-    rho_c = 0.1304 / 4 * 4  # b*rho_c ~ 0.5218 for CS with b = 4 -> rho_c ~ 0.1304
+    rho_c = 0.1304  # critical density of Carnahan-Starling with b = 4 (b rho_c / 4 = 0.1304)
     gc = capi.GpuCase(capi.make_case('PP16', 'fp64', **kw), 48, 40, False)
     gc.init('pp_noise', [rho_c, 0.01], seed=2024)
     o = Oracle('PP16', 48, 40, False, 'pp_noise', noise_rho0=rho_c, noise_amp=0.01, seed=2024, **kw)
     assert rel_err(gc.dist('f'), o.dists('f')) == 0.0
     gc.step(150)
     o.step(150)
-    for k in ('rho', 'u', 'v', 'psi', 'fx', 'fy'):
-        e = rel_err(gc.get(k), o.get(k))
-        assert e <= TOL, f'{k} rel err {e:.3e}'
+    ref = {k: o.get(k) for k in ('rho', 'u', 'v', 'psi', 'fx', 'fy')}
+    compare_state(gc, ref, TOL, 'D2V16 pseudopotential', exact=True)
 
 
 def test_step_split_and_finalize_are_invisible():
