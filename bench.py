@@ -278,12 +278,23 @@ def main():
     ap.add_argument('--cpu-steps', type=int, default=0, help='CPU baseline steps (0: about --cpu-seconds)')
     ap.add_argument('--cpu-seconds', type=float, default=15.0)
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--profile-steps', type=int, default=0,
+                    help='only run this many steps of the workload (for ncu) and exit')
     ap.add_argument('--precision', default='fp64', choices=['fp64', 'fp64fma'],
                     help='fp64: reference-exact rounding (default); fp64fma: FMA-contracted FP64')
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     rank, world, local = env_dist()
+    if args.profile_steps:
+        # a short plain run of the workload for profilers (ncu); no timing, no JSON line
+        from mpdugks_gb300 import capi
+        gc = capi.GpuCase(capi.make_case('HCZ', args.precision, **CASE_KW), NX, NY, True)
+        gc.init('ac_rt')
+        gc.step(args.profile_steps)
+        r = gc.reduce()
+        print(f'profile run: {args.profile_steps} steps, precision {args.precision}, sum rho {r.sum_rho!r}')
+        return 0
     if args.impl == 'reference':
         return run_reference(args, rank, world)
     return run_ours(args, rank, world, local)

@@ -560,7 +560,6 @@ static void one_step(orc_state *s) {
     const int nx = s->nx, ny = s->ny, Q = s->Q, model = s->in.model;
     const int walls = s->in.y_walls;
     const int AC = (model == ORC_AC || model == ORC_HCZ);
-    const int PP = !AC;
     /* P1: collision pre-step */
 #pragma omp parallel for schedule(static)
     for (int j = 0; j < ny; ++j)

@@ -8,7 +8,7 @@
 // in the order of Ark/Cpp/DUGKS2DSolver.cpp:175-327, then dumps binary FP64
 // fields for the parity tests.
 //
-// Deliberate differences from the reference loop, each also in the design doc:
+// Deliberate differences from the reference loop:
 //  * fixed step count instead of the residual stop;
 //  * no Output_* calls (file output is not part of the parity check);
 //  * the pseudopotential face force (Ark/Cpp/PseudoP.cpp:39-46) reads the
