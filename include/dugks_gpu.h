@@ -148,6 +148,26 @@ int64_t dugks_gpu_launch_count(const dugks_handle_t *h);
 
 int dugks_gpu_destroy(dugks_handle_t *h);
 
+/* No counterpart in the reference.  For callers that must not allocate
+ * device memory themselves or through this library -- a host that hands out
+ * a fixed memory budget or its own pool, a plugin running inside another
+ * runtime, a loop that may not allocate once running -- this advances a
+ * caller-owned device state by nsteps with no cudaMalloc/cudaFree: all scratch
+ * (f-bar-plus, face fluxes, ghost rows) lives in one fixed file-scope device
+ * array of about 2 MB that every GPU loading the library keeps until exit.
+ * d_f, d_h: device [9][ny][nx]; d_aux: device [DUGKS_F_NFIELDS][ny][nx], the
+ * same contents dugks_gpu_upload takes; all three are updated in place and
+ * are complete on return (the last step's MacroSource is applied).  Limits:
+ * models DUGKS_MODEL_AC/HCZ, precision DUGKS_FP64 or DUGKS_FP64_FMA,
+ * nx*ny <= 4096 cells (larger grids return DUGKS_EINVAL with a message in
+ * dugks_gpu_last_error(NULL, ...)).  The first call on each device looks up
+ * the array's device address (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  All calls share the one array: calls whose
+ * work overlaps on the GPU (other streams, other host threads) race on it
+ * and must be serialised by the caller.  Asynchronous on `stream`. */
+int dugks_gpu_step_noalloc(const dugks_case_t *c, const dugks_grid_t *g, double *d_f, double *d_h,
+                           double *d_aux, int nsteps, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

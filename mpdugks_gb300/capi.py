@@ -62,6 +62,8 @@ SIGNATURES = {
     'dugks_gpu_last_error': (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     'dugks_gpu_launch_count': (C.c_int64, [C.c_void_p]),
     'dugks_gpu_destroy': (C.c_int, [C.c_void_p]),
+    'dugks_gpu_step_noalloc': (C.c_int, [C.POINTER(CaseT), C.POINTER(GridT), C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_int, C.c_void_p]),
 }
 
 _lib = None

@@ -59,6 +59,11 @@ struct dugks_handle {
 
 static std::string g_create_err;
 
+namespace dugks {
+// error text for entry points that have no handle (read by dugks_gpu_last_error(NULL, ...))
+void set_global_error(const std::string &msg) { g_create_err = msg; }
+}  // namespace dugks
+
 using step_fn = void (*)(const Params &, const State &, int, int, int, cudaStream_t, int64_t *, cudaEvent_t *);
 static step_fn step_launcher(const dugks_handle *h) {
     return h->cs.precision == DUGKS_FP64_FMA ? fast::launch_fp64_step : exact::launch_fp64_step;
