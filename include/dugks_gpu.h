@@ -45,8 +45,10 @@ typedef enum dugks_precision {
     DUGKS_FP64 = 0,       /* plain FP64 drop-in: every operation rounded like the
                              reference (no FMA contraction), bit-identical results */
     DUGKS_FP32_DEV = 1,   /* FP32 storage of deviations from rest equilibrium */
-    DUGKS_FP64_FMA = 2    /* FP64 with FMA contraction and reciprocal multiplies:
+    DUGKS_FP64_FMA = 2,   /* FP64 with FMA contraction and reciprocal multiplies:
                              equal to the reference to rounding, fewer FP64 ops */
+    DUGKS_FP64_FUSED = 3  /* the fused one-kernel deviation-form step of
+                             DUGKS_FP32_DEV, carried out in FP64 */
 } dugks_precision;
 
 /* Case parameters: the primary inputs of Ark/Constant/ZeroReference.h and

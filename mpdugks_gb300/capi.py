@@ -16,7 +16,7 @@ DUGKS_OK, DUGKS_EINVAL, DUGKS_ENOMEM, DUGKS_ECUDA, DUGKS_ETIMEOUT, DUGKS_ENAN = 
 STATUS_NAMES = {0: 'DUGKS_OK', 1: 'DUGKS_EINVAL', 2: 'DUGKS_ENOMEM', 3: 'DUGKS_ECUDA', 4: 'DUGKS_ETIMEOUT',
                 5: 'DUGKS_ENAN'}
 MODELS = {'AC': 0, 'HCZ': 1, 'PP9': 2, 'PP16': 3}
-PRECISION = {'fp64': 0, 'fp32dev': 1, 'fp64fma': 2}
+PRECISION = {'fp64': 0, 'fp32dev': 1, 'fp64fma': 2, 'fp64fused': 3}
 FIELDS = ['rho', 'u', 'v', 'p', 'phi', 'tauf', 'phix', 'phiy', 'rhox', 'rhoy', 'fx', 'fy', 'prevphiu', 'prevphiv',
           'psi', 'scg']
 INIT_KINDS = {'ac_drop': 0, 'ac_drop_inside': 1, 'ac_rt': 2, 'scmp_drop': 3, 'pp_noise': 4}

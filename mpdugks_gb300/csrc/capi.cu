@@ -28,6 +28,35 @@ namespace dugks {
     }
 DUGKS_DECLARE_FP64(exact)
 DUGKS_DECLARE_FP64(fast)
+}  // namespace dugks
+#include "fp32_state.cuh"
+namespace dugks {
+namespace f32 {
+cudaError_t launch_step32(const P32 &P, const S32 &S, int first, int gin, int gout, cudaStream_t st,
+                          int64_t *launches, uint32_t step);
+void launch_macros32(const P32 &P, const S32 &S, double *rho, double *u, double *v, double *p, double *phi,
+                     int opitch, cudaStream_t st, int64_t *launches);
+cudaError_t launch_step64f(const PR<double> &P, const SR<double> &S, int first, int gin, int gout,
+                           cudaStream_t st, int64_t *launches, uint32_t step);
+void launch_macros64f(const PR<double> &P, const SR<double> &S, double *rho, double *u, double *v, double *p,
+                      double *phi, int opitch, cudaStream_t st, int64_t *launches);
+inline cudaError_t launch_stepX(const P32 &P, const S32 &S, int a, int b, int c, cudaStream_t st, int64_t *l,
+                                uint32_t step) {
+    return launch_step32(P, S, a, b, c, st, l, step);
+}
+inline cudaError_t launch_stepX(const PR<double> &P, const SR<double> &S, int a, int b, int c, cudaStream_t st,
+                                int64_t *l, uint32_t step) {
+    return launch_step64f(P, S, a, b, c, st, l, step);
+}
+inline void launch_macrosX(const P32 &P, const S32 &S, double *rho, double *u, double *v, double *p, double *phi,
+                           int op, cudaStream_t st, int64_t *l) {
+    launch_macros32(P, S, rho, u, v, p, phi, op, st, l);
+}
+inline void launch_macrosX(const PR<double> &P, const SR<double> &S, double *rho, double *u, double *v, double *p,
+                           double *phi, int op, cudaStream_t st, int64_t *l) {
+    launch_macros64f(P, S, rho, u, v, p, phi, op, st, l);
+}
+}  // namespace f32
 using exact::launch_reduce;
 using exact::launch_check_finite;
 void build_d2v16_matrix(double c, double out[16][16]);
@@ -55,6 +84,15 @@ struct dugks_handle {
     int64_t steps = 0;
     cudaStream_t last_stream = nullptr;
     std::string err;
+    // fused deviation-form step (FP32 storage, or the same step in FP64)
+    bool fp32 = false;        // any fused variant
+    bool fused64 = false;     // the FP64 instance
+    f32::P32 P32{};
+    f32::S32 S32{};
+    f32::PR<double> P64f{};
+    f32::SR<double> S64f{};
+    int first = 1;            // next step is the first after an upload
+    bool macros_fresh = false;
 };
 
 static std::string g_create_err;
@@ -81,6 +119,152 @@ static int cuda_fail(dugks_handle *h, cudaError_t e, const char *what) {
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
+// constants of the fused step: FP64 reference expressions, rounded once to R.
+template <typename R>
+static void derive_p32(const Params &P, f32::PR<R> &Q) {
+    Q = f32::PR<R>{};
+    Q.nx = P.nx; Q.ny = P.ny; Q.pitch = P.pitch; Q.walls = P.walls; Q.model = P.model; Q.gravity = P.gravity;
+    Q.phi0 = (R)DUGKS_F32_PHI0; Q.p0 = R(1.0);
+    Q.aPhi = (R)P.aPhi; Q.bPhi = (R)P.bPhi; Q.Kp = (R)P.Kp; Q.RT = (R)P.RT;
+    Q.invRT = (R)(1.0 / P.RT); Q.hDt = (R)P.hDt; Q.dt = (R)P.dt; Q.Lambda0 = (R)P.Lambda0;
+    Q.Beta = (R)P.Beta; Q.Kappa = (R)P.Kappa; Q.PhiL = (R)P.PhiL; Q.PhiV = (R)P.PhiV;
+    Q.RhoL = (R)P.RhoL; Q.Gy = (R)P.Gy;
+    Q.inv_12dx = (R)(1.0 / (P._2dx * 6)); Q.inv_12dy = (R)(1.0 / (P._2dy * 6));
+    Q.inv_6dd = (R)(1.0 / (6 * P.MinL * P.MinL));
+    Q.inv_wI_dphi = (R)(1.0 / (P.wI * (P.PhiL - P.PhiV)));
+    Q.inv_RTdt = (R)(1.0 / (P.RT * P.dt));
+    // after the first step tau = Mu/(rho RT) = Tau0 for both Allen-Cahn models (nu_L = nu_V = nu0)
+    const double tau = P.Tau0;
+    const double aBP = (2.0 * tau - P.hDt) / (2.0 * tau + P.dt), ah = 2.0 * tau / (2.0 * tau + P.hDt);
+    Q.tauf = (R)tau; Q.aBP_f = (R)aBP; Q.ah_f = (R)ah;
+    Q.h_aBP = (R)P.h_aBP; Q.h_bBP = (R)P.h_bBP; Q.h_cBP = (R)P.h_cBP;
+    Q.h_ah = (R)P.h_ah; Q.h_bh = (R)P.h_bh; Q.h_ch = (R)P.h_ch;
+    Q.r_2dy = (R)P.r_2dy; Q.r_ndx = (R)P.r_ndx; Q.r_n2dx = (R)P.r_n2dx; Q.r_ndy = (R)P.r_ndy;
+    Q.aTP = (R)P.aTP; Q.bTP = (R)P.bTP; Q.dtV = (R)P.dtV;
+}
+
+// rest equilibria the deviations are taken from
+static double f_rest(const Params &P, int q) {
+    const double p0 = 1.0;
+    if (P.model == AC) return P.omega[q] * p0 / P.RT - (q == 0 ? p0 / P.RT : 0.0);
+    return P.omega[q] * p0;
+}
+static double h_rest(const Params &P, int q) { return P.omega[q] * DUGKS_F32_PHI0; }
+
+template <typename R>
+static int create_fused(dugks_handle *h, dugks_handle_t **out, f32::PR<R> &PQ, f32::SR<R> &S) {
+    Params &P = h->P;
+    h->fp32 = true;
+    derive_p32<R>(P, PQ);
+    const size_t rowf = (size_t)P.pitch * sizeof(R);
+    const size_t cellf = align256(rowf * P.ny);
+    const size_t rowd = (size_t)P.pitch * sizeof(double);
+    const size_t celld = align256(rowd * P.ny);
+    h->nblocks = 152 * 4;
+    size_t total = 18 * cellf + f32::A_N * cellf + f32::I_N * cellf + align256(4 * rowf) +
+                   6 * celld /* rho u v p phi + rho_last */ + align256(sizeof(double) * 4 * h->nblocks) + 512;
+    cudaError_t e = cudaMalloc(&h->arena, total);
+    if (e != cudaSuccess) {
+        delete h;
+        return fail(nullptr, e == cudaErrorMemoryAllocation ? DUGKS_ENOMEM : DUGKS_ECUDA,
+                    std::string("cudaMalloc of device state failed: ") + cudaGetErrorString(e));
+    }
+    h->arena_bytes = total;
+    cudaMemset(h->arena, 0, total);
+    char *cur = h->arena;
+    auto takef = [&](size_t b) { R *p = reinterpret_cast<R *>(cur); cur += b; return p; };
+    auto taked = [&](size_t b) { double *p = reinterpret_cast<double *>(cur); cur += b; return p; };
+    S.qs = cellf / sizeof(R);
+    S.df = takef(9 * cellf);
+    S.dh = takef(9 * cellf);
+    S.aux = takef(f32::A_N * cellf);
+    S.init = takef(f32::I_N * cellf);
+    S.gphi = takef(align256(4 * rowf));
+    const int fids[5] = {F_RHO, F_U, F_V, F_P, F_PHI};
+    for (int k : fids) h->S.fld[k] = taked(celld);
+    h->rho_last = taked(celld);
+    h->partial = taked(align256(sizeof(double) * 4 * h->nblocks));
+    h->out4 = taked(256);
+    h->flag = reinterpret_cast<int *>(taked(256));
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        cudaFree(h->arena);
+        delete h;
+        return fail(nullptr, DUGKS_ECUDA, std::string("device setup failed: ") + cudaGetErrorString(e));
+    }
+    *out = h;
+    return DUGKS_OK;
+}
+
+static int create_fp32(dugks_handle *h, dugks_handle_t **out) {
+    if (h->cs.precision == DUGKS_FP64_FUSED) {
+        h->fused64 = true;
+        return create_fused<double>(h, out, h->P64f, h->S64f);
+    }
+    return create_fused<float>(h, out, h->P32, h->S32);
+}
+
+// FP64 [Q][ny][nx] state -> deviations and first-step planes on the device
+template <typename R>
+static int upload_fused(dugks_handle *h, f32::SR<R> &S, const double *f, const double *hd, const double *aux) {
+    const Params &P = h->P;
+    const int nx = P.nx, ny = P.ny;
+    const size_t n = (size_t)nx * ny;
+    std::vector<R> tmp(n);
+    auto put = [&](R *dst) {
+        return cudaMemcpy2D(dst, (size_t)P.pitch * sizeof(R), tmp.data(), (size_t)nx * sizeof(R),
+                            (size_t)nx * sizeof(R), ny, cudaMemcpyHostToDevice);
+    };
+    cudaError_t e;
+    for (int q = 0; q < 9; ++q) {
+        const double f0 = f_rest(P, q), h0 = h_rest(P, q);
+        for (size_t k = 0; k < n; ++k) tmp[k] = (R)(f[q * n + k] - f0);
+        if ((e = put(S.df + q * S.qs)) != cudaSuccess) return cuda_fail(h, e, "upload f");
+        for (size_t k = 0; k < n; ++k) tmp[k] = (R)(hd[q * n + k] - h0);
+        if ((e = put(S.dh + q * S.qs)) != cudaSuccess) return cuda_fail(h, e, "upload h");
+    }
+    const int src[f32::I_N] = {F_PHI, F_RHO, F_U, F_V, F_P, F_TAU, F_PHIX, F_PHIY, F_RHOX, F_RHOY, F_FX, F_FY};
+    for (int k = 0; k < f32::I_N; ++k) {
+        const double *a = aux + (size_t)src[k] * n;
+        const double sub = k == f32::I_DPHI ? DUGKS_F32_PHI0 : (k == f32::I_DP ? 1.0 : 0.0);
+        for (size_t m = 0; m < n; ++m) tmp[m] = (R)(a[m] - sub);
+        if ((e = put(S.init + k * S.qs)) != cudaSuccess) return cuda_fail(h, e, "upload init");
+    }
+    // previous MacroSource outputs as the first step's successor will read them
+    const int asrc[f32::A_N] = {F_FX, F_FY, F_RHOX, F_RHOY, F_PPU, F_PPV};
+    for (int k = 0; k < f32::A_N; ++k) {
+        const double *a = aux + (size_t)asrc[k] * n;
+        for (size_t m = 0; m < n; ++m) tmp[m] = (R)a[m];
+        if ((e = put(S.aux + k * S.qs)) != cudaSuccess) return cuda_fail(h, e, "upload aux");
+    }
+    cudaMemset(h->rho_last, 0, (size_t)P.pitch * ny * sizeof(double));
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(h, e, "upload");
+    h->first = 1;
+    h->gcur = 0;
+    h->steps = 0;
+    h->macros_fresh = false;
+    return DUGKS_OK;
+}
+
+static int upload_fp32(dugks_handle *h, const double *f, const double *hd, const double *aux) {
+    return h->fused64 ? upload_fused<double>(h, h->S64f, f, hd, aux) : upload_fused<float>(h, h->S32, f, hd, aux);
+}
+
+static int macros_fp32(dugks_handle *h) {
+    if (h->macros_fresh) return DUGKS_OK;
+    if (h->fused64)
+        f32::launch_macrosX(h->P64f, h->S64f, h->S.fld[F_RHO], h->S.fld[F_U], h->S.fld[F_V], h->S.fld[F_P],
+                            h->S.fld[F_PHI], h->P.pitch, h->last_stream, &h->launches);
+    else
+        f32::launch_macrosX(h->P32, h->S32, h->S.fld[F_RHO], h->S.fld[F_U], h->S.fld[F_V], h->S.fld[F_P],
+                            h->S.fld[F_PHI], h->P.pitch, h->last_stream, &h->launches);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(h, e, "macros launch");
+    h->macros_fresh = true;
+    return DUGKS_OK;
+}
+
 extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, dugks_handle_t **out) {
     if (!c || !g || !out) return fail(nullptr, DUGKS_EINVAL, "null argument");
     *out = nullptr;
@@ -90,10 +274,11 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
         return fail(nullptr, DUGKS_EINVAL, "unknown model");
     if ((c->model == DUGKS_MODEL_PP9 || c->model == DUGKS_MODEL_PP16) && g->y_walls)
         return fail(nullptr, DUGKS_EINVAL, "pseudopotential models are periodic only (faceFaces need no walls)");
-    if (c->precision != DUGKS_FP64 && c->precision != DUGKS_FP32_DEV && c->precision != DUGKS_FP64_FMA)
+    if (c->precision < DUGKS_FP64 || c->precision > DUGKS_FP64_FUSED)
         return fail(nullptr, DUGKS_EINVAL, "unknown precision");
-    if (c->precision == DUGKS_FP32_DEV)
-        return fail(nullptr, DUGKS_EINVAL, "FP32 deviation storage is served by dugks_f32_* entry points");
+    if ((c->precision == DUGKS_FP32_DEV || c->precision == DUGKS_FP64_FUSED) &&
+        !(c->model == DUGKS_MODEL_AC || c->model == DUGKS_MODEL_HCZ))
+        return fail(nullptr, DUGKS_EINVAL, "the fused deviation-form step supports the Allen-Cahn models (AC, HCZ)");
     dugks_handle *h = new (std::nothrow) dugks_handle();
     if (!h) return fail(nullptr, DUGKS_ENOMEM, "host allocation failed");
     h->cs = *c;
@@ -101,6 +286,7 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
     derive_params(*c, *g, h->P);
     Params &P = h->P;
     if (P.model == PP16) build_d2v16_matrix(P.c16, h->iM);
+    if (c->precision == DUGKS_FP32_DEV || c->precision == DUGKS_FP64_FUSED) return create_fp32(h, out);
     // ---- carve the arena
     const size_t rowb = (size_t)P.pitch * sizeof(double);
     const size_t cellb = align256(rowb * P.ny), ycellb = align256(rowb * (P.ny + 1));
@@ -199,6 +385,7 @@ extern "C" int dugks_gpu_upload(dugks_handle_t *h, const double *f, const double
     const size_t n = (size_t)P.nx * P.ny;
     const bool hasH = (P.model == AC || P.model == HCZ);
     if (hasH && !hd) return fail(h, DUGKS_EINVAL, "Allen-Cahn models need the h distribution");
+    if (h->fp32) return upload_fp32(h, f, hd, aux);
     cudaError_t e;
     for (int q = 0; q < P.Q; ++q) {
         if ((e = to_dev(h, h->S.f + q * h->S.qs, f + q * n)) != cudaSuccess) return cuda_fail(h, e, "upload f");
@@ -241,6 +428,21 @@ extern "C" int dugks_gpu_step(dugks_handle_t *h, int nsteps, void *stream) {
         if (e != cudaSuccess) return cuda_fail(h, e, "stream switch");
         h->last_stream = st;
     }
+    if (h->fp32) {
+        for (int s = 0; s < nsteps; ++s) {
+            const uint32_t sn = (uint32_t)(h->steps + s);
+            cudaError_t e = h->fused64 ? f32::launch_stepX(h->P64f, h->S64f, h->first, h->gcur, h->gcur ^ 1, st,
+                                                           &h->launches, sn)
+                                       : f32::launch_stepX(h->P32, h->S32, h->first, h->gcur, h->gcur ^ 1, st,
+                                                           &h->launches, sn);
+            if (e != cudaSuccess) return cuda_fail(h, e, "fp32 step launch");
+            h->gcur ^= 1;
+            h->first = 0;
+        }
+        h->steps += nsteps;
+        if (nsteps) h->macros_fresh = false;
+        return DUGKS_OK;
+    }
     for (int s = 0; s < nsteps; ++s) {
         step_launcher(h)(h->P, h->S, h->pending, h->gcur, h->gcur ^ 1, st, &h->launches, nullptr);
         h->gcur ^= 1;
@@ -254,6 +456,27 @@ extern "C" int dugks_gpu_step(dugks_handle_t *h, int nsteps, void *stream) {
 
 extern "C" int dugks_gpu_step_profiled(dugks_handle_t *h, int nsteps, void *stream, double *ms, int *nph) {
     if (!h || !ms || !nph) return fail(h, DUGKS_EINVAL, "null argument");
+    if (h->fp32) {  // one fused kernel per step: phase 0 is the whole step
+        int rc0 = dugks_gpu_step(h, 0, stream);
+        if (rc0) return rc0;
+        cudaStream_t st0 = static_cast<cudaStream_t>(stream);
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, st0);
+        int rc = dugks_gpu_step(h, nsteps, stream);
+        cudaEventRecord(b, st0);
+        cudaError_t e = cudaEventSynchronize(b);
+        float t = 0;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, a, b);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        if (rc) return rc;
+        if (e != cudaSuccess) return cuda_fail(h, e, "profiled step");
+        ms[0] = t;
+        *nph = 1;
+        return DUGKS_OK;
+    }
     int rc = dugks_gpu_step(h, 0, stream);  // adopt the stream
     if (rc) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -294,6 +517,10 @@ static int finalize(dugks_handle *h) {
 extern "C" int dugks_gpu_reduce(dugks_handle_t *h, dugks_reductions_t *r) {
     if (!h || !r) return fail(h, DUGKS_EINVAL, "null argument");
     const bool hasH = (h->P.model == AC || h->P.model == HCZ);
+    if (h->fp32) {
+        int rc = macros_fp32(h);
+        if (rc) return rc;
+    }
     launch_reduce(h->P, h->S.fld[F_RHO], h->S.fld[F_PHI], h->rho_last, h->partial, h->nblocks, h->out4, hasH ? 1 : 0,
                   h->last_stream, &h->launches);
     double o[4];
@@ -314,6 +541,16 @@ static bool is_msrc_field(const Params &P, int f) {
 
 extern "C" int dugks_gpu_get_field(dugks_handle_t *h, int field, double *out) {
     if (!h || !out || field < 0 || field >= NFIELDS) return fail(h, DUGKS_EINVAL, "bad field or null pointer");
+    if (h->fp32) {
+        if (!(field == F_RHO || field == F_U || field == F_V || field == F_P || field == F_PHI))
+            return fail(h, DUGKS_EINVAL, "FP32 storage exposes rho, u, v, p and phi");
+        int rc = macros_fp32(h);
+        if (rc) return rc;
+        if ((rc = sync_last(h))) return rc;
+        cudaError_t e = to_host(h, out, h->S.fld[field]);
+        if (e != cudaSuccess) return cuda_fail(h, e, "download field");
+        return DUGKS_OK;
+    }
     if (is_msrc_field(h->P, field)) {
         int rc = finalize(h);
         if (rc) return rc;
@@ -327,6 +564,7 @@ extern "C" int dugks_gpu_get_field(dugks_handle_t *h, int field, double *out) {
 
 extern "C" int dugks_gpu_set_field(dugks_handle_t *h, int field, const double *in) {
     if (!h || !in || field < 0 || field >= NFIELDS) return fail(h, DUGKS_EINVAL, "bad field or null pointer");
+    if (h->fp32) return fail(h, DUGKS_EINVAL, "FP32 storage: set the state with dugks_gpu_upload");
     int rc = finalize(h);
     if (rc) return rc;
     if ((rc = sync_last(h))) return rc;
@@ -342,6 +580,22 @@ extern "C" int dugks_gpu_get_dist(dugks_handle_t *h, int which, double *out) {
     int rc = sync_last(h);
     if (rc) return rc;
     const size_t n = (size_t)h->P.nx * h->P.ny;
+    if (h->fp32) {
+        const size_t es = h->fused64 ? sizeof(double) : sizeof(float);
+        std::vector<unsigned char> tmp(n * es);
+        for (int q = 0; q < 9; ++q) {
+            const void *src = h->fused64 ? (const void *)((which ? h->S64f.dh : h->S64f.df) + q * h->S64f.qs)
+                                         : (const void *)((which ? h->S32.dh : h->S32.df) + q * h->S32.qs);
+            cudaError_t e = cudaMemcpy2D(tmp.data(), (size_t)h->P.nx * es, src, (size_t)h->P.pitch * es,
+                                         (size_t)h->P.nx * es, h->P.ny, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) return cuda_fail(h, e, "download distribution");
+            const double r0 = which ? h_rest(h->P, q) : f_rest(h->P, q);
+            for (size_t k = 0; k < n; ++k)
+                out[q * n + k] = r0 + (h->fused64 ? reinterpret_cast<const double *>(tmp.data())[k]
+                                                  : (double)reinterpret_cast<const float *>(tmp.data())[k]);
+        }
+        return DUGKS_OK;
+    }
     for (int q = 0; q < h->P.Q; ++q) {
         cudaError_t e = to_host(h, out + q * n, (which ? h->S.h : h->S.f) + q * h->S.qs);
         if (e != cudaSuccess) return cuda_fail(h, e, "download distribution");
@@ -367,9 +621,17 @@ extern "C" int dugks_gpu_check_finite(dugks_handle_t *h) {
     cudaStream_t st = h->last_stream;
     cudaMemsetAsync(h->flag, 0, sizeof(int), st);
     const bool hasH = (P.model == AC || P.model == HCZ);
-    launch_check_finite(h->S.f, (size_t)P.Q * h->S.qs, h->flag, st, &h->launches);
-    if (hasH) launch_check_finite(h->S.h, (size_t)P.Q * h->S.qs, h->flag, st, &h->launches);
-    launch_check_finite(h->S.fld[F_RHO], h->S.qs, h->flag, st, &h->launches);
+    if (h->fp32) {
+        int rc = macros_fp32(h);
+        if (rc) return rc;
+        const size_t qs = (size_t)P.pitch * P.ny;
+        const int fids[5] = {F_RHO, F_U, F_V, F_P, F_PHI};
+        for (int k : fids) launch_check_finite(h->S.fld[k], qs, h->flag, st, &h->launches);
+    } else {
+        launch_check_finite(h->S.f, (size_t)P.Q * h->S.qs, h->flag, st, &h->launches);
+        if (hasH) launch_check_finite(h->S.h, (size_t)P.Q * h->S.qs, h->flag, st, &h->launches);
+        launch_check_finite(h->S.fld[F_RHO], h->S.qs, h->flag, st, &h->launches);
+    }
     int flag = 0;
     cudaError_t e = cudaMemcpyAsync(&flag, h->flag, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);

@@ -1,0 +1,51 @@
+// Case constants and device state of the FP32 deviation-storage path.
+#pragma once
+#include <cstddef>
+
+// rest phase-field value the h deviations are taken from
+#ifndef DUGKS_F32_PHI0
+#define DUGKS_F32_PHI0 0.5
+#endif
+// |d phi/dx| below this is zero before grad(phi) is normalised (the reference's
+// SetZero, Ark/Cpp/GradScheme.cpp:374-375, uses 1e-14 in FP64)
+#ifndef DUGKS_F32_GCLAMP
+#define DUGKS_F32_GCLAMP 1.0e-14
+#endif
+
+namespace dugks {
+namespace f32 {
+
+// Case constants of the fused deviation-form step in the storage type R
+// (derived in FP64 on the host with the reference's expressions, then
+// rounded once).  R = float is the FP32 storage path; R = double runs the
+// same fused formulation in FP64.
+template <typename R>
+struct PR {
+    int nx, ny, pitch, walls, model, gravity;
+    R phi0, p0, aPhi, bPhi, Kp, RT, invRT, hDt, dt, Lambda0;
+    R Beta, Kappa, PhiL, PhiV, RhoL, Gy;
+    R inv_12dx, inv_12dy, inv_6dd, inv_wI_dphi, inv_RTdt;
+    R tauf, aBP_f, ah_f;                       // flow relaxation after the first step
+    R h_aBP, h_bBP, h_cBP, h_ah, h_bh, h_ch;  // phase-field relaxation
+    R r_2dy, r_ndx, r_n2dx, r_ndy;             // reconstruction multipliers
+    R aTP, bTP, dtV;
+};
+using P32 = PR<float>;
+
+// init planes (first step only): the macroscopic state an initialisation left
+enum { I_DPHI = 0, I_RHO, I_U, I_V, I_DP, I_TAU, I_SRCX, I_SRCY, I_RHOX, I_RHOY, I_FX, I_FY, I_N };
+// aux planes: previous MacroSource outputs read by the next step
+enum { A_FX = 0, A_FY, A_RHOX, A_RHOY, A_PPU, A_PPV, A_N };
+
+template <typename R>
+struct SR {
+    R *df, *dh;   // deviations [9][ny][pitch]
+    R *aux;       // [A_N][ny][pitch]
+    R *init;      // [I_N][ny][pitch]
+    R *gphi;      // ghost phi rows [2 buffers][bottom, top][pitch]
+    size_t qs;    // ny * pitch
+};
+using S32 = SR<float>;
+
+}  // namespace f32
+}  // namespace dugks
