@@ -1,24 +1,30 @@
 """Benchmark of the DUGKS time step on GB300.
 
-Workload (default): the Rayleigh-Taylor configuration -- 512x2048 cells,
-bounce-back walls top/bottom, periodic sides, D2Q9 HCZ flow + D2Q9
-Allen-Cahn phase field, Atwood 0.5, Re = 3000, gravity from the reduced
-time T = sqrt(L/(g At)), FP64 throughout.  One "step" is one DUGKS time
-step over all cells; the metric is cell updates per second (MLUPS).
+Workloads (--workload):
+  rt8192 (default)  large Allen-Cahn Rayleigh-Taylor: 8192x8192 cells, bounce-back
+                    walls top/bottom, periodic sides, D2Q9 HCZ flow + D2Q9 Allen-Cahn
+                    phase field, Atwood 0.5, Re = 10000, single-mode cosine interface
+                    at mid-height (amplitude 0.05 L) plus seeded 1e-4 white noise on
+                    phi; FP32 deviation storage, with the plain FP64 path timed on the
+                    same grid and the per-field FP32-vs-FP64 error reported
+  rt512x2048        Rayleigh-Taylor 512x2048 cells, Re = 3000, interface at y = 2L
+                    (amplitude 0.1 L); plain FP64 by default
+One "step" is one DUGKS time step over all cells; the metric is cell updates
+per second (MLUPS), with the fused step's HBM traffic against the measured peak.
 
 Arms:
   (default)          this library through its C ABI; state resident in HBM
   --impl reference   the CPU restatement of the reference solver (the
                      reference's own C++ cannot be built on the GPU machine),
-                     all host threads, a bounded number of steps
+                     all host threads, a bounded sample
 One JSON line is printed by rank 0.  Multi-GPU: one process per GPU, each a
 full independent replica of the workload (weak scaling, no collective).
 """
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
-import math
 import os
 import statistics
 import subprocess
@@ -30,16 +36,30 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-NX, NY = 512, 2048
-L = NX
 SQRT_GL = 0.04                  # sqrt(g L) in lattice units (low-Mach gravity wave speed)
-RE = 3000.0
-ATWOOD = 0.5
 RHO_H, RHO_L = 3.0, 1.0         # Atwood (3-1)/(3+1) = 0.5
-G = SQRT_GL ** 2 / L
-CASE_KW = dict(Mu0=SQRT_GL * L / RE, M_Phi=0.02, W=4.0, Sigma=5e-5, RhoL=RHO_H, RhoV=RHO_L, Gy=G)
-BYTES_PER_CELL_FP64 = 320       # (18 distributions + 2 aux) x 8 B x (read + write)
-WORKLOAD = 'rayleigh_taylor_512x2048_hcz_walls_fp64'
+
+WORKLOADS = {
+    'rt8192': dict(nx=8192, ny=8192, re=10000.0, init=[0.5, 0.05, 1e-4], precision='fp32dev',
+                   name='rayleigh_taylor_8192x8192_hcz_walls'),
+    'rt512x2048': dict(nx=512, ny=2048, re=3000.0, init=[], precision='fp64',
+                       name='rayleigh_taylor_512x2048_hcz_walls'),
+}
+
+# algorithmic HBM bytes per cell and step (state read once + written once)
+#   FP32 storage, HCZ: 18 deviations + 6 aux planes, 4 B each, read and written = 192 B
+#   FP64 (multi-kernel step): 18 distributions + 2 aux planes, 8 B, read and written = 320 B
+ALGO_BYTES = {'fp32dev': 192, 'fp64': 320, 'fp64fma': 320, 'fp64fused': 384}
+# DRAM bytes per cell and step of the fused FP32 kernel, ncu dram__bytes_read.sum +
+# dram__bytes_write.sum of one k_step32 launch on 2048x2048 / cells
+# (profiles/k_step32_rt2048_fp32.md)
+TRAFFIC_BYTES = {'fp32dev': None}
+
+
+def case_kw(wl: dict) -> dict:
+    L = wl['nx']
+    return dict(Mu0=SQRT_GL * L / wl['re'], M_Phi=0.02, W=4.0, Sigma=5e-5, RhoL=RHO_H, RhoV=RHO_L,
+                Gy=SQRT_GL ** 2 / L)
 
 
 def env_dist():
@@ -113,41 +133,90 @@ class ClockSampler:
                 'samples': len(sm)}
 
 
-def cpu_baseline_sample(steps: int, threads: int):
-    """The CPU restatement of the reference step on the same workload (bounded)."""
+# ---------------------------------------------------------------- CPU restatement
+
+CPU_SAMPLE = (512, 2048)  # cells of the bounded CPU sample (Rayleigh-Taylor, interface at y = 2L)
+
+
+def cpu_sample(wl: dict, steps: int, threads: int):
+    """The CPU restatement of the reference step on a bounded sample of the workload:
+    the same case constants on a 512x2048 Rayleigh-Taylor grid (the per-cell work of
+    the step does not depend on the grid size)."""
     from oracle.oracle import Oracle
-    o = Oracle('HCZ', NX, NY, True, 'ac_rt', **CASE_KW)
+    nx, ny = CPU_SAMPLE if wl['nx'] * wl['ny'] > CPU_SAMPLE[0] * CPU_SAMPLE[1] else (wl['nx'], wl['ny'])
+    o = Oracle('HCZ', nx, ny, True, 'ac_rt', **case_kw(wl))
     o.step(1, threads)  # first-touch / warm-up
     t0 = time.perf_counter()
     o.step(steps, threads)
     dt = time.perf_counter() - t0
-    return NX * NY * steps / dt / 1e6, dt
+    return nx * ny * steps / dt / 1e6, dt, (nx, ny)
 
 
-def run_reference(args, rank, world):
+def cpu_baseline(wl: dict, seconds: float, fixed_steps: int = 0):
+    thr = os.cpu_count() or 1
+    _, one, _ = cpu_sample(wl, 1, thr)
+    nsteps = fixed_steps or max(2, int(seconds / max(one, 1e-3)))
+    mlups, secs, (nx, ny) = cpu_sample(wl, nsteps, thr)
+    return {'value': round(mlups, 4), 'unit': 'MLUPS', 'cores': thr, 'kind': 'port',
+            'sample': f'{nsteps} steps of a {nx}x{ny} Rayleigh-Taylor grid with the case constants of '
+                      f'{wl["name"]} on the CPU restatement (OpenMP, {thr} threads, {secs:.1f} s)'}, nsteps, secs
+
+
+def run_reference(args, wl, rank, world):
     if rank != 0:
         return 0
-    threads = os.cpu_count() or 1
-    # bounded sample: as many of the K steps as fit in about a minute
-    _, one = cpu_baseline_sample(1, threads)
-    steps = max(1, min(args.steps, int(60.0 / max(one, 1e-3))))
-    mlups, secs = cpu_baseline_sample(steps, threads)
+    cpu, steps, secs = cpu_baseline(wl, 60.0, 0)
+    cpu['sample'] += ' [reference arm]'
     line = {
-        'impl': 'reference', 'metric': 'MLUPS', 'value': round(mlups, 4), 'unit': 'MLUPS', 'n_gpus': world,
+        'impl': 'reference', 'metric': 'MLUPS', 'value': cpu['value'], 'unit': 'MLUPS', 'n_gpus': world,
         'steps': steps, 'warmup': args.warmup, 'ms_per_step': round(1e3 * secs / steps, 4),
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
         'data': 'synthetic (seeded Rayleigh-Taylor initial condition, no dataset)',
-        'config': {'workload': WORKLOAD, 'cells': NX * NY, 'l2_flush': 'n/a (CPU)'},
-        'cpu_baseline': {'value': round(mlups, 4), 'unit': 'MLUPS', 'cores': threads, 'kind': 'port',
-                         'sample': f'{steps} full steps of the {NX}x{NY} workload on the CPU restatement '
-                                   f'(OpenMP, {threads} threads)'},
-        'e2e': {'value': round(mlups, 4), 'unit': 'MLUPS', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+        'config': {'workload': wl['name'], 'cells': wl['nx'] * wl['ny'], 'l2_flush': 'n/a (CPU)'},
+        'cpu_baseline': cpu,
+        'e2e': {'value': cpu['value'], 'unit': 'MLUPS', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
     }
     print(json.dumps(line), flush=True)
     return 0
 
 
-def run_ours(args, rank, world, local):
+# ---------------------------------------------------------------- GPU arms
+
+def field_errors(a, b):
+    """Per-field max-norm and L2 error of case a against case b, relative to b."""
+    import numpy as np
+    out = {}
+    for k in ('rho', 'u', 'v', 'p', 'phi'):
+        x, y = a.get(k), b.get(k)
+        d = x - y
+        ny = float(np.max(np.abs(y)))
+        out[k] = {'linf': float(np.max(np.abs(d))) / ny if ny else float(np.max(np.abs(d))),
+                  'l2': float(np.linalg.norm(d) / np.linalg.norm(y)) if ny else 0.0}
+    return out
+
+
+def timed_steps(gc, n: int, stream, clocks_idx=None):
+    """n steps on `stream` bracketed by CUDA events on that stream; (ms, launches, clocks)."""
+    import torch
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(clocks_idx) if clocks_idx is not None else None
+    if sampler:
+        sampler.__enter__()
+    l0 = gc.launches
+    ev0.record(stream)
+    gc.step(n, stream.cuda_stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = gc.launches - l0
+    if sampler:
+        sampler.__exit__(None, None, None)
+    return ev0.elapsed_time(ev1), launches, (sampler.summary() if sampler else None)
+
+
+def run_ours(args, wl, rank, world, local):
+    import numpy as np
     import torch
     import torch.distributed as dist
     from mpdugks_gb300 import capi
@@ -155,113 +224,133 @@ def run_ours(args, rank, world, local):
     torch.cuda.set_device(local)
     dev_index = torch.cuda.current_device()
     if world > 1:
-        dist.init_process_group('nccl' if torch.cuda.is_available() else 'gloo')
+        dist.init_process_group('nccl')
 
     def barrier():
         if world > 1:
             dist.barrier()
 
-    case = capi.make_case('HCZ', args.precision, **CASE_KW)
-    gc = capi.GpuCase(case, NX, NY, True)
-    gc.init('ac_rt')
+    def max_over_ranks(x: float) -> float:
+        t = torch.tensor([x], dtype=torch.float64, device='cuda')
+        if world > 1:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    nx, ny = wl['nx'], wl['ny']
+    cells = nx * ny
+    kw = case_kw(wl)
+    prec = args.precision or wl['precision']
     stream = torch.cuda.Stream()
-    sp = stream.cuda_stream
-    launches0 = gc.launches
-    # warm-up
-    gc.step(args.warmup, sp)
-    torch.cuda.synchronize()
-    # timed region: K steps, inputs resident (state > L2, no flush needed)
+
+    gc = capi.GpuCase(capi.make_case('HCZ', prec, **kw), nx, ny, True)
+    gc.init('ac_rt', wl['init'])
+    gc.step(args.warmup, stream.cuda_stream)
     barrier()
-    torch.cuda.synchronize()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    with ClockSampler(dev_index) as clk:
-        launches_before = gc.launches
-        with torch.cuda.stream(stream):
-            ev0.record(stream)
-            gc.step(args.steps, sp)
-            ev1.record(stream)
-        torch.cuda.synchronize()
-        launches_timed = gc.launches - launches_before
+    ms, launches, clocks = timed_steps(gc, args.steps, stream, dev_index)
     barrier()
-    ms = ev0.elapsed_time(ev1)
-    t = torch.tensor([ms], dtype=torch.float64, device='cuda')
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
-    cells = NX * NY
+    ms_max = max_over_ranks(ms)
     mlups_total = world * cells * args.steps / (ms_max * 1e-3) / 1e6
+    finite = gc.check_finite() == 0
+    red = gc.reduce()
 
-    # per-kernel device times of the same step (events between the launches)
-    phases = gc.step_profiled(max(20, min(200, args.steps)), sp)
-    nprof = max(20, min(200, args.steps))
-    ph_ms = [p / nprof for p in phases]
-    step_ms = sum(ph_ms)
-    names = ['k_collide', 'k_faces_ac', 'k_update']
-    dom = max(range(3), key=lambda k: ph_ms[k])
     hbm_peak, peak_kind = load_peaks()
-    achieved_step = BYTES_PER_CELL_FP64 * cells / (step_ms * 1e-3) / 1e9
+    step_ms = ms / args.steps
+    algo = ALGO_BYTES[prec]
+    achieved = algo * cells / (step_ms * 1e-3) / 1e9
+    if prec == 'fp32dev':
+        kernel = 'k_step32 (the fused step: one launch per step)'
+        phase = None
+    else:
+        nprof = max(10, min(100, args.steps))
+        ph = gc.step_profiled(nprof, stream.cuda_stream)
+        phase = [round(p / nprof, 5) for p in ph]
+        kernel = 'one DUGKS step (k_collide + k_faces_ac + k_update)'
+    traffic = TRAFFIC_BYTES.get(prec)
+    roofline = {'bound': 'hbm', 'achieved': round(achieved, 2), 'peak': hbm_peak, 'unit': 'GB/s',
+                'frac': round(achieved / hbm_peak, 5),
+                'traffic': None if traffic is None else int(traffic * cells),
+                'kernel': kernel, 'algorithmic_bytes_per_cell': algo,
+                'cells_per_launch': cells, 'peak_source': f'{peak_kind} hbm_gbs (copy bandwidth)'}
+    if phase:
+        roofline['phase_ms'] = phase
+        roofline['note'] = 'FP64 path: bound by the FP64 pipe (1.2 TFLOP/s on GB300), not HBM'
 
-    # end to end through the C ABI with host buffers: upload the state from
-    # pinned host memory, K steps, reductions and field download to the host
-    import numpy as np
-    f0 = gc.dist('f')
-    h0 = gc.dist('h')
-    aux0 = np.stack([gc.get(nm) for nm in capi.FIELDS])
-    pin = {k: torch.from_numpy(v).pin_memory() for k, v in (('f', f0), ('h', h0), ('aux', aux0))}
-    outs = {k: torch.empty((NY, NX), dtype=torch.float64).pin_memory() for k in ('rho', 'u', 'v', 'phi', 'p')}
+    # ---- the plain FP64 path on the same grid, and the FP32-vs-FP64 field errors
+    fp64 = None
+    gx = None
+    if prec == 'fp32dev' and not args.no_fp64:
+        g64 = capi.GpuCase(capi.make_case('HCZ', 'fp64', **kw), nx, ny, True)
+        g64.init('ac_rt', wl['init'])
+        g64.step(3, stream.cuda_stream)
+        k64 = args.fp64_steps
+        ms64, _, _ = timed_steps(g64, k64, stream)
+        n_cmp = 3 + k64
+        g32 = capi.GpuCase(capi.make_case('HCZ', 'fp32dev', **kw), nx, ny, True)
+        g32.init('ac_rt', wl['init'])
+        g32.step(n_cmp, stream.cuda_stream)
+        torch.cuda.synchronize()
+        errs = field_errors(g32, g64)
+        del g32
+        m64 = cells * k64 / (ms64 * 1e-3) / 1e6
+        fp64 = {'value': round(m64, 3), 'unit': 'MLUPS', 'steps': k64, 'ms_per_step': round(ms64 / k64, 4),
+                'precision': 'fp64 (reference-exact rounding)',
+                'fp32_speedup': round(mlups_total / world / m64, 2),
+                'fp32_error_vs_fp64': {'steps': n_cmp, 'fields': errs}}
+        gx = g64
+    # ---- end to end through the C ABI with host buffers: upload the FP64 initial
+    # state (the reference's CellArray contents) from pinned host memory, K steps,
+    # reductions, and the five macroscopic fields back to pinned host memory
+    src = gx
+    if src is None:
+        src = capi.GpuCase(capi.make_case('HCZ', 'fp64', **kw), nx, ny, True)
+    src.init('ac_rt', wl['init'])
+    pf = torch.empty((9, ny, nx), dtype=torch.float64).pin_memory()
+    ph_ = torch.empty((9, ny, nx), dtype=torch.float64).pin_memory()
+    pa = torch.empty((len(capi.FIELDS), ny, nx), dtype=torch.float64).pin_memory()
+    src._check(src.lib.dugks_gpu_get_dist(src.h, 0, pf.data_ptr()))
+    src._check(src.lib.dugks_gpu_get_dist(src.h, 1, ph_.data_ptr()))
+    for k in range(len(capi.FIELDS)):
+        src._check(src.lib.dugks_gpu_get_field(src.h, k, C.c_void_p(pa[k].data_ptr())))
+    del src, gx
+    outs = [torch.empty((ny, nx), dtype=torch.float64).pin_memory() for _ in range(5)]
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    gc.upload(pin['f'].numpy(), pin['h'].numpy(), pin['aux'].numpy())
-    gc.step(args.steps, sp)
-    red = gc.reduce()
-    ptrs = [outs[k].data_ptr() for k in ('rho', 'u', 'v', 'phi', 'p')]
-    gc._check(gc.lib.dugks_gpu_download(gc.h, *ptrs))
+    gc._check(gc.lib.dugks_gpu_upload(gc.h, pf.data_ptr(), ph_.data_ptr(), pa.data_ptr()))
+    gc.step(args.steps, stream.cuda_stream)
+    r2 = gc.reduce()
+    gc._check(gc.lib.dugks_gpu_download(gc.h, *[o.data_ptr() for o in outs]))
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    te = torch.tensor([e2e_s], dtype=torch.float64, device='cuda')
-    if world > 1:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_mlups = world * cells * args.steps / float(te.item()) / 1e6
-    h2d = sum(v.numel() * 8 for v in pin.values()) / args.steps
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_mlups = world * cells * args.steps / e2e_s / 1e6
+    h2d = (pf.numel() + ph_.numel() + pa.numel()) * 8 / args.steps
     d2h = (5 * cells * 8 + 32) / args.steps
-    finite = gc.check_finite() == 0
 
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
-            thr = os.cpu_count() or 1
-            _, one = cpu_baseline_sample(1, thr)
-            nsteps = args.cpu_steps or max(2, int(args.cpu_seconds / max(one, 1e-3)))
-            cmlups, csecs = cpu_baseline_sample(nsteps, thr)
-            cpu = {'value': round(cmlups, 4), 'unit': 'MLUPS', 'cores': thr, 'kind': 'port',
-                   'sample': f'{nsteps} steps of the {NX}x{NY} workload on the CPU restatement '
-                             f'(OpenMP, {thr} threads, {csecs:.1f} s)'}
-        clocks = clk.summary()
+            cpu, _, _ = cpu_baseline(wl, args.cpu_seconds, args.cpu_steps)
         line = {
             'metric': 'MLUPS', 'value': round(mlups_total, 3), 'unit': 'MLUPS', 'n_gpus': world,
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_max / args.steps, 5),
-            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f32 storage, f32 arithmetic, float-float/f64 moment sums' if prec == 'fp32dev' else 'f64',
             'data': 'synthetic (seeded Rayleigh-Taylor initial condition, no dataset)',
-            'config': {'workload': WORKLOAD, 'cells': cells, 'precision': args.precision,
-                       'l2_flush': 'none needed: resident state ~0.9 GB > 129 MB L2',
+            'config': {'workload': wl['name'], 'cells': cells, 'precision': prec,
+                       'l2_flush': 'none needed: the state read and written each step is larger than the 129 MB L2',
                        'parallelism': f'{world} independent replicas' if world > 1 else 'single GPU'},
-            'roofline': {'bound': 'hbm', 'achieved': round(achieved_step, 2), 'peak': hbm_peak, 'unit': 'GB/s',
-                         'frac': round(achieved_step / hbm_peak, 5), 'traffic': None,
-                         'kernel': 'one DUGKS step (k_collide + k_faces_ac + k_update)',
-                         'algorithmic_bytes_per_cell': BYTES_PER_CELL_FP64,
-                         'peak_source': f'{peak_kind} hbm_gbs',
-                         'dominant_kernel': names[dom], 'phase_ms': [round(x, 5) for x in ph_ms],
-                         'note': 'FP64 path: bound by the FP64 pipe, not HBM'},
+            'roofline': roofline,
+            'fp64_same_grid': fp64,
             'cpu_baseline': cpu,
             'e2e': {'value': round(e2e_mlups, 3), 'unit': 'MLUPS', 'h2d_bytes_per_step': int(h2d),
                     'd2h_bytes_per_step': int(d2h),
-                    'how': 'C ABI with pinned host buffers: upload full state, K steps, reduce, download 5 fields'},
-            'gpu_launches': int(launches_timed),
+                    'how': 'C ABI with pinned host buffers: upload the FP64 initial state, K steps, '
+                           'reductions, download 5 fields'},
+            'gpu_launches': int(launches),
             'clocks': clocks,
             'state_finite': finite,
             'sum_rho': red.sum_rho,
+            'sum_rho_e2e': r2.sum_rho,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -275,29 +364,40 @@ def main():
     ap.add_argument('--steps', type=int, default=1000)
     ap.add_argument('--warmup', type=int, default=20)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--workload', default='rt8192', choices=sorted(WORKLOADS))
+    ap.add_argument('--precision', default=None, choices=['fp32dev', 'fp64', 'fp64fma'],
+                    help='default: fp32dev for rt8192, fp64 (reference-exact rounding) for rt512x2048')
+    ap.add_argument('--fp64-steps', type=int, default=10, help='timed steps of the FP64 arm on the same grid')
+    ap.add_argument('--no-fp64', action='store_true', help='skip the FP64 arm on the same grid')
     ap.add_argument('--cpu-steps', type=int, default=0, help='CPU baseline steps (0: about --cpu-seconds)')
     ap.add_argument('--cpu-seconds', type=float, default=15.0)
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--profile-steps', type=int, default=0,
                     help='only run this many steps of the workload (for ncu) and exit')
-    ap.add_argument('--precision', default='fp64', choices=['fp64', 'fp64fma'],
-                    help='fp64: reference-exact rounding (default); fp64fma: FMA-contracted FP64')
+    ap.add_argument('--grid', default=None, help='NXxNY override of the grid (profiling runs only)')
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    wl = dict(WORKLOADS[args.workload])
     rank, world, local = env_dist()
     if args.profile_steps:
         # a short plain run of the workload for profilers (ncu); no timing, no JSON line
         from mpdugks_gb300 import capi
-        gc = capi.GpuCase(capi.make_case('HCZ', args.precision, **CASE_KW), NX, NY, True)
-        gc.init('ac_rt')
+        if args.grid:
+            wl['nx'], wl['ny'] = (int(x) for x in args.grid.lower().split('x'))
+        prec = args.precision or wl['precision']
+        gc = capi.GpuCase(capi.make_case('HCZ', prec, **case_kw(wl)), wl['nx'], wl['ny'], True)
+        gc.init('ac_rt', wl['init'])
         gc.step(args.profile_steps)
         r = gc.reduce()
-        print(f'profile run: {args.profile_steps} steps, precision {args.precision}, sum rho {r.sum_rho!r}')
+        print(f'profile run: {wl["nx"]}x{wl["ny"]}, {args.profile_steps} steps, precision {prec}, '
+              f'sum rho {r.sum_rho!r}')
         return 0
+    if args.grid:
+        ap.error('--grid is for --profile-steps runs only')
     if args.impl == 'reference':
-        return run_reference(args, rank, world)
-    return run_ours(args, rank, world, local)
+        return run_reference(args, wl, rank, world)
+    return run_ours(args, wl, rank, world, local)
 
 
 if __name__ == '__main__':

@@ -115,8 +115,10 @@ int dugks_gpu_upload(dugks_handle_t *h, const double *f, const double *hdist, co
  * interface y = Lx(2 + 0.1 cos(2 pi x/Lx)) (heavy above), 3 SCMP_Drop
  * (Ark/Cpp/Preprocess.cpp:337-401), 4 seeded density noise
  * rho = p0 (1 + p1 U(-1,1)) with a 64-bit LCG.  params: kind 0/1: radius
- * (<0: 0.36 ChLength); kind 3: rho_l, rho_v, radius (<0: 0.25 ChLength);
- * kind 4: rho0, amplitude; seed used by kind 4. */
+ * (<0: 0.36 ChLength); kind 2: interface height and cosine amplitude in
+ * units of nx (default 2, 0.1) and white-noise amplitude on phi (default 0);
+ * kind 3: rho_l, rho_v, radius (<0: 0.25 ChLength); kind 4: rho0, amplitude;
+ * seed used by kinds 2 (noise) and 4. */
 int dugks_gpu_init(dugks_handle_t *h, int kind, const double *params, int nparams, uint64_t seed);
 
 /* Advance nsteps time steps on `stream` (a cudaStream_t, NULL = default). */

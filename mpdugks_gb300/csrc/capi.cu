@@ -40,6 +40,9 @@ cudaError_t launch_step64f(const PR<double> &P, const SR<double> &S, int first, 
                            cudaStream_t st, int64_t *launches, uint32_t step);
 void launch_macros64f(const PR<double> &P, const SR<double> &S, double *rho, double *u, double *v, double *p,
                       double *phi, int opitch, cudaStream_t st, int64_t *launches);
+template <typename R>
+cudaError_t launch_plane_from_f64(R *dst, int dpitch, const double *src, int nx, int ny, double sub,
+                                  cudaStream_t st, int64_t *launches);
 inline cudaError_t launch_stepX(const P32 &P, const S32 &S, int a, int b, int c, cudaStream_t st, int64_t *l,
                                 uint32_t step) {
     return launch_step32(P, S, a, b, c, st, l, step);
@@ -161,7 +164,7 @@ static int create_fused(dugks_handle *h, dugks_handle_t **out, f32::PR<R> &PQ, f
     const size_t rowd = (size_t)P.pitch * sizeof(double);
     const size_t celld = align256(rowd * P.ny);
     h->nblocks = 152 * 4;
-    size_t total = 18 * cellf + f32::A_N * cellf + f32::I_N * cellf + align256(4 * rowf) +
+    size_t total = 2 * (18 + f32::A_N) * cellf + f32::I_N * cellf + align256(4 * rowf) +
                    6 * celld /* rho u v p phi + rho_last */ + align256(sizeof(double) * 4 * h->nblocks) + 512;
     cudaError_t e = cudaMalloc(&h->arena, total);
     if (e != cudaSuccess) {
@@ -178,6 +181,9 @@ static int create_fused(dugks_handle *h, dugks_handle_t **out, f32::PR<R> &PQ, f
     S.df = takef(9 * cellf);
     S.dh = takef(9 * cellf);
     S.aux = takef(f32::A_N * cellf);
+    S.odf = takef(9 * cellf);
+    S.odh = takef(9 * cellf);
+    S.oaux = takef(f32::A_N * cellf);
     S.init = takef(f32::I_N * cellf);
     S.gphi = takef(align256(4 * rowf));
     const int fids[5] = {F_RHO, F_U, F_V, F_P, F_PHI};
@@ -204,41 +210,40 @@ static int create_fp32(dugks_handle *h, dugks_handle_t **out) {
     return create_fused<float>(h, out, h->P32, h->S32);
 }
 
-// FP64 [Q][ny][nx] state -> deviations and first-step planes on the device
+// FP64 [Q][ny][nx] state -> deviations and first-step planes on the device.
+// Each FP64 plane is copied as-is into a device staging plane (one of the
+// FP64 output fields, which an upload invalidates anyway) and converted there.
 template <typename R>
 static int upload_fused(dugks_handle *h, f32::SR<R> &S, const double *f, const double *hd, const double *aux) {
     const Params &P = h->P;
     const int nx = P.nx, ny = P.ny;
     const size_t n = (size_t)nx * ny;
-    std::vector<R> tmp(n);
-    auto put = [&](R *dst) {
-        return cudaMemcpy2D(dst, (size_t)P.pitch * sizeof(R), tmp.data(), (size_t)nx * sizeof(R),
-                            (size_t)nx * sizeof(R), ny, cudaMemcpyHostToDevice);
-    };
+    cudaStream_t st = h->last_stream;
+    double *stage = h->S.fld[F_RHO];
     cudaError_t e;
+    auto put = [&](R *dst, const double *src, double sub) -> cudaError_t {
+        cudaError_t r = cudaMemcpyAsync(stage, src, n * sizeof(double), cudaMemcpyHostToDevice, st);
+        if (r != cudaSuccess) return r;
+        return f32::launch_plane_from_f64<R>(dst, P.pitch, stage, nx, ny, sub, st, &h->launches);
+    };
     for (int q = 0; q < 9; ++q) {
-        const double f0 = f_rest(P, q), h0 = h_rest(P, q);
-        for (size_t k = 0; k < n; ++k) tmp[k] = (R)(f[q * n + k] - f0);
-        if ((e = put(S.df + q * S.qs)) != cudaSuccess) return cuda_fail(h, e, "upload f");
-        for (size_t k = 0; k < n; ++k) tmp[k] = (R)(hd[q * n + k] - h0);
-        if ((e = put(S.dh + q * S.qs)) != cudaSuccess) return cuda_fail(h, e, "upload h");
+        if ((e = put(S.df + q * S.qs, f + q * n, f_rest(P, q))) != cudaSuccess) return cuda_fail(h, e, "upload f");
+        if ((e = put(S.dh + q * S.qs, hd + q * n, h_rest(P, q))) != cudaSuccess) return cuda_fail(h, e, "upload h");
     }
     const int src[f32::I_N] = {F_PHI, F_RHO, F_U, F_V, F_P, F_TAU, F_PHIX, F_PHIY, F_RHOX, F_RHOY, F_FX, F_FY};
     for (int k = 0; k < f32::I_N; ++k) {
-        const double *a = aux + (size_t)src[k] * n;
         const double sub = k == f32::I_DPHI ? DUGKS_F32_PHI0 : (k == f32::I_DP ? 1.0 : 0.0);
-        for (size_t m = 0; m < n; ++m) tmp[m] = (R)(a[m] - sub);
-        if ((e = put(S.init + k * S.qs)) != cudaSuccess) return cuda_fail(h, e, "upload init");
+        if ((e = put(S.init + k * S.qs, aux + (size_t)src[k] * n, sub)) != cudaSuccess)
+            return cuda_fail(h, e, "upload init");
     }
     // previous MacroSource outputs as the first step's successor will read them
     const int asrc[f32::A_N] = {F_FX, F_FY, F_RHOX, F_RHOY, F_PPU, F_PPV};
-    for (int k = 0; k < f32::A_N; ++k) {
-        const double *a = aux + (size_t)asrc[k] * n;
-        for (size_t m = 0; m < n; ++m) tmp[m] = (R)a[m];
-        if ((e = put(S.aux + k * S.qs)) != cudaSuccess) return cuda_fail(h, e, "upload aux");
-    }
-    cudaMemset(h->rho_last, 0, (size_t)P.pitch * ny * sizeof(double));
-    e = cudaDeviceSynchronize();
+    for (int k = 0; k < f32::A_N; ++k)
+        if ((e = put(S.aux + k * S.qs, aux + (size_t)asrc[k] * n, 0.0)) != cudaSuccess)
+            return cuda_fail(h, e, "upload aux");
+    if ((e = cudaMemsetAsync(h->rho_last, 0, (size_t)P.pitch * ny * sizeof(double), st)) != cudaSuccess)
+        return cuda_fail(h, e, "upload");
+    e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(h, e, "upload");
     h->first = 1;
     h->gcur = 0;
@@ -436,6 +441,8 @@ extern "C" int dugks_gpu_step(dugks_handle_t *h, int nsteps, void *stream) {
                                        : f32::launch_stepX(h->P32, h->S32, h->first, h->gcur, h->gcur ^ 1, st,
                                                            &h->launches, sn);
             if (e != cudaSuccess) return cuda_fail(h, e, "fp32 step launch");
+            if (h->fused64) f32::swap_io(h->S64f);
+            else f32::swap_io(h->S32);
             h->gcur ^= 1;
             h->first = 0;
         }

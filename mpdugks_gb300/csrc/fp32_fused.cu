@@ -20,6 +20,8 @@
 // threads then apply the finite-volume update and write their deviations.
 // Cells in two tiles' halos are computed by both with the same operation
 // order, so shared faces carry bit-identical fluxes and mass is conserved.
+// A step reads one copy of the state and writes the other (tiles read their
+// neighbours' cells as halo, so an in-place update would race across waves).
 //
 // Phase references: P1 Ark/Cpp/DUGKS2DSolver.cpp:175-183 (Ark/Lib/D2Q9HCZ.cpp:54-92,
 // Ark/Lib/D2Q9AC.cpp:69-105); P4 :219-250 (CD_Interior_phi_Bh :604-687);
@@ -62,12 +64,7 @@ __device__ __forceinline__ R sym8(const R *a) {
 }
 __device__ __forceinline__ float rsq(float x) { return rsqrtf(x); }
 
-// Stochastic rounding of a + b to the storage type.  The exact sum is
-// s + err (two-sum); s is moved to its neighbour toward err with probability
-// |err| / ulp.  Without it, a state that is nearly steady repeats the same
-// FP32 rounding every step and the error grows linearly with the step count;
-// with it the rounding errors are unbiased and uncorrelated (random-walk
-// growth).  key: a per (cell, velocity, step) counter hashed to 24 bits.
+// 32-bit integer hash (per cell and step random bits for stochastic rounding)
 __device__ __forceinline__ uint32_t mix32(uint32_t x) {
     x ^= x >> 16;
     x *= 0x7feb352dU;
@@ -76,20 +73,6 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
     x ^= x >> 16;
     return x;
 }
-__device__ __forceinline__ float add_sr(float a, float b, uint32_t key) {
-    const float s = a + b;
-#if defined(DUGKS_F32_NO_SR)
-    return s;
-#endif
-    const float bb = s - a;
-    const float err = (a - (s - bb)) + (b - bb);
-    if (err == 0.f) return s;
-    const float nb = nextafterf(s, err > 0.f ? INFINITY : -INFINITY);
-    const float ulp = fabsf(nb - s);
-    const float u = (float)(mix32(key) >> 8) * (1.0f / 16777216.0f);
-    return (u * ulp < fabsf(err)) ? nb : s;
-}
-__device__ __forceinline__ double add_sr(double a, double b, uint32_t) { return a + b; }
 __device__ __forceinline__ double rsq(double x) { return 1.0 / sqrt(x); }
 __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
@@ -159,62 +142,250 @@ __device__ __forceinline__ void macro_source32(const PR<R> &P, const R (*sphi)[B
     }
 }
 
-constexpr size_t SMEM_ELEMS = (size_t)(BY + 2) * (BX + 2) + (18 + 6 + 18) * BY * BX;
+// ---- packed pairs: every per-direction quantity of the step is carried as the
+// pair (flow f_q, phase field h_q); for R = float the pair arithmetic is the
+// sm_100+ packed FP32x2 instructions (one issue slot for two lanes' worth).
+template <typename R> struct Pair;
+template <> struct Pair<float> { using T = float2; };
+template <> struct Pair<double> { using T = double2; };
 
+__device__ __forceinline__ float2 mk2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ double2 mk2(double a, double b) { return make_double2(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ double2 add2(double2 a, double2 b) { return make_double2(__dadd_rn(a.x, b.x), __dadd_rn(a.y, b.y)); }
+__device__ __forceinline__ double2 sub2(double2 a, double2 b) { return make_double2(__dsub_rn(a.x, b.x), __dsub_rn(a.y, b.y)); }
+__device__ __forceinline__ double2 mul2(double2 a, double2 b) { return make_double2(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)); }
+__device__ __forceinline__ double2 fma2(double2 a, double2 b, double2 c) {
+    return make_double2(__fma_rn(a.x, b.x, c.x), __fma_rn(a.y, b.y, c.y));
+}
+template <typename T> __device__ __forceinline__ T neg2(T a) { return mk2(-a.x, -a.y); }
+// x * s for a compile-time sign s in {-1, 0, 1}
+template <int S, typename T> __device__ __forceinline__ T sgn2(T a) { return S > 0 ? a : (S < 0 ? neg2(a) : mk2(decltype(a.x)(0), decltype(a.x)(0))); }
+
+// Knuth two-sum accumulation of pairs
+template <typename T>
+struct FF2 {
+    T hi, lo;
+    __device__ __forceinline__ void init(T b) { hi = b; lo = mk2(decltype(b.x)(0), decltype(b.x)(0)); }
+    __device__ __forceinline__ void add(T b) {
+        const T s = add2(hi, b);
+        const T bb = sub2(s, hi);
+        const T err = add2(sub2(hi, sub2(s, bb)), sub2(b, bb));
+        hi = s;
+        lo = add2(lo, err);
+    }
+    __device__ __forceinline__ T value() const { return add2(hi, lo); }
+};
+
+// mirror-symmetric sum of directions 1..8 (see sym8)
+template <typename T>
+__device__ __forceinline__ T sym8p(const T *a) {
+    return add2(add2(add2(a[1], a[5]), add2(a[3], a[7])), add2(add2(a[2], a[6]), add2(a[4], a[8])));
+}
+
+// Stochastic rounding of the pair a + b into storage.  The exact sum is
+// s + err (two-sum); each lane moves to its neighbour toward err with
+// probability |err| / spacing, drawn from 16 random bits.  Without it a state
+// that is nearly steady repeats the same FP32 rounding every step and the
+// error grows linearly with the step count; with it the rounding errors are
+// unbiased and uncorrelated (random-walk growth).
+__device__ __forceinline__ float sr_lane(float s, float err, uint32_t bits16) {
+    if (err == 0.f) return s;
+    // neighbour of s toward err (s != 0 here: a + b == 0 is exact)
+    const int away = ((err > 0.f) == (s > 0.f)) ? 1 : -1;
+    const float nb = __int_as_float(__float_as_int(s) + away);
+    const float u = __int_as_float(0x3F800000u | (bits16 << 7)) - 1.0f;  // [0, 1)
+    return (u * fabsf(nb - s) < fabsf(err)) ? nb : s;
+}
+__device__ __forceinline__ float2 add_sr2(float2 a, float2 b, uint32_t bits) {
+    const float2 s = add2(a, b);
+    const float2 bb = sub2(s, a);
+    const float2 err = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+    return make_float2(sr_lane(s.x, err.x, bits & 0xFFFFu), sr_lane(s.y, err.y, bits >> 16));
+}
+__device__ __forceinline__ double2 add_sr2(double2 a, double2 b, uint32_t) { return add2(a, b); }
+
+__device__ __forceinline__ float rcp(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
+
+// direction slots of the faces: the six directions with a non-zero normal velocity
+__host__ __device__ constexpr int xslot(int q) { return q == 1 ? 0 : q == 2 ? 1 : q == 4 ? 2 : q == 5 ? 3 : q == 6 ? 4 : q == 8 ? 5 : -1; }
+__host__ __device__ constexpr int yslot(int q) { return q == 2 ? 0 : q == 3 ? 1 : q == 4 ? 2 : q == 6 ? 3 : q == 7 ? 4 : q == 8 ? 5 : -1; }
+
+// Equilibrium deviations and the force terms of direction q != 0, as pairs
+// (f, h): Eq = w (dp + rho RT G, dphi + u1 phi) (HCZ) or w (dp/RT, dphi) (AC);
+// So = (w ((1+G)(c.F) + G RT (c.grad rho)), w (xi.src)) with c = xi - u.
+template <int MODEL, int Q, typename R>
+__device__ __forceinline__ void eq_src(const PR<R> &P, R U, R V, R uu, R rho, R phi, R dp, R dphi, R fx, R fy,
+                                       R rx, R ry, R sx_, R sy_, typename Pair<R>::T &Eq,
+                                       typename Pair<R>::T &So) {
+    constexpr int xu = d2q9_xu(Q), xv = d2q9_xv(Q);
+    const R wq = (R)d2q9_w(Q);
+    const R hS = wq * (sxf(xu, sx_) + sxf(xv, sy_));
+    if (MODEL == AC) {
+        Eq = mk2(wq * (dp * P.invRT), wq * dphi);
+        So = mk2(wq * ((sxf(xu, fx) + sxf(xv, fy)) * P.invRT), hS);
+    } else {
+        const R u1 = (sxf(xu, U) + sxf(xv, V)) * P.invRT;
+        const R G = u1 + R(0.5) * u1 * u1 - uu * P.Lambda0;
+        const R cu = (R)xu - U, cv = (R)xv - V;
+        Eq = mul2(mk2(wq, wq), fma2(mk2(rho * P.RT, phi), mk2(G, u1), mk2(dp, dphi)));
+        So = mk2(wq * ((R(1.) + G) * (cu * fx + cv * fy) + G * P.RT * (cu * rx + cv * ry)), hS);
+    }
+}
+
+constexpr size_t SMEM_ELEMS = (size_t)(BY + 2) * (BX + 2) + (18 + 6 + 12) * BY * BX;
+// Prefetch staging (storage type float only): the next tile's own-cell planes
+// (9 f, 9 h, 6 aux) and the h planes of its phi ring, copied asynchronously
+// (cp.async) while the current tile computes.
+constexpr int RING_MAX = 2 * (TW + 4) + 2 * (TH + 2);  // ring cells of a full tile
+constexpr size_t STG_ELEMS = (size_t)24 * BY * BX + 9 * RING_MAX;
+template <typename R>
+constexpr bool prefetched() { return sizeof(R) == 4; }
+template <typename R>
+constexpr size_t smem_elems() { return SMEM_ELEMS + (prefetched<R>() ? STG_ELEMS : 0); }
+
+template <typename R>
+__device__ __forceinline__ void cp_async(R *smem, const R *gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    if (sizeof(R) == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Geometry of tile t as seen by thread (e, r): the tile's interior origin and
+// size, and this thread's extended cell (interior plus a one-cell ring).
+template <bool WALLS>
+struct TileCell {
+    int x0, y0, w, hh, gi, gj;
+    bool act, ghost, real;
+    size_t c;
+    __device__ __forceinline__ TileCell(int t, int ntx, int e, int r, int nx, int ny, int pitch) {
+        x0 = (t % ntx) * TW;
+        y0 = (t / ntx) * TH;
+        w = min(TW, nx - x0);
+        hh = min(TH, ny - y0);
+        act = (e <= w + 1) && (r <= hh + 1);
+        gi = wrapi(x0 + e - 1, nx);
+        gj = y0 + r - 1;
+        ghost = false;  // wall ghost row (values extrapolated in shared memory)
+        if (WALLS) {
+            if (gj < 0 || gj >= ny) ghost = true;
+        } else {
+            gj = wrapi(gj, ny);
+        }
+        real = act && !ghost;
+        c = real ? (size_t)gj * pitch + gi : 0;
+    }
+    // ring of the phi region (halo 2): index k in [0, nring) -> (re, rr) in
+    // tile coordinates, e in {-1, w+2} or r in {-1, hh+2}
+    __device__ __forceinline__ int nring() const { return 2 * (w + 4) + 2 * (hh + 2); }
+    __device__ __forceinline__ void ring(int k, int &re, int &rr) const {
+        const int RW = w + 4;
+        if (k < RW) { re = k - 1; rr = -1; }
+        else if (k < 2 * RW) { re = k - RW - 1; rr = hh + 2; }
+        else if (k < 2 * RW + hh + 2) { re = -1; rr = k - 2 * RW; }
+        else { re = w + 2; rr = k - 2 * RW - (hh + 2); }
+    }
+};
+
+// Issue the asynchronous copies of tile t's inputs into the staging area.
+template <int MODEL, bool WALLS>
+__device__ __forceinline__ void prefetch_tile(const PR<float> &P, const SR<float> &S, int t, int ntx, int e, int r,
+                                              int tid, float *stg, float *stg_ring) {
+    const TileCell<WALLS> g(t, ntx, e, r, P.nx, P.ny, P.pitch);
+    if (g.real) {
+        float *d = stg + r * BX + e;
+        constexpr int BS = BY * BX;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            cp_async(d + q * BS, S.df + (size_t)q * S.qs + g.c);
+            cp_async(d + (9 + q) * BS, S.dh + (size_t)q * S.qs + g.c);
+        }
+        if (MODEL != AC) {
+#pragma unroll
+            for (int k = 0; k < A_N; ++k) cp_async(d + (18 + k) * BS, S.aux + (size_t)k * S.qs + g.c);
+        }
+    }
+    const int nr = g.nring();
+    for (int k = tid; k < nr; k += BX * BY) {
+        int re, rr;
+        g.ring(k, re, rr);
+        int rj = g.y0 + rr - 1;
+        if (WALLS && (rj < 0 || rj >= P.ny)) continue;  // ghost phi or unused
+        if (!WALLS) rj = wrapi(rj, P.ny);
+        const size_t cc = (size_t)rj * P.pitch + wrapi(g.x0 + re - 1, P.nx);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) cp_async(stg_ring + q * RING_MAX + k, S.dh + (size_t)q * S.qs + cc);
+    }
+    cp_async_commit();
+}
+
+// Persistent kernel: each CTA (one per SM) walks the tiles t = blockIdx.x,
+// blockIdx.x + gridDim.x, ...; tile t + gridDim.x's inputs are in flight while
+// tile t computes.
 template <int MODEL, bool WALLS, typename R>
 __global__ void __launch_bounds__(BX *BY, 1) k_step32(PR<R> P, SR<R> S, int first, int gin, int gout,
-                                                      uint32_t step) {
+                                                      uint32_t step, int ntx, int ntiles) {
+    using T = typename Pair<R>::T;
+    constexpr bool PF = prefetched<R>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R *smem = reinterpret_cast<R *>(smem_raw);
-    R(*sphi)[BX + 2] = reinterpret_cast<R(*)[BX + 2]>(smem);                             // phi, halo 2
-    R(*sB)[BY][BX] = reinterpret_cast<R(*)[BY][BX]>(smem + (BY + 2) * (BX + 2));        // f-bar-plus (f 0..8, h 9..17)
-    R(*sA)[BY][BX] = sB + 18;                                                             // srcx srcy rhox rhoy fx fy
-    R(*sFS)[BY][BX] = sA + 6;                                                             // south-face fluxes
+    T(*sB)[BY][BX] = reinterpret_cast<T(*)[BY][BX]>(smem);                              // f-bar-plus pairs
+    T(*sFS)[BY][BX] = sB + 9;                                                             // south-face flux pairs (6 slots)
+    R(*sA)[BY][BX] = reinterpret_cast<R(*)[BY][BX]>(sFS + 6);                             // srcx srcy rhox rhoy fx fy
+    R(*sphi)[BX + 2] = reinterpret_cast<R(*)[BX + 2]>(smem + (18 + 12 + 6) * BY * BX);  // phi, halo 2
+    R *stg = smem + SMEM_ELEMS;                                                           // [24][BY][BX] (PF)
+    R *stg_ring = stg + 24 * BY * BX;                                                     // [9][RING_MAX] (PF)
     const int e = threadIdx.x, r = threadIdx.y;
     const int tid = r * BX + e;
     const int nx = P.nx, ny = P.ny, pitch = P.pitch;
-    const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
-    const int w = min(TW, nx - x0), hh = min(TH, ny - y0);
-    // extended cell of this thread
-    const bool act = (e <= w + 1) && (r <= hh + 1);
-    int gi = wrapi(x0 + e - 1, nx);
-    int gj = y0 + r - 1;
-    bool ghost = false;  // wall ghost row (values extrapolated in shared memory)
-    if (WALLS) {
-        if (gj < 0 || gj >= ny) ghost = true;
-    } else {
-        gj = wrapi(gj, ny);
+    if constexpr (PF) {
+        if ((int)blockIdx.x < ntiles) prefetch_tile<MODEL, WALLS>(P, S, blockIdx.x, ntx, e, r, tid, stg, stg_ring);
     }
-    const bool real = act && !ghost;
-    const size_t c = real ? (size_t)gj * pitch + gi : 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const TileCell<WALLS> g(t, ntx, e, r, nx, ny, pitch);
+    const int x0 = g.x0, y0 = g.y0, w = g.w, hh = g.hh, gi = g.gi, gj = g.gj;
+    const bool act = g.act, ghost = g.ghost, real = g.real;
+    const size_t c = g.c;
+    if constexpr (PF) cp_async_wait_all();
+    __syncthreads();  // staged inputs visible; the previous tile is done with shared memory
 
-    // ---- stage 0: own deviations, phi of the halo-2 region
-    R df[9], dh[9];
-    R dphi = R(0.);
+    // ---- stage 0: own deviations (f, h pairs), phi of the halo-2 region
+    T Pq[9];
+    R dphi = R(0.), sfz = R(0.);
     if (real) {
+        if constexpr (PF) {
 #pragma unroll
-        for (int q = 0; q < 9; ++q) {
-            df[q] = S.df[(size_t)q * S.qs + c];
-            dh[q] = S.dh[(size_t)q * S.qs + c];
+            for (int q = 0; q < 9; ++q) Pq[q] = mk2(stg[(q * BY + r) * BX + e], stg[((9 + q) * BY + r) * BX + e]);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 9; ++q) Pq[q] = mk2(S.df[(size_t)q * S.qs + c], S.dh[(size_t)q * S.qs + c]);
         }
-        FFs<R> sh;
+        // (sum f, sum h) as a float-float pair; the Allen-Cahn pressure omits f_0
+        FF2<T> s0;
+        s0.init(mk2(MODEL == AC ? R(0.) : Pq[0].x, Pq[0].y));
 #pragma unroll
-        for (int q = 0; q < 9; ++q) sh.add(dh[q]);
-        dphi = sh.value();
+        for (int q = 1; q < 9; ++q) s0.add(Pq[q]);
+        const T z = s0.value();
+        sfz = z.x;
+        dphi = z.y;
         sphi[r + 1][e + 1] = P.phi0 + dphi;
     } else if (act && WALLS) {
         // ghost phi: the previous step's extrapolation (Ark/Cpp/Boundary.cpp:38-63)
         sphi[r + 1][e + 1] = S.gphi[(size_t)(gin * 2 + (gj < 0 ? 0 : 1)) * pitch + gi];
     }
-    {   // ring of the phi region: e in {-1, w+2} or r in {-1, hh+2}
-        const int RW = w + 4, RH = hh + 4;  // ring spans e in [-1, w+2], r in [-1, hh+2]
-        const int nring = 2 * RW + 2 * (RH - 2);
-        for (int k = tid; k < nring; k += BX * BY) {
+    {   // ring of the phi region
+        const int nr = g.nring();
+        for (int k = tid; k < nr; k += BX * BY) {
             int re, rr;
-            if (k < RW) { re = k - 1; rr = -1; }
-            else if (k < 2 * RW) { re = k - RW - 1; rr = hh + 2; }
-            else if (k < 2 * RW + (RH - 2)) { re = -1; rr = k - 2 * RW; }
-            else { re = w + 2; rr = k - 2 * RW - (RH - 2); }
+            g.ring(k, re, rr);
             const int ri = wrapi(x0 + re - 1, nx);
             int rj = y0 + rr - 1;
             R v = R(0.);
@@ -227,7 +398,7 @@ __global__ void __launch_bounds__(BX *BY, 1) k_step32(PR<R> P, SR<R> S, int firs
                 const size_t cc = (size_t)rj * pitch + ri;
                 FFs<R> sh;
 #pragma unroll
-                for (int q = 0; q < 9; ++q) sh.add(S.dh[(size_t)q * S.qs + cc]);
+                for (int q = 0; q < 9; ++q) sh.add(PF ? stg_ring[q * RING_MAX + k] : S.dh[(size_t)q * S.qs + cc]);
                 v = P.phi0 + sh.value();
             }
             sphi[rr + 1][re + 1] = v;
@@ -238,10 +409,9 @@ __global__ void __launch_bounds__(BX *BY, 1) k_step32(PR<R> P, SR<R> S, int firs
     // ---- stage 1: macros, MacroSource, f-bar-plus of every real cell of the region
     R phi = P.phi0 + dphi, rho = R(0.), U = R(0.), V = R(0.), dp = R(0.);
     R srcx = R(0.), srcy = R(0.), rhox = R(0.), rhoy = R(0.), fx = R(0.), fy = R(0.);
-    R aBP = R(0.), bBP = R(0.), cBP = R(0.);
-    R rxo_c = R(0.), ryo_c = R(0.);  // previous density gradient (HCZ pressure)
-    R inc[18];  // collision increments B - T of this cell
+    T inc[9];  // collision increments B - T of this cell
     if (real) {
+        R aBP, cBP, rxo = R(0.), ryo = R(0.);
         if (first) {
             // first step after an initialisation: the reference uses the state the
             // initialisation left (p0, zero forces, tau from Mu0), as uploaded
@@ -260,91 +430,80 @@ __global__ void __launch_bounds__(BX *BY, 1) k_step32(PR<R> P, SR<R> S, int firs
             fy = I[I_FY * ps + c];
             const R tau = I[I_TAU * ps + c];
             aBP = (R(2.) * tau - P.hDt) / (R(2.) * tau + P.dt);
+            cBP = tau * (R(1.) - aBP);
         } else {
-            R fxo = R(0.), fyo = R(0.), rxo = R(0.), ryo = R(0.), ppu = R(0.), ppv = R(0.);
-            if (MODEL != AC) {
-                fxo = S.aux[A_FX * S.qs + c];
-                fyo = S.aux[A_FY * S.qs + c];
-                rxo = S.aux[A_RHOX * S.qs + c];
-                ryo = S.aux[A_RHOY * S.qs + c];
-                ppu = S.aux[A_PPU * S.qs + c];
-                ppv = S.aux[A_PPV * S.qs + c];
+            rho = P.aPhi * phi + P.bPhi;
+            R ppu = R(0.), ppv = R(0.);
+            if (MODEL == AC) {
+                dp = sfz * P.Kp;
+            } else {
+                R a6[A_N];
+#pragma unroll
+                for (int k = 0; k < A_N; ++k)
+                    a6[k] = PF ? stg[((18 + k) * BY + r) * BX + e] : S.aux[(size_t)k * S.qs + c];
+                const R fxo = a6[A_FX], fyo = a6[A_FY];
+                rxo = a6[A_RHOX];
+                ryo = a6[A_RHOY];
+                ppu = a6[A_PPU];
+                ppv = a6[A_PPV];
+                // first moments as a float-float pair (sum xi_x f, sum xi_y f)
+                FF2<T> m;
+                m.init(mk2(Pq[1].x, R(0.)));
+                m.add(mk2(Pq[2].x, Pq[2].x));
+                m.add(mk2(R(0.), Pq[3].x));
+                m.add(mk2(-Pq[4].x, Pq[4].x));
+                m.add(mk2(-Pq[5].x, R(0.)));
+                m.add(mk2(-Pq[6].x, -Pq[6].x));
+                m.add(mk2(R(0.), -Pq[7].x));
+                m.add(mk2(Pq[8].x, -Pq[8].x));
+                const T mv = m.value();
+                const R inv = rcp(rho * P.RT);
+                U = mv.x * inv + P.hDt * fxo * inv;
+                V = mv.y * inv + P.hDt * fyo * inv;
+                dp = sfz + P.hDt * (rxo * U + ryo * V) * P.RT;
             }
-            R d;
-            cell_macros<MODEL>(P, df, dh, fxo, fyo, rxo, ryo, d, rho, U, V, dp);
-            rxo_c = rxo;
-            ryo_c = ryo;
             macro_source32(P, sphi, r, e, phi, rho, U, V, ppu, ppv, srcx, srcy, rhox, rhoy, fx, fy);
             aBP = P.aBP_f;  // tau is constant after the first step (nu_L = nu_V)
+            cBP = P.tauf * (R(1.) - aBP);
         }
-        bBP = R(1.) - aBP;
-        // f-bar-plus deviations
+        const R bBP = R(1.) - aBP;
         const R uu = U * U + V * V;
         // dphi itself, not (phi0 + dphi) - phi0: one rounding less in the zeroth moment
         const R dphi_c = first ? phi - P.phi0 : dphi;
-        if (first) {
-            // tau = Mu0 / (rho RT) of the initialisation
-            const R tau = S.init[I_TAU * S.qs + c];
-            cBP = tau * bBP;
-        } else {
-            cBP = P.tauf * bBP;
-        }
         // equilibria of q != 0; q = 0 from the exact zeroth moment (sum dEq = dp for
         // HCZ, 0 for AC; sum dhEq = dphi), so FP32 weights cannot leak mass
-        R dEqv[9], fSov[9], dhEqv[9];
-        R sEq, shEq;
-#pragma unroll
-        for (int q = 1; q < 9; ++q) {
-            const int xu = d2q9_xu(q), xv = d2q9_xv(q);
-            const R wq = (R)d2q9_w(q);
-            if (MODEL == AC) {
-                dEqv[q] = wq * dp * P.invRT;
-                fSov[q] = wq * ((sxf(xu, fx) + sxf(xv, fy)) * P.invRT);
-                dhEqv[q] = wq * dphi_c;
-            } else {
-                const R u1 = (sxf(xu, U) + sxf(xv, V)) * P.invRT;
-                const R G = u1 + R(0.5) * u1 * u1 - uu * P.Lambda0;
-                const R cu = (R)xu - U, cv = (R)xv - V;
-                dEqv[q] = wq * (dp + rho * G * P.RT);
-                fSov[q] = wq * ((R(1.) + G) * (cu * fx + cv * fy) + G * P.RT * (cu * rhox + cv * rhoy));
-                dhEqv[q] = wq * (dphi_c + u1 * phi);
-            }
-        }
-        sEq = sym8(dEqv);
-        shEq = sym8(dhEqv);
-        dEqv[0] = (MODEL == AC ? R(0.) : dp) - sEq;
-        dhEqv[0] = dphi_c - shEq;
+        T Eq[9], So[9];
+        eq_src<MODEL, 1>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[1], So[1]);
+        eq_src<MODEL, 2>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[2], So[2]);
+        eq_src<MODEL, 3>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[3], So[3]);
+        eq_src<MODEL, 4>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[4], So[4]);
+        eq_src<MODEL, 5>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[5], So[5]);
+        eq_src<MODEL, 6>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[6], So[6]);
+        eq_src<MODEL, 7>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[7], So[7]);
+        eq_src<MODEL, 8>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[8], So[8]);
+        const T sEq = sym8p(Eq);
+        Eq[0] = sub2(mk2(MODEL == AC ? R(0.) : dp, dphi_c), sEq);
         if (MODEL == AC) {
-            fSov[0] = R(0.);
+            So[0] = mk2(R(0.), R(0.));
         } else {
             const R G0 = -uu * P.Lambda0;
             const R wq = (R)d2q9_w(0);
-            fSov[0] = wq * ((R(1.) + G0) * (-U * fx - V * fy) + G0 * P.RT * (-U * rhox - V * rhoy));
+            So[0] = mk2(wq * ((R(1.) + G0) * (-U * fx - V * fy) + G0 * P.RT * (-U * rhox - V * rhoy)), R(0.));
         }
+        // collision increment B - T = (1-a)(Eq - T) + c S: small near equilibrium,
+        // so B = T + increment keeps the rest state and rounds relative to the increment
+        const T b2 = mk2(bBP, P.h_bBP), c2 = mk2(cBP, P.h_cBP);
 #pragma unroll
-        for (int q = 0; q < 9; ++q) {
-            const int xu = d2q9_xu(q), xv = d2q9_xv(q);
-            const R wq = (R)d2q9_w(q);
-            const R hSo = (sxf(xu, srcx) + sxf(xv, srcy)) * wq;
-            // collision increment B - T = (1-a)(Eq - T) + c S: small near equilibrium,
-            // so B = T + increment keeps the rest state and rounds relative to the increment
-            inc[q] = bBP * (dEqv[q] - df[q]) + cBP * fSov[q];
-            inc[9 + q] = P.h_bBP * (dhEqv[q] - dh[q]) + P.h_cBP * hSo;
-        }
-        // the phase-field collision conserves sum_q h exactly (sum Eq = phi, sum S = 0):
-        // the rest direction takes the exact negative of the others' increments
-        inc[9] = -sym8(inc + 9);
-        if (MODEL == HCZ) {
-            // zeroth moment of the flow collision: (1-a)(p - sum f) + c sum S
-            //   = (1-a) hDt RT (grad rho_old . u) + c RT (u . grad rho)
-            inc[0] = (bBP * P.hDt * P.RT * (rxo_c * U + ryo_c * V) + cBP * P.RT * (U * rhox + V * rhoy)) -
-                     sym8(inc);
-        }
+        for (int q = 0; q < 9; ++q) inc[q] = fma2(b2, sub2(Eq[q], Pq[q]), mul2(c2, So[q]));
+        // the rest directions take the exact zeroth moments of the collision:
+        // phase field sum_q h is conserved (sum Eq = phi, sum S = 0); HCZ flow
+        //   (1-a)(p - sum f) + c sum S = (1-a) hDt RT (grad rho_old . u) + c RT (u . grad rho)
+        const T sInc = sym8p(inc);
+        const R z0 = MODEL == HCZ ? (bBP * P.hDt * P.RT * (rxo * U + ryo * V) + cBP * P.RT * (U * rhox + V * rhoy)) - sInc.x
+                                  : inc[0].x;
+        inc[0] = mk2(z0, -sInc.y);
 #pragma unroll
-        for (int q = 0; q < 9; ++q) {
-            sB[q][r][e] = df[q] + inc[q];
-            sB[9 + q][r][e] = dh[q] + inc[9 + q];
-        }
+        for (int q = 0; q < 9; ++q) sB[q][r][e] = add2(Pq[q], inc[q]);
         sA[0][r][e] = srcx;
         sA[1][r][e] = srcy;
         sA[2][r][e] = rhox;
@@ -357,8 +516,9 @@ __global__ void __launch_bounds__(BX *BY, 1) k_step32(PR<R> P, SR<R> S, int firs
         // P2: ghost rows of f-bar-plus and of the averaged fields (2 a0 - a1)
         if (act && ghost) {
             const int r0 = gj < 0 ? r + 1 : r - 1, r1 = gj < 0 ? r + 2 : r - 2;
+            const T two = mk2(R(2.), R(2.));
 #pragma unroll
-            for (int k = 0; k < 18; ++k) sB[k][r][e] = R(2.) * sB[k][r0][e] - sB[k][r1][e];
+            for (int q = 0; q < 9; ++q) sB[q][r][e] = sub2(mul2(two, sB[q][r0][e]), sB[q][r1][e]);
 #pragma unroll
             for (int k = 0; k < 6; ++k) sA[k][r][e] = R(2.) * sA[k][r0][e] - sA[k][r1][e];
         }
@@ -369,11 +529,16 @@ __global__ void __launch_bounds__(BX *BY, 1) k_step32(PR<R> P, SR<R> S, int firs
         }
     }
     __syncthreads();
+    if constexpr (PF) {  // every read of the staged inputs of tile t is done
+        if (t + (int)gridDim.x < ntiles)
+            prefetch_tile<MODEL, WALLS>(P, S, t + gridDim.x, ntx, e, r, tid, stg, stg_ring);
+    }
 
     // ---- stage 2: west x-face and south y-face of this thread's cell
-    R FW[18], FSo[18];
+    T FW[6], FSo[6];
     const bool do_x = act && e >= 1 && r >= 1 && r <= hh;           // faces x0-1|x0 .. x0+w-1|x0+w
     const bool do_y = act && r >= 1 && e >= 1 && e <= w;            // faces below rows 0..hh (hh+1 with the top)
+    const T half = mk2(R(0.5), R(0.5));
 #pragma unroll
     for (int pass = 0; pass < 2; ++pass) {
         const bool xf = pass == 0;
@@ -384,137 +549,134 @@ __global__ void __launch_bounds__(BX *BY, 1) k_step32(PR<R> P, SR<R> S, int firs
         R av[6];
 #pragma unroll
         for (int k = 0; k < 6; ++k) av[k] = R(0.5) * (sA[k][ro][eo] + sA[k][r][e]);
-        R bh[18];
+        // half-step reconstruction at the face midpoint: CD average minus hDt xi.grad
+        T bh[9];
+        const T hdt = mk2(P.hDt, P.hDt);
 #pragma unroll
-        for (int k = 0; k < 18; ++k) {
-            const int q = k % 9;
-            const R xu = (R)d2q9_xu(q), xv = (R)d2q9_xv(q);
-            const R o = sB[k][ro][eo], n = sB[k][r][e];
-            R gx, gy;
-            if (xf) {
-                gy = (R(0.5) * ((sB[k][r + 1][e] - sB[k][r - 1][e]) + (sB[k][r + 1][e - 1] - sB[k][r - 1][e - 1]))) * P.r_2dy;
-                gx = (o - n) * P.r_ndx;
-            } else {
-                gx = (R(0.5) * ((sB[k][r][e - 1] - sB[k][r][e + 1]) + (sB[k][r - 1][e - 1] - sB[k][r - 1][e + 1]))) * P.r_n2dx;
-                gy = (o - n) * P.r_ndy;
+        for (int q = 0; q < 9; ++q) {
+            const int xu = d2q9_xu(q), xv = d2q9_xv(q);
+            const T o = sB[q][ro][eo], n = sB[q][r][e];
+            const T avg = mul2(half, add2(o, n));
+            const int sn = xf ? xu : xv, st = xf ? xv : xu;  // normal / tangential velocity
+            if (sn == 0 && st == 0) {
+                bh[q] = avg;
+                continue;
             }
-            bh[k] = R(0.5) * (o + n) - P.hDt * (gx * xu + gy * xv);
+            // xi.grad as the sum of the normal part (o - n)/(-d) and the tangential
+            // central difference averaged over the two cells of the face
+            T g = mk2(R(0.), R(0.));
+            bool have = false;
+            if (sn != 0) {
+                const R rn = xf ? P.r_ndx : P.r_ndy;
+                g = mul2(sub2(o, n), mk2(sn * rn, sn * rn));
+                have = true;
+            }
+            if (st != 0) {
+                T d;
+                R rt;
+                if (xf) {
+                    d = add2(sub2(sB[q][r + 1][e], sB[q][r - 1][e]), sub2(sB[q][r + 1][e - 1], sB[q][r - 1][e - 1]));
+                    rt = P.r_2dy;
+                } else {
+                    d = add2(sub2(sB[q][r][e - 1], sB[q][r][e + 1]), sub2(sB[q][r - 1][e - 1], sB[q][r - 1][e + 1]));
+                    rt = P.r_n2dx;
+                }
+                const R k = R(0.5) * (R)st * rt;
+                g = have ? fma2(d, mk2(k, k), g) : mul2(d, mk2(k, k));
+            }
+            bh[q] = sub2(avg, mul2(hdt, g));
         }
-        // face moments
-        // symmetric pairwise sums (0, E,NE,N,NW,W,SW,S,SE = 0..8)
-        const R dphif = bh[9] + sym8(bh + 9);
-        const R sf = (MODEL == AC ? R(0.) : bh[0]) + sym8(bh);
-        const R su = (bh[1] - bh[5]) + ((bh[2] - bh[6]) + (bh[8] - bh[4]));
-        const R sv = (bh[3] - bh[7]) + ((bh[2] - bh[6]) + (bh[4] - bh[8]));
+        // face moments (sum f, sum h) with the mirror-symmetric association
+        const T z = add2(mk2(MODEL == AC ? R(0.) : bh[0].x, bh[0].y), sym8p(bh));
+        const R sf = z.x, dphif = z.y;
+        const R su = (bh[1].x - bh[5].x) + ((bh[2].x - bh[6].x) + (bh[8].x - bh[4].x));
+        const R sv = (bh[3].x - bh[7].x) + ((bh[2].x - bh[6].x) + (bh[4].x - bh[8].x));
         const R phif = P.phi0 + dphif;
         const R rhof = P.aPhi * phif + P.bPhi;
-        R Uf, Vf, dpf, ah, bh_, ch;
+        R Uf, Vf, dpf;
         if (MODEL == AC) {
             Uf = R(0.);
             Vf = R(0.);
             dpf = sf * P.Kp;
-            ah = P.ah_f;
         } else {
-            const R inv = R(1.) / (rhof * P.RT);
+            const R inv = rcp(rhof * P.RT);
             Uf = su * inv + R(0.5) * P.hDt * av[4] * inv;
             Vf = sv * inv + R(0.5) * P.hDt * av[5] * inv;
             dpf = sf + R(0.5) * P.hDt * P.RT * (av[2] * Uf + av[3] * Vf);
-            ah = P.ah_f;
         }
-        bh_ = R(1.) - ah;
-        ch = P.tauf * bh_;
         const R uu = Uf * Uf + Vf * Vf;
-        R out[18];
-        R dEqv[9], fSov[9], dhEqv[9];
-        R sEq, shEq;
-#pragma unroll
-        for (int q = 1; q < 9; ++q) {
-            const int xu = d2q9_xu(q), xv = d2q9_xv(q);
-            const R wq = (R)d2q9_w(q);
-            if (MODEL == AC) {
-                dEqv[q] = wq * dpf * P.invRT;
-                fSov[q] = wq * ((sxf(xu, av[4]) + sxf(xv, av[5])) * P.invRT);
-                dhEqv[q] = wq * dphif;
-            } else {
-                const R u1 = (sxf(xu, Uf) + sxf(xv, Vf)) * P.invRT;
-                const R G = u1 + R(0.5) * u1 * u1 - uu * P.Lambda0;
-                const R cu = (R)xu - Uf, cv = (R)xv - Vf;
-                dEqv[q] = wq * (dpf + rhof * P.RT * G);
-                fSov[q] = wq * ((R(1.) + G) * (cu * av[4] + cv * av[5]) + G * P.RT * (cu * av[2] + cv * av[3]));
-                dhEqv[q] = wq * (dphif + u1 * phif);
-            }
+        const T a2 = mk2(P.ah_f, P.h_ah), c2 = mk2(P.tauf * (R(1.) - P.ah_f), P.h_ch);
+        // face distributions of the six directions crossing the face:
+        // Eq + a (bh - Eq) + c S
+        T out[9];
+#define DUGKS_FACE_Q(Q)                                                                                   \
+        if ((xf ? d2q9_xu(Q) : d2q9_xv(Q)) != 0) {                                                        \
+            T Eq, So;                                                                                     \
+            eq_src<MODEL, Q>(P, Uf, Vf, uu, rhof, phif, dpf, dphif, av[4], av[5], av[2], av[3], av[0],    \
+                             av[1], Eq, So);                                                              \
+            out[Q] = fma2(c2, So, fma2(a2, sub2(bh[Q], Eq), Eq));                                         \
         }
-        sEq = sym8(dEqv);
-        shEq = sym8(dhEqv);
-        dEqv[0] = (MODEL == AC ? R(0.) : dpf) - sEq;
-        dhEqv[0] = dphif - shEq;
-        if (MODEL == AC) {
-            fSov[0] = R(0.);
-        } else {
-            const R G0 = -uu * P.Lambda0;
-            const R wq = (R)d2q9_w(0);
-            fSov[0] = wq * ((R(1.) + G0) * (-Uf * av[4] - Vf * av[5]) + G0 * P.RT * (-Uf * av[2] - Vf * av[3]));
-        }
-#pragma unroll
-        for (int q = 0; q < 9; ++q) {
-            const int xu = d2q9_xu(q), xv = d2q9_xv(q);
-            const R wq = (R)d2q9_w(q);
-            const R hSo = (sxf(xu, av[0]) + sxf(xv, av[1])) * wq;
-            out[9 + q] = dhEqv[q] + P.h_ah * (bh[9 + q] - dhEqv[q]) + P.h_ch * hSo;
-            out[q] = dEqv[q] + ah * (bh[q] - dEqv[q]) + ch * fSov[q];
-        }
+        DUGKS_FACE_Q(1) DUGKS_FACE_Q(2) DUGKS_FACE_Q(3) DUGKS_FACE_Q(4)
+        DUGKS_FACE_Q(5) DUGKS_FACE_Q(6) DUGKS_FACE_Q(7) DUGKS_FACE_Q(8)
+#undef DUGKS_FACE_Q
         if (WALLS && !xf && (gj == 0 || gj == ny)) {
             // bounce-back of the directions entering the fluid (Ark/Cpp/Boundary.cpp:118-139)
             const bool bottom = gj == 0;
 #pragma unroll
-            for (int q = 0; q < 9; ++q) {
+            for (int q = 1; q < 9; ++q) {
                 const int xv = d2q9_xv(q);
-                if (bottom ? xv > 0 : xv < 0) {
-                    out[q] = out[d2q9_bb(q)];
-                    out[9 + q] = out[9 + d2q9_bb(q)];
-                }
+                if (xv != 0 && (bottom ? xv > 0 : xv < 0)) out[q] = out[d2q9_bb(q)];
             }
         }
+        // fluxes xi.n (f, h) of the six directions
 #pragma unroll
-        for (int k = 0; k < 18; ++k) {
-            const int q = k % 9;
-            const R v = sxf(xf ? d2q9_xu(q) : d2q9_xv(q), out[k]);
-            if (xf) FW[k] = v;
-            else FSo[k] = v;
+        for (int q = 1; q < 9; ++q) {
+            if (xf && d2q9_xu(q) != 0) FW[xslot(q)] = d2q9_xu(q) > 0 ? out[q] : neg2(out[q]);
+            if (!xf && d2q9_xv(q) != 0) FSo[yslot(q)] = d2q9_xv(q) > 0 ? out[q] : neg2(out[q]);
         }
     }
     if (do_y) {
 #pragma unroll
-        for (int k = 0; k < 18; ++k) sFS[k][r][e] = FSo[k];
+        for (int s = 0; s < 6; ++s) sFS[s][r][e] = FSo[s];
     }
     // east face = west face of the next lane
-    R FE[18];
+    T FE[6];
 #pragma unroll
-    for (int k = 0; k < 18; ++k) FE[k] = __shfl_down_sync(0xffffffffu, do_x ? FW[k] : R(0.), 1);
+    for (int s = 0; s < 6; ++s) {
+        const T v = do_x ? FW[s] : mk2(R(0.), R(0.));
+        FE[s] = mk2(__shfl_down_sync(0xffffffffu, v.x, 1), __shfl_down_sync(0xffffffffu, v.y, 1));
+    }
     __syncthreads();
 
     // ---- stage 3: finite-volume update of the interior cells (Update_phi_T) + aux
     if (real && e >= 1 && e <= w && r >= 1 && r <= hh) {
+        const uint32_t h0 = mix32((uint32_t)c * 0x9E3779B1U ^ step * 0x85EBCA77U);
+        const T btp = mk2(P.bTP, P.bTP), dtv = mk2(P.dtV, P.dtV);
 #pragma unroll
-        for (int k = 0; k < 18; ++k) {
-            // net flux with mirror-symmetric association
-            const R s = (FW[k] - FE[k]) + (FSo[k] - sFS[k][r + 1][e]);
-            const R dold = k < 9 ? df[k] : dh[k - 9];
+        for (int q = 0; q < 9; ++q) {
+            // net flux (W - E) + (S - N) with the mirror-symmetric association
+            T s = mk2(R(0.), R(0.));
+            const int xs = xslot(q), ys = yslot(q);
+            if (xs >= 0 && ys >= 0) s = add2(sub2(FW[xs], FE[xs]), sub2(FSo[ys], sFS[ys][r + 1][e]));
+            else if (xs >= 0) s = sub2(FW[xs], FE[xs]);
+            else if (ys >= 0) s = sub2(FSo[ys], sFS[ys][r + 1][e]);
             // 4/3 B - 1/3 T = T + (4/3)(B - T): old value plus one small increment,
             // rounded stochastically into storage
-            const uint32_t key = (uint32_t)(c * 18 + k) * 0x9E3779B1U ^ (uint32_t)step * 0x85EBCA77U;
-            const R dn = add_sr(dold, (inc[k] + P.bTP * inc[k]) + P.dtV * s, key);
-            R *dst = k < 9 ? S.df : S.dh;
-            dst[(size_t)(k % 9) * S.qs + c] = dn;
+            const T incr = (xs >= 0 || ys >= 0) ? fma2(dtv, s, fma2(btp, inc[q], inc[q])) : fma2(btp, inc[q], inc[q]);
+            const T dn = add_sr2(Pq[q], incr, h0 * (2u * q + 1u) + (uint32_t)q * 0x632BE5ABU);
+            S.odf[(size_t)q * S.qs + c] = dn.x;
+            S.odh[(size_t)q * S.qs + c] = dn.y;
         }
-        if (MODEL == AC) return;  // u = 0: the next step needs no previous force, gradient or phi*u
-        S.aux[A_FX * S.qs + c] = fx;
-        S.aux[A_FY * S.qs + c] = fy;
-        S.aux[A_RHOX * S.qs + c] = rhox;
-        S.aux[A_RHOY * S.qs + c] = rhoy;
-        S.aux[A_PPU * S.qs + c] = phi * U;
-        S.aux[A_PPV * S.qs + c] = phi * V;
+        if (MODEL != AC) {  // AC: u = 0, the next step needs no previous force, gradient or phi*u
+            S.oaux[A_FX * S.qs + c] = fx;
+            S.oaux[A_FY * S.qs + c] = fy;
+            S.oaux[A_RHOX * S.qs + c] = rhox;
+            S.oaux[A_RHOY * S.qs + c] = rhoy;
+            S.oaux[A_PPU * S.qs + c] = phi * U;
+            S.oaux[A_PPV * S.qs + c] = phi * V;
+        }
     }
+    }  // tiles
 }
 
 // Macroscopic fields of the FP32 state as FP64 arrays: the quantities the
@@ -545,10 +707,33 @@ __global__ void __launch_bounds__(256) k_macros32(PR<R> P, SR<R> S, double *rho_
     phi_o[o] = (double)P.phi0 + (double)dphi;
 }
 
+// One FP64 plane (dense [ny][nx], as the C ABI passes it) to the storage type,
+// minus a rest value: dst[j][i] = (R)(src[j][i] - sub)
+template <typename R>
+__global__ void __launch_bounds__(256) k_plane_from_f64(R *dst, int dpitch, const double *__restrict__ src, int nx,
+                                                        int ny, double sub) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= nx || j >= ny) return;
+    dst[(size_t)j * dpitch + i] = (R)(src[(size_t)j * nx + i] - sub);
+}
+
+template <typename R>
+cudaError_t launch_plane_from_f64(R *dst, int dpitch, const double *src, int nx, int ny, double sub,
+                                  cudaStream_t st, int64_t *launches) {
+    const dim3 grd((nx + 255) / 256, ny);
+    k_plane_from_f64<R><<<grd, 256, 0, st>>>(dst, dpitch, src, nx, ny, sub);
+    *launches += 1;
+    return cudaGetLastError();
+}
+template cudaError_t launch_plane_from_f64<float>(float *, int, const double *, int, int, double, cudaStream_t,
+                                                  int64_t *);
+template cudaError_t launch_plane_from_f64<double>(double *, int, const double *, int, int, double, cudaStream_t,
+                                                   int64_t *);
+
 template <int MODEL, bool WALLS, typename R>
 static cudaError_t launch_t(const PR<R> &P, const SR<R> &S, int first, int gin, int gout, cudaStream_t st,
                             uint32_t step) {
-    const size_t bytes = SMEM_ELEMS * sizeof(R);
+    const size_t bytes = smem_elems<R>() * sizeof(R);
     static bool attr_set = false;  // per instantiation; idempotent, set before the first launch
     if (!attr_set) {
         cudaError_t e = cudaFuncSetAttribute(k_step32<MODEL, WALLS, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -556,9 +741,16 @@ static cudaError_t launch_t(const PR<R> &P, const SR<R> &S, int first, int gin, 
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
+    static int nsm = 0;  // SMs of the device (one persistent CTA each)
+    if (!nsm) {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+    }
+    const int ntx = (P.nx + TW - 1) / TW, nty = (P.ny + TH - 1) / TH, ntiles = ntx * nty;
     const dim3 blk(BX, BY);
-    const dim3 grd((P.nx + TW - 1) / TW, (P.ny + TH - 1) / TH);
-    k_step32<MODEL, WALLS, R><<<grd, blk, bytes, st>>>(P, S, first, gin, gout, step);
+    k_step32<MODEL, WALLS, R><<<min(ntiles, nsm), blk, bytes, st>>>(P, S, first, gin, gout, step, ntx, ntiles);
     return cudaGetLastError();
 }
 

@@ -39,13 +39,22 @@ enum { A_FX = 0, A_FY, A_RHOX, A_RHOY, A_PPU, A_PPV, A_N };
 
 template <typename R>
 struct SR {
-    R *df, *dh;   // deviations [9][ny][pitch]
+    R *df, *dh;   // deviations [9][ny][pitch]: the state a step reads
     R *aux;       // [A_N][ny][pitch]
+    R *odf, *odh, *oaux;  // the state a step writes (swapped with the above after each step)
     R *init;      // [I_N][ny][pitch]
     R *gphi;      // ghost phi rows [2 buffers][bottom, top][pitch]
     size_t qs;    // ny * pitch
 };
 using S32 = SR<float>;
+
+// after a step the written state becomes the one the next step reads
+template <typename R>
+inline void swap_io(SR<R> &S) {
+    R *t = S.df; S.df = S.odf; S.odf = t;
+    t = S.dh; S.dh = S.odh; S.odh = t;
+    t = S.aux; S.aux = S.oaux; S.oaux = t;
+}
 
 }  // namespace f32
 }  // namespace dugks

@@ -198,6 +198,16 @@ int host_init_state(const Params &P, const double iM[16][16], int kind, const do
         h.assign((size_t)Q * n, 0.0);
         const double centerX = 0.5 * ChLength, centerY = 0.5 * ChLength;
         const double radius = (nparams >= 1 && params && params[0] >= 0) ? params[0] : 0.36 * ChLength;
+        // Rayleigh-Taylor interface y = Lx (yc + amp cos(2 pi x / Lx)); optional params
+        // {yc, amp, noise}: mean height and amplitude in units of Lx (default 2, 0.1), and
+        // the amplitude of seeded uniform white noise added to phi (default 0)
+        double rt_yc = 2.0, rt_amp = 0.1, rt_noise = 0.0;
+        if (kind == 2 && params) {
+            if (nparams >= 1) rt_yc = params[0];
+            if (nparams >= 2) rt_amp = params[1];
+            if (nparams >= 3) rt_noise = params[2];
+        }
+        uint64_t rng = seed;
         // Mu0 of the reference header, not Tau0*RT: the first step's tau is Mu0/(Rho*RT)
         const double mu0 = P.NuL * Rho0;  // NuL = Nu0 = Mu0/Rho0
         for (int j = 0; j < ny; ++j)
@@ -212,8 +222,13 @@ int host_init_state(const Params &P, const double iM[16][16], int kind, const do
                     const double r = std::sqrt((x - centerX) * (x - centerX) + (y - centerY) * (y - centerY));
                     Phi = 0.5 * (P.PhiL + P.PhiV) + 0.5 * (P.PhiL - P.PhiV) * std::tanh((radius - r) * 2 / P.wI);
                 } else {
-                    const double yi = Lx * (2.0 + 0.1 * std::cos(2.0 * 3.141592653589793 * x / Lx));
+                    const double yi = Lx * (rt_yc + rt_amp * std::cos(2.0 * 3.141592653589793 * x / Lx));
                     Phi = 0.5 * (P.PhiL + P.PhiV) + 0.5 * (P.PhiL - P.PhiV) * std::tanh((y - yi) * 2 / P.wI);
+                    if (rt_noise != 0.0) {
+                        rng = rng * 6364136223846793005ULL + 1442695040888963407ULL;  // 64-bit LCG (Knuth MMIX)
+                        const double u01 = (double)(rng >> 11) * (1.0 / 9007199254740992.0);
+                        Phi += rt_noise * (2.0 * u01 - 1.0);
+                    }
                 }
                 const double Rho = P.aPhi * (Phi) + P.bPhi;
                 A(F_PHI, j, i) = Phi;
