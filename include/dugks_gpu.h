@@ -172,6 +172,70 @@ int dugks_gpu_destroy(dugks_handle_t *h);
 int dugks_gpu_step_noalloc(const dugks_case_t *c, const dugks_grid_t *g, double *d_f, double *d_h,
                            double *d_aux, int nsteps, void *stream);
 
+/* ---- Serving: a request loop that solves many cases on one GPU.
+ *
+ * No reference counterpart (the reference solves one case per process,
+ * Ark/Cpp/main.cpp:134).  Cases are admitted first-in first-out while their
+ * device footprint fits the byte budget; each case's state stays resident
+ * until it finishes.  FP32-storage Allen-Cahn cases (AC, HCZ) run together:
+ * every chunk of `chunk_steps` steps is one captured CUDA graph of persistent
+ * launches over a table of (case, tile) entries, so cases that arrive while
+ * others run join at the next chunk and finished cases leave.  Other cases
+ * (FP64, pseudopotential) run one at a time on a second stream, overlapping
+ * the batched work.  A case's result does not depend on the other cases
+ * (bit-identical alone and in a mix). */
+typedef struct dugks_srv dugks_srv_t;
+
+typedef struct dugks_srv_config {
+    size_t max_bytes;  /* device bytes for resident cases; 0: 85% of the free memory */
+    int chunk_steps;   /* steps per captured graph launch; 0: 64 */
+    int reserved[6];
+} dugks_srv_config_t;
+
+typedef enum dugks_srv_state {
+    DUGKS_SRV_QUEUED = 0,
+    DUGKS_SRV_RUNNING = 1,
+    DUGKS_SRV_DONE = 2,
+    DUGKS_SRV_CANCELLED = 3,
+    DUGKS_SRV_FAILED = 4
+} dugks_srv_state_t;
+
+typedef struct dugks_srv_status {
+    int state;         /* dugks_srv_state_t */
+    int batched;       /* 1: runs in the batched lane */
+    int64_t nsteps, steps_done;
+    size_t bytes;      /* device footprint */
+    double t_submit, t_start, t_done;  /* seconds since dugks_srv_create */
+} dugks_srv_status_t;
+
+typedef struct dugks_srv_stats {
+    int64_t submitted, completed, cancelled, failed;
+    int64_t cell_updates;     /* of completed cases */
+    int64_t chunks, graphs_captured, launches;
+    int max_resident;         /* most cases resident at once */
+    size_t bytes_in_use, bytes_peak, max_bytes;
+    double busy_s;            /* batched lane: time with work on the device */
+} dugks_srv_stats_t;
+
+int dugks_srv_create(const dugks_srv_config_t *cfg, dugks_srv_t **out);
+/* Queue a case: initialise it like dugks_gpu_init(kind, params, nparams,
+ * seed) and run nsteps steps.  Returns at once with the case id. */
+int dugks_srv_submit(dugks_srv_t *s, const dugks_case_t *c, const dugks_grid_t *g, int init_kind,
+                     const double *params, int nparams, uint64_t seed, int64_t nsteps, int64_t *id);
+int dugks_srv_poll(dugks_srv_t *s, int64_t id, dugks_srv_status_t *st);
+/* Block until the case is done, cancelled or failed, or timeout_s passes
+ * (DUGKS_ETIMEOUT; timeout_s < 0: no limit). */
+int dugks_srv_wait(dugks_srv_t *s, int64_t id, double timeout_s, dugks_srv_status_t *st);
+/* Fields of a finished case ([ny][nx] each, like dugks_gpu_download); any
+ * pointer may be NULL.  The result is kept until dugks_srv_release. */
+int dugks_srv_result(dugks_srv_t *s, int64_t id, double *rho, double *u, double *v, double *phi, double *p);
+int dugks_srv_release(dugks_srv_t *s, int64_t id);
+int dugks_srv_cancel(dugks_srv_t *s, int64_t id);
+int dugks_srv_stats(dugks_srv_t *s, dugks_srv_stats_t *out);
+int dugks_srv_last_error(dugks_srv_t *s, char *buf, size_t len);
+/* Cancels what has not finished and waits for the device work to end. */
+int dugks_srv_destroy(dugks_srv_t *s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -44,6 +44,24 @@ class ReductionsT(C.Structure):
                 ('steps', C.c_int64)]
 
 
+class SrvConfigT(C.Structure):
+    _fields_ = [('max_bytes', C.c_size_t), ('chunk_steps', C.c_int), ('reserved', C.c_int * 6)]
+
+
+class SrvStatusT(C.Structure):
+    _fields_ = [('state', C.c_int), ('batched', C.c_int), ('nsteps', C.c_int64), ('steps_done', C.c_int64),
+                ('bytes', C.c_size_t), ('t_submit', C.c_double), ('t_start', C.c_double), ('t_done', C.c_double)]
+
+
+class SrvStatsT(C.Structure):
+    _fields_ = [('submitted', C.c_int64), ('completed', C.c_int64), ('cancelled', C.c_int64), ('failed', C.c_int64),
+                ('cell_updates', C.c_int64), ('chunks', C.c_int64), ('graphs_captured', C.c_int64),
+                ('launches', C.c_int64), ('max_resident', C.c_int), ('bytes_in_use', C.c_size_t),
+                ('bytes_peak', C.c_size_t), ('max_bytes', C.c_size_t), ('busy_s', C.c_double)]
+
+
+SRV_STATES = {0: 'queued', 1: 'running', 2: 'done', 3: 'cancelled', 4: 'failed'}
+
 # every symbol declared in include/dugks_gpu.h, with its ctypes signature
 SIGNATURES = {
     'dugks_gpu_create': (C.c_int, [C.POINTER(CaseT), C.POINTER(GridT), C.POINTER(C.c_void_p)]),
@@ -64,6 +82,17 @@ SIGNATURES = {
     'dugks_gpu_destroy': (C.c_int, [C.c_void_p]),
     'dugks_gpu_step_noalloc': (C.c_int, [C.POINTER(CaseT), C.POINTER(GridT), C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.c_int, C.c_void_p]),
+    'dugks_srv_create': (C.c_int, [C.POINTER(SrvConfigT), C.POINTER(C.c_void_p)]),
+    'dugks_srv_submit': (C.c_int, [C.c_void_p, C.POINTER(CaseT), C.POINTER(GridT), C.c_int, C.POINTER(C.c_double),
+                                   C.c_int, C.c_uint64, C.c_int64, C.POINTER(C.c_int64)]),
+    'dugks_srv_poll': (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(SrvStatusT)]),
+    'dugks_srv_wait': (C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.POINTER(SrvStatusT)]),
+    'dugks_srv_result': (C.c_int, [C.c_void_p, C.c_int64] + [C.c_void_p] * 5),
+    'dugks_srv_release': (C.c_int, [C.c_void_p, C.c_int64]),
+    'dugks_srv_cancel': (C.c_int, [C.c_void_p, C.c_int64]),
+    'dugks_srv_stats': (C.c_int, [C.c_void_p, C.POINTER(SrvStatsT)]),
+    'dugks_srv_last_error': (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
+    'dugks_srv_destroy': (C.c_int, [C.c_void_p]),
 }
 
 _lib = None
@@ -180,3 +209,70 @@ class GpuCase:
     @property
     def launches(self) -> int:
         return self.lib.dugks_gpu_launch_count(self.h)
+
+
+class Server:
+    """A serving loop on the GPU (dugks_srv_*): submit cases, poll or wait, read results."""
+
+    def __init__(self, max_bytes: int = 0, chunk_steps: int = 0):
+        self.lib = load()
+        cfg = SrvConfigT(max_bytes, chunk_steps)
+        h = C.c_void_p()
+        rc = self.lib.dugks_srv_create(C.byref(cfg), C.byref(h))
+        if rc != DUGKS_OK:
+            raise DugksError(rc, 'dugks_srv_create failed')
+        self.s = h
+        self.shapes: dict[int, tuple[int, int]] = {}
+
+    def _check(self, rc: int) -> None:
+        if rc != DUGKS_OK:
+            buf = C.create_string_buffer(512)
+            self.lib.dugks_srv_last_error(self.s, buf, 512)
+            raise DugksError(rc, buf.value.decode())
+
+    def submit(self, case: CaseT, nx: int, ny: int, y_walls: bool, init: str, params=(), seed: int = 12345,
+               nsteps: int = 100) -> int:
+        arr = (C.c_double * max(1, len(params)))(*params)
+        cid = C.c_int64()
+        grid = GridT(nx, ny, int(y_walls))
+        self._check(self.lib.dugks_srv_submit(self.s, C.byref(case), C.byref(grid), INIT_KINDS[init], arr,
+                                              len(params), seed, nsteps, C.byref(cid)))
+        self.shapes[cid.value] = (ny, nx)
+        return cid.value
+
+    def poll(self, cid: int) -> SrvStatusT:
+        st = SrvStatusT()
+        self._check(self.lib.dugks_srv_poll(self.s, cid, C.byref(st)))
+        return st
+
+    def wait(self, cid: int, timeout: float = -1.0) -> SrvStatusT:
+        st = SrvStatusT()
+        self._check(self.lib.dugks_srv_wait(self.s, cid, timeout, C.byref(st)))
+        return st
+
+    def result(self, cid: int) -> dict[str, np.ndarray]:
+        ny, nx = self.shapes[cid]
+        out = {k: np.empty((ny, nx), dtype=np.float64) for k in ('rho', 'u', 'v', 'phi', 'p')}
+        self._check(self.lib.dugks_srv_result(self.s, cid, *[out[k].ctypes.data for k in ('rho', 'u', 'v', 'phi',
+                                                                                             'p')]))
+        return out
+
+    def release(self, cid: int) -> None:
+        self._check(self.lib.dugks_srv_release(self.s, cid))
+        self.shapes.pop(cid, None)
+
+    def cancel(self, cid: int) -> None:
+        self._check(self.lib.dugks_srv_cancel(self.s, cid))
+
+    def stats(self) -> SrvStatsT:
+        st = SrvStatsT()
+        self._check(self.lib.dugks_srv_stats(self.s, C.byref(st)))
+        return st
+
+    def close(self) -> None:
+        if getattr(self, 's', None):
+            self.lib.dugks_srv_destroy(self.s)
+            self.s = None
+
+    def __del__(self):
+        self.close()

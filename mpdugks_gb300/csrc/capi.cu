@@ -154,6 +154,35 @@ static double f_rest(const Params &P, int q) {
 }
 static double h_rest(const Params &P, int q) { return P.omega[q] * DUGKS_F32_PHI0; }
 
+constexpr int REDUCE_BLOCKS = 152 * 4;
+
+// device bytes of one case of the fused step with storage type of rsize bytes
+static size_t fused_arena_bytes(const Params &P, size_t rsize) {
+    const size_t rowf = (size_t)P.pitch * rsize;
+    const size_t cellf = align256(rowf * P.ny);
+    const size_t celld = align256((size_t)P.pitch * sizeof(double) * P.ny);
+    return 2 * (18 + f32::A_N) * cellf + f32::I_N * cellf + align256(4 * rowf) +
+           6 * celld /* rho u v p phi + rho_last */ + align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 512;
+}
+
+// device bytes of one case of the multi-kernel FP64 step
+static size_t fp64_arena_bytes(const Params &P) {
+    const size_t rowb = (size_t)P.pitch * sizeof(double);
+    const size_t cellb = align256(rowb * P.ny), ycellb = align256(rowb * (P.ny + 1));
+    const int Q = P.Q;
+    const bool pp = !(P.model == AC || P.model == HCZ);
+    size_t total = 0;
+    total += 2 * Q * cellb;                       // f, h (h unused by PP but kept simple)
+    total += 2 * Q * cellb;                       // bf, bh
+    total += 2 * Q * cellb + 2 * Q * ycellb;      // x/y face fluxes
+    total += NFIELDS * cellb;                     // macro fields
+    total += align256(4 * rowb);                  // ghost phi rows
+    if (pp) total += 14 * cellb + 2 * Q * cellb;  // pseudopotential face state + face BhDt
+    total += cellb;                               // rho_last
+    total += align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 256 + 256;
+    return total;
+}
+
 template <typename R>
 static int create_fused(dugks_handle *h, dugks_handle_t **out, f32::PR<R> &PQ, f32::SR<R> &S) {
     Params &P = h->P;
@@ -163,9 +192,8 @@ static int create_fused(dugks_handle *h, dugks_handle_t **out, f32::PR<R> &PQ, f
     const size_t cellf = align256(rowf * P.ny);
     const size_t rowd = (size_t)P.pitch * sizeof(double);
     const size_t celld = align256(rowd * P.ny);
-    h->nblocks = 152 * 4;
-    size_t total = 2 * (18 + f32::A_N) * cellf + f32::I_N * cellf + align256(4 * rowf) +
-                   6 * celld /* rho u v p phi + rho_last */ + align256(sizeof(double) * 4 * h->nblocks) + 512;
+    h->nblocks = REDUCE_BLOCKS;
+    const size_t total = fused_arena_bytes(P, sizeof(R));
     cudaError_t e = cudaMalloc(&h->arena, total);
     if (e != cudaSuccess) {
         delete h;
@@ -173,7 +201,7 @@ static int create_fused(dugks_handle *h, dugks_handle_t **out, f32::PR<R> &PQ, f
                     std::string("cudaMalloc of device state failed: ") + cudaGetErrorString(e));
     }
     h->arena_bytes = total;
-    cudaMemset(h->arena, 0, total);
+    cudaMemsetAsync(h->arena, 0, total, nullptr);
     char *cur = h->arena;
     auto takef = [&](size_t b) { R *p = reinterpret_cast<R *>(cur); cur += b; return p; };
     auto taked = [&](size_t b) { double *p = reinterpret_cast<double *>(cur); cur += b; return p; };
@@ -192,7 +220,7 @@ static int create_fused(dugks_handle *h, dugks_handle_t **out, f32::PR<R> &PQ, f
     h->partial = taked(align256(sizeof(double) * 4 * h->nblocks));
     h->out4 = taked(256);
     h->flag = reinterpret_cast<int *>(taked(256));
-    e = cudaDeviceSynchronize();
+    e = cudaStreamSynchronize(nullptr);  // the clear above (legacy stream; leaves non-blocking streams running)
     if (e != cudaSuccess) {
         cudaFree(h->arena);
         delete h;
@@ -296,18 +324,9 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
     const size_t rowb = (size_t)P.pitch * sizeof(double);
     const size_t cellb = align256(rowb * P.ny), ycellb = align256(rowb * (P.ny + 1));
     const int Q = P.Q;
-    const bool hasH = (P.model == AC || P.model == HCZ);
-    const bool pp = !hasH;
-    size_t total = 0;
-    total += 2 * Q * cellb;                       // f, h (h unused by PP but kept simple)
-    total += 2 * Q * cellb;                       // bf, bh
-    total += 2 * Q * cellb + 2 * Q * ycellb;      // x/y face fluxes
-    total += NFIELDS * cellb;                     // macro fields
-    total += align256(4 * rowb);                  // ghost phi rows
-    if (pp) total += 14 * cellb + 2 * Q * cellb;  // pseudopotential face state + face BhDt
-    total += cellb;                               // rho_last
-    h->nblocks = 152 * 4;
-    total += align256(sizeof(double) * 4 * h->nblocks) + 256 + 256;
+    const bool pp = !(P.model == AC || P.model == HCZ);
+    h->nblocks = REDUCE_BLOCKS;
+    const size_t total = fp64_arena_bytes(P);
     cudaError_t e = cudaMalloc(&h->arena, total);
     if (e != cudaSuccess) {
         delete h;
@@ -662,3 +681,45 @@ extern "C" int dugks_gpu_destroy(dugks_handle_t *h) {
     delete h;
     return DUGKS_OK;
 }
+
+// ---- internal interface for the serving layer (serving.cu)
+namespace dugks {
+namespace internal {
+
+size_t footprint(const dugks_case_t &c, const dugks_grid_t &g) {
+    Params P;
+    derive_params(c, g, P);
+    if (c.precision == DUGKS_FP32_DEV) return fused_arena_bytes(P, sizeof(float));
+    if (c.precision == DUGKS_FP64_FUSED) return fused_arena_bytes(P, sizeof(double));
+    return fp64_arena_bytes(P);
+}
+
+bool batchable(const dugks_handle_t *h) {
+    return h && h->fp32 && !h->fused64 && (h->P.model == AC || h->P.model == HCZ);
+}
+
+void fp32_views(const dugks_handle_t *h, f32::P32 *P, f32::S32 *S) {
+    *P = h->P32;
+    *S = h->S32;
+}
+
+int64_t steps_done(const dugks_handle_t *h) { return h->steps; }
+int model_of(const dugks_handle_t *h) { return h->P.model; }
+int walls_of(const dugks_handle_t *h) { return h->P.walls ? 1 : 0; }
+
+// n steps were run outside the handle (by the batched kernel) from its current
+// state with step numbers steps .. steps+n-1: adopt the ping-pong orientation,
+// ghost-row buffer, first-step flag and counters those steps leave
+void fp32_adopt_steps(dugks_handle_t *h, int64_t n) {
+    if (n <= 0) return;
+    if (n & 1) f32::swap_io(h->S32);
+    h->steps += n;
+    h->gcur = (int)(h->steps & 1);
+    h->first = 0;
+    h->macros_fresh = false;
+}
+
+void set_stream(dugks_handle_t *h, cudaStream_t st) { h->last_stream = st; }
+
+}  // namespace internal
+}  // namespace dugks

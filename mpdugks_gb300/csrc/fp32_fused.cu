@@ -327,41 +327,52 @@ __device__ __forceinline__ void prefetch_tile(const PR<float> &P, const SR<float
     cp_async_commit();
 }
 
-// Persistent kernel: each CTA (one per SM) walks the tiles t = blockIdx.x,
-// blockIdx.x + gridDim.x, ...; tile t + gridDim.x's inputs are in flight while
-// tile t computes.
-template <int MODEL, bool WALLS, typename R>
-__global__ void __launch_bounds__(BX *BY, 1) k_step32(PR<R> P, SR<R> S, int first, int gin, int gout,
-                                                      uint32_t step, int ntx, int ntiles) {
+// Shared-memory views of one CTA
+template <typename R>
+struct Views {
     using T = typename Pair<R>::T;
-    constexpr bool PF = prefetched<R>();
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    R *smem = reinterpret_cast<R *>(smem_raw);
-    T(*sB)[BY][BX] = reinterpret_cast<T(*)[BY][BX]>(smem);                              // f-bar-plus pairs
-    T(*sFS)[BY][BX] = sB + 9;                                                             // south-face flux pairs (6 slots)
-    R(*sA)[BY][BX] = reinterpret_cast<R(*)[BY][BX]>(sFS + 6);                             // srcx srcy rhox rhoy fx fy
-    R(*sphi)[BX + 2] = reinterpret_cast<R(*)[BX + 2]>(smem + (18 + 12 + 6) * BY * BX);  // phi, halo 2
-    R *stg = smem + SMEM_ELEMS;                                                           // [24][BY][BX] (PF)
-    R *stg_ring = stg + 24 * BY * BX;                                                     // [9][RING_MAX] (PF)
+    T (*sB)[BY][BX];       // f-bar-plus pairs
+    T (*sFS)[BY][BX];      // south-face flux pairs (6 slots)
+    R (*sA)[BY][BX];       // srcx srcy rhox rhoy fx fy
+    R (*sphi)[BX + 2];     // phi, halo 2
+    R *stg;                // [24][BY][BX] staged own-cell inputs (prefetch)
+    R *stg_ring;           // [9][RING_MAX] staged ring h (prefetch)
+    __device__ __forceinline__ explicit Views(unsigned char *raw) {
+        R *smem = reinterpret_cast<R *>(raw);
+        sB = reinterpret_cast<T(*)[BY][BX]>(smem);
+        sFS = sB + 9;
+        sA = reinterpret_cast<R(*)[BY][BX]>(sFS + 6);
+        sphi = reinterpret_cast<R(*)[BX + 2]>(smem + (18 + 12 + 6) * BY * BX);
+        stg = smem + SMEM_ELEMS;
+        stg_ring = stg + 24 * BY * BX;
+    }
+};
+
+// One DUGKS step of one tile (stages 0-3).  The caller has made the tile's
+// inputs visible (staged == true: in the staging area) and synchronised the
+// CTA; `hook` runs right after the last read of the staged inputs.
+template <int MODEL, bool WALLS, typename R, typename Hook>
+__device__ __forceinline__ void tile_step(const PR<R> &P, const SR<R> &S, int first, int gin, int gout,
+                                          uint32_t step, const TileCell<WALLS> &g, const Views<R> &sv,
+                                          bool staged, Hook &&hook) {
+    using T = typename Pair<R>::T;
+    const auto sB = sv.sB;
+    const auto sFS = sv.sFS;
+    const auto sA = sv.sA;
+    const auto sphi = sv.sphi;
+    const R *stg = sv.stg, *stg_ring = sv.stg_ring;
     const int e = threadIdx.x, r = threadIdx.y;
     const int tid = r * BX + e;
     const int nx = P.nx, ny = P.ny, pitch = P.pitch;
-    if constexpr (PF) {
-        if ((int)blockIdx.x < ntiles) prefetch_tile<MODEL, WALLS>(P, S, blockIdx.x, ntx, e, r, tid, stg, stg_ring);
-    }
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const TileCell<WALLS> g(t, ntx, e, r, nx, ny, pitch);
     const int x0 = g.x0, y0 = g.y0, w = g.w, hh = g.hh, gi = g.gi, gj = g.gj;
     const bool act = g.act, ghost = g.ghost, real = g.real;
     const size_t c = g.c;
-    if constexpr (PF) cp_async_wait_all();
-    __syncthreads();  // staged inputs visible; the previous tile is done with shared memory
 
     // ---- stage 0: own deviations (f, h pairs), phi of the halo-2 region
     T Pq[9];
     R dphi = R(0.), sfz = R(0.);
     if (real) {
-        if constexpr (PF) {
+        if (staged) {
 #pragma unroll
             for (int q = 0; q < 9; ++q) Pq[q] = mk2(stg[(q * BY + r) * BX + e], stg[((9 + q) * BY + r) * BX + e]);
         } else {
@@ -398,7 +409,7 @@ __global__ void __launch_bounds__(BX *BY, 1) k_step32(PR<R> P, SR<R> S, int firs
                 const size_t cc = (size_t)rj * pitch + ri;
                 FFs<R> sh;
 #pragma unroll
-                for (int q = 0; q < 9; ++q) sh.add(PF ? stg_ring[q * RING_MAX + k] : S.dh[(size_t)q * S.qs + cc]);
+                for (int q = 0; q < 9; ++q) sh.add(staged ? stg_ring[q * RING_MAX + k] : S.dh[(size_t)q * S.qs + cc]);
                 v = P.phi0 + sh.value();
             }
             sphi[rr + 1][re + 1] = v;
@@ -440,7 +451,7 @@ __global__ void __launch_bounds__(BX *BY, 1) k_step32(PR<R> P, SR<R> S, int firs
                 R a6[A_N];
 #pragma unroll
                 for (int k = 0; k < A_N; ++k)
-                    a6[k] = PF ? stg[((18 + k) * BY + r) * BX + e] : S.aux[(size_t)k * S.qs + c];
+                    a6[k] = staged ? stg[((18 + k) * BY + r) * BX + e] : S.aux[(size_t)k * S.qs + c];
                 const R fxo = a6[A_FX], fyo = a6[A_FY];
                 rxo = a6[A_RHOX];
                 ryo = a6[A_RHOY];
@@ -529,10 +540,7 @@ __global__ void __launch_bounds__(BX *BY, 1) k_step32(PR<R> P, SR<R> S, int firs
         }
     }
     __syncthreads();
-    if constexpr (PF) {  // every read of the staged inputs of tile t is done
-        if (t + (int)gridDim.x < ntiles)
-            prefetch_tile<MODEL, WALLS>(P, S, t + gridDim.x, ntx, e, r, tid, stg, stg_ring);
-    }
+    hook();  // every read of the staged inputs of this tile is done
 
     // ---- stage 2: west x-face and south y-face of this thread's cell
     T FW[6], FSo[6];
@@ -676,7 +684,156 @@ __global__ void __launch_bounds__(BX *BY, 1) k_step32(PR<R> P, SR<R> S, int firs
             S.oaux[A_PPV * S.qs + c] = phi * V;
         }
     }
-    }  // tiles
+}
+
+// Persistent kernel: each CTA (one per SM) walks the tiles t = blockIdx.x,
+// blockIdx.x + gridDim.x, ...; tile t + gridDim.x's inputs are in flight while
+// tile t computes.
+template <int MODEL, bool WALLS, typename R>
+__global__ void __launch_bounds__(BX *BY, 1) k_step32(PR<R> P, SR<R> S, int first, int gin, int gout,
+                                                      uint32_t step, int ntx, int ntiles) {
+    constexpr bool PF = prefetched<R>();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Views<R> sv(smem_raw);
+    const int e = threadIdx.x, r = threadIdx.y, tid = r * BX + e;
+    if constexpr (PF) {
+        if ((int)blockIdx.x < ntiles)
+            prefetch_tile<MODEL, WALLS>(P, S, blockIdx.x, ntx, e, r, tid, sv.stg, sv.stg_ring);
+    }
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const TileCell<WALLS> g(t, ntx, e, r, P.nx, P.ny, P.pitch);
+        if constexpr (PF) cp_async_wait_all();
+        __syncthreads();  // staged inputs visible; the previous tile is done with shared memory
+        tile_step<MODEL, WALLS, R>(P, S, first, gin, gout, step, g, sv, PF, [&] {
+            if constexpr (PF) {
+                if (t + (int)gridDim.x < ntiles)
+                    prefetch_tile<MODEL, WALLS>(P, S, t + gridDim.x, ntx, e, r, tid, sv.stg, sv.stg_ring);
+            }
+        });
+    }
+}
+
+// ---- many cases in one launch (serving): a case table in constant memory and
+// a tile table (case slot, tile of that case) in device memory.  Each tile
+// runs the same tile_step as the single-case kernel with its own case's
+// constants, state and step number, so a case's result does not depend on
+// what else is in the launch.
+struct BatchCase {
+    P32 P;
+    S32 S[2];  // state views for even / odd step numbers (ping-pong buffers)
+    int ntx;   // tiles per row
+    int pad;
+};
+__constant__ BatchCase c_batch[BATCH_MAX_CASES];
+
+// tiles[t] = (case slot, tile index within the case), all cases of one model
+// and wall kind; case_base[slot] = the case's step number at the start of this
+// launch sequence, kstep = the launch within the sequence; tiles of a case
+// whose step number reached case_stop are skipped.
+template <int MODEL, bool WALLS>
+__global__ void __launch_bounds__(BX *BY, 1) k_batch32(const int2 *__restrict__ tiles, int ntiles, int kstep,
+                                                       const int *__restrict__ case_base,
+                                                       const int *__restrict__ case_stop) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Views<float> sv(smem_raw);
+    const int e = threadIdx.x, r = threadIdx.y, tid = r * BX + e;
+    auto issue = [&](int t) {
+        if (t >= ntiles) return;
+        const int2 bt = tiles[t];
+        const int sn = case_base[bt.x] + kstep;
+        if (sn >= case_stop[bt.x]) return;
+        const BatchCase &B = c_batch[bt.x];
+        prefetch_tile<MODEL, WALLS>(B.P, B.S[sn & 1], bt.y, B.ntx, e, r, tid, sv.stg, sv.stg_ring);
+    };
+    issue(blockIdx.x);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int2 bt = tiles[t];
+        const int sn = case_base[bt.x] + kstep;
+        if (sn >= case_stop[bt.x]) {  // the whole CTA skips: nothing staged for this tile
+            issue(t + gridDim.x);
+            continue;
+        }
+        const BatchCase &B = c_batch[bt.x];
+        const int par = sn & 1;
+        cp_async_wait_all();
+        __syncthreads();
+        const TileCell<WALLS> g(bt.y, B.ntx, e, r, B.P.nx, B.P.ny, B.P.pitch);
+        tile_step<MODEL, WALLS, float>(B.P, B.S[par], sn == 0, par, par ^ 1, (uint32_t)sn, g, sv, true,
+                                       [&] { issue(t + gridDim.x); });
+    }
+}
+
+// case_base[slots[k]] += n for the k < count slots of a launch sequence
+__global__ void k_batch_advance(int *case_base, const int *slots, int count, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < count) case_base[slots[k]] += n;
+}
+
+cudaError_t batch_set_case(int slot, const P32 &P, const S32 &S0, cudaStream_t st) {
+    if (slot < 0 || slot >= BATCH_MAX_CASES) return cudaErrorInvalidValue;
+    BatchCase b{};
+    b.P = P;
+    b.S[0] = S0;
+    b.S[1] = S0;
+    swap_io(b.S[1]);
+    b.ntx = (P.nx + TW - 1) / TW;
+    return cudaMemcpyToSymbolAsync(c_batch, &b, sizeof(b), (size_t)slot * sizeof(BatchCase), cudaMemcpyHostToDevice,
+                                   st);
+}
+
+int batch_tiles_of(int nx, int ny) { return ((nx + TW - 1) / TW) * ((ny + TH - 1) / TH); }
+
+static int g_batch_nsm = 0;  // SMs of the device, set by batch_prepare
+
+template <int MODEL, bool WALLS>
+static cudaError_t batch_attr() {
+    return cudaFuncSetAttribute(k_batch32<MODEL, WALLS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(smem_elems<float>() * sizeof(float)));
+}
+
+// kernel attributes of the batched launches; called before any stream capture
+cudaError_t batch_prepare() {
+    cudaError_t e;
+    if ((e = batch_attr<AC, false>()) != cudaSuccess) return e;
+    if ((e = batch_attr<AC, true>()) != cudaSuccess) return e;
+    if ((e = batch_attr<HCZ, false>()) != cudaSuccess) return e;
+    if ((e = batch_attr<HCZ, true>()) != cudaSuccess) return e;
+    int dev = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    return cudaDeviceGetAttribute(&g_batch_nsm, cudaDevAttrMultiProcessorCount, dev);
+}
+
+template <int MODEL, bool WALLS>
+static cudaError_t launch_batch_t(const int2 *tiles, int ntiles, int kstep, const int *case_base,
+                                  const int *case_stop, cudaStream_t st) {
+    if (g_batch_nsm <= 0) return cudaErrorNotReady;
+    const size_t bytes = smem_elems<float>() * sizeof(float);
+    k_batch32<MODEL, WALLS><<<min(ntiles, g_batch_nsm), dim3(BX, BY), bytes, st>>>(tiles, ntiles, kstep,
+                                                                                    case_base, case_stop);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch32(int model, int walls, const int2 *tiles, int ntiles, int kstep, const int *case_base,
+                           const int *case_stop, cudaStream_t st, int64_t *launches) {
+    if (ntiles <= 0) return cudaSuccess;
+    cudaError_t e = cudaErrorInvalidValue;
+    switch (model * 2 + (walls ? 1 : 0)) {
+        case AC * 2 + 0: e = launch_batch_t<AC, false>(tiles, ntiles, kstep, case_base, case_stop, st); break;
+        case AC * 2 + 1: e = launch_batch_t<AC, true>(tiles, ntiles, kstep, case_base, case_stop, st); break;
+        case HCZ * 2 + 0: e = launch_batch_t<HCZ, false>(tiles, ntiles, kstep, case_base, case_stop, st); break;
+        case HCZ * 2 + 1: e = launch_batch_t<HCZ, true>(tiles, ntiles, kstep, case_base, case_stop, st); break;
+        default: break;
+    }
+    if (e == cudaSuccess) *launches += 1;
+    return e;
+}
+
+cudaError_t launch_batch_advance(int *case_base, const int *slots, int count, int n, cudaStream_t st,
+                                 int64_t *launches) {
+    if (count <= 0) return cudaSuccess;
+    k_batch_advance<<<(count + 127) / 128, 128, 0, st>>>(case_base, slots, count, n);
+    *launches += 1;
+    return cudaGetLastError();
 }
 
 // Macroscopic fields of the FP32 state as FP64 arrays: the quantities the

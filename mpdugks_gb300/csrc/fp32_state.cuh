@@ -48,6 +48,9 @@ struct SR {
 };
 using S32 = SR<float>;
 
+// cases one batched launch (serving) can hold: the size of the constant-memory case table
+constexpr int BATCH_MAX_CASES = 64;
+
 // after a step the written state becomes the one the next step reads
 template <typename R>
 inline void swap_io(SR<R> &S) {

@@ -9,7 +9,7 @@ ROOT = Path(__file__).resolve().parents[1]
 
 def declared_symbols():
     text = (ROOT / 'include' / 'dugks_gpu.h').read_text()
-    return sorted(set(re.findall(r'\b(dugks_gpu_\w+)\s*\(', text)))
+    return sorted(set(re.findall(r'\b(dugks_(?:gpu|srv)_\w+)\s*\(', text)))
 
 
 def test_header_declares_abi():
@@ -42,3 +42,16 @@ def test_create_fails_cleanly_without_valid_grid():
     buf = ctypes.create_string_buffer(256)
     lib.dugks_gpu_last_error(None, buf, 256)
     assert b'nx' in buf.value
+
+
+def test_serving_create_reports_missing_gpu():
+    """Without a GPU the server is not created: an error code, no fallback."""
+    import ctypes
+    import torch
+    from mpdugks_gb300 import capi
+    if torch.cuda.is_available():
+        pytest.skip('a GPU is present')
+    lib = capi.load(build_if_missing=True)
+    h = ctypes.c_void_p()
+    rc = lib.dugks_srv_create(None, ctypes.byref(h))
+    assert rc == capi.DUGKS_ECUDA and not h.value
