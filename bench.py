@@ -180,6 +180,130 @@ def run_reference(args, wl, rank, world):
     return 0
 
 
+# ---------------------------------------------------------------- serving stream
+
+SERVING = dict(cases=256, rate=20.0, median_n=256, sigma_ln=0.6931471805599453, n_min=64, n_max=1024,
+               steps=5000, ac_share=0.7, seed=2026)
+
+
+def serving_stream(cases: int, steps: int, seed: int):
+    """The seeded serving workload: Poisson arrivals (mean 20/s), N ~ lognormal
+    (median 256, sigma_ln = ln 4 / 2) clipped to [64, 1024], 70% Allen-Cahn
+    droplets / bubbles (R = N/5, density ratio U[2, 100], sigma U[1e-4, 1e-2])
+    and 30% pseudopotential D2V16 cases.  Returns the Allen-Cahn cases (the
+    pseudopotential share is listed separately: it has no FP32 path)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / SERVING['rate'], cases))
+    n = np.clip(np.round(SERVING['median_n'] * np.exp(rng.normal(0.0, np.log(4.0) / 2, cases))),
+                SERVING['n_min'], SERVING['n_max']).astype(int)
+    kind = rng.random(cases) < SERVING['ac_share']
+    ratio = rng.uniform(2.0, 100.0, cases)
+    sigma = rng.uniform(1e-4, 1e-2, cases)
+    bubble = rng.random(cases) < 0.5
+    out, pp = [], 0
+    for k in range(cases):
+        if not kind[k]:
+            pp += 1
+            continue
+        out.append(dict(t=float(t[k]), n=int(n[k]), rho_v=float(1.0 / ratio[k]), sigma=float(sigma[k]),
+                        init='ac_drop' if bubble[k] else 'ac_drop_inside', radius=float(n[k]) / 5.0, steps=steps))
+    return out, pp
+
+
+def serving_case(c: dict, precision: str):
+    from mpdugks_gb300 import capi
+    return capi.make_case('AC', precision, Mu0=0.02, M_Phi=0.02, W=4.0, Sigma=c['sigma'], RhoL=1.0,
+                          RhoV=c['rho_v'])
+
+
+def serving_bench(args) -> dict:
+    """Cases arrive on their schedule and are submitted to the server as they
+    arrive; p50/p99 time to solution (submit to result on the host) and the
+    aggregate rate.  Beside it: the same cases solved one at a time (FP64 plain
+    path and FP32 storage, no batching) on a sample, as cases/s."""
+    import numpy as np
+    import torch
+    from mpdugks_gb300 import capi
+    stream, npp = serving_stream(args.serving_cases, args.serving_steps, SERVING['seed'])
+
+    def serve(paced: bool):
+        srv = capi.Server(chunk_steps=64)
+        t0 = time.perf_counter()
+        ids = []
+        for c in stream:
+            dt = c['t'] - (time.perf_counter() - t0)
+            if paced and dt > 0:
+                time.sleep(dt)
+            ids.append(srv.submit(serving_case(c, 'fp32dev'), c['n'], c['n'], False, c['init'], [c['radius']],
+                                  nsteps=c['steps']))
+        tts, finite, lu = [], 0, 0
+        t_first, t_last = None, 0.0
+        for cid, c in zip(ids, stream):
+            st = srv.wait(cid, 3600.0)
+            if st.state != 2:
+                continue
+            r = srv.result(cid)
+            finite += int(np.isfinite(r['rho']).all())
+            srv.release(cid)
+            tts.append(st.t_done - st.t_submit)
+            t_first = st.t_submit if t_first is None else min(t_first, st.t_submit)
+            t_last = max(t_last, st.t_done)
+            lu += c['n'] * c['n'] * c['steps']
+        stats = srv.stats()
+        srv.close()
+        return tts, finite, lu, t_last - (t_first or 0.0), stats
+
+    tts, finite, lu, span, stats = serve(True)
+    btts, bfinite, blu, bspan, bstats = serve(False)
+    done = len(tts)
+    # one case at a time on a sample of the stream (the first cases)
+    sample = stream[:args.serving_sample]
+
+    def one_at_a_time(precision):
+        torch.cuda.synchronize()
+        ta = time.perf_counter()
+        slu = 0
+        for c in sample:
+            gc = capi.GpuCase(serving_case(c, precision), c['n'], c['n'], False)
+            gc.init(c['init'], [c['radius']])
+            gc.step(c['steps'])
+            gc.get('rho')
+            slu += c['n'] * c['n'] * c['steps']
+            del gc
+        torch.cuda.synchronize()
+        el = time.perf_counter() - ta
+        return {'cases': len(sample), 'seconds': round(el, 3), 'cases_per_s': round(len(sample) / el, 4),
+                'mlups': round(slu / el / 1e6, 2),
+                'stream_cases_per_s_projected': round(done / (lu / (slu / el)), 4) if lu else None}
+
+    fp64 = one_at_a_time('fp64')
+    fp32 = one_at_a_time('fp32dev')
+    cps = done / span if span > 0 else 0.0
+    return {
+        'workload': f'{len(stream)} Allen-Cahn cases of a {args.serving_cases}-case seeded stream (Poisson 20/s, '
+                    f'N lognormal median 256 in [64,1024], R=N/5, density ratio U[2,100], sigma U[1e-4,1e-2], '
+                    f'{args.serving_steps} steps, FP32 storage); the {npp} pseudopotential D2V16 cases of the '
+                    'stream are not run (no FP32 D2V16 path)',
+        'completed': done, 'finite': finite, 'span_s': round(span, 3), 'cases_per_s': round(cps, 4),
+        'mlups': round(lu / span / 1e6, 2) if span > 0 else None,
+        'tts_p50_s': round(float(np.percentile(tts, 50)), 4) if tts else None,
+        'tts_p99_s': round(float(np.percentile(tts, 99)), 4) if tts else None,
+        'max_resident': stats.max_resident, 'graphs_captured': stats.graphs_captured, 'chunks': stats.chunks,
+        'bytes_peak': stats.bytes_peak, 'max_bytes': stats.max_bytes,
+        'burst': {'how': 'the same cases all submitted at once (capacity)', 'completed': len(btts),
+                  'finite': bfinite, 'span_s': round(bspan, 3),
+                  'cases_per_s': round(len(btts) / bspan, 4) if bspan > 0 else None,
+                  'mlups': round(blu / bspan / 1e6, 2) if bspan > 0 else None,
+                  'tts_p50_s': round(float(np.percentile(btts, 50)), 4) if btts else None,
+                  'tts_p99_s': round(float(np.percentile(btts, 99)), 4) if btts else None,
+                  'max_resident': bstats.max_resident, 'bytes_peak': bstats.bytes_peak},
+        'one_at_a_time_fp64': fp64, 'one_at_a_time_fp32': fp32,
+        'vs_one_at_a_time_fp64': round(cps / fp64['stream_cases_per_s_projected'], 2)
+        if fp64['stream_cases_per_s_projected'] else None,
+    }
+
+
 # ---------------------------------------------------------------- GPU arms
 
 def field_errors(a, b):
@@ -326,6 +450,10 @@ def run_ours(args, wl, rank, world, local):
     h2d = (pf.numel() + ph_.numel() + pa.numel()) * 8 / args.steps
     d2h = (5 * cells * 8 + 32) / args.steps
 
+    serving = None
+    if rank == 0 and not args.no_serving:
+        serving = serving_bench(args)
+
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
@@ -346,6 +474,7 @@ def run_ours(args, wl, rank, world, local):
                     'd2h_bytes_per_step': int(d2h),
                     'how': 'C ABI with pinned host buffers: upload the FP64 initial state, K steps, '
                            'reductions, download 5 fields'},
+            'serving': serving,
             'gpu_launches': int(launches),
             'clocks': clocks,
             'state_finite': finite,
@@ -372,6 +501,11 @@ def main():
     ap.add_argument('--cpu-steps', type=int, default=0, help='CPU baseline steps (0: about --cpu-seconds)')
     ap.add_argument('--cpu-seconds', type=float, default=15.0)
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--no-serving', action='store_true', help='skip the serving-stream measurement')
+    ap.add_argument('--serving-only', action='store_true', help='run only the serving-stream measurement')
+    ap.add_argument('--serving-cases', type=int, default=SERVING['cases'])
+    ap.add_argument('--serving-steps', type=int, default=SERVING['steps'])
+    ap.add_argument('--serving-sample', type=int, default=3, help='cases solved one at a time for comparison')
     ap.add_argument('--profile-steps', type=int, default=0,
                     help='only run this many steps of the workload (for ncu) and exit')
     ap.add_argument('--grid', default=None, help='NXxNY override of the grid (profiling runs only)')
@@ -397,6 +531,11 @@ def main():
         ap.error('--grid is for --profile-steps runs only')
     if args.impl == 'reference':
         return run_reference(args, wl, rank, world)
+    if args.serving_only:
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps({'serving': serving_bench(args)}), flush=True)
+        return 0
     return run_ours(args, wl, rank, world, local)
 
 
