@@ -12,6 +12,8 @@ CSRC = PKG / 'csrc'
 BUILD = PKG / '_build'
 LIB = BUILD / 'libdugks_gpu.so'
 INCLUDE = PKG.parent / 'include'
+HOST = PKG / 'host'
+RUNNER = BUILD / 'dugks_run'
 
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 # host code: no FMA contraction, so the host-side initial states are the same
@@ -41,6 +43,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     deps = srcs + sorted(CSRC.glob('*.cuh')) + sorted(CSRC.glob('*.h')) + sorted(INCLUDE.glob('*.h'))
     newest = max(p.stat().st_mtime for p in deps)
     if not force and LIB.exists() and LIB.stat().st_mtime >= newest and not extra:
+        build_host()
         return LIB
     exe = nvcc()
     flags = NVFLAGS + (extra or [])
@@ -65,7 +68,25 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     if r.returncode != 0:
         raise RuntimeError(f'nvcc link failed:\n{r.stderr}')
     tmp.replace(LIB)
+    build_host(force=True)
     return LIB
+
+
+def build_host(force: bool = False) -> Path:
+    """The host driver dugks_run (C++, links libdugks_gpu.so)."""
+    srcs = sorted(HOST.glob('*.cpp'))
+    deps = srcs + sorted(HOST.glob('*.hpp')) + sorted(INCLUDE.glob('*.h')) + [LIB]
+    if not force and RUNNER.exists() and RUNNER.stat().st_mtime >= max(p.stat().st_mtime for p in deps):
+        return RUNNER
+    gxx = shutil.which('g++') or 'g++'
+    tmp = RUNNER.with_suffix('.tmp')
+    cmd = [gxx, '-O2', '-std=c++17', '-ffp-contract=off', f'-I{INCLUDE}'] + [str(x) for x in srcs] + \
+          [f'-L{BUILD}', '-ldugks_gpu', "-Wl,-rpath,$ORIGIN", '-o', str(tmp)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f'g++ failed on the host driver:\n{r.stderr}')
+    tmp.replace(RUNNER)
+    return RUNNER
 
 
 if __name__ == '__main__':

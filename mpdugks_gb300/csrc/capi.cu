@@ -43,6 +43,9 @@ void launch_macros64f(const PR<double> &P, const SR<double> &S, double *rho, dou
 template <typename R>
 cudaError_t launch_plane_from_f64(R *dst, int dpitch, const double *src, int nx, int ny, double sub,
                                   cudaStream_t st, int64_t *launches);
+template <typename R>
+void launch_out_forces(const PR<R> &P, const SR<R> &S, const double *phi, const double *rho, int opitch, int first,
+                       double *tau, double *fx, double *fy, cudaStream_t st, int64_t *launches);
 inline cudaError_t launch_stepX(const P32 &P, const S32 &S, int a, int b, int c, cudaStream_t st, int64_t *l,
                                 uint32_t step) {
     return launch_step32(P, S, a, b, c, st, l, step);
@@ -96,6 +99,7 @@ struct dugks_handle {
     f32::SR<double> S64f{};
     int first = 1;            // next step is the first after an upload
     bool macros_fresh = false;
+    double *out3 = nullptr;   // tau, Fx, Fy for output (allocated on first request)
 };
 
 static std::string g_create_err;
@@ -568,12 +572,29 @@ static bool is_msrc_field(const Params &P, int f) {
 extern "C" int dugks_gpu_get_field(dugks_handle_t *h, int field, double *out) {
     if (!h || !out || field < 0 || field >= NFIELDS) return fail(h, DUGKS_EINVAL, "bad field or null pointer");
     if (h->fp32) {
-        if (!(field == F_RHO || field == F_U || field == F_V || field == F_P || field == F_PHI))
-            return fail(h, DUGKS_EINVAL, "FP32 storage exposes rho, u, v, p and phi");
+        const bool forces = field == F_TAU || field == F_FX || field == F_FY;
+        if (!(field == F_RHO || field == F_U || field == F_V || field == F_P || field == F_PHI || forces))
+            return fail(h, DUGKS_EINVAL, "FP32 storage exposes rho, u, v, p, phi, tau, Fx and Fy");
         int rc = macros_fp32(h);
         if (rc) return rc;
+        const double *src = h->S.fld[field];
+        if (forces) {
+            const size_t plane = (size_t)h->P.pitch * h->P.ny;
+            if (!h->out3) {
+                cudaError_t e = cudaMalloc(&h->out3, 3 * plane * sizeof(double));
+                if (e != cudaSuccess) return cuda_fail(h, e, "output buffer");
+            }
+            double *t = h->out3, *fx = t + plane, *fy = fx + plane;
+            if (h->fused64)
+                f32::launch_out_forces(h->P64f, h->S64f, h->S.fld[F_PHI], h->S.fld[F_RHO], h->P.pitch, h->first, t,
+                                       fx, fy, h->last_stream, &h->launches);
+            else
+                f32::launch_out_forces(h->P32, h->S32, h->S.fld[F_PHI], h->S.fld[F_RHO], h->P.pitch, h->first, t, fx,
+                                       fy, h->last_stream, &h->launches);
+            src = field == F_TAU ? t : (field == F_FX ? fx : fy);
+        }
         if ((rc = sync_last(h))) return rc;
-        cudaError_t e = to_host(h, out, h->S.fld[field]);
+        cudaError_t e = to_host(h, out, src);
         if (e != cudaSuccess) return cuda_fail(h, e, "download field");
         return DUGKS_OK;
     }
@@ -678,6 +699,7 @@ extern "C" int dugks_gpu_destroy(dugks_handle_t *h) {
     if (!h) return DUGKS_OK;
     cudaStreamSynchronize(h->last_stream);
     cudaFree(h->arena);
+    if (h->out3) cudaFree(h->out3);
     delete h;
     return DUGKS_OK;
 }

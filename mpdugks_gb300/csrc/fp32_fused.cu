@@ -887,6 +887,57 @@ template cudaError_t launch_plane_from_f64<float>(float *, int, const double *, 
 template cudaError_t launch_plane_from_f64<double>(double *, int, const double *, int, int, double, cudaStream_t,
                                                    int64_t *);
 
+// tau, Fx, Fy of a deviation-storage case in FP64, for output: tau is Tau0
+// after the first step (before it, the initialisation's, in the init planes);
+// F = mu grad(phi) (+ gravity) with the MacroSource stencil
+// (Ark/Cpp/SourceM.cpp:35-62) on the FP64 phi field, wall ghost rows
+// extrapolated as 2 phi_0 - phi_1 (Ark/Cpp/Boundary.cpp:38-63).
+template <typename R>
+__global__ void __launch_bounds__(256) k_out_forces(PR<R> P, const double *__restrict__ phi,
+                                                    const double *__restrict__ rho, int opitch,
+                                                    const R *__restrict__ init_tau, int first, double *tau,
+                                                    double *fx, double *fy) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= P.nx || j >= P.ny) return;
+    auto at = [&](int ii, int jj) -> double {
+        ii = wrapi(ii, P.nx);
+        if (P.walls) {
+            if (jj < 0) return 2.0 * phi[(size_t)ii] - phi[(size_t)opitch + ii];
+            if (jj >= P.ny)
+                return 2.0 * phi[(size_t)(P.ny - 1) * opitch + ii] - phi[(size_t)(P.ny - 2) * opitch + ii];
+        } else {
+            jj = wrapi(jj, P.ny);
+        }
+        return phi[(size_t)jj * opitch + ii];
+    };
+    const double c = at(i, j), E = at(i + 1, j), W = at(i - 1, j), N = at(i, j + 1), S = at(i, j - 1);
+    const double NE = at(i + 1, j + 1), NW = at(i - 1, j + 1), SE = at(i + 1, j - 1), SW = at(i - 1, j - 1);
+    double gx = (4.0 * (E - W) + ((NE - NW) + (SE - SW))) * (double)P.inv_12dx;
+    double gy = (4.0 * (N - S) + ((NE - SE) + (NW - SW))) * (double)P.inv_12dy;
+    const double lap = (4.0 * ((E + W) + (N + S)) + ((NE + SW) + (NW + SE)) - 20.0 * c) * (double)P.inv_6dd;
+    if (fabs(gx) < DUGKS_F32_GCLAMP) gx = 0.0;
+    if (fabs(gy) < DUGKS_F32_GCLAMP) gy = 0.0;
+    const double PhiL = P.PhiL, PhiV = P.PhiV;
+    const double F = 2.0 * (double)P.Beta * (c - PhiL) * (c - PhiV) * (2.0 * c - PhiL - PhiV) - (double)P.Kappa * lap;
+    const size_t o = (size_t)j * opitch + i;
+    fx[o] = F * gx;
+    fy[o] = F * gy - (P.gravity ? (double)P.Gy * (rho[o] - (double)P.RhoL) : 0.0);
+    tau[o] = first ? (double)init_tau[(size_t)j * P.pitch + i] : (double)P.tauf;
+}
+
+template <typename R>
+void launch_out_forces(const PR<R> &P, const SR<R> &S, const double *phi, const double *rho, int opitch, int first,
+                       double *tau, double *fx, double *fy, cudaStream_t st, int64_t *launches) {
+    const dim3 blk(32, 8);
+    const dim3 grd((P.nx + 31) / 32, (P.ny + 7) / 8);
+    k_out_forces<R><<<grd, blk, 0, st>>>(P, phi, rho, opitch, S.init + (size_t)I_TAU * S.qs, first, tau, fx, fy);
+    *launches += 1;
+}
+template void launch_out_forces<float>(const PR<float> &, const SR<float> &, const double *, const double *, int, int,
+                                       double *, double *, double *, cudaStream_t, int64_t *);
+template void launch_out_forces<double>(const PR<double> &, const SR<double> &, const double *, const double *, int,
+                                        int, double *, double *, double *, cudaStream_t, int64_t *);
+
 template <int MODEL, bool WALLS, typename R>
 static cudaError_t launch_t(const PR<R> &P, const SR<R> &S, int first, int gin, int gout, cudaStream_t st,
                             uint32_t step) {

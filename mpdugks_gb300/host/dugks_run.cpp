@@ -1,0 +1,163 @@
+// dugks_run: the host-side solver driver around libdugks_gpu.so, the GPU
+// counterpart of the reference's main() + DUGKS2DSolver()
+// (Ark/Cpp/main.cpp:134, Ark/Cpp/DUGKS2DSolver.cpp:148-337).
+//
+//   dugks_run run <Case.ark> [--out DIR] [--precision P] [--steps N]
+//                 [--set key=value ...]
+//       Reads the case from a Case.ark (the reference's OutputCase layout),
+//       initialises it on the GPU, writes DIR/Case.ark and the FlowField at
+//       step 0, then steps until End_Step (or --steps) or until the density
+//       residual, evaluated every ResidualControl steps, falls below
+//       RESIDUAL; FlowField files every writeFileControl steps and at the end
+//       (DIR/global/, the reference's names and layout).
+//   dugks_run rewrite-ark <in> <out>        parse a Case.ark and write it back
+//   dugks_run rewrite-flowfield <in> <out>  parse a FlowField file and write it back
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <sys/stat.h>
+#include <vector>
+
+#include "../../include/dugks_gpu.h"
+#include "case_ark.hpp"
+#include "flowfield.hpp"
+
+using namespace dugks_host;
+
+namespace {
+
+void check(dugks_handle_t *h, int rc, const char *what) {
+    if (rc == DUGKS_OK) return;
+    char buf[512] = {0};
+    dugks_gpu_last_error(h, buf, sizeof(buf));
+    throw std::runtime_error(std::string(what) + ": " + buf);
+}
+
+void make_dir(const std::string &d) {
+    if (mkdir(d.c_str(), 0755) != 0) {
+        struct stat st;
+        if (stat(d.c_str(), &st) != 0 || !S_ISDIR(st.st_mode)) throw std::runtime_error("cannot create " + d);
+    }
+}
+
+FlowField fields(dugks_handle_t *h, const RunConfig &c) {
+    FlowField ff;
+    ff.cells = (size_t)c.grid.nx * c.grid.ny;
+    for (auto *v : {&ff.rho, &ff.u, &ff.v, &ff.p, &ff.T, &ff.phi, &ff.tau, &ff.fx, &ff.fy}) v->assign(ff.cells, 0.0);
+    check(h, dugks_gpu_download(h, ff.rho.data(), ff.u.data(), ff.v.data(), ff.phi.data(), ff.p.data()), "download");
+    check(h, dugks_gpu_get_field(h, DUGKS_F_TAU, ff.tau.data()), "tau");
+    check(h, dugks_gpu_get_field(h, DUGKS_F_FX, ff.fx.data()), "Fx");
+    check(h, dugks_gpu_get_field(h, DUGKS_F_FY, ff.fy.data()), "Fy");
+    ff.T.assign(ff.cells, c.T0);  // isothermal models keep the reference temperature
+    return ff;
+}
+
+void output(dugks_handle_t *h, const RunConfig &c, const std::string &dir, int64_t step) {
+    const std::string path =
+        dir + "/global/" + flowfield_name(step, (double)step * c.dt, c.mach, c.mesh_type, c.nl, c.cfl);
+    write_flowfield(path, fields(h, c));
+}
+
+int run(int argc, char **argv) {
+    if (argc < 3) throw std::runtime_error("run: missing Case.ark");
+    CaseArk ark = read_case_ark(argv[2]);
+    std::string out = "FlowField";
+    int64_t steps_override = -1;
+    for (int k = 3; k < argc; ++k) {
+        const std::string a = argv[k];
+        auto next = [&]() -> std::string {
+            if (k + 1 >= argc) throw std::runtime_error(a + ": missing value");
+            return argv[++k];
+        };
+        if (a == "--out") out = next();
+        else if (a == "--precision") ark.set("precision", next());
+        else if (a == "--steps") steps_override = std::atoll(next().c_str());
+        else if (a == "--set") {
+            const std::string kv = next();
+            const size_t eq = kv.find('=');
+            if (eq == std::string::npos) throw std::runtime_error("--set wants key=value");
+            ark.set(kv.substr(0, eq), kv.substr(eq + 1));
+        } else throw std::runtime_error("unknown option " + a);
+    }
+    RunConfig c = config_from_case_ark(ark);
+    if (steps_override >= 0) c.end_step = steps_override;
+    make_dir(out);
+    make_dir(out + "/global");
+    write_case_ark(out + "/Case.ark", ark);
+
+    dugks_handle_t *h = nullptr;
+    int rc = dugks_gpu_create(&c.cs, &c.grid, &h);
+    if (rc != DUGKS_OK) check(nullptr, rc, "create");
+    try {
+        check(h, dugks_gpu_init(h, c.init_kind, c.init_params.empty() ? nullptr : c.init_params.data(),
+                                (int)c.init_params.size(), c.seed),
+              "init");
+        output(h, c, out, 0);
+        std::printf("iteration start    cells : %d x %d    steps : %lld\n", c.grid.nx, c.grid.ny,
+                    (long long)c.end_step);
+        int64_t step = 0;
+        double residual = 1.0;
+        while (step < c.end_step && residual > c.residual_stop) {
+            // up to the next residual / output point
+            int64_t n = c.residual_every - step % c.residual_every;
+            const int64_t to_write = c.write_every - step % c.write_every;
+            if (to_write < n) n = to_write;
+            if (c.end_step - step < n) n = c.end_step - step;
+            check(h, dugks_gpu_step(h, (int)n, nullptr), "step");
+            step += n;
+            if (step % c.residual_every == 0) {
+                dugks_reductions_t r{};
+                check(h, dugks_gpu_reduce(h, &r), "reduce");
+                residual = r.residual;
+                std::printf("%lld    %.6g    %.12e    %.6e\n", (long long)step, (double)step * c.dt, r.sum_rho,
+                            r.residual);
+                std::fflush(stdout);
+            }
+            if (step % c.write_every == 0 && step < c.end_step) output(h, c, out, step);
+        }
+        output(h, c, out, step);
+        std::printf("iteration End    step : %lld\n", (long long)step);
+    } catch (...) {
+        dugks_gpu_destroy(h);
+        throw;
+    }
+    dugks_gpu_destroy(h);
+    return 0;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    try {
+        if (argc >= 2 && std::strcmp(argv[1], "run") == 0) return run(argc, argv);
+        if (argc == 4 && std::strcmp(argv[1], "rewrite-ark") == 0) {
+            write_case_ark(argv[3], read_case_ark(argv[2]));
+            return 0;
+        }
+        if (argc == 4 && std::strcmp(argv[1], "rewrite-flowfield") == 0) {
+            write_flowfield(argv[3], read_flowfield(argv[2]));
+            return 0;
+        }
+        if (argc == 3 && std::strcmp(argv[1], "show-config") == 0) {
+            const RunConfig c = config_from_case_ark(read_case_ark(argv[2]));
+            std::printf("model %d precision %d nx %d ny %d walls %d init %d nparams %zu steps %lld Mu0 %.17g "
+                        "M_Phi %.17g W %.17g Sigma %.17g RhoL %.17g RhoV %.17g Gy %.17g\n",
+                        c.cs.model, c.cs.precision, c.grid.nx, c.grid.ny, c.grid.y_walls, c.init_kind,
+                        c.init_params.size(), (long long)c.end_step, c.cs.Mu0, c.cs.M_Phi, c.cs.W, c.cs.Sigma,
+                        c.cs.RhoL, c.cs.RhoV, c.cs.Gy);
+            for (double p : c.init_params) std::printf("param %.17g\n", p);
+            return 0;
+        }
+        std::fprintf(stderr,
+                     "usage: dugks_run run <Case.ark> [--out DIR] [--precision P] [--steps N] [--set k=v]...\n"
+                     "       dugks_run rewrite-ark <in> <out>\n"
+                     "       dugks_run rewrite-flowfield <in> <out>\n"
+                     "       dugks_run show-config <Case.ark>\n");
+        return 2;
+    } catch (const std::exception &e) {
+        std::fprintf(stderr, "dugks_run: %s\n", e.what());
+        return 1;
+    }
+}

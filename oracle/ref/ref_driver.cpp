@@ -10,7 +10,9 @@
 //
 // Deliberate differences from the reference loop:
 //  * fixed step count instead of the residual stop;
-//  * no Output_* calls (file output is not part of the parity check);
+//  * Output_* is called only with REF_FLOWFIELD set in the environment: the
+//    reference's Case.ark and FlowField writers at step 0 and after the
+//    last step (golden files for the host reader and writer tests);
 //  * the pseudopotential face force (Ark/Cpp/PseudoP.cpp:39-46) reads the
 //    face psi of neighbouring faces while the same loop writes them (a data
 //    race at >1 thread, order-dependent at 1 thread).  Here the face loop is
@@ -58,6 +60,8 @@ extern void Update_DVDF_Source_h(Face_2D &face);
 extern void MacroSource(Cell_2D *cellptr);
 extern void Update_PseudoForce(Cell_2D &cell);
 extern void Update_PseudoForce(Face_2D &face);
+extern void OutputCase();
+extern void Output_Flowfield(double const &t, int step);
 extern void WallShadowC_fBP(Cell_2D &shadowCell);
 extern void Wall_3_BB(Face_2D &face);
 
@@ -332,6 +336,13 @@ int main(int argc, char **argv) {
         fprintf(stderr, "unknown init %s\n", init.c_str());
         return 2;
     }
+    // REF_FLOWFIELD set: the reference's own Case.ark and FlowField writers, at
+    // step 0 and after the last step (into ../FlowField relative to the cwd)
+    const bool flowfield = getenv("REF_FLOWFIELD") != nullptr;
+    if (flowfield) {
+        OutputCase();
+        Output_Flowfield(0.0, 0);
+    }
     if (every > 0) dump((dumpbase + ".0").c_str(), 0);
     auto t0 = std::chrono::steady_clock::now();
     for (int s = 1; s <= nsteps; ++s) {
@@ -347,5 +358,6 @@ int main(int argc, char **argv) {
     printf("done steps %d cells %d seconds %.6f mlups %.4f sumrho %.15e\n", nsteps, Cells, secs,
            nsteps > 0 ? 1e-6 * Cells * (double)nsteps / secs : 0.0, sum_rho());
     dump(dumpbase.c_str(), nsteps);
+    if (flowfield) Output_Flowfield(nsteps * dt, nsteps);
     return 0;
 }

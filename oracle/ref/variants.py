@@ -38,6 +38,10 @@ VARIANTS = {
     'hcz_rt': dict(model='D2Q9HCZ', nx=16, ny=64, walls=True, init='ac_rt',
                    consts=dict(Mu0=0.01, M_Phi=0.05, W=4.0, Sigma=1e-4, RhoL=3.0, RhoV=1.0,
                                Gy=1e-4)),
+    # The reference's own AC_Drop init (light bubble, case name AC_Drop) on a
+    # small grid: golden Case.ark / FlowField files of the reference writers.
+    'ac_ff': dict(model='D2Q9AC', nx=32, ny=24, walls=False, init='ac_drop',
+                  consts=dict(Mu0=0.02, W=4.0, Sigma=1e-3, RhoL=1.0, RhoV=0.1, radius=7.0)),
     # Pseudopotential D2Q9 with the reference's own SCMP_Drop init.
     'pp_drop': dict(model='D2Q9PP', nx=32, ny=32, walls=False, init='scmp_drop', consts={}),
 }

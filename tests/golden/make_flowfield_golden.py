@@ -1,0 +1,45 @@
+"""Golden Case.ark and FlowField files written by the reference's own writers.
+
+OutputCase (Ark/Cpp/Output.cpp:65-141) and Output_Flowfield
+(Ark/Cpp/Output.cpp:541-606) run inside the reference driver
+(oracle/ref/ref_driver.cpp, with REF_FLOWFIELD set) for a few steps of two
+small cases: the reference's AC_Drop init on a 32x24 periodic grid (ac_ff)
+and a 16x64 Rayleigh-Taylor box with walls (hcz_rt).  The files land in
+tests/golden/flowfield/<case>/ (FlowField .dat files gzip-compressed).
+Needs the reference sources, so it runs only where they are present:
+
+    python tests/golden/make_flowfield_golden.py
+"""
+import gzip
+import shutil
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT / 'oracle' / 'ref'))
+
+import build_ref  # noqa: E402
+
+STEPS = {'ac_ff': 20, 'hcz_rt': 20}
+
+
+def main() -> None:
+    for name, steps in STEPS.items():
+        build_ref.build(name)
+        vdir = build_ref.OUT / name
+        ff = vdir / 'FlowField'
+        shutil.rmtree(ff, ignore_errors=True)
+        (ff / 'global').mkdir(parents=True)
+        build_ref.run(name, steps, threads=1, extra_env={'REF_FLOWFIELD': '1'})
+        out = ROOT / 'tests' / 'golden' / 'flowfield' / name
+        shutil.rmtree(out, ignore_errors=True)
+        out.mkdir(parents=True)
+        shutil.copy(ff / 'Case.ark', out / 'Case.ark')
+        for f in sorted((ff / 'global').glob('*.dat')):
+            with open(f, 'rb') as src, gzip.GzipFile(out / (f.name + '.gz'), 'wb', mtime=0) as dst:
+                shutil.copyfileobj(src, dst)
+        print(name, sorted(p.name for p in out.iterdir()))
+
+
+if __name__ == '__main__':
+    main()
