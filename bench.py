@@ -50,10 +50,10 @@ WORKLOADS = {
 #   FP32 storage, HCZ: 18 deviations + 6 aux planes, 4 B each, read and written = 192 B
 #   FP64 (multi-kernel step): 18 distributions + 2 aux planes, 8 B, read and written = 320 B
 ALGO_BYTES = {'fp32dev': 192, 'fp64': 320, 'fp64fma': 320, 'fp64fused': 384}
-# DRAM bytes per cell and step of the fused FP32 kernel, ncu dram__bytes_read.sum +
-# dram__bytes_write.sum of one k_step32 launch on 2048x2048 / cells
-# (profiles/k_step32_rt2048_fp32.md)
-TRAFFIC_BYTES = {'fp32dev': None}
+# DRAM bytes per cell and step of the fused FP32 kernel: ncu dram__bytes_read.sum +
+# dram__bytes_write.sum of one k_step32 launch on 2048x2048 cells, divided by the cells
+# (profiles/k_step32_rt2048x2048_fp32.md); scaled by the cell count to a full launch
+TRAFFIC_BYTES = {'fp32dev': (402.798848e6 + 354.459904e6) / (2048 * 2048)}
 
 
 def case_kw(wl: dict) -> dict:
@@ -393,6 +393,8 @@ def run_ours(args, wl, rank, world, local):
     roofline = {'bound': 'hbm', 'achieved': round(achieved, 2), 'peak': hbm_peak, 'unit': 'GB/s',
                 'frac': round(achieved / hbm_peak, 5),
                 'traffic': None if traffic is None else int(traffic * cells),
+                'traffic_source': None if traffic is None else 'ncu DRAM bytes of one launch at 2048x2048, '
+                                                               'scaled by the cell count',
                 'kernel': kernel, 'algorithmic_bytes_per_cell': algo,
                 'cells_per_launch': cells, 'peak_source': f'{peak_kind} hbm_gbs (copy bandwidth)'}
     if phase:
