@@ -40,6 +40,8 @@ cudaError_t launch_step64f(const PR<double> &P, const SR<double> &S, int first, 
                            cudaStream_t st, int64_t *launches, uint32_t step);
 void launch_macros64f(const PR<double> &P, const SR<double> &S, double *rho, double *u, double *v, double *p,
                       double *phi, int opitch, cudaStream_t st, int64_t *launches);
+cudaError_t launch_stream32(const P32 &P, const S32 &S, int first, int gin, int gout, cudaStream_t st,
+                            int64_t *launches, uint32_t step);
 template <typename R>
 cudaError_t launch_plane_from_f64(R *dst, int dpitch, const double *src, int nx, int ny, double sub,
                                   cudaStream_t st, int64_t *launches);
@@ -459,10 +461,11 @@ extern "C" int dugks_gpu_step(dugks_handle_t *h, int nsteps, void *stream) {
     if (h->fp32) {
         for (int s = 0; s < nsteps; ++s) {
             const uint32_t sn = (uint32_t)(h->steps + s);
+            // FP32 storage: the streaming kernel; the FP64 instance of the fused step: the tile kernel
             cudaError_t e = h->fused64 ? f32::launch_stepX(h->P64f, h->S64f, h->first, h->gcur, h->gcur ^ 1, st,
                                                            &h->launches, sn)
-                                       : f32::launch_stepX(h->P32, h->S32, h->first, h->gcur, h->gcur ^ 1, st,
-                                                           &h->launches, sn);
+                                       : f32::launch_stream32(h->P32, h->S32, h->first, h->gcur, h->gcur ^ 1, st,
+                                                              &h->launches, sn);
             if (e != cudaSuccess) return cuda_fail(h, e, "fp32 step launch");
             if (h->fused64) f32::swap_io(h->S64f);
             else f32::swap_io(h->S32);

@@ -32,6 +32,7 @@
 
 #include "dugks_device.cuh"
 #include "fp32_state.cuh"
+#include "fp32_math.cuh"
 
 namespace dugks {
 namespace f32 {
@@ -39,203 +40,6 @@ namespace f32 {
 constexpr int TW = 30, TH = 14;  // interior tile
 constexpr int BX = 32, BY = 16;  // threads = tile + halo ring
 
-// Knuth two-sum accumulation (float-float for R = float)
-template <typename R>
-struct FFs {
-    R hi = 0, lo = 0;
-    __device__ __forceinline__ void add(R b) {
-        const R s = hi + b;
-        const R bb = s - hi;
-        const R err = (hi - (s - bb)) + (b - bb);
-        hi = s;
-        lo += err;
-    }
-    __device__ __forceinline__ R value() const { return hi + lo; }
-};
-
-template <typename R>
-__device__ __forceinline__ R sxf(int s, R x) { return s > 0 ? x : (s < 0 ? -x : R(0)); }
-
-// sum of directions 1..8 (E,NE,N,NW,W,SW,S,SE) in an order that every mirror of
-// the lattice maps onto itself: ((E+W)+(N+S)) + ((NE+SW)+(NW+SE))
-template <typename R>
-__device__ __forceinline__ R sym8(const R *a) {
-    return ((a[1] + a[5]) + (a[3] + a[7])) + ((a[2] + a[6]) + (a[4] + a[8]));
-}
-__device__ __forceinline__ float rsq(float x) { return rsqrtf(x); }
-
-// 32-bit integer hash (per cell and step random bits for stochastic rounding)
-__device__ __forceinline__ uint32_t mix32(uint32_t x) {
-    x ^= x >> 16;
-    x *= 0x7feb352dU;
-    x ^= x >> 15;
-    x *= 0x846ca68bU;
-    x ^= x >> 16;
-    return x;
-}
-__device__ __forceinline__ double rsq(double x) { return 1.0 / sqrt(x); }
-__device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
-
-// Macroscopic state of one cell after the update of the previous step
-// (Update_MacroVar), from its deviations; HCZ needs the previous force and
-// density gradient (aux), AC has u = 0.
-template <int MODEL, typename R>
-__device__ __forceinline__ void cell_macros(const PR<R> &P, const R *df, const R *dh, R fx_old,
-                                            R fy_old, R rx_old, R ry_old, R &dphi, R &rho,
-                                            R &U, R &V, R &dp) {
-    FFs<R> sh, sf, su, sv;
-#pragma unroll
-    for (int q = 0; q < 9; ++q) sh.add(dh[q]);  // two-sum: exact to 2^-48, order-independent after rounding
-    dphi = sh.value();
-    const R phi = P.phi0 + dphi;
-    rho = P.aPhi * phi + P.bPhi;
-    if (MODEL == AC) {
-#pragma unroll
-        for (int q = 1; q < 9; ++q) sf.add(df[q]);
-        U = R(0.);
-        V = R(0.);
-        dp = sf.value() * P.Kp;
-    } else {
-#pragma unroll
-        for (int q = 0; q < 9; ++q) {
-            sf.add(df[q]);
-            if (d2q9_xu(q)) su.add(sxf(d2q9_xu(q), df[q]));
-            if (d2q9_xv(q)) sv.add(sxf(d2q9_xv(q), df[q]));
-        }
-        const R inv = R(1.) / (rho * P.RT);
-        U = su.value() * inv + P.hDt * fx_old * inv;
-        V = sv.value() * inv + P.hDt * fy_old * inv;
-        dp = sf.value() + P.hDt * (rx_old * U + ry_old * V) * P.RT;
-    }
-}
-
-// MacroSource (Ark/Cpp/SourceM.cpp:35-62) on the shared phi tile.
-template <typename R>
-__device__ __forceinline__ void macro_source32(const PR<R> &P, const R (*sphi)[BX + 2], int r, int e, R phi,
-                                               R rho, R U, R V, R ppu, R ppv, R &srcx,
-                                               R &srcy, R &rhox, R &rhoy, R &fx, R &fy) {
-    // sphi[r+1][e+1] is this cell
-    const R E = sphi[r + 1][e + 2], W = sphi[r + 1][e], N = sphi[r + 2][e + 1], S = sphi[r][e + 1];
-    const R NE = sphi[r + 2][e + 2], NW = sphi[r + 2][e], SE = sphi[r][e + 2], SW = sphi[r][e];
-    // mirror-symmetric association: x -> -x maps every sum onto its exact negation
-    R gx = (R(4.) * (E - W) + ((NE - NW) + (SE - SW))) * P.inv_12dx;
-    R gy = (R(4.) * (N - S) + ((NE - SE) + (NW - SW))) * P.inv_12dy;
-    const R lap = (R(4.) * ((E + W) + (N + S)) + ((NE + SW) + (NW + SE)) - R(20.) * phi) * P.inv_6dd;
-    if (fabs(gx) < R(DUGKS_F32_GCLAMP)) gx = R(0.);
-    if (fabs(gy) < R(DUGKS_F32_GCLAMP)) gy = R(0.);
-    const R F = R(2.) * P.Beta * (phi - P.PhiL) * (phi - P.PhiV) * (R(2.) * phi - P.PhiL - P.PhiV) - P.Kappa * lap;
-    rhox = P.aPhi * gx;
-    rhoy = P.aPhi * gy;
-    fx = F * gx;
-    fy = F * gy;
-    if (P.gravity) fy -= P.Gy * (rho - P.RhoL);
-    const R L2 = gx * gx + gy * gy;
-    const R dU = phi * U - ppu, dV = phi * V - ppv;
-    if (L2 != R(0.)) {
-        const R tmp = -R(4.) * (phi - P.PhiL) * (phi - P.PhiV) * P.inv_wI_dphi;
-        const R k = tmp * rsq(L2);
-        srcx = gx * k + dU * P.inv_RTdt;
-        srcy = gy * k + dV * P.inv_RTdt;
-    } else {
-        srcx = dU * P.inv_RTdt;
-        srcy = dV * P.inv_RTdt;
-    }
-}
-
-// ---- packed pairs: every per-direction quantity of the step is carried as the
-// pair (flow f_q, phase field h_q); for R = float the pair arithmetic is the
-// sm_100+ packed FP32x2 instructions (one issue slot for two lanes' worth).
-template <typename R> struct Pair;
-template <> struct Pair<float> { using T = float2; };
-template <> struct Pair<double> { using T = double2; };
-
-__device__ __forceinline__ float2 mk2(float a, float b) { return make_float2(a, b); }
-__device__ __forceinline__ double2 mk2(double a, double b) { return make_double2(a, b); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ double2 add2(double2 a, double2 b) { return make_double2(__dadd_rn(a.x, b.x), __dadd_rn(a.y, b.y)); }
-__device__ __forceinline__ double2 sub2(double2 a, double2 b) { return make_double2(__dsub_rn(a.x, b.x), __dsub_rn(a.y, b.y)); }
-__device__ __forceinline__ double2 mul2(double2 a, double2 b) { return make_double2(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)); }
-__device__ __forceinline__ double2 fma2(double2 a, double2 b, double2 c) {
-    return make_double2(__fma_rn(a.x, b.x, c.x), __fma_rn(a.y, b.y, c.y));
-}
-template <typename T> __device__ __forceinline__ T neg2(T a) { return mk2(-a.x, -a.y); }
-// x * s for a compile-time sign s in {-1, 0, 1}
-template <int S, typename T> __device__ __forceinline__ T sgn2(T a) { return S > 0 ? a : (S < 0 ? neg2(a) : mk2(decltype(a.x)(0), decltype(a.x)(0))); }
-
-// Knuth two-sum accumulation of pairs
-template <typename T>
-struct FF2 {
-    T hi, lo;
-    __device__ __forceinline__ void init(T b) { hi = b; lo = mk2(decltype(b.x)(0), decltype(b.x)(0)); }
-    __device__ __forceinline__ void add(T b) {
-        const T s = add2(hi, b);
-        const T bb = sub2(s, hi);
-        const T err = add2(sub2(hi, sub2(s, bb)), sub2(b, bb));
-        hi = s;
-        lo = add2(lo, err);
-    }
-    __device__ __forceinline__ T value() const { return add2(hi, lo); }
-};
-
-// mirror-symmetric sum of directions 1..8 (see sym8)
-template <typename T>
-__device__ __forceinline__ T sym8p(const T *a) {
-    return add2(add2(add2(a[1], a[5]), add2(a[3], a[7])), add2(add2(a[2], a[6]), add2(a[4], a[8])));
-}
-
-// Stochastic rounding of the pair a + b into storage.  The exact sum is
-// s + err (two-sum); each lane moves to its neighbour toward err with
-// probability |err| / spacing, drawn from 16 random bits.  Without it a state
-// that is nearly steady repeats the same FP32 rounding every step and the
-// error grows linearly with the step count; with it the rounding errors are
-// unbiased and uncorrelated (random-walk growth).
-__device__ __forceinline__ float sr_lane(float s, float err, uint32_t bits16) {
-    if (err == 0.f) return s;
-    // neighbour of s toward err (s != 0 here: a + b == 0 is exact)
-    const int away = ((err > 0.f) == (s > 0.f)) ? 1 : -1;
-    const float nb = __int_as_float(__float_as_int(s) + away);
-    const float u = __int_as_float(0x3F800000u | (bits16 << 7)) - 1.0f;  // [0, 1)
-    return (u * fabsf(nb - s) < fabsf(err)) ? nb : s;
-}
-__device__ __forceinline__ float2 add_sr2(float2 a, float2 b, uint32_t bits) {
-    const float2 s = add2(a, b);
-    const float2 bb = sub2(s, a);
-    const float2 err = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
-    return make_float2(sr_lane(s.x, err.x, bits & 0xFFFFu), sr_lane(s.y, err.y, bits >> 16));
-}
-__device__ __forceinline__ double2 add_sr2(double2 a, double2 b, uint32_t) { return add2(a, b); }
-
-__device__ __forceinline__ float rcp(float x) { return __frcp_rn(x); }
-__device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
-
-// direction slots of the faces: the six directions with a non-zero normal velocity
-__host__ __device__ constexpr int xslot(int q) { return q == 1 ? 0 : q == 2 ? 1 : q == 4 ? 2 : q == 5 ? 3 : q == 6 ? 4 : q == 8 ? 5 : -1; }
-__host__ __device__ constexpr int yslot(int q) { return q == 2 ? 0 : q == 3 ? 1 : q == 4 ? 2 : q == 6 ? 3 : q == 7 ? 4 : q == 8 ? 5 : -1; }
-
-// Equilibrium deviations and the force terms of direction q != 0, as pairs
-// (f, h): Eq = w (dp + rho RT G, dphi + u1 phi) (HCZ) or w (dp/RT, dphi) (AC);
-// So = (w ((1+G)(c.F) + G RT (c.grad rho)), w (xi.src)) with c = xi - u.
-template <int MODEL, int Q, typename R>
-__device__ __forceinline__ void eq_src(const PR<R> &P, R U, R V, R uu, R rho, R phi, R dp, R dphi, R fx, R fy,
-                                       R rx, R ry, R sx_, R sy_, typename Pair<R>::T &Eq,
-                                       typename Pair<R>::T &So) {
-    constexpr int xu = d2q9_xu(Q), xv = d2q9_xv(Q);
-    const R wq = (R)d2q9_w(Q);
-    const R hS = wq * (sxf(xu, sx_) + sxf(xv, sy_));
-    if (MODEL == AC) {
-        Eq = mk2(wq * (dp * P.invRT), wq * dphi);
-        So = mk2(wq * ((sxf(xu, fx) + sxf(xv, fy)) * P.invRT), hS);
-    } else {
-        const R u1 = (sxf(xu, U) + sxf(xv, V)) * P.invRT;
-        const R G = u1 + R(0.5) * u1 * u1 - uu * P.Lambda0;
-        const R cu = (R)xu - U, cv = (R)xv - V;
-        Eq = mul2(mk2(wq, wq), fma2(mk2(rho * P.RT, phi), mk2(G, u1), mk2(dp, dphi)));
-        So = mk2(wq * ((R(1.) + G) * (cu * fx + cv * fy) + G * P.RT * (cu * rx + cv * ry)), hS);
-    }
-}
 
 constexpr size_t SMEM_ELEMS = (size_t)(BY + 2) * (BX + 2) + (18 + 6 + 12) * BY * BX;
 // Prefetch staging (storage type float only): the next tile's own-cell planes
@@ -248,16 +52,6 @@ constexpr bool prefetched() { return sizeof(R) == 4; }
 template <typename R>
 constexpr size_t smem_elems() { return SMEM_ELEMS + (prefetched<R>() ? STG_ELEMS : 0); }
 
-template <typename R>
-__device__ __forceinline__ void cp_async(R *smem, const R *gmem) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    if (sizeof(R) == 4)
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
-    else
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // Geometry of tile t as seen by thread (e, r): the tile's interior origin and
 // size, and this thread's extended cell (interior plus a one-cell ring).
@@ -418,109 +212,24 @@ __device__ __forceinline__ void tile_step(const PR<R> &P, const SR<R> &S, int fi
     __syncthreads();
 
     // ---- stage 1: macros, MacroSource, f-bar-plus of every real cell of the region
-    R phi = P.phi0 + dphi, rho = R(0.), U = R(0.), V = R(0.), dp = R(0.);
-    R srcx = R(0.), srcy = R(0.), rhox = R(0.), rhoy = R(0.), fx = R(0.), fy = R(0.);
+    R phi = P.phi0 + dphi, U = R(0.), V = R(0.);
     T inc[9];  // collision increments B - T of this cell
+    R src[6];
     if (real) {
-        R aBP, cBP, rxo = R(0.), ryo = R(0.);
-        if (first) {
-            // first step after an initialisation: the reference uses the state the
-            // initialisation left (p0, zero forces, tau from Mu0), as uploaded
-            const R *I = S.init;
-            const size_t ps = S.qs;
-            phi = P.phi0 + I[I_DPHI * ps + c];
-            rho = I[I_RHO * ps + c];
-            U = I[I_U * ps + c];
-            V = I[I_V * ps + c];
-            dp = I[I_DP * ps + c];
-            srcx = I[I_SRCX * ps + c];
-            srcy = I[I_SRCY * ps + c];
-            rhox = I[I_RHOX * ps + c];
-            rhoy = I[I_RHOY * ps + c];
-            fx = I[I_FX * ps + c];
-            fy = I[I_FY * ps + c];
-            const R tau = I[I_TAU * ps + c];
-            aBP = (R(2.) * tau - P.hDt) / (R(2.) * tau + P.dt);
-            cBP = tau * (R(1.) - aBP);
-        } else {
-            rho = P.aPhi * phi + P.bPhi;
-            R ppu = R(0.), ppv = R(0.);
-            if (MODEL == AC) {
-                dp = sfz * P.Kp;
-            } else {
-                R a6[A_N];
+        R a6[A_N];
+        if (MODEL != AC && !first) {
 #pragma unroll
-                for (int k = 0; k < A_N; ++k)
-                    a6[k] = staged ? stg[((18 + k) * BY + r) * BX + e] : S.aux[(size_t)k * S.qs + c];
-                const R fxo = a6[A_FX], fyo = a6[A_FY];
-                rxo = a6[A_RHOX];
-                ryo = a6[A_RHOY];
-                ppu = a6[A_PPU];
-                ppv = a6[A_PPV];
-                // first moments as a float-float pair (sum xi_x f, sum xi_y f)
-                FF2<T> m;
-                m.init(mk2(Pq[1].x, R(0.)));
-                m.add(mk2(Pq[2].x, Pq[2].x));
-                m.add(mk2(R(0.), Pq[3].x));
-                m.add(mk2(-Pq[4].x, Pq[4].x));
-                m.add(mk2(-Pq[5].x, R(0.)));
-                m.add(mk2(-Pq[6].x, -Pq[6].x));
-                m.add(mk2(R(0.), -Pq[7].x));
-                m.add(mk2(Pq[8].x, -Pq[8].x));
-                const T mv = m.value();
-                const R inv = rcp(rho * P.RT);
-                U = mv.x * inv + P.hDt * fxo * inv;
-                V = mv.y * inv + P.hDt * fyo * inv;
-                dp = sfz + P.hDt * (rxo * U + ryo * V) * P.RT;
-            }
-            macro_source32(P, sphi, r, e, phi, rho, U, V, ppu, ppv, srcx, srcy, rhox, rhoy, fx, fy);
-            aBP = P.aBP_f;  // tau is constant after the first step (nu_L = nu_V)
-            cBP = P.tauf * (R(1.) - aBP);
+            for (int k = 0; k < A_N; ++k)
+                a6[k] = staged ? stg[((18 + k) * BY + r) * BX + e] : S.aux[(size_t)k * S.qs + c];
         }
-        const R bBP = R(1.) - aBP;
-        const R uu = U * U + V * V;
-        // dphi itself, not (phi0 + dphi) - phi0: one rounding less in the zeroth moment
-        const R dphi_c = first ? phi - P.phi0 : dphi;
-        // equilibria of q != 0; q = 0 from the exact zeroth moment (sum dEq = dp for
-        // HCZ, 0 for AC; sum dhEq = dphi), so FP32 weights cannot leak mass
-        T Eq[9], So[9];
-        eq_src<MODEL, 1>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[1], So[1]);
-        eq_src<MODEL, 2>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[2], So[2]);
-        eq_src<MODEL, 3>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[3], So[3]);
-        eq_src<MODEL, 4>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[4], So[4]);
-        eq_src<MODEL, 5>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[5], So[5]);
-        eq_src<MODEL, 6>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[6], So[6]);
-        eq_src<MODEL, 7>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[7], So[7]);
-        eq_src<MODEL, 8>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[8], So[8]);
-        const T sEq = sym8p(Eq);
-        Eq[0] = sub2(mk2(MODEL == AC ? R(0.) : dp, dphi_c), sEq);
-        if (MODEL == AC) {
-            So[0] = mk2(R(0.), R(0.));
-        } else {
-            const R G0 = -uu * P.Lambda0;
-            const R wq = (R)d2q9_w(0);
-            So[0] = mk2(wq * ((R(1.) + G0) * (-U * fx - V * fy) + G0 * P.RT * (-U * rhox - V * rhoy)), R(0.));
-        }
-        // collision increment B - T = (1-a)(Eq - T) + c S: small near equilibrium,
-        // so B = T + increment keeps the rest state and rounds relative to the increment
-        const T b2 = mk2(bBP, P.h_bBP), c2 = mk2(cBP, P.h_cBP);
-#pragma unroll
-        for (int q = 0; q < 9; ++q) inc[q] = fma2(b2, sub2(Eq[q], Pq[q]), mul2(c2, So[q]));
-        // the rest directions take the exact zeroth moments of the collision:
-        // phase field sum_q h is conserved (sum Eq = phi, sum S = 0); HCZ flow
-        //   (1-a)(p - sum f) + c sum S = (1-a) hDt RT (grad rho_old . u) + c RT (u . grad rho)
-        const T sInc = sym8p(inc);
-        const R z0 = MODEL == HCZ ? (bBP * P.hDt * P.RT * (rxo * U + ryo * V) + cBP * P.RT * (U * rhox + V * rhoy)) - sInc.x
-                                  : inc[0].x;
-        inc[0] = mk2(z0, -sInc.y);
+        // sphi[r+1][e+1] is this cell
+        const R ph[8] = {sphi[r + 1][e + 2], sphi[r + 1][e], sphi[r + 2][e + 1], sphi[r][e + 1],
+                         sphi[r + 2][e + 2], sphi[r + 2][e], sphi[r][e + 2], sphi[r][e]};
+        collide_cell<MODEL, R>(P, S, c, first, Pq, sfz, dphi, a6, ph, inc, src, phi, U, V);
 #pragma unroll
         for (int q = 0; q < 9; ++q) sB[q][r][e] = add2(Pq[q], inc[q]);
-        sA[0][r][e] = srcx;
-        sA[1][r][e] = srcy;
-        sA[2][r][e] = rhox;
-        sA[3][r][e] = rhoy;
-        sA[4][r][e] = fx;
-        sA[5][r][e] = fy;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) sA[k][r][e] = src[k];
     }
     if (WALLS) {
         __syncthreads();
@@ -546,102 +255,28 @@ __device__ __forceinline__ void tile_step(const PR<R> &P, const SR<R> &S, int fi
     T FW[6], FSo[6];
     const bool do_x = act && e >= 1 && r >= 1 && r <= hh;           // faces x0-1|x0 .. x0+w-1|x0+w
     const bool do_y = act && r >= 1 && e >= 1 && e <= w;            // faces below rows 0..hh (hh+1 with the top)
-    const T half = mk2(R(0.5), R(0.5));
-#pragma unroll
-    for (int pass = 0; pass < 2; ++pass) {
-        const bool xf = pass == 0;
-        if (xf ? !do_x : !do_y) continue;
-        // neighbours in the shared tile: x-face between (r, e-1) and (r, e);
-        // y-face between (r-1, e) and (r, e)
-        const int ro = xf ? r : r - 1, eo = xf ? e - 1 : e;
+    if (do_x) {
         R av[6];
 #pragma unroll
-        for (int k = 0; k < 6; ++k) av[k] = R(0.5) * (sA[k][ro][eo] + sA[k][r][e]);
-        // half-step reconstruction at the face midpoint: CD average minus hDt xi.grad
-        T bh[9];
-        const T hdt = mk2(P.hDt, P.hDt);
+        for (int k = 0; k < 6; ++k) av[k] = R(0.5) * (sA[k][r][e - 1] + sA[k][r][e]);
+        face_flux<MODEL, true, R>(
+            P, [&](int q) { return sB[q][r][e - 1]; }, [&](int q) { return sB[q][r][e]; },
+            [&](int q) {
+                return add2(sub2(sB[q][r + 1][e], sB[q][r - 1][e]), sub2(sB[q][r + 1][e - 1], sB[q][r - 1][e - 1]));
+            },
+            av, 0, FW);
+    }
+    if (do_y) {
+        R av[6];
 #pragma unroll
-        for (int q = 0; q < 9; ++q) {
-            const int xu = d2q9_xu(q), xv = d2q9_xv(q);
-            const T o = sB[q][ro][eo], n = sB[q][r][e];
-            const T avg = mul2(half, add2(o, n));
-            const int sn = xf ? xu : xv, st = xf ? xv : xu;  // normal / tangential velocity
-            if (sn == 0 && st == 0) {
-                bh[q] = avg;
-                continue;
-            }
-            // xi.grad as the sum of the normal part (o - n)/(-d) and the tangential
-            // central difference averaged over the two cells of the face
-            T g = mk2(R(0.), R(0.));
-            bool have = false;
-            if (sn != 0) {
-                const R rn = xf ? P.r_ndx : P.r_ndy;
-                g = mul2(sub2(o, n), mk2(sn * rn, sn * rn));
-                have = true;
-            }
-            if (st != 0) {
-                T d;
-                R rt;
-                if (xf) {
-                    d = add2(sub2(sB[q][r + 1][e], sB[q][r - 1][e]), sub2(sB[q][r + 1][e - 1], sB[q][r - 1][e - 1]));
-                    rt = P.r_2dy;
-                } else {
-                    d = add2(sub2(sB[q][r][e - 1], sB[q][r][e + 1]), sub2(sB[q][r - 1][e - 1], sB[q][r - 1][e + 1]));
-                    rt = P.r_n2dx;
-                }
-                const R k = R(0.5) * (R)st * rt;
-                g = have ? fma2(d, mk2(k, k), g) : mul2(d, mk2(k, k));
-            }
-            bh[q] = sub2(avg, mul2(hdt, g));
-        }
-        // face moments (sum f, sum h) with the mirror-symmetric association
-        const T z = add2(mk2(MODEL == AC ? R(0.) : bh[0].x, bh[0].y), sym8p(bh));
-        const R sf = z.x, dphif = z.y;
-        const R su = (bh[1].x - bh[5].x) + ((bh[2].x - bh[6].x) + (bh[8].x - bh[4].x));
-        const R sv = (bh[3].x - bh[7].x) + ((bh[2].x - bh[6].x) + (bh[4].x - bh[8].x));
-        const R phif = P.phi0 + dphif;
-        const R rhof = P.aPhi * phif + P.bPhi;
-        R Uf, Vf, dpf;
-        if (MODEL == AC) {
-            Uf = R(0.);
-            Vf = R(0.);
-            dpf = sf * P.Kp;
-        } else {
-            const R inv = rcp(rhof * P.RT);
-            Uf = su * inv + R(0.5) * P.hDt * av[4] * inv;
-            Vf = sv * inv + R(0.5) * P.hDt * av[5] * inv;
-            dpf = sf + R(0.5) * P.hDt * P.RT * (av[2] * Uf + av[3] * Vf);
-        }
-        const R uu = Uf * Uf + Vf * Vf;
-        const T a2 = mk2(P.ah_f, P.h_ah), c2 = mk2(P.tauf * (R(1.) - P.ah_f), P.h_ch);
-        // face distributions of the six directions crossing the face:
-        // Eq + a (bh - Eq) + c S
-        T out[9];
-#define DUGKS_FACE_Q(Q)                                                                                   \
-        if ((xf ? d2q9_xu(Q) : d2q9_xv(Q)) != 0) {                                                        \
-            T Eq, So;                                                                                     \
-            eq_src<MODEL, Q>(P, Uf, Vf, uu, rhof, phif, dpf, dphif, av[4], av[5], av[2], av[3], av[0],    \
-                             av[1], Eq, So);                                                              \
-            out[Q] = fma2(c2, So, fma2(a2, sub2(bh[Q], Eq), Eq));                                         \
-        }
-        DUGKS_FACE_Q(1) DUGKS_FACE_Q(2) DUGKS_FACE_Q(3) DUGKS_FACE_Q(4)
-        DUGKS_FACE_Q(5) DUGKS_FACE_Q(6) DUGKS_FACE_Q(7) DUGKS_FACE_Q(8)
-#undef DUGKS_FACE_Q
-        if (WALLS && !xf && (gj == 0 || gj == ny)) {
-            // bounce-back of the directions entering the fluid (Ark/Cpp/Boundary.cpp:118-139)
-            const bool bottom = gj == 0;
-#pragma unroll
-            for (int q = 1; q < 9; ++q) {
-                const int xv = d2q9_xv(q);
-                if (xv != 0 && (bottom ? xv > 0 : xv < 0)) out[q] = out[d2q9_bb(q)];
-            }
-        }
-        // fluxes xi.n (f, h) of the six directions
-#pragma unroll
-        for (int q = 1; q < 9; ++q) {
-            if (xf && d2q9_xu(q) != 0) FW[xslot(q)] = d2q9_xu(q) > 0 ? out[q] : neg2(out[q]);
-            if (!xf && d2q9_xv(q) != 0) FSo[yslot(q)] = d2q9_xv(q) > 0 ? out[q] : neg2(out[q]);
-        }
+        for (int k = 0; k < 6; ++k) av[k] = R(0.5) * (sA[k][r - 1][e] + sA[k][r][e]);
+        const int wall = (WALLS && gj == 0) ? 1 : ((WALLS && gj == ny) ? 2 : 0);
+        face_flux<MODEL, false, R>(
+            P, [&](int q) { return sB[q][r - 1][e]; }, [&](int q) { return sB[q][r][e]; },
+            [&](int q) {
+                return add2(sub2(sB[q][r][e - 1], sB[q][r][e + 1]), sub2(sB[q][r - 1][e - 1], sB[q][r - 1][e + 1]));
+            },
+            av, wall, FSo);
     }
     if (do_y) {
 #pragma unroll
@@ -658,28 +293,20 @@ __device__ __forceinline__ void tile_step(const PR<R> &P, const SR<R> &S, int fi
 
     // ---- stage 3: finite-volume update of the interior cells (Update_phi_T) + aux
     if (real && e >= 1 && e <= w && r >= 1 && r <= hh) {
-        const uint32_t h0 = mix32((uint32_t)c * 0x9E3779B1U ^ step * 0x85EBCA77U);
-        const T btp = mk2(P.bTP, P.bTP), dtv = mk2(P.dtV, P.dtV);
+        T FN[6], dn[9];
+#pragma unroll
+        for (int s = 0; s < 6; ++s) FN[s] = sFS[s][r + 1][e];
+        update_cell<R>(P, Pq, inc, FW, FE, FSo, FN, sr_bits(c, step), dn);
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
-            // net flux (W - E) + (S - N) with the mirror-symmetric association
-            T s = mk2(R(0.), R(0.));
-            const int xs = xslot(q), ys = yslot(q);
-            if (xs >= 0 && ys >= 0) s = add2(sub2(FW[xs], FE[xs]), sub2(FSo[ys], sFS[ys][r + 1][e]));
-            else if (xs >= 0) s = sub2(FW[xs], FE[xs]);
-            else if (ys >= 0) s = sub2(FSo[ys], sFS[ys][r + 1][e]);
-            // 4/3 B - 1/3 T = T + (4/3)(B - T): old value plus one small increment,
-            // rounded stochastically into storage
-            const T incr = (xs >= 0 || ys >= 0) ? fma2(dtv, s, fma2(btp, inc[q], inc[q])) : fma2(btp, inc[q], inc[q]);
-            const T dn = add_sr2(Pq[q], incr, h0 * (2u * q + 1u) + (uint32_t)q * 0x632BE5ABU);
-            S.odf[(size_t)q * S.qs + c] = dn.x;
-            S.odh[(size_t)q * S.qs + c] = dn.y;
+            S.odf[(size_t)q * S.qs + c] = dn[q].x;
+            S.odh[(size_t)q * S.qs + c] = dn[q].y;
         }
         if (MODEL != AC) {  // AC: u = 0, the next step needs no previous force, gradient or phi*u
-            S.oaux[A_FX * S.qs + c] = fx;
-            S.oaux[A_FY * S.qs + c] = fy;
-            S.oaux[A_RHOX * S.qs + c] = rhox;
-            S.oaux[A_RHOY * S.qs + c] = rhoy;
+            S.oaux[A_FX * S.qs + c] = src[4];
+            S.oaux[A_FY * S.qs + c] = src[5];
+            S.oaux[A_RHOX * S.qs + c] = src[2];
+            S.oaux[A_RHOY * S.qs + c] = src[3];
             S.oaux[A_PPU * S.qs + c] = phi * U;
             S.oaux[A_PPV * S.qs + c] = phi * V;
         }
