@@ -174,11 +174,9 @@ __device__ __forceinline__ void tile_step(const PR<R> &P, const SR<R> &S, int fi
             for (int q = 0; q < 9; ++q) Pq[q] = mk2(S.df[(size_t)q * S.qs + c], S.dh[(size_t)q * S.qs + c]);
         }
         // (sum f, sum h) as a float-float pair; the Allen-Cahn pressure omits f_0
-        FF2<T> s0;
-        s0.init(mk2(MODEL == AC ? R(0.) : Pq[0].x, Pq[0].y));
-#pragma unroll
-        for (int q = 1; q < 9; ++q) s0.add(Pq[q]);
-        const T z = s0.value();
+        const T za[9] = {mk2(MODEL == AC ? R(0.) : Pq[0].x, Pq[0].y), Pq[1], Pq[2], Pq[3], Pq[4],
+                         Pq[5], Pq[6], Pq[7], Pq[8]};
+        const T z = ff_sum9(za);
         sfz = z.x;
         dphi = z.y;
         sphi[r + 1][e + 1] = P.phi0 + dphi;
@@ -201,10 +199,10 @@ __device__ __forceinline__ void tile_step(const PR<R> &P, const SR<R> &S, int fi
             } else {
                 if (!WALLS) rj = wrapi(rj, ny);
                 const size_t cc = (size_t)rj * pitch + ri;
-                FFs<R> sh;
+                R ha[9];
 #pragma unroll
-                for (int q = 0; q < 9; ++q) sh.add(staged ? stg_ring[q * RING_MAX + k] : S.dh[(size_t)q * S.qs + cc]);
-                v = P.phi0 + sh.value();
+                for (int q = 0; q < 9; ++q) ha[q] = staged ? stg_ring[q * RING_MAX + k] : S.dh[(size_t)q * S.qs + cc];
+                v = P.phi0 + ff_sum9(ha);
             }
             sphi[rr + 1][re + 1] = v;
         }

@@ -48,6 +48,31 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
 __device__ __forceinline__ double rsq(double x) { return 1.0 / sqrt(x); }
 __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
+// Float-float sum of the nine directions, in a mirror-symmetric tree: the
+// pairs of opposite directions first, ((E+W) + (N+S)) + ((NE+SW) + (NW+SE)),
+// then the rest direction; a Knuth two-sum at every node and the node errors
+// summed in the same tree (depth 4, where a running sum is a chain of 8).
+template <typename V, typename Add, typename Sub>
+__device__ __forceinline__ V ff_tree9(const V (&a)[9], Add add, Sub sub) {
+    auto ts = [&](V x, V y, V &e) {
+        const V s = add(x, y);
+        const V bb = sub(s, x);
+        e = add(sub(x, sub(s, bb)), sub(y, bb));
+        return s;
+    };
+    V e15, e37, e26, e48, eA, eB, eC, eD;
+    const V s15 = ts(a[1], a[5], e15), s37 = ts(a[3], a[7], e37);
+    const V s26 = ts(a[2], a[6], e26), s48 = ts(a[4], a[8], e48);
+    const V sA = ts(s15, s37, eA), sB = ts(s26, s48, eB);
+    const V sC = ts(sA, sB, eC);
+    const V sD = ts(sC, a[0], eD);
+    const V err = add(add(add(add(e15, e37), eA), add(add(e26, e48), eB)), add(eC, eD));
+    return add(sD, err);
+}
+template <typename V>
+__device__ __forceinline__ V ff_sum9(const V (&a)[9]) {
+    return ff_tree9(a, [](V x, V y) { return x + y; }, [](V x, V y) { return x - y; });
+}
 // Macroscopic state of one cell after the update of the previous step
 // (Update_MacroVar), from its deviations; HCZ needs the previous force and
 // density gradient (aux), AC has u = 0.
@@ -55,29 +80,30 @@ template <int MODEL, typename R>
 __device__ __forceinline__ void cell_macros(const PR<R> &P, const R *df, const R *dh, R fx_old,
                                             R fy_old, R rx_old, R ry_old, R &dphi, R &rho,
                                             R &U, R &V, R &dp) {
-    FFs<R> sh, sf, su, sv;
+    R ha[9];
 #pragma unroll
-    for (int q = 0; q < 9; ++q) sh.add(dh[q]);  // two-sum: exact to 2^-48, order-independent after rounding
-    dphi = sh.value();
+    for (int q = 0; q < 9; ++q) ha[q] = dh[q];
+    dphi = ff_sum9(ha);
     const R phi = P.phi0 + dphi;
     rho = P.aPhi * phi + P.bPhi;
     if (MODEL == AC) {
-#pragma unroll
-        for (int q = 1; q < 9; ++q) sf.add(df[q]);
+        const R fa[9] = {R(0.), df[1], df[2], df[3], df[4], df[5], df[6], df[7], df[8]};
         U = R(0.);
         V = R(0.);
-        dp = sf.value() * P.Kp;
+        dp = ff_sum9(fa) * P.Kp;
     } else {
+        R ua[9], va[9], fa[9];
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
-            sf.add(df[q]);
-            if (d2q9_xu(q)) su.add(sxf(d2q9_xu(q), df[q]));
-            if (d2q9_xv(q)) sv.add(sxf(d2q9_xv(q), df[q]));
+            fa[q] = df[q];
+            ua[q] = sxf(d2q9_xu(q), df[q]);
+            va[q] = sxf(d2q9_xv(q), df[q]);
         }
+        const R su = ff_sum9(ua), sv = ff_sum9(va), sfv = ff_sum9(fa);
         const R inv = R(1.) / (rho * P.RT);
-        U = su.value() * inv + P.hDt * fx_old * inv;
-        V = sv.value() * inv + P.hDt * fy_old * inv;
-        dp = sf.value() + P.hDt * (rx_old * U + ry_old * V) * P.RT;
+        U = su * inv + P.hDt * fx_old * inv;
+        V = sv * inv + P.hDt * fy_old * inv;
+        dp = sfv + P.hDt * (rx_old * U + ry_old * V) * P.RT;
     }
 }
 
@@ -148,6 +174,13 @@ struct FF2 {
     }
     __device__ __forceinline__ T value() const { return add2(hi, lo); }
 };
+
+__device__ __forceinline__ float2 ff_sum9(const float2 (&a)[9]) {
+    return ff_tree9(a, [](float2 x, float2 y) { return add2(x, y); }, [](float2 x, float2 y) { return sub2(x, y); });
+}
+__device__ __forceinline__ double2 ff_sum9(const double2 (&a)[9]) {
+    return ff_tree9(a, [](double2 x, double2 y) { return add2(x, y); }, [](double2 x, double2 y) { return sub2(x, y); });
+}
 
 // mirror-symmetric sum of directions 1..8 (see sym8)
 template <typename T>
@@ -265,16 +298,10 @@ __device__ __forceinline__ void collide_cell(const PR<R> &P, const SR<R> &S, siz
             ppu = a6[A_PPU];
             ppv = a6[A_PPV];
             // first moments as a float-float pair (sum xi_x f, sum xi_y f)
-            FF2<T> m;
-            m.init(mk2(Pq[1].x, R(0.)));
-            m.add(mk2(Pq[2].x, Pq[2].x));
-            m.add(mk2(R(0.), Pq[3].x));
-            m.add(mk2(-Pq[4].x, Pq[4].x));
-            m.add(mk2(-Pq[5].x, R(0.)));
-            m.add(mk2(-Pq[6].x, -Pq[6].x));
-            m.add(mk2(R(0.), -Pq[7].x));
-            m.add(mk2(Pq[8].x, -Pq[8].x));
-            const T mv = m.value();
+            const T mt[9] = {mk2(R(0.), R(0.)),     mk2(Pq[1].x, R(0.)),    mk2(Pq[2].x, Pq[2].x),
+                             mk2(R(0.), Pq[3].x),   mk2(-Pq[4].x, Pq[4].x), mk2(-Pq[5].x, R(0.)),
+                             mk2(-Pq[6].x, -Pq[6].x), mk2(R(0.), -Pq[7].x), mk2(Pq[8].x, -Pq[8].x)};
+            const T mv = ff_sum9(mt);
             const R inv = rcp(rho * P.RT);
             U = mv.x * inv + P.hDt * fxo * inv;
             V = mv.y * inv + P.hDt * fyo * inv;

@@ -8,7 +8,7 @@
 // Per row k the warp does, in order:
 //   phi of row k+2 (float-float sum of its h deviations, staged in shared
 //     memory); cp.async of row k+3's deviations into the stage ring (the
-//     aux of a row is read directly, at the start of the row before its
+//     aux of a row is read directly into registers one row ahead of its
 //     collision);
 //   collision of row k+1 (macros, MacroSource on the 3x3 phi stencil from
 //     the phi of rows k..k+2 and the adjacent lanes, f-bar-plus) into the
@@ -99,6 +99,7 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
         // south-face flux
         float ph0 = 0.f, ph1 = 0.f, ph2 = 0.f;
         float sfz1 = 0.f, dph1 = 0.f;
+        float a6c[A_N];  // aux of row k+1 (loaded at the previous row)
         T inc_cur[9], FS[6];
 #pragma unroll
         for (int q = 0; q < 9; ++q) inc_cur[q] = mk2(0.f, 0.f);
@@ -109,13 +110,13 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
             T *const Bm = bring + m3(k - 1) * 288, *const B0 = bring + m3(k) * 288, *const Bp = bring + m3(k + 1) * 288;
             float *const Am = aring + m3(k - 1) * 192, *const A0 = aring + m3(k) * 192,
                          *const Ap = aring + m3(k + 1) * 192;
-            // aux of row k+1 (read directly; used by its collision below)
-            float a6[A_N];
+            // aux of row k+2, read directly one row ahead of its collision
             const bool coll = k + 1 >= y0 - 1 && row_ok(k + 1) && colL;
-            if (MODEL != AC && !first && coll) {
-                const size_t c1 = cell(k + 1);
+            float a6n[A_N];
+            if (MODEL != AC && !first && k + 2 >= y0 - 1 && row_ok(k + 2) && colL) {
+                const size_t c2 = cell(k + 2);
 #pragma unroll
-                for (int a = 0; a < A_N; ++a) a6[a] = __ldg(S.aux + (size_t)a * S.qs + c1);
+                for (int a = 0; a < A_N; ++a) a6n[a] = __ldg(S.aux + (size_t)a * S.qs + c2);
             }
             cp_async_wait_all();
             __syncwarp();
@@ -126,11 +127,11 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
                 float phv = 0.f;
                 if (row_ok(j)) {
                     const int sl = m4(j);
-                    FF2<T> s0;
-                    s0.init(mk2(MODEL == AC ? 0.f : STG(sl, 0), STG(sl, 9)));
+                    T za[9];
+                    za[0] = mk2(MODEL == AC ? 0.f : STG(sl, 0), STG(sl, 9));
 #pragma unroll
-                    for (int q = 1; q < 9; ++q) s0.add(mk2(STG(sl, q), STG(sl, 9 + q)));
-                    const T z = s0.value();
+                    for (int q = 1; q < 9; ++q) za[q] = mk2(STG(sl, q), STG(sl, 9 + q));
+                    const T z = ff_sum9(za);
                     sfz2 = z.x;
                     dph2 = z.y;
                     phv = P.phi0 + dph2;
@@ -160,7 +161,7 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
                     const float ph[8] = {E, W, ph2, ph0, NE, NW, SE, SWv};
                     const size_t c = cell(j);
                     float src[6], phi, U, V;
-                    collide_cell<MODEL, float>(P, S, c, first, Pq, sfz1, dph1, a6, ph, inc_nx, src, phi, U, V);
+                    collide_cell<MODEL, float>(P, S, c, first, Pq, sfz1, dph1, a6c, ph, inc_nx, src, phi, U, V);
 #pragma unroll
                     for (int q = 0; q < 9; ++q) Bp[q * 32 + lane] = add2(Pq[q], inc_nx[q]);
 #pragma unroll
@@ -271,6 +272,10 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
             ph1 = ph2;
             sfz1 = sfz2;
             dph1 = dph2;
+            if (MODEL != AC) {
+#pragma unroll
+                for (int a = 0; a < A_N; ++a) a6c[a] = a6n[a];
+            }
         }
         cp_async_wait_all();  // nothing in flight into this warp's buffers
     }
