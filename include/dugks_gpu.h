@@ -236,6 +236,26 @@ int dugks_srv_last_error(dugks_srv_t *s, char *buf, size_t len);
 /* Cancels what has not finished and waits for the device work to end. */
 int dugks_srv_destroy(dugks_srv_t *s);
 
+/* ---- Slab decomposition: one FP32-storage Allen-Cahn case split along y into
+ * partitions (on one or several devices), each with two halo rows per side
+ * exchanged after every step; bit-identical to the undivided case.  No
+ * reference counterpart (the reference runs one OpenMP process per case). */
+typedef struct dugks_slabs dugks_slabs_t;
+
+/* Host-only plan: partition p owns rows [row0[p], row0[p] + nrows[p]); lo[p] /
+ * hi[p] is the partition below / above (-1: the grid's wall).  Needs at least
+ * 8 rows per partition. */
+int dugks_slabs_plan(int ny, int y_walls, int nparts, int *row0, int *nrows, int *lo, int *hi);
+/* devices: the CUDA device of each partition (NULL: all on the current one). */
+int dugks_slabs_create(const dugks_case_t *c, const dugks_grid_t *g, int nparts, const int *devices,
+                       dugks_slabs_t **out);
+int dugks_slabs_init(dugks_slabs_t *s, int kind, const double *params, int nparams, uint64_t seed);
+int dugks_slabs_step(dugks_slabs_t *s, int nsteps);
+/* the whole grid's fields ([ny][nx] each); any pointer may be NULL */
+int dugks_slabs_download(dugks_slabs_t *s, double *rho, double *u, double *v, double *phi, double *p);
+int64_t dugks_slabs_launch_count(const dugks_slabs_t *s);
+int dugks_slabs_destroy(dugks_slabs_t *s);
+
 #ifdef __cplusplus
 }
 #endif

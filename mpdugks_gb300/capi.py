@@ -93,6 +93,14 @@ SIGNATURES = {
     'dugks_srv_stats': (C.c_int, [C.c_void_p, C.POINTER(SrvStatsT)]),
     'dugks_srv_last_error': (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     'dugks_srv_destroy': (C.c_int, [C.c_void_p]),
+    'dugks_slabs_plan': (C.c_int, [C.c_int, C.c_int, C.c_int] + [C.POINTER(C.c_int)] * 4),
+    'dugks_slabs_create': (C.c_int, [C.POINTER(CaseT), C.POINTER(GridT), C.c_int, C.POINTER(C.c_int),
+                                     C.POINTER(C.c_void_p)]),
+    'dugks_slabs_init': (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_int, C.c_uint64]),
+    'dugks_slabs_step': (C.c_int, [C.c_void_p, C.c_int]),
+    'dugks_slabs_download': (C.c_int, [C.c_void_p] + [C.c_void_p] * 5),
+    'dugks_slabs_launch_count': (C.c_int64, [C.c_void_p]),
+    'dugks_slabs_destroy': (C.c_int, [C.c_void_p]),
 }
 
 _lib = None
@@ -273,6 +281,58 @@ class Server:
         if getattr(self, 's', None):
             self.lib.dugks_srv_destroy(self.s)
             self.s = None
+
+    def __del__(self):
+        self.close()
+
+
+def slab_plan(ny: int, y_walls: bool, nparts: int):
+    """Host-only partition plan: (row0, nrows, lo, hi) lists (lo/hi -1: a wall)."""
+    lib = load()
+    arrs = [(C.c_int * nparts)() for _ in range(4)]
+    rc = lib.dugks_slabs_plan(ny, int(y_walls), nparts, *arrs)
+    if rc != DUGKS_OK:
+        buf = C.create_string_buffer(512)
+        lib.dugks_gpu_last_error(None, buf, 512)
+        raise DugksError(rc, buf.value.decode())
+    return tuple([list(a) for a in arrs])
+
+
+class Slabs:
+    """One FP32-storage case split along y into partitions with halo exchange (dugks_slabs_*)."""
+
+    def __init__(self, case: CaseT, nx: int, ny: int, y_walls: bool, nparts: int, devices=None):
+        self.lib = load()
+        self.nx, self.ny = nx, ny
+        grid = GridT(nx, ny, int(y_walls))
+        dev = (C.c_int * nparts)(*devices) if devices else None
+        h = C.c_void_p()
+        self._check(self.lib.dugks_slabs_create(C.byref(case), C.byref(grid), nparts, dev, C.byref(h)))
+        self.h = h
+
+    def _check(self, rc: int) -> None:
+        if rc != DUGKS_OK:
+            buf = C.create_string_buffer(512)
+            self.lib.dugks_gpu_last_error(None, buf, 512)
+            raise DugksError(rc, buf.value.decode())
+
+    def init(self, kind: str, params=(), seed: int = 12345) -> None:
+        arr = (C.c_double * max(1, len(params)))(*params)
+        self._check(self.lib.dugks_slabs_init(self.h, INIT_KINDS[kind], arr, len(params), seed))
+
+    def step(self, n: int = 1) -> None:
+        self._check(self.lib.dugks_slabs_step(self.h, n))
+
+    def fields(self) -> dict[str, np.ndarray]:
+        out = {k: np.empty((self.ny, self.nx), dtype=np.float64) for k in ('rho', 'u', 'v', 'phi', 'p')}
+        self._check(self.lib.dugks_slabs_download(self.h, *[out[k].ctypes.data for k in ('rho', 'u', 'v', 'phi',
+                                                                                           'p')]))
+        return out
+
+    def close(self) -> None:
+        if getattr(self, 'h', None):
+            self.lib.dugks_slabs_destroy(self.h)
+            self.h = None
 
     def __del__(self):
         self.close()

@@ -746,5 +746,10 @@ void fp32_adopt_steps(dugks_handle_t *h, int64_t n) {
 
 void set_stream(dugks_handle_t *h, cudaStream_t st) { h->last_stream = st; }
 
+// for the slab decomposition (slabs.cu)
+void derive_fp32(const Params &P, f32::P32 *Q) { derive_p32<float>(P, *Q); }
+double rest_f(const Params &P, int q) { return f_rest(P, q); }
+double rest_h(const Params &P, int q) { return h_rest(P, q); }
+
 }  // namespace internal
 }  // namespace dugks

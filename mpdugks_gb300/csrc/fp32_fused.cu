@@ -294,7 +294,7 @@ __device__ __forceinline__ void tile_step(const PR<R> &P, const SR<R> &S, int fi
         T FN[6], dn[9];
 #pragma unroll
         for (int s = 0; s < 6; ++s) FN[s] = sFS[s][r + 1][e];
-        update_cell<R>(P, Pq, inc, FW, FE, FSo, FN, sr_bits(c, step), dn);
+        update_cell<R>(P, Pq, inc, FW, FE, FSo, FN, sr_bits(P, gj, gi, step), dn);
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
             S.odf[(size_t)q * S.qs + c] = dn[q].x;

@@ -259,7 +259,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // inc = B - T of every direction (f, h pairs).  src = {srcx, srcy, rhox, rhoy,
 // fx, fy}; phi_o, U_o, V_o for the caller's outputs.
 template <int MODEL, typename R>
-__device__ __forceinline__ void collide_cell(const PR<R> &P, const SR<R> &S, size_t c, int first,
+__device__ __forceinline__ void collide_cell(const PR<R> &P, const SR<R> &S, long long c, int first,
                                              const typename Pair<R>::T (&Pq)[9], R sfz, R dphi, const R (&a6)[A_N],
                                              const R (&ph)[8], typename Pair<R>::T (&inc)[9], R (&src)[6], R &phi_o,
                                              R &U_o, R &V_o) {
@@ -271,7 +271,7 @@ __device__ __forceinline__ void collide_cell(const PR<R> &P, const SR<R> &S, siz
         // first step after an initialisation: the reference uses the state the
         // initialisation left (p0, zero forces, tau from Mu0), as uploaded
         const R *I = S.init;
-        const size_t ps = S.qs;
+        const long long ps = (long long)S.qs;
         phi = P.phi0 + I[I_DPHI * ps + c];
         rho = I[I_RHO * ps + c];
         U = I[I_U * ps + c];
@@ -476,8 +476,12 @@ __device__ __forceinline__ void update_cell(const PR<R> &P, const typename Pair<
     }
 }
 
-// per (cell, step) random bits of the stochastic rounding
-__device__ __forceinline__ uint32_t sr_bits(size_t c, uint32_t step) {
+// per (cell, step) random bits of the stochastic rounding; the cell is
+// numbered on the whole grid (global row j + row0), so a slab partition draws
+// the same bits as the undivided grid
+template <typename R>
+__device__ __forceinline__ uint32_t sr_bits(const PR<R> &P, int j, int gi, uint32_t step) {
+    const size_t c = (size_t)(j + P.row0) * P.pitch + gi;
     return mix32((uint32_t)c * 0x9E3779B1U ^ step * 0x85EBCA77U);
 }
 

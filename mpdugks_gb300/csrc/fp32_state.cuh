@@ -22,6 +22,10 @@ namespace f32 {
 template <typename R>
 struct PR {
     int nx, ny, pitch, walls, model, gravity;
+    // slab partitions: global row of local row 0, and whether the rows below 0 /
+    // from ny up are a neighbour's halo (2 rows of device memory) instead of a
+    // wall or the periodic wrap; 0 for a whole grid
+    int row0, halo_lo, halo_hi;
     R phi0, p0, aPhi, bPhi, Kp, RT, invRT, hDt, dt, Lambda0;
     R Beta, Kappa, PhiL, PhiV, RhoL, Gy;
     R inv_12dx, inv_12dy, inv_6dd, inv_wI_dphi, inv_RTdt;
@@ -47,6 +51,9 @@ struct SR {
     size_t qs;    // ny * pitch
 };
 using S32 = SR<float>;
+
+// halo rows of a slab partition on each side
+constexpr int SLAB_HALO = 2;
 
 // cases one batched launch (serving) can hold: the size of the constant-memory case table
 constexpr int BATCH_MAX_CASES = 64;

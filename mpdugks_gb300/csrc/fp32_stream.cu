@@ -74,15 +74,22 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
         const bool interior = lane >= 2 && lane < 2 + w;
         const bool colL = lane >= 1 && lane <= 2 + w;  // lanes whose f-bar-plus is needed
         const bool xfL = lane >= 2 && lane <= 2 + w;   // lanes whose west x-face is needed
-        auto row_ok = [&](int j) { return WALLS ? (j >= 0 && j < ny) : true; };
-        // rows of the window lie in [y0-4, y1+3] (the launcher ensures ny >= 8)
-        auto cell = [&](int j) {
-            const int jj = WALLS ? j : (j < 0 ? j + ny : (j >= ny ? j - ny : j));
-            return (size_t)jj * pitch + gi;
+        // rows of the window lie in [y0-4, y1+3] (the launcher ensures ny >= 8).  A
+        // slab partition (WALLS instance) reads rows below 0 / from ny up from its
+        // halo rows where halo_lo / halo_hi is set; elsewhere they are walls.
+        const bool hlo = WALLS && P.halo_lo, hhi = WALLS && P.halo_hi;
+        auto row_ok = [&](int j) {
+            return WALLS ? ((j >= 0 || (hlo && j >= -SLAB_HALO)) && (j < ny || (hhi && j < ny + SLAB_HALO))) : true;
         };
+        auto cell = [&](int j) -> long long {  // signed: halo rows lie below row 0
+            const int jj = WALLS ? j : (j < 0 ? j + ny : (j >= ny ? j - ny : j));
+            return (long long)jj * pitch + gi;
+        };
+        // wall sides (no halo)
+        const bool wlo = WALLS && !hlo, whi = WALLS && !hhi;
         auto prefetch = [&](int j) {
             if (j <= y1 + 1 && row_ok(j)) {
-                const size_t c = cell(j);
+                const long long c = cell(j);
                 float *d = stg + m4(j) * NPL * 32 + lane;
 #pragma unroll
                 for (int q = 0; q < 9; ++q) {
@@ -114,7 +121,7 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
             const bool coll = k + 1 >= y0 - 1 && row_ok(k + 1) && colL;
             float a6n[A_N];
             if (MODEL != AC && !first && k + 2 >= y0 - 1 && row_ok(k + 2) && colL) {
-                const size_t c2 = cell(k + 2);
+                const long long c2 = cell(k + 2);
 #pragma unroll
                 for (int a = 0; a < A_N; ++a) a6n[a] = __ldg(S.aux + (size_t)a * S.qs + c2);
             }
@@ -135,7 +142,7 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
                     sfz2 = z.x;
                     dph2 = z.y;
                     phv = P.phi0 + dph2;
-                } else if (WALLS && (j == -1 || j == ny)) {
+                } else if ((wlo && j == -1) || (whi && j == ny)) {
                     // ghost phi: the previous step's extrapolation (Ark/Cpp/Boundary.cpp:38-63)
                     phv = S.gphi[(size_t)(gin * 2 + (j < 0 ? 0 : 1)) * pitch + gi];
                 }
@@ -159,7 +166,7 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
 #pragma unroll
                     for (int q = 0; q < 9; ++q) Pq[q] = mk2(STG(sl, q), STG(sl, 9 + q));
                     const float ph[8] = {E, W, ph2, ph0, NE, NW, SE, SWv};
-                    const size_t c = cell(j);
+                    const long long c = cell(j);
                     float src[6], phi, U, V;
                     collide_cell<MODEL, float>(P, S, c, first, Pq, sfz1, dph1, a6c, ph, inc_nx, src, phi, U, V);
 #pragma unroll
@@ -176,14 +183,14 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
                             S.oaux[A_PPV * S.qs + c] = phi * V;
                         }
                         // ghost phi for the next step's MacroSource
-                        if (WALLS && j == 0) S.gphi[(size_t)(gout * 2 + 0) * pitch + gi] = 2.f * phi - ph2;
-                        if (WALLS && j == ny - 1) S.gphi[(size_t)(gout * 2 + 1) * pitch + gi] = 2.f * phi - ph0;
+                        if (wlo && j == 0) S.gphi[(size_t)(gout * 2 + 0) * pitch + gi] = 2.f * phi - ph2;
+                        if (whi && j == ny - 1) S.gphi[(size_t)(gout * 2 + 1) * pitch + gi] = 2.f * phi - ph0;
                     }
                 }
             }
             __syncwarp();
             // ---- wall ghost rows of f-bar-plus and of the averaged fields (2 a0 - a1)
-            if (WALLS && (k == 0 || k == ny - 1) && colL) {
+            if (((wlo && k == 0) || (whi && k == ny - 1)) && colL) {
                 // bottom: row -1 (slot of k-1) from rows 0 (k), 1 (k+1); top: row ny (slot of
                 // k+1) from rows ny-1 (k), ny-2 (k-1)
                 T *const Bg = k == 0 ? Bm : Bp, *const B1 = k == 0 ? Bp : Bm;
@@ -196,7 +203,7 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
             }
             __syncwarp();
             // ---- y-face between rows k-1 and k at the bottom wall (row 0's south face)
-            if (WALLS && k == 0 && interior) {
+            if (wlo && k == 0 && interior) {
                 float av[6];
 #pragma unroll
                 for (int a = 0; a < 6; ++a) av[a] = 0.5f * (Am[a * 32 + lane] + A0[a * 32 + lane]);
@@ -212,12 +219,13 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
             T FN[6];
 #pragma unroll
             for (int s = 0; s < 6; ++s) FN[s] = mk2(0.f, 0.f);
-            const bool yface = k >= y0 - 1 && (WALLS ? (k >= 0 && k <= ny - 1) : true);
+            const bool top_wall = whi && k == ny - 1;
+            const bool yface = k >= y0 - 1 && ((row_ok(k) && row_ok(k + 1)) || top_wall);
             if (yface && interior) {
                 float av[6];
 #pragma unroll
                 for (int a = 0; a < 6; ++a) av[a] = 0.5f * (A0[a * 32 + lane] + Ap[a * 32 + lane]);
-                const int wall = (WALLS && k == ny - 1) ? 2 : 0;
+                const int wall = top_wall ? 2 : 0;
                 face_flux<MODEL, false, float>(
                     P, [&](int q) { return B0[q * 32 + lane]; }, [&](int q) { return Bp[q * 32 + lane]; },
                     [&](int q) {
@@ -253,8 +261,8 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
                 T Pq[9], dn[9];
 #pragma unroll
                 for (int q = 0; q < 9; ++q) Pq[q] = mk2(STG(sl, q), STG(sl, 9 + q));
-                const size_t c = cell(k);
-                update_cell<float>(P, Pq, inc_cur, FW, FE, FS, FN, sr_bits(c, step), dn);
+                const long long c = cell(k);
+                update_cell<float>(P, Pq, inc_cur, FW, FE, FS, FN, sr_bits(P, k, gi, step), dn);
 #pragma unroll
                 for (int q = 0; q < 9; ++q) {
                     S.odf[(size_t)q * S.qs + c] = dn[q].x;
@@ -264,10 +272,8 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
             // ---- roll the per-lane state one row up
 #pragma unroll
             for (int q = 0; q < 9; ++q) inc_cur[q] = inc_nx[q];
-            if (!(WALLS && k == -1)) {
 #pragma unroll
-                for (int s = 0; s < 6; ++s) FS[s] = FN[s];
-            }
+            for (int s = 0; s < 6; ++s) FS[s] = FN[s];
             ph0 = ph1;
             ph1 = ph2;
             sfz1 = sfz2;

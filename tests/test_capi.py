@@ -9,7 +9,7 @@ ROOT = Path(__file__).resolve().parents[1]
 
 def declared_symbols():
     text = (ROOT / 'include' / 'dugks_gpu.h').read_text()
-    return sorted(set(re.findall(r'\b(dugks_(?:gpu|srv)_\w+)\s*\(', text)))
+    return sorted(set(re.findall(r'\b(dugks_(?:gpu|srv|slabs)_\w+)\s*\(', text)))
 
 
 def test_header_declares_abi():
