@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "dugks_device.cuh"
 #include "fp32_state.cuh"
@@ -217,27 +218,6 @@ __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
 __host__ __device__ constexpr int xslot(int q) { return q == 1 ? 0 : q == 2 ? 1 : q == 4 ? 2 : q == 5 ? 3 : q == 6 ? 4 : q == 8 ? 5 : -1; }
 __host__ __device__ constexpr int yslot(int q) { return q == 2 ? 0 : q == 3 ? 1 : q == 4 ? 2 : q == 6 ? 3 : q == 7 ? 4 : q == 8 ? 5 : -1; }
 
-// Equilibrium deviations and the force terms of direction q != 0, as pairs
-// (f, h): Eq = w (dp + rho RT G, dphi + u1 phi) (HCZ) or w (dp/RT, dphi) (AC);
-// So = (w ((1+G)(c.F) + G RT (c.grad rho)), w (xi.src)) with c = xi - u.
-template <int MODEL, int Q, typename R>
-__device__ __forceinline__ void eq_src(const PR<R> &P, R U, R V, R uu, R rho, R phi, R dp, R dphi, R fx, R fy,
-                                       R rx, R ry, R sx_, R sy_, typename Pair<R>::T &Eq,
-                                       typename Pair<R>::T &So) {
-    constexpr int xu = d2q9_xu(Q), xv = d2q9_xv(Q);
-    const R wq = (R)d2q9_w(Q);
-    const R hS = wq * (sxf(xu, sx_) + sxf(xv, sy_));
-    if (MODEL == AC) {
-        Eq = mk2(wq * (dp * P.invRT), wq * dphi);
-        So = mk2(wq * ((sxf(xu, fx) + sxf(xv, fy)) * P.invRT), hS);
-    } else {
-        const R u1 = (sxf(xu, U) + sxf(xv, V)) * P.invRT;
-        const R G = u1 + R(0.5) * u1 * u1 - uu * P.Lambda0;
-        const R cu = (R)xu - U, cv = (R)xv - V;
-        Eq = mul2(mk2(wq, wq), fma2(mk2(rho * P.RT, phi), mk2(G, u1), mk2(dp, dphi)));
-        So = mk2(wq * ((R(1.) + G) * (cu * fx + cv * fy) + G * P.RT * (cu * rx + cv * ry)), hS);
-    }
-}
 // asynchronous 4- or 8-byte global -> shared copies (cp.async)
 template <typename R>
 __device__ __forceinline__ void cp_async(R *smem, const R *gmem) {
@@ -249,6 +229,76 @@ __device__ __forceinline__ void cp_async(R *smem, const R *gmem) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Site terms of the equilibria and force sources (a cell or a face), shared by
+// all directions: u/RT, |u|^2 lambda, rho RT, u.F, u.grad rho, and the pairs
+// (rho RT, phi), (dp, dphi) of the packed equilibria.
+template <typename R>
+struct EqSite {
+    typename Pair<R>::T A2, D2;
+    R Ux, Vx, uuL, UF, UR, fx, fy, rx, ry, sx, sy, fxI, fyI, dpI;
+};
+template <int MODEL, typename R>
+__device__ __forceinline__ EqSite<R> eq_site(const PR<R> &P, R U, R V, R uu, R rho, R phi, R dp, R dphi, R fx,
+                                              R fy, R rx, R ry, R sx_, R sy_) {
+    EqSite<R> e;
+    e.fx = fx;
+    e.fy = fy;
+    e.sx = sx_;
+    e.sy = sy_;
+    if (MODEL == AC) {
+        e.fxI = fx * P.invRT;
+        e.fyI = fy * P.invRT;
+        e.dpI = dp * P.invRT;
+        e.D2 = mk2(e.dpI, dphi);
+    } else {
+        e.Ux = U * P.invRT;
+        e.Vx = V * P.invRT;
+        e.uuL = uu * P.Lambda0;
+        e.UF = U * fx + V * fy;
+        e.UR = U * rx + V * ry;
+        e.rx = rx;
+        e.ry = ry;
+        e.A2 = mk2(rho * P.RT, phi);
+        e.D2 = mk2(dp, dphi);
+    }
+    return e;
+}
+
+// Equilibrium deviations and force terms, as (f, h) pairs, of direction Q in
+// {1, 2, 3, 4} and of its opposite Q+4, which share every term up to a sign:
+//   Eq = w (dp + rho RT G, dphi + u1 phi) (HCZ) or w (dp/RT, dphi) (AC),
+//   So = (w (A + G (A + RT B)), w xi.src) with A = xi.F - u.F, B = xi.grad rho -
+//   u.grad rho, G = u1 + u1^2/2 - |u|^2 lambda (= (1+G)(c.F) + G RT (c.grad rho),
+//   c = xi - u), u1 = xi.u / RT.
+template <int MODEL, int Q, typename R>
+__device__ __forceinline__ void eq_pair(const PR<R> &P, const EqSite<R> &e, typename Pair<R>::T &Eq,
+                                        typename Pair<R>::T &So, typename Pair<R>::T &Eqb,
+                                        typename Pair<R>::T &Sob) {
+    constexpr int xu = d2q9_xu(Q), xv = d2q9_xv(Q);
+    const R wq = (R)d2q9_w(Q);
+    const R hS = wq * (sxf(xu, e.sx) + sxf(xv, e.sy));
+    if (MODEL == AC) {
+        Eq = mul2(mk2(wq, wq), e.D2);
+        Eqb = Eq;
+        const R sf = wq * (sxf(xu, e.fxI) + sxf(xv, e.fyI));
+        So = mk2(sf, hS);
+        Sob = mk2(-sf, -hS);
+    } else {
+        const R u1 = sxf(xu, e.Ux) + sxf(xv, e.Vx);
+        const R H = (R(0.5) * u1) * u1 - e.uuL;
+        const R G = H + u1, Gb = H - u1;
+        const R eF = sxf(xu, e.fx) + sxf(xv, e.fy), eR = sxf(xu, e.rx) + sxf(xv, e.ry);
+        const R A = eF - e.UF, Ab = -eF - e.UF;
+        const R B = eR - e.UR, Bb = -eR - e.UR;
+        const R C = P.RT * B + A, Cb = P.RT * Bb + Ab;
+        const auto w2 = mk2(wq, wq);
+        Eq = mul2(w2, fma2(e.A2, mk2(G, u1), e.D2));
+        Eqb = mul2(w2, fma2(e.A2, mk2(Gb, -u1), e.D2));
+        So = mk2(wq * (G * C + A), hS);
+        Sob = mk2(wq * (Gb * Cb + Ab), -hS);
+    }
+}
 
 // ---- the three per-cell stages of one step, shared by the tile kernel and
 // the streaming kernel (same operations in the same order in both)
@@ -319,14 +369,11 @@ __device__ __forceinline__ void collide_cell(const PR<R> &P, const SR<R> &S, lon
     // equilibria of q != 0; q = 0 from the exact zeroth moment (sum dEq = dp for
     // HCZ, 0 for AC; sum dhEq = dphi), so FP32 weights cannot leak mass
     T Eq[9], So[9];
-    eq_src<MODEL, 1>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[1], So[1]);
-    eq_src<MODEL, 2>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[2], So[2]);
-    eq_src<MODEL, 3>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[3], So[3]);
-    eq_src<MODEL, 4>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[4], So[4]);
-    eq_src<MODEL, 5>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[5], So[5]);
-    eq_src<MODEL, 6>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[6], So[6]);
-    eq_src<MODEL, 7>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[7], So[7]);
-    eq_src<MODEL, 8>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy, Eq[8], So[8]);
+    const EqSite<R> es = eq_site<MODEL, R>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy);
+    eq_pair<MODEL, 1>(P, es, Eq[1], So[1], Eq[5], So[5]);
+    eq_pair<MODEL, 2>(P, es, Eq[2], So[2], Eq[6], So[6]);
+    eq_pair<MODEL, 3>(P, es, Eq[3], So[3], Eq[7], So[7]);
+    eq_pair<MODEL, 4>(P, es, Eq[4], So[4], Eq[8], So[8]);
     const T sEq = sym8p(Eq);
     Eq[0] = sub2(mk2(MODEL == AC ? R(0.) : dp, dphi_c), sEq);
     if (MODEL == AC) {
@@ -422,18 +469,22 @@ __device__ __forceinline__ void face_flux(const PR<R> &P, FO &&O, FN &&N, FD &&D
     }
     const R uu = Uf * Uf + Vf * Vf;
     const T a2 = mk2(P.ah_f, P.h_ah), c2 = mk2(P.tauf * (R(1.) - P.ah_f), P.h_ch);
-    // face distributions of the six directions crossing the face: Eq + a (bh - Eq) + c S
+    // face distributions of the six directions crossing the face (three opposite
+    // pairs): Eq + a (bh - Eq) + c S
     T out[9];
-#define DUGKS_FACE_Q(Q)                                                                                   \
-    if ((XF ? d2q9_xu(Q) : d2q9_xv(Q)) != 0) {                                                            \
-        T Eq, So;                                                                                         \
-        eq_src<MODEL, Q>(P, Uf, Vf, uu, rhof, phif, dpf, dphif, av[4], av[5], av[2], av[3], av[0], av[1], \
-                         Eq, So);                                                                         \
-        out[Q] = fma2(c2, So, fma2(a2, sub2(bh[Q], Eq), Eq));                                             \
-    }
-    DUGKS_FACE_Q(1) DUGKS_FACE_Q(2) DUGKS_FACE_Q(3) DUGKS_FACE_Q(4)
-    DUGKS_FACE_Q(5) DUGKS_FACE_Q(6) DUGKS_FACE_Q(7) DUGKS_FACE_Q(8)
-#undef DUGKS_FACE_Q
+    const EqSite<R> es = eq_site<MODEL, R>(P, Uf, Vf, uu, rhof, phif, dpf, dphif, av[4], av[5], av[2], av[3], av[0],
+                                           av[1]);
+    auto face_pair = [&](auto QC) {
+        constexpr int Qa = decltype(QC)::value, Qb = Qa + 4;
+        T Eq, So, Eqb, Sob;
+        eq_pair<MODEL, Qa>(P, es, Eq, So, Eqb, Sob);
+        out[Qa] = fma2(c2, So, fma2(a2, sub2(bh[Qa], Eq), Eq));
+        out[Qb] = fma2(c2, Sob, fma2(a2, sub2(bh[Qb], Eqb), Eqb));
+    };
+    if (XF) face_pair(std::integral_constant<int, 1>());  // E, W
+    else face_pair(std::integral_constant<int, 3>());     // N, S
+    face_pair(std::integral_constant<int, 2>());          // NE, SW
+    face_pair(std::integral_constant<int, 4>());          // NW, SE
     if (!XF && wall) {
         // bounce-back of the directions entering the fluid (Ark/Cpp/Boundary.cpp:118-139)
         const bool bottom = wall == 1;

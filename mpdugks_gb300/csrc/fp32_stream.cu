@@ -36,7 +36,7 @@ namespace dugks {
 namespace f32 {
 
 constexpr int SW = 28;   // interior columns of a strip
-constexpr int SEG = 128; // rows of a segment
+constexpr int SEG_MAX = 128;  // rows of a segment: 128, 64 or 32 (enough segments per warp)
 constexpr int WPB = 2;   // warps per block
 constexpr int NSTG = 4;  // stage ring: rows k .. k+3
 constexpr int NPL = 18;  // staged planes per row: f and h deviations (aux is read directly)
@@ -54,7 +54,7 @@ __device__ __forceinline__ int wrap_any(int j, int n) { return ((j % n) + n) % n
 
 template <int MODEL, bool WALLS>
 __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, int gin, int gout, uint32_t step,
-                                                       int nstrips, int nsegs) {
+                                                       int nstrips, int nsegs, int seg_rows) {
     using T = float2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
     for (int item = gw; item < nstrips * nsegs; item += nw) {
         const int strip = item % nstrips, seg = item / nstrips;
         const int x0 = strip * SW, w = min(SW, nx - x0);
-        const int y0 = seg * SEG, y1 = min(y0 + SEG, ny);
+        const int y0 = seg * seg_rows, y1 = min(y0 + seg_rows, ny);
         const int gi = wrap_any(x0 - 2 + lane, nx);
         const bool interior = lane >= 2 && lane < 2 + w;
         const bool colL = lane >= 1 && lane <= 2 + w;  // lanes whose f-bar-plus is needed
@@ -314,10 +314,16 @@ static cudaError_t launch_stream_t(const P32 &P, const S32 &S, int first, int gi
         if ((e = cudaDeviceGetAttribute(&g_stream_nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
         ready = true;
     }
-    const int nstrips = (P.nx + SW - 1) / SW, nsegs = (P.ny + SEG - 1) / SEG;
+    // the longest segment that still gives every resident warp about 4 segments
+    // (a long segment costs fewer warm-up rows, a short one less idle tail)
+    const int nstrips = (P.nx + SW - 1) / SW, warps = g_stream_nsm * g_stream_blocks * WPB;
+    int seg = SEG_MAX;
+    while (seg > 32 && (long long)nstrips * ((P.ny + seg - 1) / seg) < 4LL * warps) seg /= 2;
+    const int nsegs = (P.ny + seg - 1) / seg;
     const int items = nstrips * nsegs;
     const int blocks = min((items + WPB - 1) / WPB, g_stream_nsm * g_stream_blocks);
-    k_stream32<MODEL, WALLS><<<blocks, WPB * 32, STREAM_SMEM, st>>>(P, S, first, gin, gout, step, nstrips, nsegs);
+    k_stream32<MODEL, WALLS><<<blocks, WPB * 32, STREAM_SMEM, st>>>(P, S, first, gin, gout, step, nstrips, nsegs,
+                                                                     seg);
     return cudaGetLastError();
 }
 
