@@ -51,9 +51,9 @@ WORKLOADS = {
 #   FP64 (multi-kernel step): 18 distributions + 2 aux planes, 8 B, read and written = 320 B
 ALGO_BYTES = {'fp32dev': 192, 'fp64': 320, 'fp64fma': 320, 'fp64fused': 384}
 # DRAM bytes per cell and step of the fused FP32 kernel: ncu dram__bytes_read.sum +
-# dram__bytes_write.sum of one k_step32 launch on 2048x2048 cells, divided by the cells
-# (profiles/k_step32_rt2048x2048_fp32.md); scaled by the cell count to a full launch
-TRAFFIC_BYTES = {'fp32dev': (402.798848e6 + 354.459904e6) / (2048 * 2048)}
+# dram__bytes_write.sum of one k_stream32 launch on 3072x3072 cells, divided by the cells
+# (profiles/k_stream32_rt3072x3072_fp32.md); scaled by the cell count to a full launch
+TRAFFIC_BYTES = {'fp32dev': (1012.259e6 + 860.715e6) / (3072 * 3072)}
 
 
 def case_kw(wl: dict) -> dict:
@@ -382,7 +382,7 @@ def run_ours(args, wl, rank, world, local):
     algo = ALGO_BYTES[prec]
     achieved = algo * cells / (step_ms * 1e-3) / 1e9
     if prec == 'fp32dev':
-        kernel = 'k_step32 (the fused step: one launch per step)'
+        kernel = 'k_stream32 (the fused step: one launch per step)'
         phase = None
     else:
         nprof = max(10, min(100, args.steps))
@@ -393,7 +393,7 @@ def run_ours(args, wl, rank, world, local):
     roofline = {'bound': 'hbm', 'achieved': round(achieved, 2), 'peak': hbm_peak, 'unit': 'GB/s',
                 'frac': round(achieved / hbm_peak, 5),
                 'traffic': None if traffic is None else int(traffic * cells),
-                'traffic_source': None if traffic is None else 'ncu DRAM bytes of one launch at 2048x2048, '
+                'traffic_source': None if traffic is None else 'ncu DRAM bytes of one launch at 3072x3072, '
                                                                'scaled by the cell count',
                 'kernel': kernel, 'algorithmic_bytes_per_cell': algo,
                 'cells_per_launch': cells, 'peak_source': f'{peak_kind} hbm_gbs (copy bandwidth)'}
