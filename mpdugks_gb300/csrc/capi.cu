@@ -42,6 +42,10 @@ void launch_macros64f(const PR<double> &P, const SR<double> &S, double *rho, dou
                       double *phi, int opitch, cudaStream_t st, int64_t *launches);
 cudaError_t launch_stream32(const P32 &P, const S32 &S, int first, int gin, int gout, cudaStream_t st,
                             int64_t *launches, uint32_t step);
+cudaError_t launch_pp32_step(const PPP &P, const PPS &S, int do_msrc, cudaStream_t st, int64_t *launches,
+                             uint32_t step);
+cudaError_t launch_pp32_force(const PPP &P, const PPS &S, cudaStream_t st, int64_t *launches);
+void set_d2v16_matrix_f32(const double *m256, cudaStream_t st);
 template <typename R>
 cudaError_t launch_plane_from_f64(R *dst, int dpitch, const double *src, int nx, int ny, double sub,
                                   cudaStream_t st, int64_t *launches);
@@ -71,6 +75,7 @@ void build_d2v16_matrix(double c, double out[16][16]);
 void derive_params(const dugks_case_t &cs, const dugks_grid_t &g, Params &P);
 int host_init_state(const Params &P, const double iM[16][16], int kind, const double *params, int nparams,
                     uint64_t seed, std::vector<double> &f, std::vector<double> &h, std::vector<double> &aux);
+void pp_rest_eq(const Params &P, const double iM[16][16], double rho, double *eq);
 }  // namespace dugks
 
 using namespace dugks;
@@ -102,6 +107,11 @@ struct dugks_handle {
     int first = 1;            // next step is the first after an upload
     bool macros_fresh = false;
     double *out3 = nullptr;   // tau, Fx, Fy for output (allocated on first request)
+    // FP32 storage of the pseudopotential models
+    bool pp32 = false;
+    f32::PPP PPc{};
+    f32::PPS PPs{};
+    int pp_pending = 0;       // the next collision computes the cell force from psi
 };
 
 static std::string g_create_err;
@@ -187,6 +197,157 @@ static size_t fp64_arena_bytes(const Params &P) {
     total += cellb;                               // rho_last
     total += align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 256 + 256;
     return total;
+}
+
+static cudaError_t to_dev(const dugks_handle *h, double *d, const double *src, int rows = -1);
+
+// device bytes of one FP32 pseudopotential case
+static size_t pp32_arena_bytes(const Params &P) {
+    const size_t cf = align256((size_t)P.pitch * P.ny * sizeof(float));
+    const size_t cd = align256((size_t)P.pitch * P.ny * sizeof(double));
+    return (6 * (size_t)P.Q + 18) * cf + 6 * cd + align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 512;
+}
+
+static int create_pp32(dugks_handle *h, dugks_handle_t **out) {
+    Params &P = h->P;
+    h->pp32 = true;
+    h->nblocks = REDUCE_BLOCKS;
+    const size_t cf = align256((size_t)P.pitch * P.ny * sizeof(float));
+    const size_t cd = align256((size_t)P.pitch * P.ny * sizeof(double));
+    const size_t total = pp32_arena_bytes(P);
+    cudaError_t e = cudaMalloc(&h->arena, total);
+    if (e != cudaSuccess) {
+        delete h;
+        return fail(nullptr, e == cudaErrorMemoryAllocation ? DUGKS_ENOMEM : DUGKS_ECUDA,
+                    std::string("cudaMalloc of device state failed: ") + cudaGetErrorString(e));
+    }
+    h->arena_bytes = total;
+    cudaMemsetAsync(h->arena, 0, total, nullptr);
+    char *cur = h->arena;
+    auto tf = [&](size_t n) { float *p = reinterpret_cast<float *>(cur); cur += n * cf; return p; };
+    auto td = [&]() { double *p = reinterpret_cast<double *>(cur); cur += cd; return p; };
+    f32::PPS &S = h->PPs;
+    const int Q = P.Q;
+    S.qs = cf / sizeof(float);
+    S.df = tf(Q);
+    S.bf = tf(Q);
+    S.xb = tf(Q);
+    S.yb = tf(Q);
+    S.xfl = tf(Q);
+    S.yfl = tf(Q);
+    float **scal[] = {&S.xr, &S.yr, &S.xu, &S.yu, &S.xv, &S.yv, &S.xg, &S.yg, &S.xps, &S.yps,
+                      &S.xFx, &S.xFy, &S.yFx, &S.yFy, &S.psi, &S.scg, &S.Fx, &S.Fy};
+    for (auto p : scal) *p = tf(1);
+    S.rho = td();
+    S.p = td();
+    S.U = td();
+    S.V = td();
+    h->S.fld[F_RHO] = S.rho;
+    h->S.fld[F_P] = S.p;
+    h->S.fld[F_U] = S.U;
+    h->S.fld[F_V] = S.V;
+    h->S.fld[F_PHI] = td();  // no phase field: zeros for the reductions and downloads
+    h->rho_last = td();
+    h->partial = reinterpret_cast<double *>(cur);
+    cur += align256(sizeof(double) * 4 * REDUCE_BLOCKS);
+    h->out4 = reinterpret_cast<double *>(cur);
+    cur += 256;
+    h->flag = reinterpret_cast<int *>(cur);
+    // constants
+    f32::PPP &C = h->PPc;
+    C.nx = P.nx;
+    C.ny = P.ny;
+    C.pitch = P.pitch;
+    C.model = P.model;
+    C.Q = Q;
+    C.hDt = (float)P.hDt;
+    C.dt = (float)P.dt;
+    C.RT = (float)P.RT;
+    C.invRT = (float)(1.0 / P.RT);
+    C.Lambda0 = (float)P.Lambda0;
+    C.Tau0 = (float)P.Tau0;
+    C.aTP = (float)P.aTP;
+    C.bTP = (float)P.bTP;
+    C.dtV = (float)P.dtV;
+    C.r_2dy = (float)P.r_2dy;
+    C.r_ndx = (float)P.r_ndx;
+    C.r_n2dx = (float)P.r_n2dx;
+    C.r_ndy = (float)P.r_ndy;
+    C.inv_6_2dx = (float)(1.0 / (P._2dx * 6));
+    C.inv_6_2dy = (float)(1.0 / (P._2dy * 6));
+    C.R0 = P.R0;
+    C.T_CS = P.T_CS;
+    C.aCS = P.aCS;
+    C.RTd = P.RT;
+    for (int q = 0; q < Q; ++q) {
+        C.xi_u[q] = (float)P.xi_u[q];
+        C.xi_v[q] = (float)P.xi_v[q];
+    }
+    for (int q = 0; q < 9; ++q) C.w9[q] = (float)P.omega[q];
+    if (P.model == PP16) f32::set_d2v16_matrix_f32(&h->iM[0][0], nullptr);
+    e = cudaStreamSynchronize(nullptr);
+    if (e != cudaSuccess) {
+        cudaFree(h->arena);
+        delete h;
+        return fail(nullptr, DUGKS_ECUDA, std::string("device setup failed: ") + cudaGetErrorString(e));
+    }
+    *out = h;
+    return DUGKS_OK;
+}
+
+// FP64 [Q][ny][nx] state -> deviations from the rest equilibrium at the mean density
+static int upload_pp32(dugks_handle *h, const double *f, const double *aux) {
+    const Params &P = h->P;
+    const int nx = P.nx, ny = P.ny;
+    const size_t n = (size_t)nx * ny;
+    cudaStream_t st = h->last_stream;
+    f32::PPP &C = h->PPc;
+    f32::PPS &S = h->PPs;
+    double mean = 0.0;
+    for (size_t k = 0; k < n; ++k) mean += aux[(size_t)F_RHO * n + k];
+    C.rho_ref = mean / (double)n;
+    double rest[16];
+    pp_rest_eq(P, h->iM, C.rho_ref, rest);
+    for (int q = 0; q < P.Q; ++q) C.frest[q] = (float)rest[q];
+    double *stage = nullptr;
+    cudaError_t e = cudaMalloc(&stage, n * sizeof(double));
+    if (e != cudaSuccess) return cuda_fail(h, e, "upload staging");
+    auto put = [&](float *dst, const double *src, double sub) -> cudaError_t {
+        cudaError_t r = cudaMemcpyAsync(stage, src, n * sizeof(double), cudaMemcpyHostToDevice, st);
+        if (r != cudaSuccess) return r;
+        return f32::launch_plane_from_f64<float>(dst, P.pitch, stage, nx, ny, sub, st, &h->launches);
+    };
+    for (int q = 0; q < P.Q && e == cudaSuccess; ++q)
+        e = put(S.df + (size_t)q * S.qs, f + (size_t)q * n, (double)C.frest[q]);
+    if (e == cudaSuccess) e = put(S.Fx, aux + (size_t)F_FX * n, 0.0);
+    if (e == cudaSuccess) e = put(S.Fy, aux + (size_t)F_FY * n, 0.0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(stage);
+    if (e != cudaSuccess) return cuda_fail(h, e, "upload");
+    // the FP64 planes of the state as uploaded; face forces and psi restart
+    const int fid[4] = {F_RHO, F_U, F_V, F_P};
+    for (int k : fid)
+        if ((e = to_dev(h, h->S.fld[k], aux + (size_t)k * n)) != cudaSuccess) return cuda_fail(h, e, "upload");
+    float *zero[] = {S.xFx, S.xFy, S.yFx, S.yFy, S.psi, S.scg};
+    for (auto z : zero) cudaMemsetAsync(z, 0, S.qs * sizeof(float), st);
+    cudaMemsetAsync(h->rho_last, 0, (size_t)P.pitch * ny * sizeof(double), st);
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "upload");
+    h->pp_pending = 0;
+    h->steps = 0;
+    return DUGKS_OK;
+}
+
+// an FP32 plane of the pseudopotential state as FP64 [ny][nx]
+static int pp32_plane_to_host(dugks_handle *h, const float *d, double *out) {
+    const Params &P = h->P;
+    std::vector<float> tmp((size_t)P.nx * P.ny);
+    cudaError_t e = cudaMemcpy2DAsync(tmp.data(), (size_t)P.nx * sizeof(float), d, (size_t)P.pitch * sizeof(float),
+                                      (size_t)P.nx * sizeof(float), P.ny, cudaMemcpyDeviceToHost, h->last_stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->last_stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "download field");
+    for (size_t k = 0; k < tmp.size(); ++k) out[k] = tmp[k];
+    return DUGKS_OK;
 }
 
 template <typename R>
@@ -315,8 +476,7 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
         return fail(nullptr, DUGKS_EINVAL, "pseudopotential models are periodic only (faceFaces need no walls)");
     if (c->precision < DUGKS_FP64 || c->precision > DUGKS_FP64_FUSED)
         return fail(nullptr, DUGKS_EINVAL, "unknown precision");
-    if ((c->precision == DUGKS_FP32_DEV || c->precision == DUGKS_FP64_FUSED) &&
-        !(c->model == DUGKS_MODEL_AC || c->model == DUGKS_MODEL_HCZ))
+    if (c->precision == DUGKS_FP64_FUSED && !(c->model == DUGKS_MODEL_AC || c->model == DUGKS_MODEL_HCZ))
         return fail(nullptr, DUGKS_EINVAL, "the fused deviation-form step supports the Allen-Cahn models (AC, HCZ)");
     dugks_handle *h = new (std::nothrow) dugks_handle();
     if (!h) return fail(nullptr, DUGKS_ENOMEM, "host allocation failed");
@@ -325,6 +485,7 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
     derive_params(*c, *g, h->P);
     Params &P = h->P;
     if (P.model == PP16) build_d2v16_matrix(P.c16, h->iM);
+    if (c->precision == DUGKS_FP32_DEV && (P.model == PP9 || P.model == PP16)) return create_pp32(h, out);
     if (c->precision == DUGKS_FP32_DEV || c->precision == DUGKS_FP64_FUSED) return create_fp32(h, out);
     // ---- carve the arena
     const size_t rowb = (size_t)P.pitch * sizeof(double);
@@ -390,7 +551,7 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
 extern "C" int dugks_gpu_nq(const dugks_handle_t *h) { return h ? h->P.Q : 0; }
 
 // host [ny][nx] <-> device [ny][pitch]
-static cudaError_t to_dev(const dugks_handle *h, double *d, const double *src, int rows = -1) {
+static cudaError_t to_dev(const dugks_handle *h, double *d, const double *src, int rows) {
     const Params &P = h->P;
     return cudaMemcpy2D(d, (size_t)P.pitch * sizeof(double), src, (size_t)P.nx * sizeof(double),
                         (size_t)P.nx * sizeof(double), rows < 0 ? P.ny : rows, cudaMemcpyHostToDevice);
@@ -416,6 +577,7 @@ extern "C" int dugks_gpu_upload(dugks_handle_t *h, const double *f, const double
     const bool hasH = (P.model == AC || P.model == HCZ);
     if (hasH && !hd) return fail(h, DUGKS_EINVAL, "Allen-Cahn models need the h distribution");
     if (h->fp32) return upload_fp32(h, f, hd, aux);
+    if (h->pp32) return upload_pp32(h, f, aux);
     cudaError_t e;
     for (int q = 0; q < P.Q; ++q) {
         if ((e = to_dev(h, h->S.f + q * h->S.qs, f + q * n)) != cudaSuccess) return cuda_fail(h, e, "upload f");
@@ -458,6 +620,18 @@ extern "C" int dugks_gpu_step(dugks_handle_t *h, int nsteps, void *stream) {
         if (e != cudaSuccess) return cuda_fail(h, e, "stream switch");
         h->last_stream = st;
     }
+    if (h->pp32) {
+        for (int s = 0; s < nsteps; ++s) {
+            cudaError_t e = f32::launch_pp32_step(h->PPc, h->PPs, h->pp_pending, st, &h->launches,
+                                                  (uint32_t)(h->steps + s));
+            if (e != cudaSuccess) return cuda_fail(h, e, "fp32 pseudopotential step launch");
+            h->pp_pending = 1;
+        }
+        h->steps += nsteps;
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(h, e, "step launch");
+        return DUGKS_OK;
+    }
     if (h->fp32) {
         for (int s = 0; s < nsteps; ++s) {
             const uint32_t sn = (uint32_t)(h->steps + s);
@@ -489,7 +663,7 @@ extern "C" int dugks_gpu_step(dugks_handle_t *h, int nsteps, void *stream) {
 
 extern "C" int dugks_gpu_step_profiled(dugks_handle_t *h, int nsteps, void *stream, double *ms, int *nph) {
     if (!h || !ms || !nph) return fail(h, DUGKS_EINVAL, "null argument");
-    if (h->fp32) {  // one fused kernel per step: phase 0 is the whole step
+    if (h->fp32 || h->pp32) {  // phase 0 is the whole step
         int rc0 = dugks_gpu_step(h, 0, stream);
         if (rc0) return rc0;
         cudaStream_t st0 = static_cast<cudaStream_t>(stream);
@@ -574,6 +748,27 @@ static bool is_msrc_field(const Params &P, int f) {
 
 extern "C" int dugks_gpu_get_field(dugks_handle_t *h, int field, double *out) {
     if (!h || !out || field < 0 || field >= NFIELDS) return fail(h, DUGKS_EINVAL, "bad field or null pointer");
+    if (h->pp32) {
+        int rc = sync_last(h);
+        if (rc) return rc;
+        if (field == F_RHO || field == F_U || field == F_V || field == F_P || field == F_PHI) {
+            cudaError_t e = to_host(h, out, h->S.fld[field]);
+            if (e != cudaSuccess) return cuda_fail(h, e, "download field");
+            return DUGKS_OK;
+        }
+        if (field == F_FX || field == F_FY) {  // the cell force of the current psi
+            cudaError_t e = f32::launch_pp32_force(h->PPc, h->PPs, h->last_stream, &h->launches);
+            if (e != cudaSuccess) return cuda_fail(h, e, "force launch");
+            return pp32_plane_to_host(h, field == F_FX ? h->PPs.Fx : h->PPs.Fy, out);
+        }
+        if (field == F_PSI) return pp32_plane_to_host(h, h->PPs.psi, out);
+        if (field == F_SCG) return pp32_plane_to_host(h, h->PPs.scg, out);
+        if (field == F_TAU) {
+            for (size_t k = 0; k < (size_t)h->P.nx * h->P.ny; ++k) out[k] = h->P.Tau0;
+            return DUGKS_OK;
+        }
+        return fail(h, DUGKS_EINVAL, "FP32 pseudopotential storage exposes rho, u, v, p, psi, G, tau, Fx, Fy");
+    }
     if (h->fp32) {
         const bool forces = field == F_TAU || field == F_FX || field == F_FY;
         if (!(field == F_RHO || field == F_U || field == F_V || field == F_P || field == F_PHI || forces))
@@ -630,6 +825,15 @@ extern "C" int dugks_gpu_get_dist(dugks_handle_t *h, int which, double *out) {
     int rc = sync_last(h);
     if (rc) return rc;
     const size_t n = (size_t)h->P.nx * h->P.ny;
+    if (h->pp32) {
+        for (int q = 0; q < h->P.Q; ++q) {
+            int rc2 = pp32_plane_to_host(h, h->PPs.df + (size_t)q * h->PPs.qs, out + q * n);
+            if (rc2) return rc2;
+            const double r0 = h->PPc.frest[q];
+            for (size_t k = 0; k < n; ++k) out[q * n + k] += r0;
+        }
+        return DUGKS_OK;
+    }
     if (h->fp32) {
         const size_t es = h->fused64 ? sizeof(double) : sizeof(float);
         std::vector<unsigned char> tmp(n * es);
@@ -671,7 +875,11 @@ extern "C" int dugks_gpu_check_finite(dugks_handle_t *h) {
     cudaStream_t st = h->last_stream;
     cudaMemsetAsync(h->flag, 0, sizeof(int), st);
     const bool hasH = (P.model == AC || P.model == HCZ);
-    if (h->fp32) {
+    if (h->pp32) {
+        const size_t qs = (size_t)P.pitch * P.ny;
+        const int fids[4] = {F_RHO, F_U, F_V, F_P};
+        for (int k : fids) launch_check_finite(h->S.fld[k], qs, h->flag, st, &h->launches);
+    } else if (h->fp32) {
         int rc = macros_fp32(h);
         if (rc) return rc;
         const size_t qs = (size_t)P.pitch * P.ny;
@@ -714,6 +922,7 @@ namespace internal {
 size_t footprint(const dugks_case_t &c, const dugks_grid_t &g) {
     Params P;
     derive_params(c, g, P);
+    if (c.precision == DUGKS_FP32_DEV && (P.model == PP9 || P.model == PP16)) return pp32_arena_bytes(P);
     if (c.precision == DUGKS_FP32_DEV) return fused_arena_bytes(P, sizeof(float));
     if (c.precision == DUGKS_FP64_FUSED) return fused_arena_bytes(P, sizeof(double));
     return fp64_arena_bytes(P);

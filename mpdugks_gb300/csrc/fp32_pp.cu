@@ -1,0 +1,323 @@
+// FP32 deviation-storage step of the pseudopotential models (D2Q9PP, D2V16).
+//
+// The reference's face force reads the face psi of the neighbouring faces of
+// the same step (Ark/Cpp/PseudoP.cpp:39-46, Jacobi semantics: all face psi
+// first, then the face forces), so the step keeps four passes like the FP64
+// path: collision (with the cell force from the psi of the previous update),
+// face pass 1 (reconstruction, face moments, face psi), face pass 2 (face
+// force, equilibrium, He-Shan-Doolen source, flux) and the update (with the
+// cell macros, pressure and psi).
+//
+// Storage: f as FP32 deviations from the rest equilibrium f_rest =
+// eq(rho_ref, 0, 0); the step's scratch in FP32; the density in FP64.  Every
+// relation of the step is affine with coefficients summing to one and the rest
+// parts of a cell's four face fluxes cancel, so the step runs on deviations.
+// Equilibria are evaluated as deviations directly: eq(rho, u) - f_rest =
+// iM (M(rho, u) - M(rho_ref, 0)) with d rho = rho - rho_ref taken in FP64, so
+// nothing cancels.  Cell moment sums are FP64; stores are stochastically
+// rounded as in the Allen-Cahn path.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "dugks_device.cuh"
+#include "fp32_math.cuh"
+#include "fp32_state.cuh"
+
+namespace dugks {
+namespace f32 {
+
+__constant__ float c_iM16f[16][16];  // D2V16 inverse moment matrix (Ark/Lib/D2V16.cpp:34-52), FP32
+
+void set_d2v16_matrix_f32(const double *m256, cudaStream_t st) {
+    float m[256];
+    for (int k = 0; k < 256; ++k) m[k] = (float)m256[k];
+    cudaMemcpyToSymbolAsync(c_iM16f, m, sizeof(m), 0, cudaMemcpyHostToDevice, st);
+    cudaStreamSynchronize(st);  // m is on the stack
+}
+
+// Equilibrium deviations de_q = eq_q(rho, u, v) - f_rest_q.
+template <int MODEL>
+__device__ __forceinline__ void pp_deq(const PPP &P, float dr, float rho, float u, float v, float *de) {
+    if (MODEL == PP16) {
+        // Macro16 (Ark/Lib/D2V16.cpp:125-145) at T = T0, p = rho RT, minus its value at
+        // (rho_ref, 0, 0): linear in rho at rest
+        const float RT = P.RT, u2 = u * u, v2 = v * v, s2 = u2 + v2;
+        float M[16];
+        M[0] = dr;
+        M[1] = rho * u;
+        M[2] = rho * v;
+        M[3] = 3.f * RT * dr + rho * s2;
+        M[4] = M[1] * v;
+        M[5] = RT * dr + rho * u2;
+        M[6] = RT * dr + rho * v2;
+        M[7] = M[1] * (5.f * RT + s2);
+        M[8] = M[2] * (5.f * RT + s2);
+        M[9] = M[1] * (3.f * RT + u2);
+        M[10] = M[2] * (3.f * RT + v2);
+        M[11] = M[2] * (RT + u2);
+        M[12] = M[1] * (RT + v2);
+        M[13] = (7.f * RT + s2) * M[4];
+        M[14] = 5.f * RT * RT * dr + rho * RT * (8.f * u2 + v2) + rho * u2 * s2;
+        M[15] = 5.f * RT * RT * dr + rho * RT * (8.f * v2 + u2) + rho * v2 * s2;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            float s = 0.f;
+#pragma unroll
+            for (int k = 0; k < 16; ++k) s = fmaf(c_iM16f[j][k], M[k], s);
+            de[j] = s;
+        }
+    } else {
+        // D2Q9PP (Ark/Lib/D2Q9PP.cpp:51-62): w rho (1 + u1 + u1^2/2 - |u|^2 lambda)
+        const float uu = u * u + v * v;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const float u1 = (sxf(d2q9_xu(q), u) + sxf(d2q9_xv(q), v)) * P.invRT;
+            de[q] = P.w9[q] * (dr + rho * (u1 + 0.5f * u1 * u1 - uu * P.Lambda0));
+        }
+    }
+}
+
+// Carnahan-Starling pressure (Ark/Lib/nonidealEoS.h:114-118) and calcPsi
+// (Ark/Header/Macroscopic.h:64-68), in FP64 from the FP64 density.
+__device__ __forceinline__ double cs_p(const PPP &P, double rho) {
+    return rho * P.R0 * P.T_CS * (1.0 + rho + rho * rho - rho * rho * rho) /
+               ((1.0 - rho) * (1.0 - rho) * (1.0 - rho)) -
+           P.aCS * rho * rho;
+}
+__device__ __forceinline__ void cs_psi(const PPP &P, double rho, double p, float &scg, float &psi) {
+    const double G = (double)((p > rho * P.RTd) - (p < rho * P.RTd));
+    scg = (float)G;
+    psi = (float)sqrt(2.0 * (p - rho * P.RTd) / G);
+}
+
+__device__ __forceinline__ float sr1(float a, float b, uint32_t bits16) {
+    const float s = a + b;
+    const float bb = s - a;
+    const float err = (a - (s - bb)) + (b - bb);
+    return sr_lane(s, err, bits16);
+}
+
+// 8-neighbour isotropic gradient of a periodic field (Ark/Lib/GradSchemeBasic.h:153-208)
+__device__ __forceinline__ void iso_grad(const PPP &P, const float *__restrict__ a, int i, int j, float &gx,
+                                         float &gy) {
+    const int nx = P.nx, ny = P.ny, pitch = P.pitch;
+    const int im = wrapi(i - 1, nx), ip = wrapi(i + 1, nx), jm = wrapi(j - 1, ny), jp = wrapi(j + 1, ny);
+    auto at = [&](int jj, int ii) { return a[(size_t)jj * pitch + ii]; };
+    const float E = at(j, ip), W = at(j, im), N = at(jp, i), S = at(jm, i);
+    const float NE = at(jp, ip), NW = at(jp, im), SE = at(jm, ip), SW = at(jm, im);
+    gx = (4.f * (E - W) + ((NE - NW) + (SE - SW))) * P.inv_6_2dx;
+    gy = (4.f * (N - S) + ((NE - SE) + (NW - SW))) * P.inv_6_2dy;
+}
+
+// Collision pre-step: cell force F = -G psi grad psi (Ark/Cpp/PseudoP.cpp:31-38, from the
+// previous update's psi) when do_msrc, equilibrium, source, f-bar-plus deviations.
+template <int MODEL>
+__global__ void __launch_bounds__(256) k_pp32_collide(PPP P, PPS S, int do_msrc) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= P.nx || j >= P.ny) return;
+    constexpr int Q = MODEL == PP16 ? 16 : 9;
+    const size_t c = (size_t)j * P.pitch + i;
+    float fx, fy;
+    if (do_msrc) {
+        float gx, gy;
+        iso_grad(P, S.psi, i, j, gx, gy);
+        const float k = -S.scg[c] * S.psi[c];
+        fx = gx * k;
+        fy = gy * k;
+        S.Fx[c] = fx;
+        S.Fy[c] = fy;
+    } else {
+        fx = S.Fx[c];
+        fy = S.Fy[c];
+    }
+    const double rhod = S.rho[c];
+    const float rho = (float)rhod, dr = (float)(rhod - P.rho_ref);
+    const float U = (float)S.U[c], V = (float)S.V[c];
+    float de[Q];
+    pp_deq<MODEL>(P, dr, rho, U, V, de);
+    const float tau = P.Tau0;
+    const float aBP = (2.f * tau - P.hDt) / (2.f * tau + P.dt), bBP = 1.f - aBP, cBP = tau * bBP;
+    const float inv = 1.f / (rho * P.RT);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const float eq = P.frest[q] + de[q];
+        const float So = (fx * (P.xi_u[q] - U) + fy * (P.xi_v[q] - V)) * eq * inv;
+        const size_t o = (size_t)q * S.qs + c;
+        const float d = S.df[o];
+        S.bf[o] = d + (bBP * (de[q] - d) + cBP * So);
+    }
+}
+
+// Face pass 1 (x faces: blockIdx.z = 0, y faces: 1): half-step reconstruction,
+// face moments with the previous face force, face pressure and psi
+// (Ark/Lib/D2Q9PP.cpp:110-136, Ark/Cpp/PseudoP.cpp:23-30).
+template <int MODEL>
+__global__ void __launch_bounds__(256) k_pp32_faces1(PPP P, PPS S) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    const bool xf = blockIdx.z == 0;
+    if (i >= P.nx || j >= P.ny) return;
+    constexpr int Q = MODEL == PP16 ? 16 : 9;
+    const int nx = P.nx, ny = P.ny, pitch = P.pitch;
+    const int im = wrapi(i - 1, nx), ip = wrapi(i + 1, nx), jm = wrapi(j - 1, ny), jp = wrapi(j + 1, ny);
+    const size_t c = (size_t)j * pitch + i;
+    double sR = 0.0;
+    float su = 0.f, sv = 0.f;
+    float *B = xf ? S.xb : S.yb;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const float *F = S.bf + (size_t)q * S.qs;
+        auto at = [&](int jj, int ii) { return F[(size_t)jj * pitch + ii]; };
+        float o, n, gx, gy;
+        if (xf) {  // between (i-1, j) and (i, j)
+            o = at(j, im);
+            n = at(j, i);
+            gy = (0.5f * ((at(jp, i) - at(jm, i)) + (at(jp, im) - at(jm, im)))) * P.r_2dy;
+            gx = (o - n) * P.r_ndx;
+        } else {  // between (i, j-1) and (i, j)
+            o = at(jm, i);
+            n = at(j, i);
+            gx = (0.5f * ((at(j, im) - at(j, ip)) + (at(jm, im) - at(jm, ip)))) * P.r_n2dx;
+            gy = (o - n) * P.r_ndy;
+        }
+        const float b = 0.5f * (o + n) - P.hDt * (gx * P.xi_u[q] + gy * P.xi_v[q]);
+        B[(size_t)q * S.qs + c] = b;
+        sR += (double)b;
+        su += b * P.xi_u[q];
+        sv += b * P.xi_v[q];
+    }
+    const double R = P.rho_ref + sR;
+    const float Rf = (float)R;
+    float U = su / Rf, V = sv / Rf;
+    U += 0.5f * P.hDt * (xf ? S.xFx : S.yFx)[c] / Rf;
+    V += 0.5f * P.hDt * (xf ? S.xFy : S.yFy)[c] / Rf;
+    const double p = cs_p(P, R);
+    float scg, psi;
+    cs_psi(P, R, p, scg, psi);
+    (xf ? S.xr : S.yr)[c] = (float)(R - P.rho_ref);
+    (xf ? S.xu : S.yu)[c] = U;
+    (xf ? S.xv : S.yv)[c] = V;
+    (xf ? S.xg : S.yg)[c] = scg;
+    (xf ? S.xps : S.yps)[c] = psi;
+}
+
+// Face pass 2: face force from the face-psi stencil (Ark/Cpp/PseudoP.cpp:39-46,
+// Ark/Lib/GradSchemeBasic.h:181-208), equilibrium, source and flux xi.n.
+template <int MODEL>
+__global__ void __launch_bounds__(256) k_pp32_faces2(PPP P, PPS S) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    const bool xf = blockIdx.z == 0;
+    if (i >= P.nx || j >= P.ny) return;
+    constexpr int Q = MODEL == PP16 ? 16 : 9;
+    const size_t c = (size_t)j * P.pitch + i;
+    float gx, gy;
+    iso_grad(P, xf ? S.xps : S.yps, i, j, gx, gy);
+    const float k = -(xf ? S.xg : S.yg)[c] * (xf ? S.xps : S.yps)[c];
+    const float Fx = gx * k, Fy = gy * k;
+    (xf ? S.xFx : S.yFx)[c] = Fx;
+    (xf ? S.xFy : S.yFy)[c] = Fy;
+    const float dr = (xf ? S.xr : S.yr)[c];
+    const float R = (float)(P.rho_ref + (double)dr);
+    const float U = (xf ? S.xu : S.yu)[c], V = (xf ? S.xv : S.yv)[c];
+    float de[Q];
+    pp_deq<MODEL>(P, dr, R, U, V, de);
+    const float tauh = P.Tau0;
+    const float ah = 2.f * tauh / (2.f * tauh + P.hDt), bh = 1.f - ah, ch = tauh * bh;
+    const float inv = 1.f / (R * P.RT);
+    const float *__restrict__ B = xf ? S.xb : S.yb;
+    float *out = xf ? S.xfl : S.yfl;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const float eq = P.frest[q] + de[q];
+        const float So = (Fx * (P.xi_u[q] - U) + Fy * (P.xi_v[q] - V)) * eq * inv;
+        const float b = B[(size_t)q * S.qs + c];
+        const float t = de[q] + ah * (b - de[q]) + ch * So;
+        out[(size_t)q * S.qs + c] = t * (xf ? P.xi_u[q] : P.xi_v[q]);
+    }
+}
+
+// Update (Ark/Cpp/DUGKS2DSolver.cpp:748-792) and cell macros (Ark/Lib/D2Q9PP.cpp:89-109):
+// deviations + 4/3 (f-bar-plus - deviations) + dt/V sum(F), rounded stochastically;
+// rho, U, V, p, psi in FP64 sums.
+template <int MODEL>
+__global__ void __launch_bounds__(256) k_pp32_update(PPP P, PPS S, uint32_t step) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= P.nx || j >= P.ny) return;
+    constexpr int Q = MODEL == PP16 ? 16 : 9;
+    const int pitch = P.pitch;
+    const int ip = wrapi(i + 1, P.nx), jn = wrapi(j + 1, P.ny);
+    const size_t c = (size_t)j * pitch + i, cE = (size_t)j * pitch + ip, cN = (size_t)jn * pitch + i;
+    const uint32_t h0 = mix32((uint32_t)c * 0x9E3779B1U ^ step * 0x85EBCA77U);
+    double sR = 0.0, su = 0.0, sv = 0.0;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const size_t o = (size_t)q * S.qs;
+        float s = 0.f;
+        s += -S.xfl[o + cE];
+        s += -S.yfl[o + cN];
+        s += S.xfl[o + c];
+        s += S.yfl[o + c];
+        const float d = S.df[o + c];
+        const uint32_t bits = h0 * (2u * q + 1u) + (uint32_t)q * 0x632BE5ABU;
+        const float dn = sr1(d, P.aTP * (S.bf[o + c] - d) + P.dtV * s, bits & 0xFFFFu);
+        S.df[o + c] = dn;
+        sR += (double)dn;
+        su += (double)dn * (double)P.xi_u[q];
+        sv += (double)dn * (double)P.xi_v[q];
+    }
+    const double R = P.rho_ref + sR;
+    double U = su / R, V = sv / R;
+    U += (double)P.hDt * (double)S.Fx[c] / R;
+    V += (double)P.hDt * (double)S.Fy[c] / R;
+    const double p = cs_p(P, R);
+    float scg, psi;
+    cs_psi(P, R, p, scg, psi);
+    S.rho[c] = R;
+    S.U[c] = U;
+    S.V[c] = V;
+    S.p[c] = p;
+    S.scg[c] = scg;
+    S.psi[c] = psi;
+}
+
+// the cell force of the current psi (the state the reference holds after a step)
+__global__ void __launch_bounds__(256) k_pp32_force(PPP P, PPS S) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= P.nx || j >= P.ny) return;
+    const size_t c = (size_t)j * P.pitch + i;
+    float gx, gy;
+    iso_grad(P, S.psi, i, j, gx, gy);
+    const float k = -S.scg[c] * S.psi[c];
+    S.Fx[c] = gx * k;
+    S.Fy[c] = gy * k;
+}
+
+template <int MODEL>
+static cudaError_t launch_pp_t(const PPP &P, const PPS &S, int do_msrc, cudaStream_t st, int64_t *launches,
+                               uint32_t step) {
+    const dim3 blk(32, 8);
+    const dim3 grd((P.nx + 31) / 32, (P.ny + 7) / 8), grf(grd.x, grd.y, 2);
+    k_pp32_collide<MODEL><<<grd, blk, 0, st>>>(P, S, do_msrc);
+    k_pp32_faces1<MODEL><<<grf, blk, 0, st>>>(P, S);
+    k_pp32_faces2<MODEL><<<grf, blk, 0, st>>>(P, S);
+    k_pp32_update<MODEL><<<grd, blk, 0, st>>>(P, S, step);
+    *launches += 4;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pp32_step(const PPP &P, const PPS &S, int do_msrc, cudaStream_t st, int64_t *launches,
+                             uint32_t step) {
+    return P.model == PP16 ? launch_pp_t<PP16>(P, S, do_msrc, st, launches, step)
+                           : launch_pp_t<PP9>(P, S, do_msrc, st, launches, step);
+}
+
+cudaError_t launch_pp32_force(const PPP &P, const PPS &S, cudaStream_t st, int64_t *launches) {
+    const dim3 blk(32, 8);
+    const dim3 grd((P.nx + 31) / 32, (P.ny + 7) / 8);
+    k_pp32_force<<<grd, blk, 0, st>>>(P, S);
+    *launches += 1;
+    return cudaGetLastError();
+}
+
+}  // namespace f32
+}  // namespace dugks

@@ -52,6 +52,30 @@ struct SR {
 };
 using S32 = SR<float>;
 
+// ---- FP32 deviation storage of the pseudopotential models (D2Q9PP, D2V16)
+// Constants: FP32 step coefficients, the velocity set, the rest equilibrium
+// f_rest = eq(rho_ref, 0, 0) the deviations are taken from, and the
+// Carnahan-Starling constants in FP64 (the pressure and psi are evaluated from
+// the FP64 density).
+struct PPP {
+    int nx, ny, pitch, model, Q;
+    float hDt, dt, RT, invRT, Lambda0, Tau0, aTP, bTP, dtV;
+    float r_2dy, r_ndx, r_n2dx, r_ndy, inv_6_2dx, inv_6_2dy;
+    double rho_ref, R0, T_CS, aCS, RTd;
+    float xi_u[16], xi_v[16], w9[9], frest[16];
+};
+// State: f deviations and the step's scratch in FP32, the density (and the
+// pressure for output) in FP64.
+struct PPS {
+    float *df, *bf;                  // [Q][ny][pitch]
+    float *xb, *yb, *xfl, *yfl;      // face reconstructions and fluxes [Q][ny][pitch]
+    float *xr, *yr, *xu, *yu, *xv, *yv, *xg, *yg, *xps, *yps;  // face rho, U, V, G, psi
+    float *xFx, *xFy, *yFx, *yFy;    // face forces (kept for the next step's face velocity)
+    double *rho, *p, *U, *V;         // cell density, pressure and velocity
+    float *psi, *scg, *Fx, *Fy;
+    size_t qs;
+};
+
 // halo rows of a slab partition on each side
 constexpr int SLAB_HALO = 2;
 

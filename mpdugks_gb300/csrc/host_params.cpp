@@ -178,6 +178,16 @@ static void d2v16_eq_host(const Params &P, const double iM[16][16], double rho, 
     }
 }
 
+// Pseudopotential equilibrium at rest, eq(rho, 0, 0) (D2V16 through the
+// inverse moment matrix, D2Q9PP w rho): the rest state of the FP32 storage.
+void pp_rest_eq(const Params &P, const double iM[16][16], double rho, double *eq) {
+    if (P.model == PP16) {
+        d2v16_eq_host(P, iM, rho, 0.0, 0.0, eq);
+    } else {
+        for (int q = 0; q < 9; ++q) eq[q] = P.omega[q] * rho;
+    }
+}
+
 // kind: 0 AC_Drop, 1 droplet heavy inside, 2 Rayleigh-Taylor, 3 SCMP_Drop, 4 density noise.
 int host_init_state(const Params &P, const double iM[16][16], int kind, const double *params, int nparams,
                     uint64_t seed, std::vector<double> &f, std::vector<double> &h, std::vector<double> &aux) {
