@@ -304,7 +304,7 @@ static cudaError_t stream_prepare() {
 
 template <int MODEL, bool WALLS>
 static cudaError_t launch_stream_t(const P32 &P, const S32 &S, int first, int gin, int gout, cudaStream_t st,
-                                   uint32_t step) {
+                                   uint32_t step, bool *fallback) {
     static bool ready = false;
     if (!ready) {
         cudaError_t e = stream_prepare<MODEL, WALLS>();
@@ -317,6 +317,13 @@ static cudaError_t launch_stream_t(const P32 &P, const S32 &S, int first, int gi
     // the longest segment that still gives every resident warp about 4 segments
     // (a long segment costs fewer warm-up rows, a short one less idle tail)
     const int nstrips = (P.nx + SW - 1) / SW, warps = g_stream_nsm * g_stream_blocks * WPB;
+    // a grid with fewer 32-row strip segments than resident warps leaves most of the
+    // GPU idle in this form: the tile kernel (same arithmetic, same results) runs it
+    // (a slab partition reads halo rows, which only this form does: it always runs here)
+    if (!(P.halo_lo || P.halo_hi) && (long long)nstrips * ((P.ny + 31) / 32) < warps) {
+        *fallback = true;
+        return cudaSuccess;
+    }
     int seg = SEG_MAX;
     while (seg > 32 && (long long)nstrips * ((P.ny + seg - 1) / seg) < 4LL * warps) seg /= 2;
     const int nsegs = (P.ny + seg - 1) / seg;
@@ -336,13 +343,15 @@ cudaError_t launch_stream32(const P32 &P, const S32 &S, int first, int gin, int 
     // run the tile kernel (same arithmetic, same results)
     if (P.ny < 8) return launch_step32(P, S, first, gin, gout, st, launches, step);
     cudaError_t e = cudaErrorInvalidValue;
+    bool fallback = false;
     switch (P.model * 2 + (P.walls ? 1 : 0)) {
-        case AC * 2 + 0: e = launch_stream_t<AC, false>(P, S, first, gin, gout, st, step); break;
-        case AC * 2 + 1: e = launch_stream_t<AC, true>(P, S, first, gin, gout, st, step); break;
-        case HCZ * 2 + 0: e = launch_stream_t<HCZ, false>(P, S, first, gin, gout, st, step); break;
-        case HCZ * 2 + 1: e = launch_stream_t<HCZ, true>(P, S, first, gin, gout, st, step); break;
+        case AC * 2 + 0: e = launch_stream_t<AC, false>(P, S, first, gin, gout, st, step, &fallback); break;
+        case AC * 2 + 1: e = launch_stream_t<AC, true>(P, S, first, gin, gout, st, step, &fallback); break;
+        case HCZ * 2 + 0: e = launch_stream_t<HCZ, false>(P, S, first, gin, gout, st, step, &fallback); break;
+        case HCZ * 2 + 1: e = launch_stream_t<HCZ, true>(P, S, first, gin, gout, st, step, &fallback); break;
         default: break;
     }
+    if (e == cudaSuccess && fallback) return launch_step32(P, S, first, gin, gout, st, launches, step);
     if (e == cudaSuccess) *launches += 1;
     return e;
 }

@@ -117,13 +117,14 @@ def test_cancel_and_oversized_submit():
 
 
 @pytest.mark.parametrize('item', [
-    (lambda: ac_case(), 150, 300, False, 'ac_drop_inside', [60.0], 37),
-    (lambda: rt_case(), 90, 400, True, 'ac_rt', [2.0, 0.1, 1e-4], 41),
+    (lambda: ac_case(), 560, 3300, False, 'ac_drop_inside', [200.0], 37),
+    (lambda: rt_case(), 560, 3300, True, 'ac_rt', [3.0, 0.1, 1e-4], 41),
 ])
 def test_streaming_kernel_equals_the_tile_kernel(item):
-    """Single-case FP32 steps run the streaming kernel (warps marching 28-column
-    strips through 128-row segments); the server runs the tile kernel.  On grids
-    of several strips and segments (walls included) they agree bit for bit."""
+    """Single-case FP32 steps on a grid of more strip segments than resident warps
+    run the streaming kernel (warps marching 28-column strips through row
+    segments); the server runs the tile kernel.  With walls and without, they
+    agree bit for bit."""
     from mpdugks_gb300 import capi
     f, nx, ny, w, init, params, n = item
     srv = capi.Server(chunk_steps=16)
