@@ -12,29 +12,9 @@
 namespace dugks {
 namespace f32 {
 
-// Knuth two-sum accumulation (float-float for R = float)
-template <typename R>
-struct FFs {
-    R hi = 0, lo = 0;
-    __device__ __forceinline__ void add(R b) {
-        const R s = hi + b;
-        const R bb = s - hi;
-        const R err = (hi - (s - bb)) + (b - bb);
-        hi = s;
-        lo += err;
-    }
-    __device__ __forceinline__ R value() const { return hi + lo; }
-};
-
 template <typename R>
 __device__ __forceinline__ R sxf(int s, R x) { return s > 0 ? x : (s < 0 ? -x : R(0)); }
 
-// sum of directions 1..8 (E,NE,N,NW,W,SW,S,SE) in an order that every mirror of
-// the lattice maps onto itself: ((E+W)+(N+S)) + ((NE+SW)+(NW+SE))
-template <typename R>
-__device__ __forceinline__ R sym8(const R *a) {
-    return ((a[1] + a[5]) + (a[3] + a[7])) + ((a[2] + a[6]) + (a[4] + a[8]));
-}
 __device__ __forceinline__ float rsq(float x) { return rsqrtf(x); }
 
 // 32-bit integer hash (per cell and step random bits for stochastic rounding)
@@ -158,23 +138,6 @@ __device__ __forceinline__ double2 fma2(double2 a, double2 b, double2 c) {
     return make_double2(__fma_rn(a.x, b.x, c.x), __fma_rn(a.y, b.y, c.y));
 }
 template <typename T> __device__ __forceinline__ T neg2(T a) { return mk2(-a.x, -a.y); }
-// x * s for a compile-time sign s in {-1, 0, 1}
-template <int S, typename T> __device__ __forceinline__ T sgn2(T a) { return S > 0 ? a : (S < 0 ? neg2(a) : mk2(decltype(a.x)(0), decltype(a.x)(0))); }
-
-// Knuth two-sum accumulation of pairs
-template <typename T>
-struct FF2 {
-    T hi, lo;
-    __device__ __forceinline__ void init(T b) { hi = b; lo = mk2(decltype(b.x)(0), decltype(b.x)(0)); }
-    __device__ __forceinline__ void add(T b) {
-        const T s = add2(hi, b);
-        const T bb = sub2(s, hi);
-        const T err = add2(sub2(hi, sub2(s, bb)), sub2(b, bb));
-        hi = s;
-        lo = add2(lo, err);
-    }
-    __device__ __forceinline__ T value() const { return add2(hi, lo); }
-};
 
 __device__ __forceinline__ float2 ff_sum9(const float2 (&a)[9]) {
     return ff_tree9(a, [](float2 x, float2 y) { return add2(x, y); }, [](float2 x, float2 y) { return sub2(x, y); });
@@ -183,7 +146,8 @@ __device__ __forceinline__ double2 ff_sum9(const double2 (&a)[9]) {
     return ff_tree9(a, [](double2 x, double2 y) { return add2(x, y); }, [](double2 x, double2 y) { return sub2(x, y); });
 }
 
-// mirror-symmetric sum of directions 1..8 (see sym8)
+// mirror-symmetric sum of directions 1..8: ((E+W)+(N+S)) + ((NE+SW)+(NW+SE)), which
+// every mirror of the lattice maps onto itself
 template <typename T>
 __device__ __forceinline__ T sym8p(const T *a) {
     return add2(add2(add2(a[1], a[5]), add2(a[3], a[7])), add2(add2(a[2], a[6]), add2(a[4], a[8])));
