@@ -190,8 +190,9 @@ def serving_stream(cases: int, steps: int, seed: int):
     """The seeded serving workload: Poisson arrivals (mean 20/s), N ~ lognormal
     (median 256, sigma_ln = ln 4 / 2) clipped to [64, 1024], 70% Allen-Cahn
     droplets / bubbles (R = N/5, density ratio U[2, 100], sigma U[1e-4, 1e-2])
-    and 30% pseudopotential D2V16 cases.  Returns the Allen-Cahn cases (the
-    pseudopotential share is listed separately: it has no FP32 path)."""
+    and 30% pseudopotential D2V16 cases (T/Tc U[0.6, 0.85], Carnahan-Starling
+    a = 0.5, b = 4, R = 1, seeded density noise rho_c (1 + 0.01 U(-1, 1))), all
+    in FP32 storage."""
     import numpy as np
     rng = np.random.default_rng(seed)
     t = np.cumsum(rng.exponential(1.0 / SERVING['rate'], cases))
@@ -201,18 +202,31 @@ def serving_stream(cases: int, steps: int, seed: int):
     ratio = rng.uniform(2.0, 100.0, cases)
     sigma = rng.uniform(1e-4, 1e-2, cases)
     bubble = rng.random(cases) < 0.5
-    out, pp = [], 0
+    tr = rng.uniform(0.6, 0.85, cases)
+    out = []
     for k in range(cases):
-        if not kind[k]:
-            pp += 1
-            continue
-        out.append(dict(t=float(t[k]), n=int(n[k]), rho_v=float(1.0 / ratio[k]), sigma=float(sigma[k]),
-                        init='ac_drop' if bubble[k] else 'ac_drop_inside', radius=float(n[k]) / 5.0, steps=steps))
-    return out, pp
+        if kind[k]:
+            out.append(dict(model='AC', t=float(t[k]), n=int(n[k]), rho_v=float(1.0 / ratio[k]),
+                            sigma=float(sigma[k]), init='ac_drop' if bubble[k] else 'ac_drop_inside',
+                            params=[float(n[k]) / 5.0], steps=steps))
+        else:
+            out.append(dict(model='PP16', t=float(t[k]), n=int(n[k]), tr=float(tr[k]), init='pp_noise',
+                            params=[PP_RHO_C, 0.01], steps=steps))
+    return out
+
+
+# Carnahan-Starling with a = 0.5, b = 4, R = 1: Tc = 0.3773 a / b, rho_c = 0.13044 / b
+PP_A, PP_TC, PP_RHO_C = 0.5, 0.3773 * 0.5 / 4.0, 0.13044 / 4.0
+# the pseudopotential cases are checked every 100 steps (the Allen-Cahn cases every
+# 1000, the reference's residual cadence): the restated D2V16 model diverges within a
+# few hundred steps at these settings, and a non-finite case should stop soon
+PP_CHECK_EVERY = 100
 
 
 def serving_case(c: dict, precision: str):
     from mpdugks_gb300 import capi
+    if c['model'] == 'PP16':
+        return capi.make_case('PP16', precision, Tr=c['tr'], aCS=PP_A, Tc_CS=PP_TC)
     return capi.make_case('AC', precision, Mu0=0.02, M_Phi=0.02, W=4.0, Sigma=c['sigma'], RhoL=1.0,
                           RhoV=c['rho_v'])
 
@@ -220,45 +234,63 @@ def serving_case(c: dict, precision: str):
 def serving_bench(args) -> dict:
     """Cases arrive on their schedule and are submitted to the server as they
     arrive; p50/p99 time to solution (submit to result on the host) and the
-    aggregate rate.  Beside it: the same cases solved one at a time (FP64 plain
-    path and FP32 storage, no batching) on a sample, as cases/s."""
+    aggregate rate.  Every case is checked every 1000 steps (the reference's
+    residual control): a non-finite state stops it.  Beside it: the Allen-Cahn
+    cases solved one at a time (FP64 plain path and FP32 storage, no batching)
+    on a sample, as cases/s."""
     import numpy as np
     import torch
     from mpdugks_gb300 import capi
-    stream, npp = serving_stream(args.serving_cases, args.serving_steps, SERVING['seed'])
+    stream = serving_stream(args.serving_cases, args.serving_steps, SERVING['seed'])
+    ac = [c for c in stream if c['model'] == 'AC']
 
     def serve(paced: bool):
-        srv = capi.Server(chunk_steps=64)
+        srv = capi.Server()
         t0 = time.perf_counter()
         ids = []
         for c in stream:
             dt = c['t'] - (time.perf_counter() - t0)
             if paced and dt > 0:
                 time.sleep(dt)
-            ids.append(srv.submit(serving_case(c, 'fp32dev'), c['n'], c['n'], False, c['init'], [c['radius']],
-                                  nsteps=c['steps']))
+            ids.append(srv.submit(serving_case(c, 'fp32dev'), c['n'], c['n'], False, c['init'], c['params'],
+                                  nsteps=c['steps'], check_every=PP_CHECK_EVERY if c['model'] == 'PP16' else 0))
         tts, finite, lu = [], 0, 0
         t_first, t_last = None, 0.0
+        pp = {'submitted': 0, 'completed': 0, 'diverged': 0, 'failed': 0, 'steps_at_stop': [], 'tts': []}
         for cid, c in zip(ids, stream):
             st = srv.wait(cid, 3600.0)
+            t_first = st.t_submit if t_first is None else min(t_first, st.t_submit)
+            t_last = max(t_last, st.t_done)
+            if c['model'] == 'PP16':
+                pp['submitted'] += 1
+                pp['completed'] += int(st.state == 2)
+                pp['diverged'] += int(st.stop_reason == 2)
+                pp['failed'] += int(st.state == 4)
+                pp['steps_at_stop'].append(int(st.steps_done))
+                pp['tts'].append(st.t_done - st.t_submit)
+                srv.release(cid)
+                continue
             if st.state != 2:
                 continue
             r = srv.result(cid)
             finite += int(np.isfinite(r['rho']).all())
             srv.release(cid)
             tts.append(st.t_done - st.t_submit)
-            t_first = st.t_submit if t_first is None else min(t_first, st.t_submit)
-            t_last = max(t_last, st.t_done)
             lu += c['n'] * c['n'] * c['steps']
         stats = srv.stats()
         srv.close()
-        return tts, finite, lu, t_last - (t_first or 0.0), stats
+        steps = pp.pop('steps_at_stop')
+        ptts = pp.pop('tts')
+        if steps:
+            pp['steps_at_stop_min_max'] = [min(steps), max(steps)]
+            pp['tts_p50_s'] = round(float(np.percentile(ptts, 50)), 4)
+        return tts, finite, lu, t_last - (t_first or 0.0), stats, pp
 
-    tts, finite, lu, span, stats = serve(True)
-    btts, bfinite, blu, bspan, bstats = serve(False)
+    tts, finite, lu, span, stats, pp = serve(True)
+    btts, bfinite, blu, bspan, bstats, bpp = serve(False)
     done = len(tts)
-    # one case at a time on a sample of the stream (the first cases)
-    sample = stream[:args.serving_sample]
+    # one case at a time on a sample of the stream's Allen-Cahn cases (the first ones)
+    sample = ac[:args.serving_sample]
 
     def one_at_a_time(precision):
         torch.cuda.synchronize()
@@ -266,7 +298,7 @@ def serving_bench(args) -> dict:
         slu = 0
         for c in sample:
             gc = capi.GpuCase(serving_case(c, precision), c['n'], c['n'], False)
-            gc.init(c['init'], [c['radius']])
+            gc.init(c['init'], c['params'])
             gc.step(c['steps'])
             gc.get('rho')
             slu += c['n'] * c['n'] * c['steps']
@@ -281,22 +313,30 @@ def serving_bench(args) -> dict:
     fp32 = one_at_a_time('fp32dev')
     cps = done / span if span > 0 else 0.0
     return {
-        'workload': f'{len(stream)} Allen-Cahn cases of a {args.serving_cases}-case seeded stream (Poisson 20/s, '
-                    f'N lognormal median 256 in [64,1024], R=N/5, density ratio U[2,100], sigma U[1e-4,1e-2], '
-                    f'{args.serving_steps} steps, FP32 storage); the {npp} pseudopotential D2V16 cases of the '
-                    'stream are not run (no FP32 D2V16 path)',
+        'workload': f'{args.serving_cases}-case seeded stream (Poisson 20/s, N lognormal median 256 in '
+                    f'[64,1024], {args.serving_steps} steps each, FP32 storage): {len(ac)} Allen-Cahn droplets/'
+                    f'bubbles (R=N/5, density ratio U[2,100], sigma U[1e-4,1e-2]) and {len(stream) - len(ac)} '
+                    'D2V16 pseudopotential cases (T/Tc U[0.6,0.85], CS a=0.5 b=4, rho_c(1+0.01U) noise); '
+                    f'checked every 1000 (Allen-Cahn) / {PP_CHECK_EVERY} (D2V16) steps',
+        'allen_cahn': 'completed, span, cases_per_s, mlups and tts are of the Allen-Cahn cases',
         'completed': done, 'finite': finite, 'span_s': round(span, 3), 'cases_per_s': round(cps, 4),
         'mlups': round(lu / span / 1e6, 2) if span > 0 else None,
+        'mlups_all_cases': round(stats.cell_updates / span / 1e6, 2) if span > 0 else None,
         'tts_p50_s': round(float(np.percentile(tts, 50)), 4) if tts else None,
         'tts_p99_s': round(float(np.percentile(tts, 99)), 4) if tts else None,
+        'pseudopotential_d2v16': dict(pp, note='the restated D2V16 model diverges at these settings in FP64 '
+                                               'as well; each such case stops at the first check after it '
+                                               'becomes non-finite'),
         'max_resident': stats.max_resident, 'graphs_captured': stats.graphs_captured, 'chunks': stats.chunks,
-        'bytes_peak': stats.bytes_peak, 'max_bytes': stats.max_bytes,
+        'bytes_peak': stats.bytes_peak, 'max_bytes': stats.max_bytes, 'solo_steps': stats.solo_steps,
         'burst': {'how': 'the same cases all submitted at once (capacity)', 'completed': len(btts),
                   'finite': bfinite, 'span_s': round(bspan, 3),
                   'cases_per_s': round(len(btts) / bspan, 4) if bspan > 0 else None,
                   'mlups': round(blu / bspan / 1e6, 2) if bspan > 0 else None,
+                  'mlups_all_cases': round(bstats.cell_updates / bspan / 1e6, 2) if bspan > 0 else None,
                   'tts_p50_s': round(float(np.percentile(btts, 50)), 4) if btts else None,
                   'tts_p99_s': round(float(np.percentile(btts, 99)), 4) if btts else None,
+                  'pseudopotential_d2v16': bpp,
                   'max_resident': bstats.max_resident, 'bytes_peak': bstats.bytes_peak},
         'one_at_a_time_fp64': fp64, 'one_at_a_time_fp32': fp32,
         'vs_one_at_a_time_fp64': round(cps / fp64['stream_cases_per_s_projected'], 2)
@@ -352,6 +392,25 @@ def field_errors(a, b):
         out[k] = {'linf': float(np.max(np.abs(d))) / ny if ny else float(np.max(np.abs(d))),
                   'l2': float(np.linalg.norm(d) / np.linalg.norm(y)) if ny else 0.0}
     return out
+
+
+def developed_flow_errors(steps: int = 300) -> dict:
+    """FP32 against FP64 on the 512x2048 Rayleigh-Taylor case after `steps` steps, beside
+    the FMA-contracted FP64 variant against the same FP64 run: the instability
+    amplifies any difference (rounding included), so the FMA column shows the
+    amplification the FP32 column shares."""
+    from mpdugks_gb300 import capi
+    wl = WORKLOADS['rt512x2048']
+    kw = case_kw(wl)
+    runs = {}
+    for prec in ('fp32dev', 'fp64', 'fp64fma'):
+        g = capi.GpuCase(capi.make_case('HCZ', prec, **kw), wl['nx'], wl['ny'], True)
+        g.init('ac_rt', wl['init'])
+        g.step(steps)
+        runs[prec] = g
+    return {'workload': wl['name'], 'steps': steps,
+            'fp32_vs_fp64': field_errors(runs['fp32dev'], runs['fp64']),
+            'fp64fma_vs_fp64': field_errors(runs['fp64fma'], runs['fp64'])}
 
 
 def timed_steps(gc, n: int, stream, clocks_idx=None):
@@ -456,7 +515,8 @@ def run_ours(args, wl, rank, world, local):
         fp64 = {'value': round(m64, 3), 'unit': 'MLUPS', 'steps': k64, 'ms_per_step': round(ms64 / k64, 4),
                 'precision': 'fp64 (reference-exact rounding)',
                 'fp32_speedup': round(mlups_total / world / m64, 2),
-                'fp32_error_vs_fp64': {'steps': n_cmp, 'fields': errs}}
+                'fp32_error_vs_fp64': {'steps': n_cmp, 'fields': errs},
+                'developed_flow': developed_flow_errors()}
         gx = g64
     # ---- end to end through the C ABI with host buffers: upload the FP64 initial
     # state (the reference's CellArray contents) from pinned host memory, K steps,

@@ -181,16 +181,50 @@ int dugks_gpu_step_noalloc(const dugks_case_t *c, const dugks_grid_t *g, double 
  * every chunk of `chunk_steps` steps is one captured CUDA graph of persistent
  * launches over a table of (case, tile) entries, so cases that arrive while
  * others run join at the next chunk and finished cases leave.  Other cases
- * (FP64, pseudopotential) run one at a time on a second stream, overlapping
- * the batched work.  A case's result does not depend on the other cases
- * (bit-identical alone and in a mix). */
+ * (FP64, pseudopotential) run on `solo_lanes` lanes, one case per lane at a
+ * time, each lane on its own stream, overlapping one another and the
+ * batched work.  A case's result does not depend on the other cases
+ * (bit-identical alone and in a mix).
+ *
+ * Like the reference's time loop (Ark/Cpp/DUGKS2DSolver.cpp:164 with
+ * Update_Residual at :807-835 every ResidualControl steps,
+ * Ark/Constant/ZeroNamespace.h:173-177), a case is checked every
+ * `check_every` steps: it stops converged when the density residual is at or
+ * below `residual_tol`, and fails (DUGKS_SRV_STOP_DIVERGED) when its state is
+ * no longer finite.  With `out_dir` set, the state at step 0, every
+ * `snapshot_every` steps and at the end is written there as FlowField files
+ * in the layout and names of the reference's Output_Flowfield
+ * (Ark/Cpp/Output.cpp:537-606); the fields are copied to pinned host buffers
+ * and a writer thread formats and writes them while the case runs on. */
 typedef struct dugks_srv dugks_srv_t;
 
 typedef struct dugks_srv_config {
     size_t max_bytes;  /* device bytes for resident cases; 0: 85% of the free memory */
     int chunk_steps;   /* steps per captured graph launch; 0: 64 */
-    int reserved[6];
+    int solo_lanes;    /* lanes for the cases that are not batched; 0: 4 */
+    int reserved[5];
 } dugks_srv_config_t;
+
+/* One case for dugks_srv_submit_request. */
+typedef struct dugks_srv_request {
+    dugks_case_t cs;
+    dugks_grid_t grid;
+    int init_kind;         /* dugks_gpu_init kind, params and seed */
+    int nparams;
+    const double *params;
+    uint64_t seed;
+    int64_t nsteps;        /* step limit (the reference's End_Step) */
+    double residual_tol;   /* stop once the residual at a check is <= this (RESIDUAL); 0: never */
+    int check_every;       /* steps between residual / finiteness checks (ResidualControl); 0: 1000 */
+    int snapshot_every;    /* steps between FlowField files (writeFileControl); 0: step 0 and the end only */
+    const char *out_dir;   /* existing directory for the FlowField files; NULL: no files */
+} dugks_srv_request_t;
+
+typedef enum dugks_srv_stop {
+    DUGKS_SRV_STOP_NONE = 0,      /* running, or reached its step limit */
+    DUGKS_SRV_STOP_CONVERGED = 1, /* residual at or below residual_tol */
+    DUGKS_SRV_STOP_DIVERGED = 2   /* non-finite state at a check (state DUGKS_SRV_FAILED) */
+} dugks_srv_stop_t;
 
 typedef enum dugks_srv_state {
     DUGKS_SRV_QUEUED = 0,
@@ -206,15 +240,21 @@ typedef struct dugks_srv_status {
     int64_t nsteps, steps_done;
     size_t bytes;      /* device footprint */
     double t_submit, t_start, t_done;  /* seconds since dugks_srv_create */
+    int stop_reason;   /* dugks_srv_stop_t */
+    int files;         /* FlowField files written so far */
+    double residual;   /* residual at the last check; -1 before the first */
 } dugks_srv_status_t;
 
 typedef struct dugks_srv_stats {
     int64_t submitted, completed, cancelled, failed;
-    int64_t cell_updates;     /* of completed cases */
+    int64_t cell_updates;     /* steps x cells of the cases that ended (done or stopped) */
     int64_t chunks, graphs_captured, launches;
     int max_resident;         /* most cases resident at once */
     size_t bytes_in_use, bytes_peak, max_bytes;
     double busy_s;            /* batched lane: time with work on the device */
+    int64_t converged, diverged;  /* cases stopped by the residual rule / as non-finite */
+    int64_t files_written;
+    int64_t solo_steps;       /* steps run by the solo lanes */
 } dugks_srv_stats_t;
 
 int dugks_srv_create(const dugks_srv_config_t *cfg, dugks_srv_t **out);
@@ -222,6 +262,9 @@ int dugks_srv_create(const dugks_srv_config_t *cfg, dugks_srv_t **out);
  * seed) and run nsteps steps.  Returns at once with the case id. */
 int dugks_srv_submit(dugks_srv_t *s, const dugks_case_t *c, const dugks_grid_t *g, int init_kind,
                      const double *params, int nparams, uint64_t seed, int64_t nsteps, int64_t *id);
+/* Queue a case with the stopping rule and FlowField output of `rq`
+ * (dugks_srv_submit is this with residual_tol 0, check_every 0, no files). */
+int dugks_srv_submit_request(dugks_srv_t *s, const dugks_srv_request_t *rq, int64_t *id);
 int dugks_srv_poll(dugks_srv_t *s, int64_t id, dugks_srv_status_t *st);
 /* Block until the case is done, cancelled or failed, or timeout_s passes
  * (DUGKS_ETIMEOUT; timeout_s < 0: no limit). */

@@ -27,7 +27,8 @@ PER_FILE = {'fp64_exact.cu': ['-fmad=false']}
 
 
 def sources() -> list[Path]:
-    return sorted(CSRC.glob('*.cu')) + sorted(CSRC.glob('*.cpp'))
+    # the serving loop writes FlowField files with the host driver's writer
+    return sorted(CSRC.glob('*.cu')) + sorted(CSRC.glob('*.cpp')) + [HOST / 'flowfield.cpp']
 
 
 def nvcc() -> str:
@@ -40,7 +41,8 @@ def nvcc() -> str:
 def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> Path:
     BUILD.mkdir(exist_ok=True)
     srcs = sources()
-    deps = srcs + sorted(CSRC.glob('*.cuh')) + sorted(CSRC.glob('*.h')) + sorted(INCLUDE.glob('*.h'))
+    deps = srcs + sorted(CSRC.glob('*.cuh')) + sorted(CSRC.glob('*.h')) + sorted(INCLUDE.glob('*.h')) + \
+        sorted(HOST.glob('*.hpp'))
     newest = max(p.stat().st_mtime for p in deps)
     if not force and LIB.exists() and LIB.stat().st_mtime >= newest and not extra:
         build_host()

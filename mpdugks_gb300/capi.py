@@ -6,6 +6,7 @@ when it is missing -- there is no CPU fallback.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 import numpy as np
@@ -45,22 +46,34 @@ class ReductionsT(C.Structure):
 
 
 class SrvConfigT(C.Structure):
-    _fields_ = [('max_bytes', C.c_size_t), ('chunk_steps', C.c_int), ('reserved', C.c_int * 6)]
+    _fields_ = [('max_bytes', C.c_size_t), ('chunk_steps', C.c_int), ('solo_lanes', C.c_int),
+                ('reserved', C.c_int * 5)]
+
+
+class SrvRequestT(C.Structure):
+    _fields_ = [('cs', CaseT), ('grid', GridT), ('init_kind', C.c_int), ('nparams', C.c_int),
+                ('params', C.POINTER(C.c_double)), ('seed', C.c_uint64), ('nsteps', C.c_int64),
+                ('residual_tol', C.c_double), ('check_every', C.c_int), ('snapshot_every', C.c_int),
+                ('out_dir', C.c_char_p)]
 
 
 class SrvStatusT(C.Structure):
     _fields_ = [('state', C.c_int), ('batched', C.c_int), ('nsteps', C.c_int64), ('steps_done', C.c_int64),
-                ('bytes', C.c_size_t), ('t_submit', C.c_double), ('t_start', C.c_double), ('t_done', C.c_double)]
+                ('bytes', C.c_size_t), ('t_submit', C.c_double), ('t_start', C.c_double), ('t_done', C.c_double),
+                ('stop_reason', C.c_int), ('files', C.c_int), ('residual', C.c_double)]
 
 
 class SrvStatsT(C.Structure):
     _fields_ = [('submitted', C.c_int64), ('completed', C.c_int64), ('cancelled', C.c_int64), ('failed', C.c_int64),
                 ('cell_updates', C.c_int64), ('chunks', C.c_int64), ('graphs_captured', C.c_int64),
                 ('launches', C.c_int64), ('max_resident', C.c_int), ('bytes_in_use', C.c_size_t),
-                ('bytes_peak', C.c_size_t), ('max_bytes', C.c_size_t), ('busy_s', C.c_double)]
+                ('bytes_peak', C.c_size_t), ('max_bytes', C.c_size_t), ('busy_s', C.c_double),
+                ('converged', C.c_int64), ('diverged', C.c_int64), ('files_written', C.c_int64),
+                ('solo_steps', C.c_int64)]
 
 
 SRV_STATES = {0: 'queued', 1: 'running', 2: 'done', 3: 'cancelled', 4: 'failed'}
+SRV_STOPS = {0: 'none', 1: 'converged', 2: 'diverged'}
 
 # every symbol declared in include/dugks_gpu.h, with its ctypes signature
 SIGNATURES = {
@@ -85,6 +98,7 @@ SIGNATURES = {
     'dugks_srv_create': (C.c_int, [C.POINTER(SrvConfigT), C.POINTER(C.c_void_p)]),
     'dugks_srv_submit': (C.c_int, [C.c_void_p, C.POINTER(CaseT), C.POINTER(GridT), C.c_int, C.POINTER(C.c_double),
                                    C.c_int, C.c_uint64, C.c_int64, C.POINTER(C.c_int64)]),
+    'dugks_srv_submit_request': (C.c_int, [C.c_void_p, C.POINTER(SrvRequestT), C.POINTER(C.c_int64)]),
     'dugks_srv_poll': (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(SrvStatusT)]),
     'dugks_srv_wait': (C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.POINTER(SrvStatusT)]),
     'dugks_srv_result': (C.c_int, [C.c_void_p, C.c_int64] + [C.c_void_p] * 5),
@@ -222,9 +236,9 @@ class GpuCase:
 class Server:
     """A serving loop on the GPU (dugks_srv_*): submit cases, poll or wait, read results."""
 
-    def __init__(self, max_bytes: int = 0, chunk_steps: int = 0):
+    def __init__(self, max_bytes: int = 0, chunk_steps: int = 0, solo_lanes: int = 0):
         self.lib = load()
-        cfg = SrvConfigT(max_bytes, chunk_steps)
+        cfg = SrvConfigT(max_bytes, chunk_steps, solo_lanes)
         h = C.c_void_p()
         rc = self.lib.dugks_srv_create(C.byref(cfg), C.byref(h))
         if rc != DUGKS_OK:
@@ -239,12 +253,18 @@ class Server:
             raise DugksError(rc, buf.value.decode())
 
     def submit(self, case: CaseT, nx: int, ny: int, y_walls: bool, init: str, params=(), seed: int = 12345,
-               nsteps: int = 100) -> int:
+               nsteps: int = 100, residual_tol: float = 0.0, check_every: int = 0, snapshot_every: int = 0,
+               out_dir: str | None = None) -> int:
+        """Queue a case: nsteps steps at most; every check_every steps (0: 1000) it stops
+        converged once the residual is <= residual_tol (0: never) and fails when not
+        finite; with out_dir, FlowField files at step 0, every snapshot_every steps
+        and at the end."""
         arr = (C.c_double * max(1, len(params)))(*params)
         cid = C.c_int64()
-        grid = GridT(nx, ny, int(y_walls))
-        self._check(self.lib.dugks_srv_submit(self.s, C.byref(case), C.byref(grid), INIT_KINDS[init], arr,
-                                              len(params), seed, nsteps, C.byref(cid)))
+        rq = SrvRequestT(case, GridT(nx, ny, int(y_walls)), INIT_KINDS[init], len(params), arr, seed, nsteps,
+                         residual_tol, check_every, snapshot_every,
+                         None if out_dir is None else os.fsencode(out_dir))
+        self._check(self.lib.dugks_srv_submit_request(self.s, C.byref(rq), C.byref(cid)))
         self.shapes[cid.value] = (ny, nx)
         return cid.value
 

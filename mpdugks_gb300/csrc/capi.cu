@@ -940,6 +940,7 @@ void fp32_views(const dugks_handle_t *h, f32::P32 *P, f32::S32 *S) {
 int64_t steps_done(const dugks_handle_t *h) { return h->steps; }
 int model_of(const dugks_handle_t *h) { return h->P.model; }
 int walls_of(const dugks_handle_t *h) { return h->P.walls ? 1 : 0; }
+double dt_of(const dugks_handle_t *h) { return h->P.dt; }
 
 // n steps were run outside the handle (by the batched kernel) from its current
 // state with step numbers steps .. steps+n-1: adopt the ping-pong orientation,

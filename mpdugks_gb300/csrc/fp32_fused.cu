@@ -394,13 +394,14 @@ __global__ void k_batch_advance(int *case_base, const int *slots, int count, int
     if (k < count) case_base[slots[k]] += n;
 }
 
-cudaError_t batch_set_case(int slot, const P32 &P, const S32 &S0, cudaStream_t st) {
+// S: the case's state views for its next step, number `step`
+cudaError_t batch_set_case(int slot, const P32 &P, const S32 &S, int64_t step, cudaStream_t st) {
     if (slot < 0 || slot >= BATCH_MAX_CASES) return cudaErrorInvalidValue;
     BatchCase b{};
     b.P = P;
-    b.S[0] = S0;
-    b.S[1] = S0;
-    swap_io(b.S[1]);
+    b.S[step & 1] = S;
+    b.S[(step & 1) ^ 1] = S;
+    swap_io(b.S[(step & 1) ^ 1]);
     b.ntx = (P.nx + TW - 1) / TW;
     return cudaMemcpyToSymbolAsync(c_batch, &b, sizeof(b), (size_t)slot * sizeof(BatchCase), cudaMemcpyHostToDevice,
                                    st);

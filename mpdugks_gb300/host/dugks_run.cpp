@@ -3,15 +3,19 @@
 // (Ark/Cpp/main.cpp:134, Ark/Cpp/DUGKS2DSolver.cpp:148-337).
 //
 //   dugks_run run <Case.ark> [--out DIR] [--precision P] [--steps N]
-//                 [--set key=value ...]
+//                 [--mesh FILE.cas] [--set key=value ...]
 //       Reads the case from a Case.ark (the reference's OutputCase layout),
 //       initialises it on the GPU, writes DIR/Case.ark and the FlowField at
 //       step 0, then steps until End_Step (or --steps) or until the density
 //       residual, evaluated every ResidualControl steps, falls below
 //       RESIDUAL; FlowField files every writeFileControl steps and at the end
-//       (DIR/global/, the reference's names and layout).
+//       (DIR/global/, the reference's names and layout).  With --mesh the
+//       grid comes from a .cas mesh file, as in the reference's
+//       MeshConstruct, and the FlowField cells follow the mesh's cell order.
 //   dugks_run rewrite-ark <in> <out>        parse a Case.ark and write it back
 //   dugks_run rewrite-flowfield <in> <out>  parse a FlowField file and write it back
+//   dugks_run mesh-info <FILE.cas>          nx ny y_walls, then the grid
+//                                           position j*nx+i of every mesh cell
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -23,6 +27,7 @@
 #include "../../include/dugks_gpu.h"
 #include "case_ark.hpp"
 #include "flowfield.hpp"
+#include "mesh_cas.hpp"
 
 using namespace dugks_host;
 
@@ -42,7 +47,7 @@ void make_dir(const std::string &d) {
     }
 }
 
-FlowField fields(dugks_handle_t *h, const RunConfig &c) {
+FlowField fields(dugks_handle_t *h, const RunConfig &c, const CartesianMap *mesh) {
     FlowField ff;
     ff.cells = (size_t)c.grid.nx * c.grid.ny;
     for (auto *v : {&ff.rho, &ff.u, &ff.v, &ff.p, &ff.T, &ff.phi, &ff.tau, &ff.fx, &ff.fy}) v->assign(ff.cells, 0.0);
@@ -51,19 +56,23 @@ FlowField fields(dugks_handle_t *h, const RunConfig &c) {
     check(h, dugks_gpu_get_field(h, DUGKS_F_FX, ff.fx.data()), "Fx");
     check(h, dugks_gpu_get_field(h, DUGKS_F_FY, ff.fy.data()), "Fy");
     ff.T.assign(ff.cells, c.T0);  // isothermal models keep the reference temperature
+    if (mesh)  // the reference writes cells in its CellArray order, the mesh file's
+        for (auto *v : {&ff.rho, &ff.u, &ff.v, &ff.p, &ff.T, &ff.phi, &ff.tau, &ff.fx, &ff.fy})
+            *v = to_mesh_order(*mesh, *v);
     return ff;
 }
 
-void output(dugks_handle_t *h, const RunConfig &c, const std::string &dir, int64_t step) {
+void output(dugks_handle_t *h, const RunConfig &c, const CartesianMap *mesh, const std::string &dir,
+            int64_t step) {
     const std::string path =
         dir + "/global/" + flowfield_name(step, (double)step * c.dt, c.mach, c.mesh_type, c.nl, c.cfl);
-    write_flowfield(path, fields(h, c));
+    write_flowfield(path, fields(h, c, mesh));
 }
 
 int run(int argc, char **argv) {
     if (argc < 3) throw std::runtime_error("run: missing Case.ark");
     CaseArk ark = read_case_ark(argv[2]);
-    std::string out = "FlowField";
+    std::string out = "FlowField", mesh_file;
     int64_t steps_override = -1;
     for (int k = 3; k < argc; ++k) {
         const std::string a = argv[k];
@@ -74,6 +83,7 @@ int run(int argc, char **argv) {
         if (a == "--out") out = next();
         else if (a == "--precision") ark.set("precision", next());
         else if (a == "--steps") steps_override = std::atoll(next().c_str());
+        else if (a == "--mesh") mesh_file = next();
         else if (a == "--set") {
             const std::string kv = next();
             const size_t eq = kv.find('=');
@@ -83,6 +93,14 @@ int run(int argc, char **argv) {
     }
     RunConfig c = config_from_case_ark(ark);
     if (steps_override >= 0) c.end_step = steps_override;
+    CartesianMap mesh;
+    if (!mesh_file.empty()) {  // the grid is the mesh file's
+        mesh = cartesian_map(read_cas(mesh_file));
+        c.grid.nx = mesh.nx;
+        c.grid.ny = mesh.ny;
+        c.grid.y_walls = mesh.y_walls;
+    }
+    const CartesianMap *pm = mesh_file.empty() ? nullptr : &mesh;
     make_dir(out);
     make_dir(out + "/global");
     write_case_ark(out + "/Case.ark", ark);
@@ -94,7 +112,7 @@ int run(int argc, char **argv) {
         check(h, dugks_gpu_init(h, c.init_kind, c.init_params.empty() ? nullptr : c.init_params.data(),
                                 (int)c.init_params.size(), c.seed),
               "init");
-        output(h, c, out, 0);
+        output(h, c, pm, out, 0);
         std::printf("iteration start    cells : %d x %d    steps : %lld\n", c.grid.nx, c.grid.ny,
                     (long long)c.end_step);
         int64_t step = 0;
@@ -115,9 +133,9 @@ int run(int argc, char **argv) {
                             r.residual);
                 std::fflush(stdout);
             }
-            if (step % c.write_every == 0 && step < c.end_step) output(h, c, out, step);
+            if (step % c.write_every == 0 && step < c.end_step) output(h, c, pm, out, step);
         }
-        output(h, c, out, step);
+        output(h, c, pm, out, step);
         std::printf("iteration End    step : %lld\n", (long long)step);
     } catch (...) {
         dugks_gpu_destroy(h);
@@ -140,6 +158,13 @@ int main(int argc, char **argv) {
             write_flowfield(argv[3], read_flowfield(argv[2]));
             return 0;
         }
+        if (argc == 3 && std::strcmp(argv[1], "mesh-info") == 0) {
+            const CartesianMap m = cartesian_map(read_cas(argv[2]));
+            std::printf("%d %d %d\n", m.nx, m.ny, m.y_walls);
+            for (size_t k = 0; k < m.cell_index.size(); ++k)
+                std::printf(k + 1 < m.cell_index.size() ? "%d " : "%d\n", m.cell_index[k]);
+            return 0;
+        }
         if (argc == 3 && std::strcmp(argv[1], "show-config") == 0) {
             const RunConfig c = config_from_case_ark(read_case_ark(argv[2]));
             std::printf("model %d precision %d nx %d ny %d walls %d init %d nparams %zu steps %lld Mu0 %.17g "
@@ -151,10 +176,12 @@ int main(int argc, char **argv) {
             return 0;
         }
         std::fprintf(stderr,
-                     "usage: dugks_run run <Case.ark> [--out DIR] [--precision P] [--steps N] [--set k=v]...\n"
+                     "usage: dugks_run run <Case.ark> [--out DIR] [--precision P] [--steps N] [--mesh F.cas]\n"
+                     "                     [--set k=v]...\n"
                      "       dugks_run rewrite-ark <in> <out>\n"
                      "       dugks_run rewrite-flowfield <in> <out>\n"
-                     "       dugks_run show-config <Case.ark>\n");
+                     "       dugks_run show-config <Case.ark>\n"
+                     "       dugks_run mesh-info <F.cas>\n");
         return 2;
     } catch (const std::exception &e) {
         std::fprintf(stderr, "dugks_run: %s\n", e.what());

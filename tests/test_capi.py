@@ -55,3 +55,32 @@ def test_serving_create_reports_missing_gpu():
     h = ctypes.c_void_p()
     rc = lib.dugks_srv_create(None, ctypes.byref(h))
     assert rc == capi.DUGKS_ECUDA and not h.value
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every ctypes structure has the size and field offsets the C compiler gives the header's."""
+    import ctypes
+    import shutil
+    import subprocess
+    from mpdugks_gb300 import capi
+    gcc = shutil.which('gcc') or shutil.which('cc')
+    if gcc is None:
+        pytest.skip('no C compiler')
+    structs = {'dugks_case_t': capi.CaseT, 'dugks_grid_t': capi.GridT, 'dugks_reductions_t': capi.ReductionsT,
+               'dugks_srv_config_t': capi.SrvConfigT, 'dugks_srv_request_t': capi.SrvRequestT,
+               'dugks_srv_status_t': capi.SrvStatusT, 'dugks_srv_stats_t': capi.SrvStatsT}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "dugks_gpu.h"', 'int main(void) {']
+    want = []
+    for cname, py in structs.items():
+        lines.append(f'    printf("%zu\\n", sizeof({cname}));')
+        want.append(ctypes.sizeof(py))
+        for fname, *_ in py._fields_:
+            lines.append(f'    printf("%zu\\n", offsetof({cname}, {fname}));')
+            want.append(getattr(py, fname).offset)
+    lines += ['    return 0;', '}']
+    src = tmp_path / 'layout.c'
+    src.write_text('\n'.join(lines) + '\n')
+    exe = tmp_path / 'layout'
+    subprocess.run([gcc, f'-I{ROOT / "include"}', str(src), '-o', str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert got == want

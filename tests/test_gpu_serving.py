@@ -28,7 +28,15 @@ MIX = [
     (lambda: ac_case(Sigma=5e-3, RhoV=0.5), 130, 70, False, 'ac_drop', [15.0], 61),
     (lambda: ac_case('fp64'), 48, 48, False, 'ac_drop_inside', [10.0], 40),
     (lambda: ac_case(RhoV=0.02), 200, 40, False, 'ac_drop_inside', [12.0], 203),
+    # pseudopotential FP32 cases: solo lanes, concurrently
+    (lambda: pp_case('PP16'), 40, 40, False, 'scmp_drop', [], 80),
+    (lambda: pp_case('PP9'), 48, 48, False, 'pp_noise', [0.2, 0.01], 90),
 ]
+
+
+def pp_case(model, precision='fp32dev'):
+    from mpdugks_gb300 import capi
+    return capi.make_case(model, precision)
 
 
 def run(server, items):
@@ -135,3 +143,120 @@ def test_streaming_kernel_equals_the_tile_kernel(item):
     gc.step(n)
     for k in FIELDS:
         assert np.array_equal(r[k], gc.get(k)), k
+
+
+# ---- stopping rule and FlowField output
+
+GOLD = __import__('pathlib').Path(__file__).resolve().parent / 'golden' / 'flowfield'
+
+
+def golden_case(precision):
+    """The reference's own AC_Drop 32x24 case of tests/golden/flowfield/ac_ff."""
+    from mpdugks_gb300 import capi
+    return capi.make_case('AC', precision, Mu0=0.02, M_Phi=0.1, W=4.0, Sigma=1e-3, RhoL=1.0, RhoV=0.1)
+
+
+def golden_file(step):
+    import gzip
+    f = next((GOLD / 'ac_ff').glob(f'step{step}Ma*.dat.gz'))
+    return f.name[:-3], gzip.decompress(f.read_bytes())
+
+
+def parse_flowfield(text, cells):
+    lines = text.decode().splitlines()
+    out, k = {}, 0
+    for name in ('rho', 'uv', 'p', 'T', 'phi', 'tau', 'fx', 'fy'):
+        vals = np.array([[float(x) for x in ln.split()] for ln in lines[k + 1:k + 1 + cells]])
+        if name == 'uv':
+            out['u'], out['v'] = vals[:, 0], vals[:, 1]
+        else:
+            out[name] = vals[:, 0]
+        k += cells + 2
+    return out
+
+
+def test_flowfield_files_equal_the_reference_files(tmp_path):
+    """The plain FP64 path in a solo lane, with snapshots every 10 steps: the
+    files at steps 0 and 20 are byte-identical to the reference's own
+    Output_Flowfield files (a snapshot in between does not disturb the run)."""
+    from mpdugks_gb300 import capi
+    srv = capi.Server()
+    cid = srv.submit(golden_case('fp64'), 32, 24, False, 'ac_drop', [7.0], nsteps=20, snapshot_every=10,
+                     out_dir=str(tmp_path))
+    st = srv.wait(cid, 120.0)
+    stats = srv.stats()
+    srv.close()
+    assert st.state == 2 and st.files == 3 and stats.files_written == 3
+    for step in (0, 20):
+        name, text = golden_file(step)
+        assert (tmp_path / name).read_bytes() == text, step
+    assert (tmp_path / 'step10Ma0_Car32_CFL0.5_T5.dat').exists()
+
+
+def test_batched_flowfield_files_are_close_to_the_reference_files(tmp_path):
+    """The same case in FP32 storage, batched with another case: the file at
+    step 20 agrees with the reference's to 1e-5 (rho, p, phi, tau)."""
+    from mpdugks_gb300 import capi
+    srv = capi.Server(chunk_steps=8)
+    cid = srv.submit(golden_case('fp32dev'), 32, 24, False, 'ac_drop', [7.0], nsteps=20, snapshot_every=12,
+                     out_dir=str(tmp_path))
+    other = srv.submit(ac_case(), 64, 64, False, 'ac_drop_inside', [12.0], nsteps=60)
+    st = srv.wait(cid, 120.0)
+    assert srv.wait(other, 120.0).state == 2
+    srv.close()
+    assert st.state == 2 and st.batched == 1 and st.files == 3
+    name, text = golden_file(20)
+    a = parse_flowfield((tmp_path / name).read_bytes(), 32 * 24)
+    b = parse_flowfield(text, 32 * 24)
+    for k in ('rho', 'p', 'phi', 'tau', 'T'):
+        assert np.max(np.abs(a[k] - b[k])) <= 1e-5 * np.max(np.abs(b[k])), k
+    assert (tmp_path / 'step12Ma0_Car32_CFL0.5_T6.dat').exists()
+
+
+@pytest.mark.parametrize('precision', ['fp32dev', 'fp64'])
+def test_case_stops_at_the_first_check_below_the_tolerance(precision):
+    """Residual every 50 steps as the reference's Update_Residual; the case stops
+    at the first check at or below the tolerance, with the fields of that step."""
+    from mpdugks_gb300 import capi
+    every, checks = 50, 6
+    gc = capi.GpuCase(ac_case(precision), 64, 64, False)
+    gc.init('ac_drop_inside', [12.0], seed=7)
+    res, fields = [], []
+    for _ in range(checks):
+        gc.step(every)
+        res.append(gc.reduce().residual)
+        fields.append({k: gc.get(k) for k in FIELDS})
+    tol = res[3]
+    stop = next(k for k, r in enumerate(res) if r <= tol)
+    srv = capi.Server(chunk_steps=16)
+    cid = srv.submit(ac_case(precision), 64, 64, False, 'ac_drop_inside', [12.0], seed=7, nsteps=100000,
+                     residual_tol=tol, check_every=every)
+    other = srv.submit(ac_case(precision), 48, 48, False, 'ac_drop_inside', [10.0], nsteps=130)
+    st = srv.wait(cid, 300.0)
+    assert srv.wait(other, 300.0).state == 2
+    r = srv.result(cid)
+    stats = srv.stats()
+    srv.close()
+    assert st.state == 2 and st.stop_reason == 1, (st.state, st.stop_reason)
+    assert st.steps_done == every * (stop + 1) and st.residual == res[stop]
+    assert stats.converged == 1
+    for k in FIELDS:
+        assert np.array_equal(r[k], fields[stop][k]), k
+
+
+def test_diverging_cases_are_stopped_and_reported():
+    """A state that overflows (phi noise of 1e200) fails at the first check,
+    batched and in a solo lane, while a healthy case in the mix completes."""
+    from mpdugks_gb300 import capi
+    srv = capi.Server(chunk_steps=16)
+    bad = [srv.submit(rt_case(p), 32, 64, True, 'ac_rt', [1.0, 0.1, 1e200], nsteps=5000, check_every=40)
+           for p in ('fp32dev', 'fp64')]
+    good = srv.submit(ac_case(), 48, 48, False, 'ac_drop_inside', [10.0], nsteps=100)
+    sts = [srv.wait(c, 300.0) for c in bad]
+    assert srv.wait(good, 300.0).state == 2
+    stats = srv.stats()
+    srv.close()
+    for st in sts:
+        assert st.state == 4 and st.stop_reason == 2 and st.steps_done == 40, (st.state, st.stop_reason,
+                                                                             st.steps_done)
+    assert stats.diverged == 2 and stats.completed == 1
