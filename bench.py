@@ -362,8 +362,13 @@ def pseudopotential_bench(steps: int = 100) -> dict:
         g.init('pp_noise', [0.2, 0.01], seed=2026)
         g.step(3, st.cuda_stream)
         ms, launches, _ = timed_steps(g, steps, st)
-        out[prec] = {'mlups': round(n * n * steps / (ms * 1e-3) / 1e6, 2), 'ms_per_step': round(ms / steps, 4),
-                     'launches': launches}
+        mlups = n * n * steps / (ms * 1e-3) / 1e6
+        # compulsory bytes per cell-update: 16 distributions (+ the 2-component force)
+        # read and written, 4 B each in FP32 storage, 8 B in FP64
+        algo = 144 if prec == 'fp32dev' else 288
+        out[prec] = {'mlups': round(mlups, 2), 'ms_per_step': round(ms / steps, 4), 'launches': launches,
+                     'algorithmic_bytes_per_cell': algo, 'achieved_gbs': round(mlups * algo / 1e3, 1),
+                     'hbm_frac': round(mlups * algo / 1e3 / load_peaks()[0], 4), 'peak': load_peaks()[1]}
         cases[prec] = g
     errs = field_errors(cases['fp32dev'], cases['fp64'])
     del errs['phi']

@@ -208,6 +208,12 @@ static size_t pp32_arena_bytes(const Params &P) {
     return (6 * (size_t)P.Q + 18) * cf + 6 * cd + align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 512;
 }
 
+// a double as the unevaluated float sum hi + lo (about 48 significant bits)
+static void split_ff(double v, float &hi, float &lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
 static int create_pp32(dugks_handle *h, dugks_handle_t **out) {
     Params &P = h->P;
     h->pp32 = true;
@@ -279,6 +285,9 @@ static int create_pp32(dugks_handle *h, dugks_handle_t **out) {
     C.T_CS = P.T_CS;
     C.aCS = P.aCS;
     C.RTd = P.RT;
+    split_ff(P.R0 * P.T_CS, C.rtcs_hi, C.rtcs_lo);
+    split_ff(P.aCS, C.acs_hi, C.acs_lo);
+    split_ff(P.RT, C.rt_hi, C.rt_lo);
     for (int q = 0; q < Q; ++q) {
         C.xi_u[q] = (float)P.xi_u[q];
         C.xi_v[q] = (float)P.xi_v[q];
@@ -306,6 +315,7 @@ static int upload_pp32(dugks_handle *h, const double *f, const double *aux) {
     double mean = 0.0;
     for (size_t k = 0; k < n; ++k) mean += aux[(size_t)F_RHO * n + k];
     C.rho_ref = mean / (double)n;
+    split_ff(C.rho_ref, C.rref_hi, C.rref_lo);
     double rest[16];
     pp_rest_eq(P, h->iM, C.rho_ref, rest);
     for (int q = 0; q < P.Q; ++q) C.frest[q] = (float)rest[q];

@@ -78,18 +78,74 @@ __device__ __forceinline__ void pp_deq(const PPP &P, float dr, float rho, float 
     }
 }
 
-// Carnahan-Starling pressure (Ark/Lib/nonidealEoS.h:114-118) and calcPsi
-// (Ark/Header/Macroscopic.h:64-68), in FP64 from the FP64 density.
-__device__ __forceinline__ double cs_p(const PPP &P, double rho) {
-    return rho * P.R0 * P.T_CS * (1.0 + rho + rho * rho - rho * rho * rho) /
-               ((1.0 - rho) * (1.0 - rho) * (1.0 - rho)) -
-           P.aCS * rho * rho;
+// ---- float-float arithmetic: a value is the unevaluated sum hi + lo of two
+// floats.  TwoSum (Knuth, TAOCP vol. 2, 4.2.2), FastTwoSum (Dekker 1971), the
+// product error by fma, the cascaded sum Sum2 (Ogita, Rump and Oishi 2005) and a
+// two-step long division as in Bailey's double-double arithmetic: about 44
+// significant bits, for the moment sums and the equation of state that the FP64
+// path evaluates in double (the FP64 units of this GPU are ~1/60 of its FP32
+// rate, and these were most of this path's time).  Products that feed a TwoSum
+// use __fmul_rn so that no fma contraction changes them.
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ FF two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
 }
-__device__ __forceinline__ void cs_psi(const PPP &P, double rho, double p, float &scg, float &psi) {
-    const double G = (double)((p > rho * P.RTd) - (p < rho * P.RTd));
-    scg = (float)G;
-    psi = (float)sqrt(2.0 * (p - rho * P.RTd) / G);
+__device__ __forceinline__ FF fast_two_sum(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
 }
+__device__ __forceinline__ void ff_acc(FF &s, float x) {  // Sum2 step: s += x
+    const FF t = two_sum(s.hi, x);
+    s.hi = t.hi;
+    s.lo = __fadd_rn(s.lo, t.lo);
+}
+__device__ __forceinline__ void ff_acc_prod(FF &s, float a, float b) {  // s += a b, the product exactly
+    const float p = __fmul_rn(a, b);
+    ff_acc(s, p);
+    s.lo = __fadd_rn(s.lo, fmaf(a, b, -p));
+}
+__device__ __forceinline__ FF ff_neg(FF a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    FF t = two_sum(a.hi, b.hi);
+    t.lo = __fadd_rn(t.lo, __fadd_rn(a.lo, b.lo));
+    return two_sum(t.hi, t.lo);
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return fast_two_sum(p, e);
+}
+__device__ __forceinline__ FF ff_div(FF a, FF b) {
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const FF r = ff_add(a, ff_neg(ff_mul(b, FF{q1, 0.f})));
+    return fast_two_sum(q1, __fdiv_rn(__fadd_rn(r.hi, r.lo), b.hi));
+}
+__device__ __forceinline__ FF ff_norm(FF a) { return two_sum(a.hi, a.lo); }
+
+// Carnahan-Starling pressure (Ark/Lib/nonidealEoS.h:114-118) of the density r:
+// r R0 T (1 + r + r^2 - r^3) / (1 - r)^3 - a r^2
+__device__ __forceinline__ FF cs_p(const PPP &P, FF r) {
+    const FF one{1.f, 0.f};
+    const FF r2 = ff_mul(r, r), r3 = ff_mul(r2, r);
+    const FF num = ff_add(ff_add(ff_add(one, r), r2), ff_neg(r3));
+    const FF om = ff_add(one, ff_neg(r));
+    const FF den = ff_mul(ff_mul(om, om), om);
+    return ff_add(ff_mul(ff_mul(r, FF{P.rtcs_hi, P.rtcs_lo}), ff_div(num, den)),
+                  ff_neg(ff_mul(FF{P.acs_hi, P.acs_lo}, r2)));
+}
+// calcPsi (Ark/Header/Macroscopic.h:64-68): G = sign(p - rho RT), psi = sqrt(2 (p - rho RT) / G)
+__device__ __forceinline__ void cs_psi(const PPP &P, FF rho, FF p, float &scg, float &psi) {
+    const FF g = ff_add(p, ff_neg(ff_mul(rho, FF{P.rt_hi, P.rt_lo})));
+    const float G = (float)((g.hi > 0.f) - (g.hi < 0.f));
+    scg = G;
+    psi = sqrtf(__fdiv_rn(2.f * g.hi, G));
+}
+__device__ __forceinline__ double ff_to_double(FF a) { return (double)a.hi + (double)a.lo; }
 
 __device__ __forceinline__ float sr1(float a, float b, uint32_t bits16) {
     const float s = a + b;
@@ -161,7 +217,7 @@ __global__ void __launch_bounds__(256) k_pp32_faces1(PPP P, PPS S) {
     const int nx = P.nx, ny = P.ny, pitch = P.pitch;
     const int im = wrapi(i - 1, nx), ip = wrapi(i + 1, nx), jm = wrapi(j - 1, ny), jp = wrapi(j + 1, ny);
     const size_t c = (size_t)j * pitch + i;
-    double sR = 0.0;
+    FF sR{0.f, 0.f};
     float su = 0.f, sv = 0.f;
     float *B = xf ? S.xb : S.yb;
 #pragma unroll
@@ -182,19 +238,20 @@ __global__ void __launch_bounds__(256) k_pp32_faces1(PPP P, PPS S) {
         }
         const float b = 0.5f * (o + n) - P.hDt * (gx * P.xi_u[q] + gy * P.xi_v[q]);
         B[(size_t)q * S.qs + c] = b;
-        sR += (double)b;
+        ff_acc(sR, b);
         su += b * P.xi_u[q];
         sv += b * P.xi_v[q];
     }
-    const double R = P.rho_ref + sR;
-    const float Rf = (float)R;
+    sR = ff_norm(sR);
+    const FF R = ff_add(FF{P.rref_hi, P.rref_lo}, sR);
+    const float Rf = R.hi;
     float U = su / Rf, V = sv / Rf;
     U += 0.5f * P.hDt * (xf ? S.xFx : S.yFx)[c] / Rf;
     V += 0.5f * P.hDt * (xf ? S.xFy : S.yFy)[c] / Rf;
-    const double p = cs_p(P, R);
+    const FF p = cs_p(P, R);
     float scg, psi;
     cs_psi(P, R, p, scg, psi);
-    (xf ? S.xr : S.yr)[c] = (float)(R - P.rho_ref);
+    (xf ? S.xr : S.yr)[c] = sR.hi;
     (xf ? S.xu : S.yu)[c] = U;
     (xf ? S.xv : S.yv)[c] = V;
     (xf ? S.xg : S.yg)[c] = scg;
@@ -217,7 +274,7 @@ __global__ void __launch_bounds__(256) k_pp32_faces2(PPP P, PPS S) {
     (xf ? S.xFx : S.yFx)[c] = Fx;
     (xf ? S.xFy : S.yFy)[c] = Fy;
     const float dr = (xf ? S.xr : S.yr)[c];
-    const float R = (float)(P.rho_ref + (double)dr);
+    const float R = ff_add(FF{P.rref_hi, P.rref_lo}, FF{dr, 0.f}).hi;
     const float U = (xf ? S.xu : S.yu)[c], V = (xf ? S.xv : S.yv)[c];
     float de[Q];
     pp_deq<MODEL>(P, dr, R, U, V, de);
@@ -238,7 +295,7 @@ __global__ void __launch_bounds__(256) k_pp32_faces2(PPP P, PPS S) {
 
 // Update (Ark/Cpp/DUGKS2DSolver.cpp:748-792) and cell macros (Ark/Lib/D2Q9PP.cpp:89-109):
 // deviations + 4/3 (f-bar-plus - deviations) + dt/V sum(F), rounded stochastically;
-// rho, U, V, p, psi in FP64 sums.
+// rho, U, V, p, psi from float-float sums (rho and p kept in FP64).
 template <int MODEL>
 __global__ void __launch_bounds__(256) k_pp32_update(PPP P, PPS S, uint32_t step) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -248,7 +305,7 @@ __global__ void __launch_bounds__(256) k_pp32_update(PPP P, PPS S, uint32_t step
     const int ip = wrapi(i + 1, P.nx), jn = wrapi(j + 1, P.ny);
     const size_t c = (size_t)j * pitch + i, cE = (size_t)j * pitch + ip, cN = (size_t)jn * pitch + i;
     const uint32_t h0 = mix32((uint32_t)c * 0x9E3779B1U ^ step * 0x85EBCA77U);
-    double sR = 0.0, su = 0.0, sv = 0.0;
+    FF sR{0.f, 0.f}, su{0.f, 0.f}, sv{0.f, 0.f};
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         const size_t o = (size_t)q * S.qs;
@@ -261,21 +318,25 @@ __global__ void __launch_bounds__(256) k_pp32_update(PPP P, PPS S, uint32_t step
         const uint32_t bits = h0 * (2u * q + 1u) + (uint32_t)q * 0x632BE5ABU;
         const float dn = sr1(d, P.aTP * (S.bf[o + c] - d) + P.dtV * s, bits & 0xFFFFu);
         S.df[o + c] = dn;
-        sR += (double)dn;
-        su += (double)dn * (double)P.xi_u[q];
-        sv += (double)dn * (double)P.xi_v[q];
+        ff_acc(sR, dn);
+        ff_acc_prod(su, dn, P.xi_u[q]);
+        ff_acc_prod(sv, dn, P.xi_v[q]);
     }
-    const double R = P.rho_ref + sR;
-    double U = su / R, V = sv / R;
-    U += (double)P.hDt * (double)S.Fx[c] / R;
-    V += (double)P.hDt * (double)S.Fy[c] / R;
-    const double p = cs_p(P, R);
+    const FF R = ff_add(FF{P.rref_hi, P.rref_lo}, ff_norm(sR));
+    const float Rf = R.hi;
+    float U = __fadd_rn(su.hi, su.lo) / Rf, V = __fadd_rn(sv.hi, sv.lo) / Rf;
+    U += P.hDt * S.Fx[c] / Rf;
+    V += P.hDt * S.Fy[c] / Rf;
+    const FF p = cs_p(P, R);
     float scg, psi;
     cs_psi(P, R, p, scg, psi);
-    S.rho[c] = R;
+    // rho_ref + the sum in FP64: the next collision takes rho - rho_ref as the
+    // deviations' sum, and a representation offset of rho_ref (even of 1e-16, as
+    // in the float-float R) made the mass drift steadily
+    S.rho[c] = P.rho_ref + ff_to_double(ff_norm(sR));
     S.U[c] = U;
     S.V[c] = V;
-    S.p[c] = p;
+    S.p[c] = ff_to_double(p);
     S.scg[c] = scg;
     S.psi[c] = psi;
 }

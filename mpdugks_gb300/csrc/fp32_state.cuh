@@ -62,6 +62,9 @@ struct PPP {
     float hDt, dt, RT, invRT, Lambda0, Tau0, aTP, bTP, dtV;
     float r_2dy, r_ndx, r_n2dx, r_ndy, inv_6_2dx, inv_6_2dy;
     double rho_ref, R0, T_CS, aCS, RTd;
+    // the same constants as float-float pairs (hi + lo) for the device arithmetic:
+    // rho_ref, R0 T_CS, aCS, RT
+    float rref_hi, rref_lo, rtcs_hi, rtcs_lo, acs_hi, acs_lo, rt_hi, rt_lo;
     float xi_u[16], xi_v[16], w9[9], frest[16];
 };
 // State: f deviations and the step's scratch in FP32, the density (and the
