@@ -557,7 +557,7 @@ def run_ours(args, wl, rank, world, local):
         serving = serving_bench(args)
     pseudo = None
     if rank == 0 and not args.no_pseudopotential:
-        pseudo = pseudopotential_bench()
+        pseudo = pseudopotential_bench(args.pp_steps)
 
     if rank == 0:
         cpu = None
@@ -610,6 +610,9 @@ def main():
     ap.add_argument('--no-serving', action='store_true', help='skip the serving-stream measurement')
     ap.add_argument('--no-pseudopotential', action='store_true', help='skip the D2V16 FP32/FP64 measurement')
     ap.add_argument('--serving-only', action='store_true', help='run only the serving-stream measurement')
+    ap.add_argument('--pseudopotential-only', action='store_true',
+                    help='run only the D2V16 FP32/FP64 measurement (--pp-steps timed steps)')
+    ap.add_argument('--pp-steps', type=int, default=100)
     ap.add_argument('--serving-cases', type=int, default=SERVING['cases'])
     ap.add_argument('--serving-steps', type=int, default=SERVING['steps'])
     ap.add_argument('--serving-sample', type=int, default=3, help='cases solved one at a time for comparison')
@@ -642,6 +645,11 @@ def main():
         import torch
         torch.cuda.set_device(local)
         print(json.dumps({'serving': serving_bench(args)}), flush=True)
+        return 0
+    if args.pseudopotential_only:
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps({'pseudopotential_d2v16': pseudopotential_bench(args.pp_steps)}), flush=True)
         return 0
     return run_ours(args, wl, rank, world, local)
 
