@@ -68,7 +68,23 @@ typedef struct dugks_case {
     double aCS;         /* Carnahan-Starling attraction a (b = 4, R = 1) */
     double Tc_CS;       /* Carnahan-Starling critical temperature (0.3773 a / b) */
     double d2v16_c;     /* D2V16 lattice speed c (1.2 in the reference) */
+    int flux_scheme;    /* dugks_flux_scheme: the face reconstruction (Case.ark "Flux Scheme") */
 } dugks_case_t;
+
+/* Half-step face reconstruction (Ark/Constant/ZeroFlip.h _FLUX_SCHEME_*_ARK).
+ * CD (the reference's default): central value and gradients of the two cells
+ * at the face (CD_Interior_phi_Bh, Ark/Cpp/DUGKS2DSolver.cpp:604-687).  UW:
+ * the upwind cell's value extrapolated with its 6-point isotropic gradient
+ * (Grad_VS_6points, Ark/Lib/GradSchemeBasic.h:95-126; UW_Interior_phi_Bh,
+ * Ark/Cpp/DUGKS2DSolver.cpp:558-603,689-706), both cells averaged for
+ * velocities along the face.  UW runs with the plain FP64 precisions
+ * (DUGKS_FP64, DUGKS_FP64_FMA), the Allen-Cahn models and periodic y: the
+ * reference's UW with walls reads the gradients of its wall shadow cells,
+ * which it never writes (uninitialised memory). */
+typedef enum dugks_flux_scheme {
+    DUGKS_FLUX_CD = 0,
+    DUGKS_FLUX_UW = 1
+} dugks_flux_scheme;
 
 typedef struct dugks_grid {
     int nx, ny;         /* cells; nx, ny >= 3 */

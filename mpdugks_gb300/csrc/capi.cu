@@ -194,6 +194,8 @@ static size_t fp64_arena_bytes(const Params &P) {
     total += NFIELDS * cellb;                     // macro fields
     total += align256(4 * rowb);                  // ghost phi rows
     if (pp) total += 14 * cellb + 2 * Q * cellb;  // pseudopotential face state + face BhDt
+    if (P.uw)                                     // UW cell gradients of f and h, low-side boundary fluxes
+        total += 4 * Q * cellb + 2 * align256(sizeof(double) * Q * P.ny) + 2 * Q * rowb;
     total += cellb;                               // rho_last
     total += align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 256 + 256;
     return total;
@@ -488,6 +490,14 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
         return fail(nullptr, DUGKS_EINVAL, "unknown precision");
     if (c->precision == DUGKS_FP64_FUSED && !(c->model == DUGKS_MODEL_AC || c->model == DUGKS_MODEL_HCZ))
         return fail(nullptr, DUGKS_EINVAL, "the fused deviation-form step supports the Allen-Cahn models (AC, HCZ)");
+    if (c->flux_scheme != DUGKS_FLUX_CD && c->flux_scheme != DUGKS_FLUX_UW)
+        return fail(nullptr, DUGKS_EINVAL, "unknown flux scheme");
+    if (c->flux_scheme == DUGKS_FLUX_UW &&
+        (!(c->precision == DUGKS_FP64 || c->precision == DUGKS_FP64_FMA) ||
+         !(c->model == DUGKS_MODEL_AC || c->model == DUGKS_MODEL_HCZ) || g->y_walls))
+        return fail(nullptr, DUGKS_EINVAL,
+                    "the UW flux scheme runs with DUGKS_FP64 / DUGKS_FP64_FMA, the Allen-Cahn models and periodic y "
+                    "(the reference's UW reads unwritten gradients of its wall shadow cells)");
     dugks_handle *h = new (std::nothrow) dugks_handle();
     if (!h) return fail(nullptr, DUGKS_ENOMEM, "host allocation failed");
     h->cs = *c;
@@ -539,6 +549,16 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
         for (auto p : pf) *p = take(cellb);
         S.xbf = take(Q * cellb);
         S.ybf = take(Q * cellb);
+    }
+    if (P.uw) {
+        S.gfx = take(Q * cellb);
+        S.gfy = take(Q * cellb);
+        S.ghx = take(Q * cellb);
+        S.ghy = take(Q * cellb);
+        S.xlo_f = take(align256(sizeof(double) * Q * P.ny));
+        S.xlo_h = take(align256(sizeof(double) * Q * P.ny));
+        S.ylo_f = take(Q * rowb);
+        S.ylo_h = take(Q * rowb);
     }
     h->rho_last = take(cellb);
     h->partial = take(align256(sizeof(double) * 4 * h->nblocks));

@@ -39,7 +39,7 @@ struct Params {
     // Reconstruction denominators as multipliers: -1/dx, -1/dy, 1/(2dy), 1/(-2dx).
     // grad_mul = 1 when dx and dy are powers of two, so x/d == x*(1/d) exactly.
     double r_ndx, r_ndy, r_2dy, r_n2dx;
-    int grad_mul, pad2_;
+    int grad_mul, uw;                              // uw: upwind face reconstruction (DUGKS_FLUX_UW)
     double c16;                                    // D2V16 lattice speed
     double xi_u[16], xi_v[16], omega[16];
     int bb[16];
@@ -57,6 +57,10 @@ struct State {
     double *xfFx, *xfFy, *yfFx, *yfFy;
     double *xpsi, *ypsi, *xscg, *yscg, *xrho, *yrho, *xu, *yu, *xv, *yv;
     double *xbf, *ybf;         // face BhDt kept between the two pseudopotential face passes [Q][ny][pitch]
+    double *gfx, *gfy, *ghx, *ghy;  // UW: cell gradients of f-bar-plus and h-bar-plus [Q][ny][pitch]
+    // UW: fluxes of the periodic boundary faces as the reference's low-side faces (owner
+    // inside at column 0 / row 0): x [Q][ny] (stride ny), y [Q][pitch] (stride pitch)
+    double *xlo_f, *xlo_h, *ylo_f, *ylo_h;
     size_t qs, qsy;            // velocity strides of cell/x-face arrays and of y-face arrays
 };
 

@@ -333,21 +333,97 @@ __device__ __forceinline__ double face_bh(const Params &P, const double *__restr
     return 0.5 * (o + n) - P.hDt * (gx * xu + gy * xv);
 }
 
+// ---------------------------------------------------------------------------
+// UW flux scheme (_FLUX_SCHEME_UW_ARK), periodic grids.
+//
+// Cell gradients of f-bar-plus, Grad_VS_6points (Ark/Cpp/GradScheme.cpp:205-218,
+// Ark/Lib/GradSchemeBasic.h:95-126): apsi = 4 on the axis neighbours, bpsi = 1
+// on the diagonals (C0..C3 = E, N, W, S; D0..D3 = NE, NW, SW, SE), divided by
+// 6 _2dx, in the reference's operand order.
+template <int MODEL>
+__global__ void __launch_bounds__(256) k_grad6(Params P, State S) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= P.nx || j >= P.ny) return;
+    const int pitch = P.pitch;
+    const int im = wrapi(i - 1, P.nx), ip = wrapi(i + 1, P.nx), jm = wrapi(j - 1, P.ny), jp = wrapi(j + 1, P.ny);
+    const size_t c = (size_t)j * pitch + i;
+    const size_t cE = (size_t)j * pitch + ip, cW = (size_t)j * pitch + im, cN = (size_t)jp * pitch + i,
+                 cS = (size_t)jm * pitch + i, cNE = (size_t)jp * pitch + ip, cNW = (size_t)jp * pitch + im,
+                 cSW = (size_t)jm * pitch + im, cSE = (size_t)jm * pitch + ip;
+    const double dxd = P._2dx * 6, dyd = P._2dy * 6, rdx = 1.0 / dxd, rdy = 1.0 / dyd;
+    (void)rdx;
+    (void)rdy;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+#pragma unroll
+        for (int w = 0; w < 2; ++w) {
+            const double *B = (w ? S.bh : S.bf) + (size_t)q * S.qs;
+            const double E = B[cE], W = B[cW], N = B[cN], Sv = B[cS];
+            const double NE = B[cNE], NW = B[cNW], SW = B[cSW], SE = B[cSE];
+            const double gx = RDIV(4.0 * (E - W) + (((NE - NW) + SE) - SW), dxd, rdx);
+            const double gy = RDIV(4.0 * (N - Sv) + (((NE - SE) + NW) - SW), dyd, rdy);
+            (w ? S.ghx : S.gfx)[(size_t)q * S.qs + c] = gx;
+            (w ? S.ghy : S.gfy)[(size_t)q * S.qs + c] = gy;
+        }
+    }
+}
+
+// Reconstruction UW_Interior_phi_Bh (Ark/Cpp/DUGKS2DSolver.cpp:558-603, chosen by the
+// sign of xi.n dS at :689-706) of velocity (xu, xv) at one face: the upwind
+// cell's f-bar-plus + (dx gx + dy gy) with (dx, dy) = x_f - hDt xi - x_c; the
+// owner's and the neighbour's values averaged (owner first) along the face.
+// The face is at the origin and its two cells at -1/2 ("o", below / left) and
+// +1/2 ("n") along the normal: every offset is exact, as the reference's are
+// on the unit grid.  The reference computes a periodic boundary face twice, as
+// the high-side face (owner o, normal +x / +y: the interior form) and as the
+// low-side face (owner n inside the domain, normal -x / -y): lo selects that form.
+template <bool XF>
+__device__ __forceinline__ double face_uw(const Params &P, const double *__restrict__ B,
+                                          const double *__restrict__ GX, const double *__restrict__ GY, size_t co,
+                                          size_t cn, double xu, double xv, bool lo) {
+    const double xon = XF ? -0.5 : 0.0, yon = XF ? 0.0 : -0.5;  // centre of o
+    const double xnn = XF ? 0.5 : 0.0, ynn = XF ? 0.0 : 0.5;    // centre of n
+    const double xsh = 0.0 - P.hDt * xu, ysh = 0.0 - P.hDt * xv;
+    const double dxo = xsh - xon, dyo = ysh - yon, dxn = xsh - xnn, dyn = ysh - ynn;
+    const double Xo = dxo * GX[co] + dyo * GY[co], Xn = dxn * GX[cn] + dyn * GY[cn];
+    const double xin = XF ? xu : xv;
+    const double s = lo ? -xin : xin;  // xi.n of the reference's face
+    if (lo) {                          // owner n, neighbour o
+        if (s > 0) return B[cn] + Xn;
+        if (s < 0) return B[co] + Xo;
+        double t = B[cn] + Xn;
+        t = t + B[co];
+        t = t + Xo;
+        return t / 2;
+    }
+    if (s > 0) return B[co] + Xo;
+    if (s < 0) return B[cn] + Xn;
+    double t = B[co] + Xo;
+    t = t + B[cn];
+    t = t + Xn;
+    return t / 2;
+}
+
 // Allen-Cahn face: Update_MacroVar_h + Update_phi_Eqh + Update_DVDF_Source_h
 // + Update_phi_h + Update_phiFlux_h (+ Wall_3_BB) -- Ark/Lib/D2Q9AC.cpp:106-144,
 // 232-329,345-358; Ark/Lib/D2Q9HCZ.cpp:93-131,183-271;
 // Ark/Cpp/DUGKS2DSolver.cpp:402-441; Ark/Cpp/Boundary.cpp:118-139.
-template <int MODEL, bool WALLS>
+// UW: blockIdx.z 2 and 3 are the x and y periodic boundary faces in the
+// reference's low-side form (column 0 / row 0 only), written to xlo / ylo.
+template <int MODEL, bool WALLS, bool UW>
 __global__ void __launch_bounds__(256) k_faces_ac(Params P, State S) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-    const bool xf = blockIdx.z == 0;
+    const bool xf = (blockIdx.z & 1) == 0;
+    const bool lo = UW && blockIdx.z >= 2;
     const int nrows = xf ? P.ny : (WALLS ? P.ny + 1 : P.ny);
     if (i >= P.nx || j >= nrows) return;
+    if (lo && (xf ? i != 0 : j != 0)) return;
     const int nx = P.nx, ny = P.ny, pitch = P.pitch;
     const int im = wrapi(i - 1, nx), ip = wrapi(i + 1, nx);
     // owner/neighbour cells of this face and the averaged source fields
     int jo, io;
     if (xf) { jo = j; io = im; } else { jo = j - 1; io = i; }
+    if (UW && jo < 0) jo += ny;  // periodic y (UW runs without walls)
     double avg[6];
     const int fid[6] = {F_PHIX, F_PHIY, F_RHOX, F_RHOY, F_FX, F_FY};
 #pragma unroll
@@ -358,7 +434,17 @@ __global__ void __launch_bounds__(256) k_faces_ac(Params P, State S) {
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
         const double xu = d2q9_xu(q), xv = d2q9_xv(q);
-        if (xf) {
+        if (UW) {
+            const size_t qo = (size_t)q * S.qs;
+            const size_t co = (size_t)jo * pitch + io, cn = (size_t)j * pitch + i;
+            if (xf) {
+                bf[q] = face_uw<true>(P, S.bf + qo, S.gfx + qo, S.gfy + qo, co, cn, xu, xv, lo);
+                bh[q] = face_uw<true>(P, S.bh + qo, S.ghx + qo, S.ghy + qo, co, cn, xu, xv, lo);
+            } else {
+                bf[q] = face_uw<false>(P, S.bf + qo, S.gfx + qo, S.gfy + qo, co, cn, xu, xv, lo);
+                bh[q] = face_uw<false>(P, S.bh + qo, S.ghx + qo, S.ghy + qo, co, cn, xu, xv, lo);
+            }
+        } else if (xf) {
             bf[q] = face_bh<true, WALLS>(P, S.bf + (size_t)q * S.qs, i, im, ip, j, xu, xv);
             bh[q] = face_bh<true, WALLS>(P, S.bh + (size_t)q * S.qs, i, im, ip, j, xu, xv);
         } else {
@@ -436,10 +522,10 @@ __global__ void __launch_bounds__(256) k_faces_ac(Params P, State S) {
             }
         }
     }
-    double *outf = xf ? S.xff : S.yff;
-    double *outh = xf ? S.xfh : S.yfh;
-    const size_t qs = xf ? S.qs : S.qsy;
-    const size_t c = (size_t)j * pitch + i;
+    double *outf = lo ? (xf ? S.xlo_f : S.ylo_f) : (xf ? S.xff : S.yff);
+    double *outh = lo ? (xf ? S.xlo_h : S.ylo_h) : (xf ? S.xfh : S.yfh);
+    const size_t qs = lo ? (xf ? (size_t)ny : (size_t)pitch) : (xf ? S.qs : S.qsy);
+    const size_t c = lo ? (xf ? (size_t)j : (size_t)i) : (size_t)j * pitch + i;
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
         const int s = xf ? d2q9_xu(q) : d2q9_xv(q);
@@ -538,13 +624,16 @@ __global__ void __launch_bounds__(256) k_update(Params P, State S) {
     const size_t cE = (size_t)j * pitch + ip, cN = (size_t)jn * pitch + i;
     double sumf = 0, su = 0, sv = 0, Phi = 0, f0 = 0;
 #pragma unroll
+    // UW: the west face of column 0 and the south face of row 0 are the reference's
+    // low-side periodic boundary faces (k_faces_ac, xlo / ylo)
+    const bool xlo = P.uw && i == 0, ylo = P.uw && j == 0;
     for (int q = 0; q < Q; ++q) {
         const size_t oq = (size_t)q * S.qs, oy = (size_t)q * S.qsy;
         double s = 0.0;
         s += -S.xff[oq + cE];
         s += -S.yff[oy + cN];
-        s += S.xff[oq + c];
-        s += S.yff[oy + c];
+        s += xlo ? S.xlo_f[(size_t)q * P.ny + j] : S.xff[oq + c];
+        s += ylo ? S.ylo_f[(size_t)q * pitch + i] : S.yff[oy + c];
         const double fn = P.aTP * S.bf[oq + c] - P.bTP * S.f[oq + c] + P.dtV * s;
         S.f[oq + c] = fn;
         sumf += fn;
@@ -555,8 +644,8 @@ __global__ void __launch_bounds__(256) k_update(Params P, State S) {
             double t = 0.0;
             t += -S.xfh[oq + cE];
             t += -S.yfh[oy + cN];
-            t += S.xfh[oq + c];
-            t += S.yfh[oy + c];
+            t += xlo ? S.xlo_h[(size_t)q * P.ny + j] : S.xfh[oq + c];
+            t += ylo ? S.ylo_h[(size_t)q * pitch + i] : S.yfh[oy + c];
             const double hn = P.aTP * S.bh[oq + c] - P.bTP * S.h[oq + c] + P.dtV * t;
             S.h[oq + c] = hn;
             Phi += hn;
@@ -710,9 +799,16 @@ static void launch_step_t(const Params &P, const State &S, int do_msrc, int gin,
     k_collide<MODEL, WALLS><<<grd, blk, 0, st>>>(P, S, do_msrc, gin, gout);
     if (ev) cudaEventRecord(ev[1], st);
     if constexpr (MODEL == AC || MODEL == HCZ) {
-        const dim3 gf((P.nx + 31) / 32, (P.ny + 1 + 7) / 8, 2);
-        k_faces_ac<MODEL, WALLS><<<gf, blk, 0, st>>>(P, S);
-        *launches += 3;
+        if (!WALLS && P.uw) {  // UW: cell gradients, then the faces with the low-side boundary faces
+            k_grad6<MODEL><<<grd, blk, 0, st>>>(P, S);
+            const dim3 gf((P.nx + 31) / 32, (P.ny + 1 + 7) / 8, 4);
+            k_faces_ac<MODEL, false, true><<<gf, blk, 0, st>>>(P, S);
+            *launches += 4;
+        } else {
+            const dim3 gf((P.nx + 31) / 32, (P.ny + 1 + 7) / 8, 2);
+            k_faces_ac<MODEL, WALLS, false><<<gf, blk, 0, st>>>(P, S);
+            *launches += 3;
+        }
     } else {
         const dim3 gf((P.nx + 31) / 32, (P.ny + 7) / 8, 2);
         k_faces_pp1<MODEL><<<gf, blk, 0, st>>>(P, S);

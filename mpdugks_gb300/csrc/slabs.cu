@@ -161,8 +161,9 @@ extern "C" int dugks_slabs_create(const dugks_case_t *c, const dugks_grid_t *g, 
                                   dugks_slabs_t **out) {
     if (!c || !g || !out) return fail("null argument");
     *out = nullptr;
-    if (c->precision != DUGKS_FP32_DEV || !(c->model == DUGKS_MODEL_AC || c->model == DUGKS_MODEL_HCZ))
-        return fail("slab decomposition runs FP32-storage Allen-Cahn cases (AC, HCZ)");
+    if (c->precision != DUGKS_FP32_DEV || !(c->model == DUGKS_MODEL_AC || c->model == DUGKS_MODEL_HCZ) ||
+        c->flux_scheme != DUGKS_FLUX_CD)
+        return fail("slab decomposition runs FP32-storage Allen-Cahn cases (AC, HCZ) with the CD flux scheme");
     if (g->nx < 3) return fail("nx must be >= 3");
     std::vector<int> row0, nrows, lo, hi;
     if (!plan(g->ny, g->y_walls, nparts, row0, nrows, lo, hi))

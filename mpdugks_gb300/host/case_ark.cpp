@@ -143,6 +143,11 @@ RunConfig config_from_case_ark(const CaseArk &ark) {
     const std::string bc = ark.get("Boundary Condition");
     c.grid.y_walls = (c.mesh_name.find("Wall") != std::string::npos || bc.find("Wall") != std::string::npos) ? 1 : 0;
     if (ark.has("walls")) c.grid.y_walls = ark.num("walls", 0) != 0 ? 1 : 0;
+    // the face reconstruction (OutputCase writes _FLUX_SCHEME_ARK, Ark/Constant/ZeroFlip.h)
+    const std::string fs = ark.get("Flux Scheme", "CD");
+    if (fs == "CD") c.cs.flux_scheme = DUGKS_FLUX_CD;
+    else if (fs == "UW") c.cs.flux_scheme = DUGKS_FLUX_UW;
+    else throw std::runtime_error("Case.ark: unknown flux scheme '" + fs + "'");
     c.mesh_type = ark.get("Mesh Type", "Car");
     c.nl = ark.get("NL", std::to_string(c.grid.nx));
     c.mach = ark.get("Mach", "0");

@@ -168,10 +168,10 @@ int main(int argc, char **argv) {
         if (argc == 3 && std::strcmp(argv[1], "show-config") == 0) {
             const RunConfig c = config_from_case_ark(read_case_ark(argv[2]));
             std::printf("model %d precision %d nx %d ny %d walls %d init %d nparams %zu steps %lld Mu0 %.17g "
-                        "M_Phi %.17g W %.17g Sigma %.17g RhoL %.17g RhoV %.17g Gy %.17g\n",
+                        "M_Phi %.17g W %.17g Sigma %.17g RhoL %.17g RhoV %.17g Gy %.17g flux %d\n",
                         c.cs.model, c.cs.precision, c.grid.nx, c.grid.ny, c.grid.y_walls, c.init_kind,
                         c.init_params.size(), (long long)c.end_step, c.cs.Mu0, c.cs.M_Phi, c.cs.W, c.cs.Sigma,
-                        c.cs.RhoL, c.cs.RhoV, c.cs.Gy);
+                        c.cs.RhoL, c.cs.RhoV, c.cs.Gy, c.cs.flux_scheme);
             for (double p : c.init_params) std::printf("param %.17g\n", p);
             return 0;
         }

@@ -52,6 +52,11 @@ struct orc_state {
     /* pseudopotential face state (D2Q9PP/D2V16): previous face force, face psi */
     double *xfFx, *xfFy, *yfFx, *yfFy; /* x: [ny][nx]; y: [ny+1][nx] */
     double *xpsi, *ypsi, *xscg, *yscg, *xrho, *yrho, *xu, *yu, *xv, *yv; /* pass-1 results */
+    /* UW: cell gradients of BarP, extended [Q][ny+2][nx]; fluxes of the periodic
+     * boundary faces computed from the low side (owner in column 0 / row 0) */
+    double *gfx, *gfy, *ghx, *ghy;
+    double *Fxlo_f, *Fxlo_h;          /* [Q][ny] */
+    double *Fylo_f, *Fylo_h;          /* [Q][nx] */
     long step;
 };
 
@@ -226,6 +231,15 @@ orc_state *orc_create(const orc_inputs *in) {
     s->xpsi = xalloc(nc); s->ypsi = xalloc(ny1); s->xscg = xalloc(nc); s->yscg = xalloc(ny1);
     s->xrho = xalloc(nc); s->yrho = xalloc(ny1); s->xu = xalloc(nc); s->yu = xalloc(ny1);
     s->xv = xalloc(nc); s->yv = xalloc(ny1);
+    if (in->uw) {
+        if (!s->has_h || in->y_walls) {  /* the reference's UW with walls reads unwritten shadow-cell gradients */
+            orc_destroy(s);
+            return NULL;
+        }
+        s->gfx = xalloc(Q * ne); s->gfy = xalloc(Q * ne); s->ghx = xalloc(Q * ne); s->ghy = xalloc(Q * ne);
+        s->Fxlo_f = xalloc((size_t)Q * s->ny); s->Fxlo_h = xalloc((size_t)Q * s->ny);
+        s->Fylo_f = xalloc((size_t)Q * s->nx); s->Fylo_h = xalloc((size_t)Q * s->nx);
+    }
 
     const int nx = s->nx, ny = s->ny;
     if (s->has_h) {
@@ -319,7 +333,8 @@ void orc_destroy(orc_state *s) {
                       &s->scg, &s->phi, &s->phix, &s->phiy, &s->rhox, &s->rhoy, &s->fx, &s->fy, &s->psi,
                       &s->bf, &s->bh, &s->Fxf, &s->Fxh, &s->Fyf, &s->Fyh, &s->xfFx, &s->xfFy, &s->yfFx,
                       &s->yfFy, &s->xpsi, &s->ypsi, &s->xscg, &s->yscg, &s->xrho, &s->yrho, &s->xu,
-                      &s->yu, &s->xv, &s->yv};
+                      &s->yu, &s->xv, &s->yv, &s->gfx, &s->gfy, &s->ghx, &s->ghy, &s->Fxlo_f, &s->Fxlo_h,
+                      &s->Fylo_f, &s->Fylo_h};
     for (size_t k = 0; k < sizeof all / sizeof all[0]; ++k) free(*all[k]);
     free(s);
 }
@@ -426,6 +441,49 @@ static void face_bh(const orc_state *s, const double *B, int xface, int i, int j
             gy = (o - n) / (-s->DeltaY);
         }
         out[q] = 0.5 * (o + n) - s->hDt * (gx * (s->xi_u[q]) + gy * s->xi_v[q]);
+    }
+}
+
+/* UW flux scheme (_FLUX_SCHEME_UW_ARK), periodic grids.  Cell gradients of
+ * BarP, Grad_VS_6points (Ark/Cpp/GradScheme.cpp:205-218,
+ * Ark/Lib/GradSchemeBasic.h:95-126): apsi = 4, bpsi = 1, C0..C3 = E,N,W,S,
+ * D0..D3 = NE,NW,SW,SE. */
+static void cell_grad6(orc_state *s, const double *B, double *GX, double *GY, int i, int j) {
+    int im = wrapx(s, i - 1), ip = wrapx(s, i + 1);
+    for (int q = 0; q < s->Q; ++q) {
+        double E_ = BQ(s, B, q, j, ip), W_ = BQ(s, B, q, j, im);
+        double N_ = BQ(s, B, q, j + 1, i), S_ = BQ(s, B, q, j - 1, i);
+        double D0 = BQ(s, B, q, j + 1, ip), D1 = BQ(s, B, q, j + 1, im);
+        double D2 = BQ(s, B, q, j - 1, im), D3 = BQ(s, B, q, j - 1, ip);
+        BQ(s, GX, q, j, i) = (4.0 * (E_ - W_) + 1.0 * (D0 - D1 + D3 - D2)) / (s->_2dx * 6);
+        BQ(s, GY, q, j, i) = (4.0 * (N_ - S_) + 1.0 * (D0 - D3 + D1 - D2)) / (s->_2dy * 6);
+    }
+}
+
+/* UW_Interior_phi_Bh (Ark/Cpp/DUGKS2DSolver.cpp:558-603), chosen by the sign of
+ * xi.n dS (:689-706): the upwind cell's BarP + (dx BarP_x + dy BarP_y) with
+ * (dx, dy) = x_f - hDt xi - x_c, the two cells averaged (owner first) along the
+ * face.  Canonical orientation as face_bh: o = (i-1,j) or (i,j-1), n = (i,j),
+ * normal +x / +y; cell centres relative to the face at -1/2 and +1/2 along the
+ * normal (exact, as the reference's coordinates on the unit grid).  lo: the
+ * periodic boundary face as the reference computes it from the low side
+ * (owner n inside the domain, normal -x / -y). */
+static void face_uw(const orc_state *s, const double *B, const double *GX, const double *GY, int xface, int i,
+                    int j, int lo, double *out) {
+    int io = xface ? wrapx(s, i - 1) : i, jo = xface ? j : j - 1;
+    double xo = xface ? -0.5 : 0.0, yo = xface ? 0.0 : -0.5;
+    double xn = xface ? 0.5 : 0.0, yn = xface ? 0.0 : 0.5;
+    for (int q = 0; q < s->Q; ++q) {
+        double xsh = 0.0 - s->hDt * s->xi_u[q], ysh = 0.0 - s->hDt * s->xi_v[q];
+        double Bo = BQ(s, B, q, jo, io), Bn = BQ(s, B, q, j, i);
+        double Xo = (xsh - xo) * BQ(s, GX, q, jo, io) + (ysh - yo) * BQ(s, GY, q, jo, io);
+        double Xn = (xsh - xn) * BQ(s, GX, q, j, i) + (ysh - yn) * BQ(s, GY, q, j, i);
+        double xin = xface ? s->xi_u[q] : s->xi_v[q];
+        double sgn = lo ? -xin : xin;
+        double ow = lo ? Bn : Bo, owX = lo ? Xn : Xo, ne = lo ? Bo : Bn, neX = lo ? Xo : Xn;
+        if (sgn > 0) out[q] = ow + owX;
+        else if (sgn < 0) out[q] = ne + neX;
+        else out[q] = (ow + owX + ne + neX) / 2;
     }
 }
 
@@ -573,6 +631,19 @@ static void one_step(orc_state *s) {
         double *mf[] = {s->phi, s->phix, s->phiy, s->rhox, s->rhoy, s->fx, s->fy};
         for (int k = 0; k < 7; ++k) fill_rows(s, mf[k]);
     }
+    const int uw = s->in.uw;
+    if (uw) { /* UW: cell gradients of BarP (Ark/Cpp/DUGKS2DSolver.cpp:196-205) */
+#pragma omp parallel for schedule(static)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                cell_grad6(s, s->bf, s->gfx, s->gfy, i, j);
+                cell_grad6(s, s->bh, s->ghx, s->ghy, i, j);
+            }
+        for (int q = 0; q < Q; ++q) {
+            double *g[] = {s->gfx, s->gfy, s->ghx, s->ghy};
+            for (int k = 0; k < 4; ++k) fill_rows(s, g[k] + (size_t)q * (ny + 2) * nx);
+        }
+    }
     /* P4 + P6: faces */
     if (AC) {
 #pragma omp parallel for schedule(static)
@@ -587,12 +658,26 @@ static void one_step(orc_state *s) {
                 avg[3] = 0.5 * ((s->rhoy[a]) + (s->rhoy[b]));
                 avg[4] = 0.5 * ((s->fx[a]) + (s->fx[b]));
                 avg[5] = 0.5 * ((s->fy[a]) + (s->fy[b]));
-                face_bh(s, s->bf, 1, i, j, bf);
-                face_bh(s, s->bh, 1, i, j, bh);
+                if (uw) {
+                    face_uw(s, s->bf, s->gfx, s->gfy, 1, i, j, 0, bf);
+                    face_uw(s, s->bh, s->ghx, s->ghy, 1, i, j, 0, bh);
+                } else {
+                    face_bh(s, s->bf, 1, i, j, bf);
+                    face_bh(s, s->bh, 1, i, j, bh);
+                }
                 face_flux_ac(s, bf, bh, avg, 1, 0, of, oh);
                 for (int q = 0; q < Q; ++q) {
                     XQ(s, s->Fxf, q, j, i) = of[q];
                     XQ(s, s->Fxh, q, j, i) = oh[q];
+                }
+                if (uw && i == 0) { /* the left boundary face of the reference (owner (0,j)) */
+                    face_uw(s, s->bf, s->gfx, s->gfy, 1, i, j, 1, bf);
+                    face_uw(s, s->bh, s->ghx, s->ghy, 1, i, j, 1, bh);
+                    face_flux_ac(s, bf, bh, avg, 1, 0, of, oh);
+                    for (int q = 0; q < Q; ++q) {
+                        s->Fxlo_f[(size_t)q * ny + j] = of[q];
+                        s->Fxlo_h[(size_t)q * ny + j] = oh[q];
+                    }
                 }
             }
         int jy1 = walls ? ny + 1 : ny;
@@ -607,13 +692,27 @@ static void one_step(orc_state *s) {
                 avg[3] = 0.5 * ((s->rhoy[a]) + (s->rhoy[b]));
                 avg[4] = 0.5 * ((s->fx[a]) + (s->fx[b]));
                 avg[5] = 0.5 * ((s->fy[a]) + (s->fy[b]));
-                face_bh(s, s->bf, 0, i, j, bf);
-                face_bh(s, s->bh, 0, i, j, bh);
+                if (uw) {
+                    face_uw(s, s->bf, s->gfx, s->gfy, 0, i, j, 0, bf);
+                    face_uw(s, s->bh, s->ghx, s->ghy, 0, i, j, 0, bh);
+                } else {
+                    face_bh(s, s->bf, 0, i, j, bf);
+                    face_bh(s, s->bh, 0, i, j, bh);
+                }
                 int wall = walls ? (j == 0 ? -1 : (j == ny ? 1 : 0)) : 0;
                 face_flux_ac(s, bf, bh, avg, 0, wall, of, oh);
                 for (int q = 0; q < Q; ++q) {
                     YQ(s, s->Fyf, q, j, i) = of[q];
                     YQ(s, s->Fyh, q, j, i) = oh[q];
+                }
+                if (uw && j == 0) { /* the bottom boundary face of the reference (owner (i,0)) */
+                    face_uw(s, s->bf, s->gfx, s->gfy, 0, i, j, 1, bf);
+                    face_uw(s, s->bh, s->ghx, s->ghy, 0, i, j, 1, bh);
+                    face_flux_ac(s, bf, bh, avg, 0, 0, of, oh);
+                    for (int q = 0; q < Q; ++q) {
+                        s->Fylo_f[(size_t)q * nx + i] = of[q];
+                        s->Fylo_h[(size_t)q * nx + i] = oh[q];
+                    }
                 }
             }
         if (!walls) {
@@ -673,19 +772,21 @@ static void one_step(orc_state *s) {
     for (int j = 0; j < ny; ++j)
         for (int i = 0; i < nx; ++i) {
             int ip = wrapx(s, i + 1);
+            /* UW: the west face of column 0 / south face of row 0 are the low-side boundary faces */
+            int xlo = uw && i == 0, ylo = uw && j == 0;
             for (int q = 0; q < Q; ++q) {
                 double S = 0.0;
                 S += -1 * XQ(s, s->Fxf, q, j, ip);
                 S += -1 * YQ(s, s->Fyf, q, j + 1, i);
-                S += 1 * XQ(s, s->Fxf, q, j, i);
-                S += 1 * YQ(s, s->Fyf, q, j, i);
+                S += 1 * (xlo ? s->Fxlo_f[(size_t)q * ny + j] : XQ(s, s->Fxf, q, j, i));
+                S += 1 * (ylo ? s->Fylo_f[(size_t)q * nx + i] : YQ(s, s->Fyf, q, j, i));
                 DQ(s, s->f, q, j, i) = s->aTP * BQ(s, s->bf, q, j, i) - s->bTP * DQ(s, s->f, q, j, i) + dtV * S;
                 if (AC) {
                     double H = 0.0;
                     H += -1 * XQ(s, s->Fxh, q, j, ip);
                     H += -1 * YQ(s, s->Fyh, q, j + 1, i);
-                    H += 1 * XQ(s, s->Fxh, q, j, i);
-                    H += 1 * YQ(s, s->Fyh, q, j, i);
+                    H += 1 * (xlo ? s->Fxlo_h[(size_t)q * ny + j] : XQ(s, s->Fxh, q, j, i));
+                    H += 1 * (ylo ? s->Fylo_h[(size_t)q * nx + i] : YQ(s, s->Fyh, q, j, i));
                     DQ(s, s->h, q, j, i) = s->aTP * BQ(s, s->bh, q, j, i) - s->bTP * DQ(s, s->h, q, j, i) + dtV * H;
                 }
             }

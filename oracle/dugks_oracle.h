@@ -32,6 +32,7 @@ typedef struct orc_inputs {
     double noise_rho0, noise_amp;                          /* pp_noise init */
     uint64_t seed;
     double d2v16_c;                                        /* D2V16 lattice speed (1.2) */
+    int uw;                                                /* 1: the UW flux scheme (Allen-Cahn, periodic) */
 } orc_inputs;
 
 typedef struct orc_state orc_state;

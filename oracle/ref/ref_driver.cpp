@@ -64,6 +64,7 @@ extern void OutputCase();
 extern void Output_Flowfield(double const &t, int step);
 extern void WallShadowC_fBP(Cell_2D &shadowCell);
 extern void Wall_3_BB(Face_2D &face);
+extern void Grad_VS_6points(Cell_2D *center);
 
 
 namespace {
@@ -161,6 +162,11 @@ void run_step() {
 #ifdef _Wall_3_BCs_FLIP
 #pragma omp parallel for schedule(static)
     for (int n = 0; n < WallFaceNum; ++n) WallShadowC_fBP(WallShadowCA[n]);
+#endif
+#ifdef _FLUX_SCHEME_UW_ARK
+    // cell gradients of BarP for the UW reconstruction (Ark/Cpp/DUGKS2DSolver.cpp:196-205)
+#pragma omp parallel for schedule(static)
+    for (int n = 0; n < Cells; ++n) Grad_VS_6points(&CellArray[n]);
 #endif
 #if defined _ARK_PSEUDOPSI_FLIP && defined _ARK_FORCE_FLIP
     // pass 1: face distributions, moments and psi of every face

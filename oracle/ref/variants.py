@@ -44,4 +44,13 @@ VARIANTS = {
                   consts=dict(Mu0=0.02, W=4.0, Sigma=1e-3, RhoL=1.0, RhoV=0.1, radius=7.0)),
     # Pseudopotential D2Q9 with the reference's own SCMP_Drop init.
     'pp_drop': dict(model='D2Q9PP', nx=32, ny=32, walls=False, init='scmp_drop', consts={}),
+    # The upwind (UW) flux scheme with the 6-point cell gradients
+    # (_FLUX_SCHEME_UW_ARK, Ark/Cpp/DUGKS2DSolver.cpp:540-603,689-706;
+    # Ark/Lib/GradSchemeBasic.h:95-126) instead of the default CD: the small
+    # periodic droplet and the HCZ droplet.  (With walls the reference's UW
+    # reads the gradients of its wall shadow cells, which it never writes.)
+    'uw_small': dict(model='D2Q9AC', nx=24, ny=20, walls=False, init='ac_drop_inside', scheme='UW',
+                     consts=dict(Mu0=0.01, W=4.0, Sigma=1e-3, RhoL=1.0, RhoV=0.1, radius=6.0)),
+    'uw_hcz': dict(model='D2Q9HCZ', nx=32, ny=32, walls=False, init='ac_drop_inside', scheme='UW',
+                   consts=dict(Mu0=0.02, W=4.0, Sigma=1e-2, RhoL=10.0, RhoV=1.0, radius=8.0)),
 }

@@ -30,12 +30,17 @@ PLAN = {
     'pp_drop': (200, 200, 'all'),
     'ac_c1': (2000, 0, ['rho', 'p', 'phi']),
     'ac_default': (2000, 0, ['rho', 'p', 'phi']),
+    'uw_small': (500, 500, 'all'),
+    'uw_hcz': (200, 200, 'all'),
 }
 
 
-def main() -> None:
-    meta = {}
+def main(names=None) -> None:
+    meta_path = OUT / 'golden_meta.json'
+    meta = json.loads(meta_path.read_text()) if names and meta_path.exists() else {}
     for name, (steps, every, keep) in PLAN.items():
+        if names and name not in names:
+            continue
         build_ref.build(name)
         dump = f'/tmp/golden_{name}.bin'
         out, log = build_ref.run(name, steps, every, threads=8, dump=dump)
@@ -56,4 +61,4 @@ def main() -> None:
 
 
 if __name__ == '__main__':
-    main()
+    main(sys.argv[1:] or None)

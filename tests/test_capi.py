@@ -84,3 +84,21 @@ def test_struct_layouts_match_the_header(tmp_path):
     subprocess.run([gcc, f'-I{ROOT / "include"}', str(src), '-o', str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
     assert got == want
+
+
+@pytest.mark.parametrize('model,precision,walls', [('AC', 'fp32dev', False), ('HCZ', 'fp64', True),
+                                                   ('PP9', 'fp64', False), ('AC', 'fp64fused', False)])
+def test_uw_flux_scheme_rejected_where_not_supported(model, precision, walls):
+    """UW runs with the plain FP64 precisions, the Allen-Cahn models and periodic y; other
+    combinations are refused before any device work, with the reason."""
+    import ctypes
+    from mpdugks_gb300 import capi
+    lib = capi.load(build_if_missing=True)
+    case = capi.make_case(model, precision, scheme='UW')
+    grid = capi.GridT(16, 16, int(walls))
+    h = ctypes.c_void_p()
+    rc = lib.dugks_gpu_create(ctypes.byref(case), ctypes.byref(grid), ctypes.byref(h))
+    assert rc == capi.DUGKS_EINVAL and not h.value
+    buf = ctypes.create_string_buffer(256)
+    lib.dugks_gpu_last_error(None, buf, 256)
+    assert b'UW' in buf.value

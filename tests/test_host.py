@@ -62,6 +62,7 @@ def test_case_ark_decodes_the_reference_constants():
     assert kv['model'] == '0' and kv['nx'] == '32' and kv['ny'] == '24' and kv['walls'] == '0'
     assert kv['init'] == '0' and float(kv['param']) == 7.0
     assert float(kv['Mu0']) == 0.02 and float(kv['Sigma']) == 1e-3 and float(kv['RhoV']) == 0.1
+    assert kv['flux'] == '0'  # "CD = Flux Scheme"
     # the Rayleigh-Taylor box: walls from the mesh name; no case name, so an init entry is required
     r = subprocess.run([runner(), 'show-config', GOLD / 'hcz_rt' / 'Case.ark'], capture_output=True, text=True)
     assert r.returncode == 1 and "give an 'init' entry" in r.stderr

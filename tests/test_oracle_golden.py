@@ -9,7 +9,7 @@ import pytest
 from oracle.oracle import Oracle
 from variants import VARIANTS
 
-SMALL = ['ac_small', 'hcz_drop', 'hcz_rt', 'pp_drop']
+SMALL = ['ac_small', 'hcz_drop', 'hcz_rt', 'pp_drop', 'uw_small', 'uw_hcz']
 
 
 def _fields(o, names):
