@@ -69,7 +69,21 @@ typedef struct dugks_case {
     double Tc_CS;       /* Carnahan-Starling critical temperature (0.3773 a / b) */
     double d2v16_c;     /* D2V16 lattice speed c (1.2 in the reference) */
     int flux_scheme;    /* dugks_flux_scheme: the face reconstruction (Case.ark "Flux Scheme") */
+    int wall_scheme;    /* dugks_wall_scheme: the treatment of y_walls */
 } dugks_case_t;
+
+/* Wall faces (Ark/Constant/ZeroFlip.h _Wall_3_BCs_*).  BB (the default):
+ * the face computed like an interior face from the extrapolated ghost row,
+ * then bounce-back of the entering directions (Flux_2D + Wall_3_BB,
+ * Ark/Cpp/Boundary.cpp:118-139).  NEE: the face equilibrium at the owner's
+ * extrapolated phi and rho, its pressure and zero velocity, plus the owner's
+ * non-equilibrium part, then bounce-back (Wall_3_NEE,
+ * Ark/Cpp/Boundary.cpp:140-184).  NEE runs with DUGKS_FP64 / DUGKS_FP64_FMA
+ * and the Allen-Cahn models. */
+typedef enum dugks_wall_scheme {
+    DUGKS_WALL_BB = 0,
+    DUGKS_WALL_NEE = 1
+} dugks_wall_scheme;
 
 /* Half-step face reconstruction (Ark/Constant/ZeroFlip.h _FLUX_SCHEME_*_ARK).
  * CD (the reference's default): central value and gradients of the two cells

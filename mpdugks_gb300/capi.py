@@ -33,7 +33,7 @@ class CaseT(C.Structure):
     _fields_ = [('model', C.c_int), ('precision', C.c_int), ('Mu0', C.c_double), ('M_Phi', C.c_double),
                 ('W', C.c_double), ('Sigma', C.c_double), ('RhoL', C.c_double), ('RhoV', C.c_double),
                 ('Gy', C.c_double), ('Tr', C.c_double), ('aCS', C.c_double), ('Tc_CS', C.c_double),
-                ('d2v16_c', C.c_double), ('flux_scheme', C.c_int)]
+                ('d2v16_c', C.c_double), ('flux_scheme', C.c_int), ('wall_scheme', C.c_int)]
 
 
 class GridT(C.Structure):
@@ -145,12 +145,13 @@ def load(build_if_missing: bool = False):
 
 
 FLUX_SCHEMES = {'CD': 0, 'UW': 1}
+WALL_SCHEMES = {'BB': 0, 'NEE': 1}
 
 
 def make_case(model: str, precision: str = 'fp64', *, Mu0=0.1, M_Phi=0.1, W=5.0, Sigma=1e-2, RhoL=10.0,
-              RhoV=1.0, Gy=0.0, Tr=0.85, aCS=1.0, Tc_CS=0.0943, d2v16_c=1.2, scheme='CD') -> CaseT:
+              RhoV=1.0, Gy=0.0, Tr=0.85, aCS=1.0, Tc_CS=0.0943, d2v16_c=1.2, scheme='CD', wall='BB') -> CaseT:
     return CaseT(MODELS[model], PRECISION[precision], Mu0, M_Phi, W, Sigma, RhoL, RhoV, Gy, Tr, aCS, Tc_CS,
-                 d2v16_c, FLUX_SCHEMES[scheme])
+                 d2v16_c, FLUX_SCHEMES[scheme], WALL_SCHEMES[wall])
 
 
 class GpuCase:

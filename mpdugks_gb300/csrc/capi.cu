@@ -194,6 +194,7 @@ static size_t fp64_arena_bytes(const Params &P) {
     total += NFIELDS * cellb;                     // macro fields
     total += align256(4 * rowb);                  // ghost phi rows
     if (pp) total += 14 * cellb + 2 * Q * cellb;  // pseudopotential face state + face BhDt
+    if (P.nee) total += align256(sizeof(double) * 8 * Q * P.pitch);  // NEE wall-row equilibria/sources
     if (P.uw)                                     // UW cell gradients of f and h, low-side boundary fluxes
         total += 4 * Q * cellb + 2 * align256(sizeof(double) * Q * P.ny) + 2 * Q * rowb;
     total += cellb;                               // rho_last
@@ -492,6 +493,13 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
         return fail(nullptr, DUGKS_EINVAL, "the fused deviation-form step supports the Allen-Cahn models (AC, HCZ)");
     if (c->flux_scheme != DUGKS_FLUX_CD && c->flux_scheme != DUGKS_FLUX_UW)
         return fail(nullptr, DUGKS_EINVAL, "unknown flux scheme");
+    if (c->wall_scheme != DUGKS_WALL_BB && c->wall_scheme != DUGKS_WALL_NEE)
+        return fail(nullptr, DUGKS_EINVAL, "unknown wall scheme");
+    if (c->wall_scheme == DUGKS_WALL_NEE &&
+        (!(c->precision == DUGKS_FP64 || c->precision == DUGKS_FP64_FMA) ||
+         !(c->model == DUGKS_MODEL_AC || c->model == DUGKS_MODEL_HCZ)))
+        return fail(nullptr, DUGKS_EINVAL,
+                    "NEE walls run with DUGKS_FP64 / DUGKS_FP64_FMA and the Allen-Cahn models");
     if (c->flux_scheme == DUGKS_FLUX_UW &&
         (!(c->precision == DUGKS_FP64 || c->precision == DUGKS_FP64_FMA) ||
          !(c->model == DUGKS_MODEL_AC || c->model == DUGKS_MODEL_HCZ) || g->y_walls))
@@ -550,6 +558,7 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
         S.xbf = take(Q * cellb);
         S.ybf = take(Q * cellb);
     }
+    if (P.nee) S.weq = take(align256(sizeof(double) * 8 * Q * P.pitch));
     if (P.uw) {
         S.gfx = take(Q * cellb);
         S.gfy = take(Q * cellb);

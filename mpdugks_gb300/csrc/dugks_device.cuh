@@ -30,7 +30,7 @@ enum Field {
 // Ark/Constant/ZeroNamespace.h; all are derived on the host with the
 // reference's expressions (see host_params.cpp).
 struct Params {
-    int nx, ny, pitch, walls, model, gravity, Q, pad_;
+    int nx, ny, pitch, walls, model, gravity, Q, nee;  // nee: NEE wall faces (DUGKS_WALL_NEE)
     double R0, T0, RT, Lambda0, dt, hDt, Tau0, Kp, MinL, dx, dy, _2dx, _2dy;
     double aPhi, bPhi, Beta, Kappa, wI, PhiL, PhiV, RhoL, RhoV, Gy, NuL, NuV, TauMass;
     double h_aBP, h_bBP, h_cBP, h_ah, h_bh, h_ch;  // constant phase-field relaxation factors
@@ -61,6 +61,8 @@ struct State {
     // UW: fluxes of the periodic boundary faces as the reference's low-side faces (owner
     // inside at column 0 / row 0): x [Q][ny] (stride ny), y [Q][pitch] (stride pitch)
     double *xlo_f, *xlo_h, *ylo_f, *ylo_h;
+    // NEE walls: equilibria and sources of the wall rows, [4: fEq, fSo, hEq, hSo][2: bottom, top][Q][pitch]
+    double *weq;
     size_t qs, qsy;            // velocity strides of cell/x-face arrays and of y-face arrays
 };
 

@@ -257,6 +257,13 @@ __global__ void __launch_bounds__(256) k_collide(Params P, State S, int do_msrc,
             }
             const double hSo = (sx(xu, srcx) + sx(xv, srcy)) * w;
             const size_t o = (size_t)q * S.qs + c;
+            if (WALLS && P.nee && (j == 0 || j == P.ny - 1)) {  // kept for the NEE wall faces
+                const size_t wq = ((size_t)(j == 0 ? 0 : 1) * 9 + q) * pitch + i, ws = (size_t)2 * 9 * pitch;
+                S.weq[wq] = fEq;
+                S.weq[ws + wq] = fSo;
+                S.weq[2 * ws + wq] = hEq;
+                S.weq[3 * ws + wq] = hSo;
+            }
             S.bh[o] = P.h_aBP * S.h[o] + P.h_bBP * hEq + P.h_cBP * hSo;
             S.bf[o] = aBP * S.f[o] + bBP * fEq + cBP * fSo;
         }
@@ -534,6 +541,67 @@ __global__ void __launch_bounds__(256) k_faces_ac(Params P, State S) {
     }
 }
 
+// Wall_3_NEE (Ark/Cpp/Boundary.cpp:140-184) on the wall faces (y-face rows 0 and ny),
+// written over what k_faces_ac left there.  The face's U, V keep the initial 0 of
+// its MsQh (the routine never sets them); phi and rho are the owner's extrapolated
+// with its Phi_x/Phi_y (the phase-field source vector after MacroSource) and
+// Rho_x/Rho_y to the face (0.5 below / above the centre), p is the owner's;
+// Update_phi_Eqh at those moments (Ark/Lib/D2Q9AC.cpp:106-144,
+// Ark/Lib/D2Q9HCZ.cpp:93-131), plus the owner's non-equilibrium part
+// (Tilde - Eq + hDt So, Eq and So of this step's collision) times
+// 2 tau / (2 tau + dt); then Wall_3_BB.
+template <int MODEL>
+__global__ void __launch_bounds__(256) k_faces_nee(Params P, State S) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, side = blockIdx.y;
+    if (i >= P.nx) return;
+    const int ny = P.ny, pitch = P.pitch, jc = side ? ny - 1 : 0;
+    const size_t c = (size_t)jc * pitch + i;
+    const double dxw = 0.0, dyw = side ? 0.5 : -0.5;
+    const double Phi = S.fld[F_PHI][c] + S.fld[F_PHIX][c] * dxw + S.fld[F_PHIY][c] * dyw;
+    const double Rho = S.fld[F_RHO][c] + S.fld[F_RHOX][c] * dxw + S.fld[F_RHOY][c] * dyw;
+    const double p = S.fld[F_P][c], U = 0.0, V = 0.0;
+    const double uu = U * U + V * V;
+    const double tau = S.fld[F_TAU][c];
+    const double hNEq = 2.0 * P.TauMass / (2.0 * P.TauMass + P.dt);
+    const double fNEq = 2.0 * tau / (2.0 * tau + P.dt);
+    const size_t ws = (size_t)2 * 9 * pitch;
+    double hf[9], hh[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const double xu = d2q9_xu(q), xv = d2q9_xv(q), w = d2q9_w(q);
+        const double u1 = (xu * U + xv * V) / P.RT;
+        const double G = u1 + 0.5 * u1 * u1 - uu * P.Lambda0;
+        const double hEq = w * Phi * (1.0 + u1);
+        double fEq;
+        if (MODEL == AC) {
+            fEq = w * (p / P.RT + Rho * G);
+            if (q == 0) fEq = fEq - 1.0 * p / P.RT;
+        } else {
+            fEq = w * (p + Rho * P.RT * G);
+        }
+        const size_t wq = ((size_t)side * 9 + q) * pitch + i, o = (size_t)q * S.qs + c;
+        hh[q] = hEq + hNEq * (S.h[o] - S.weq[2 * ws + wq] + P.hDt * S.weq[3 * ws + wq]);
+        hf[q] = fEq + fNEq * (S.f[o] - S.weq[wq] + P.hDt * S.weq[ws + wq]);
+    }
+    // bounce-back of the directions entering the fluid (xi.n_out < 0)
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const int xv = d2q9_xv(q);
+        if (side ? xv < 0 : xv > 0) {
+            hh[q] = hh[d2q9_bb(q)];
+            hf[q] = hf[d2q9_bb(q)];
+        }
+    }
+    const int jf = side ? ny : 0;
+    const size_t cf = (size_t)jf * pitch + i;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const int xv = d2q9_xv(q);
+        S.yff[(size_t)q * S.qsy + cf] = sx(xv, hf[q]);
+        S.yfh[(size_t)q * S.qsy + cf] = sx(xv, hh[q]);
+    }
+}
+
 // Pseudopotential face pass 1: BhDt, face moments with the previous face
 // force, face pressure and psi (Ark/Lib/D2Q9PP.cpp:110-136, Ark/Cpp/PseudoP.cpp:23-30).
 template <int MODEL>
@@ -808,6 +876,10 @@ static void launch_step_t(const Params &P, const State &S, int do_msrc, int gin,
             const dim3 gf((P.nx + 31) / 32, (P.ny + 1 + 7) / 8, 2);
             k_faces_ac<MODEL, WALLS, false><<<gf, blk, 0, st>>>(P, S);
             *launches += 3;
+            if (WALLS && P.nee) {  // NEE wall faces over the bounce-back ones
+                k_faces_nee<MODEL><<<dim3((P.nx + 127) / 128, 2), 128, 0, st>>>(P, S);
+                *launches += 1;
+            }
         }
     } else {
         const dim3 gf((P.nx + 31) / 32, (P.ny + 7) / 8, 2);

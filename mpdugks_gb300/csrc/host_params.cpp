@@ -90,6 +90,7 @@ void derive_params(const dugks_case_t &cs, const dugks_grid_t &g, Params &P) {
         P.r_n2dx = 1.0 / (2 * (-P.dx));
     }
     P.uw = cs.flux_scheme == DUGKS_FLUX_UW ? 1 : 0;
+    P.nee = (cs.wall_scheme == DUGKS_WALL_NEE && g.y_walls) ? 1 : 0;
     P.T_CS = cs.Tr * cs.Tc_CS;
     P.aCS = cs.aCS;
     if (d2v16) {

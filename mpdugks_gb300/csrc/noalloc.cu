@@ -91,8 +91,9 @@ extern "C" int dugks_gpu_step_noalloc(const dugks_case_t *c, const dugks_grid_t 
         set_global_error("dugks_gpu_step_noalloc: precision must be DUGKS_FP64 or DUGKS_FP64_FMA");
         return DUGKS_EINVAL;
     }
-    if (c->flux_scheme != DUGKS_FLUX_CD) {
-        set_global_error("dugks_gpu_step_noalloc: the CD flux scheme only (UW needs gradient scratch)");
+    if (c->flux_scheme != DUGKS_FLUX_CD || (c->wall_scheme != DUGKS_WALL_BB && g->y_walls)) {
+        set_global_error("dugks_gpu_step_noalloc: the CD flux scheme and bounce-back walls only (UW and NEE "
+                         "need scratch)");
         return DUGKS_EINVAL;
     }
     if (g->nx < 3 || g->ny < 3 || nsteps < 0) {

@@ -162,8 +162,9 @@ extern "C" int dugks_slabs_create(const dugks_case_t *c, const dugks_grid_t *g, 
     if (!c || !g || !out) return fail("null argument");
     *out = nullptr;
     if (c->precision != DUGKS_FP32_DEV || !(c->model == DUGKS_MODEL_AC || c->model == DUGKS_MODEL_HCZ) ||
-        c->flux_scheme != DUGKS_FLUX_CD)
-        return fail("slab decomposition runs FP32-storage Allen-Cahn cases (AC, HCZ) with the CD flux scheme");
+        c->flux_scheme != DUGKS_FLUX_CD || (c->wall_scheme != DUGKS_WALL_BB && g->y_walls))
+        return fail("slab decomposition runs FP32-storage Allen-Cahn cases (AC, HCZ) with the CD flux scheme "
+                    "and bounce-back walls");
     if (g->nx < 3) return fail("nx must be >= 3");
     std::vector<int> row0, nrows, lo, hi;
     if (!plan(g->ny, g->y_walls, nparts, row0, nrows, lo, hi))

@@ -148,6 +148,11 @@ RunConfig config_from_case_ark(const CaseArk &ark) {
     if (fs == "CD") c.cs.flux_scheme = DUGKS_FLUX_CD;
     else if (fs == "UW") c.cs.flux_scheme = DUGKS_FLUX_UW;
     else throw std::runtime_error("Case.ark: unknown flux scheme '" + fs + "'");
+    // the wall treatment (_Wall_3_BCs_BB / _NEE of Ark/Constant/ZeroFlip.h; not in OutputCase)
+    const std::string ws = ark.get("wall scheme", "BB");
+    if (ws == "BB") c.cs.wall_scheme = DUGKS_WALL_BB;
+    else if (ws == "NEE") c.cs.wall_scheme = DUGKS_WALL_NEE;
+    else throw std::runtime_error("Case.ark: unknown wall scheme '" + ws + "'");
     c.mesh_type = ark.get("Mesh Type", "Car");
     c.nl = ark.get("NL", std::to_string(c.grid.nx));
     c.mach = ark.get("Mach", "0");

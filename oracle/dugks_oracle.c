@@ -57,6 +57,8 @@ struct orc_state {
     double *gfx, *gfy, *ghx, *ghy;
     double *Fxlo_f, *Fxlo_h;          /* [Q][ny] */
     double *Fylo_f, *Fylo_h;          /* [Q][nx] */
+    /* NEE walls: the cell equilibria and sources of the wall rows (bottom, top) [2][Q][nx] */
+    double *wEqf, *wSof, *wEqh, *wSoh;
     long step;
 };
 
@@ -231,6 +233,14 @@ orc_state *orc_create(const orc_inputs *in) {
     s->xpsi = xalloc(nc); s->ypsi = xalloc(ny1); s->xscg = xalloc(nc); s->yscg = xalloc(ny1);
     s->xrho = xalloc(nc); s->yrho = xalloc(ny1); s->xu = xalloc(nc); s->yu = xalloc(ny1);
     s->xv = xalloc(nc); s->yv = xalloc(ny1);
+    if (in->nee) {
+        if (!s->has_h || !in->y_walls) {
+            orc_destroy(s);
+            return NULL;
+        }
+        s->wEqf = xalloc((size_t)2 * Q * s->nx); s->wSof = xalloc((size_t)2 * Q * s->nx);
+        s->wEqh = xalloc((size_t)2 * Q * s->nx); s->wSoh = xalloc((size_t)2 * Q * s->nx);
+    }
     if (in->uw) {
         if (!s->has_h || in->y_walls) {  /* the reference's UW with walls reads unwritten shadow-cell gradients */
             orc_destroy(s);
@@ -334,7 +344,7 @@ void orc_destroy(orc_state *s) {
                       &s->bf, &s->bh, &s->Fxf, &s->Fxh, &s->Fyf, &s->Fyh, &s->xfFx, &s->xfFy, &s->yfFx,
                       &s->yfFy, &s->xpsi, &s->ypsi, &s->xscg, &s->yscg, &s->xrho, &s->yrho, &s->xu,
                       &s->yu, &s->xv, &s->yv, &s->gfx, &s->gfy, &s->ghx, &s->ghy, &s->Fxlo_f, &s->Fxlo_h,
-                      &s->Fylo_f, &s->Fylo_h};
+                      &s->Fylo_f, &s->Fylo_h, &s->wEqf, &s->wSof, &s->wEqh, &s->wSoh};
     for (size_t k = 0; k < sizeof all / sizeof all[0]; ++k) free(*all[k]);
     free(s);
 }
@@ -391,6 +401,13 @@ static void cell_barp(orc_state *s, int i, int j) {
                            GAMMA * s->RT * ((xu - U) * (Rho_x) + (xv - V) * (Rho_y)));
             }
             double hSo = ((Phi_x) * (xu) + (Phi_y) * xv) * w;
+            if (s->in.nee && (j == 0 || j == s->ny - 1)) { /* kept for Wall_3_NEE */
+                size_t o = ((size_t)(j == 0 ? 0 : 1) * Q + q) * s->nx + i;
+                s->wEqf[o] = fEq;
+                s->wSof[o] = fSo;
+                s->wEqh[o] = hEq;
+                s->wSoh[o] = hSo;
+            }
             BQ(s, s->bh, q, j, i) = s->h_aBP * DQ(s, s->h, q, j, i) + s->h_bBP * hEq + s->h_cBP * hSo;
             double b = aBP * DQ(s, s->f, q, j, i) + bBP * fEq;
             b += cBP * fSo;
@@ -563,6 +580,48 @@ static void face_flux_ac(const orc_state *s, const double *bhf, const double *bh
     }
 }
 
+/* Wall_3_NEE (Ark/Cpp/Boundary.cpp:140-184) on the wall face of column i; side 0 the
+ * bottom wall (owner (i,0), the face 0.5 below its centre), 1 the top wall (owner
+ * (i,ny-1)).  The face's U, V keep the initial value 0 of its MsQh (the routine never
+ * sets them); phi and rho are the owner's extrapolated with its Phi_x/Phi_y (the
+ * phase-field source vector after MacroSource) and Rho_x/Rho_y; p is the owner's;
+ * Update_phi_Eqh at those moments, the owner's non-equilibrium part
+ * (Tilde - Eq + hDt So) scaled by 2 tau / (2 tau + dt), then bounce-back. */
+static void face_nee(const orc_state *s, int i, int side, double *outf, double *outh) {
+    const int Q = s->Q, model = s->in.model, jc = side ? s->ny - 1 : 0;
+    size_t c = C(s, jc, i), e = E(s, jc, i);
+    double dxw = 0.0, dyw = side ? 0.5 : -0.5; /* face centre - cell centre */
+    double Phi = s->phi[e] + s->phix[e] * dxw + s->phiy[e] * dyw;
+    double Rho = s->rho[c] + s->rhox[e] * dxw + s->rhoy[e] * dyw;
+    double p = s->p[c], U = 0.0, V = 0.0;
+    double uu = U * U + V * V;
+    double hNEq = 2.0 * s->TauMass / (2.0 * s->TauMass + s->dt);
+    double fNEq = 2.0 * s->tauf[c] / (2.0 * s->tauf[c] + s->dt);
+    double hf[MAXQ], hh[MAXQ];
+    for (int q = 0; q < Q; ++q) {
+        double xu = s->xi_u[q], xv = s->xi_v[q], w = s->omega[q];
+        double u1 = (xu * U + xv * V) / s->RT;
+        double GAMMA = u1 + 0.5 * u1 * u1 - uu * s->Lambda0;
+        double hEq = w * Phi * (1.0 + u1);
+        double fEq = model == ORC_AC ? w * (p / s->RT + Rho * GAMMA) - (double)(!q) * p / s->RT
+                                     : w * (p + Rho * s->RT * GAMMA);
+        size_t o = ((size_t)side * Q + q) * s->nx + i;
+        hh[q] = hEq + hNEq * (DQ(s, s->h, q, jc, i) - s->wEqh[o] + s->hDt * s->wSoh[o]);
+        hf[q] = fEq + fNEq * (DQ(s, s->f, q, jc, i) - s->wEqf[o] + s->hDt * s->wSof[o]);
+    }
+    for (int q = 0; q < Q; ++q) { /* Wall_3_BB */
+        double xn = side ? s->xi_v[q] : -s->xi_v[q];
+        if (xn < 0) {
+            hh[q] = hh[s->bb[q]];
+            hf[q] = hf[s->bb[q]];
+        }
+    }
+    for (int q = 0; q < Q; ++q) {
+        outf[q] = hf[q] * s->xi_v[q];
+        outh[q] = hh[q] * s->xi_v[q];
+    }
+}
+
 /* ----------------------- pseudopotential faces -------------------- */
 static void face_pp_pass1(orc_state *s, const double *bhf, double prevFx, double prevFy,
                           double *rho, double *u, double *v, double *scg, double *psi) {
@@ -700,7 +759,8 @@ static void one_step(orc_state *s) {
                     face_bh(s, s->bh, 0, i, j, bh);
                 }
                 int wall = walls ? (j == 0 ? -1 : (j == ny ? 1 : 0)) : 0;
-                face_flux_ac(s, bf, bh, avg, 0, wall, of, oh);
+                if (wall && s->in.nee) face_nee(s, i, wall > 0, of, oh);
+                else face_flux_ac(s, bf, bh, avg, 0, wall, of, oh);
                 for (int q = 0; q < Q; ++q) {
                     YQ(s, s->Fyf, q, j, i) = of[q];
                     YQ(s, s->Fyh, q, j, i) = oh[q];

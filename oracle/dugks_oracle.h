@@ -33,6 +33,7 @@ typedef struct orc_inputs {
     uint64_t seed;
     double d2v16_c;                                        /* D2V16 lattice speed (1.2) */
     int uw;                                                /* 1: the UW flux scheme (Allen-Cahn, periodic) */
+    int nee;                                               /* 1: NEE walls instead of bounce-back */
 } orc_inputs;
 
 typedef struct orc_state orc_state;

@@ -25,7 +25,8 @@ class _Inputs(C.Structure):
                 ('RhoL', C.c_double), ('RhoV', C.c_double), ('Gy', C.c_double), ('radius', C.c_double),
                 ('Tr', C.c_double), ('aCS', C.c_double), ('Tc_CS', C.c_double), ('PP_RhoL', C.c_double),
                 ('PP_RhoV', C.c_double), ('PP_radius', C.c_double), ('noise_rho0', C.c_double),
-                ('noise_amp', C.c_double), ('seed', C.c_uint64), ('d2v16_c', C.c_double), ('uw', C.c_int)]
+                ('noise_amp', C.c_double), ('seed', C.c_uint64), ('d2v16_c', C.c_double), ('uw', C.c_int),
+                ('nee', C.c_int)]
 
 
 _lib = None
@@ -56,7 +57,7 @@ def lib():
 
 DEFAULTS = dict(Mu0=0.1, M_Phi=0.1, W=5.0, Sigma=1e-2, RhoL=10.0, RhoV=1.0, Gy=0.0, radius=-1.0,
                 Tr=0.85, aCS=1.0, Tc_CS=0.0943, PP_RhoL=2.4806e-1, PP_RhoV=4.5435e-2, PP_radius=-1.0,
-                noise_rho0=0.2, noise_amp=0.01, seed=12345, d2v16_c=1.2, uw=0)
+                noise_rho0=0.2, noise_amp=0.01, seed=12345, d2v16_c=1.2, uw=0, nee=0)
 
 
 class Oracle:
@@ -81,7 +82,7 @@ class Oracle:
     @classmethod
     def from_variant(cls, v: dict) -> 'Oracle':
         return cls(REF_MODEL[v['model']], v['nx'], v['ny'], v['walls'], v['init'], **v['consts'],
-                   uw=int(v.get('scheme', 'CD') == 'UW'))
+                   uw=int(v.get('scheme', 'CD') == 'UW'), nee=int(v.get('wall', 'BB') == 'NEE'))
 
     def __del__(self):
         h = getattr(self, '_h', None)

@@ -97,7 +97,8 @@ def gen_headers(name: str, v: dict, inc: Path) -> None:
         t = _sub(t, '#ifndef _ARK_ALLENCAHN_FLIP\n#define _ARK_ALLENCAHN_FLIP\n#endif', '', 'AC flip')
         extra.append('#define _ARK_PSEUDOPSI_FLIP')
     if v['walls']:
-        extra += ['#define _Wall_3_BCs_FLIP 3', '#define _Wall_3_BCs_BB']
+        extra += ['#define _Wall_3_BCs_FLIP 3',
+                  '#define _Wall_3_BCs_NEE' if v.get('wall') == 'NEE' else '#define _Wall_3_BCs_BB']
     if extra:
         idx = t.rfind('#endif')
         t = t[:idx] + '\n'.join(extra) + '\n' + t[idx:]

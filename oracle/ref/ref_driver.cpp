@@ -64,6 +64,7 @@ extern void OutputCase();
 extern void Output_Flowfield(double const &t, int step);
 extern void WallShadowC_fBP(Cell_2D &shadowCell);
 extern void Wall_3_BB(Face_2D &face);
+extern void Wall_3_NEE(Face_2D &face);
 extern void Grad_VS_6points(Cell_2D *center);
 
 
@@ -192,10 +193,16 @@ void run_step() {
 #endif
 #endif
 #ifdef _Wall_3_BCs_FLIP
+    // wall faces (Ark/Cpp/DUGKS2DSolver.cpp:230-250): NEE or bounce-back
 #pragma omp parallel for schedule(static)
     for (int n = 0; n < WallFaceNum; ++n) {
+#ifdef _Wall_3_BCs_NEE
+        Wall_3_NEE(*WallFaceA[n]);
+#endif
+#ifdef _Wall_3_BCs_BB
         Flux_2D(*WallFaceA[n]);
         Wall_3_BB(*WallFaceA[n]);
+#endif
     }
 #endif
 #pragma omp parallel for schedule(static)

@@ -53,4 +53,10 @@ VARIANTS = {
                      consts=dict(Mu0=0.01, W=4.0, Sigma=1e-3, RhoL=1.0, RhoV=0.1, radius=6.0)),
     'uw_hcz': dict(model='D2Q9HCZ', nx=32, ny=32, walls=False, init='ac_drop_inside', scheme='UW',
                    consts=dict(Mu0=0.02, W=4.0, Sigma=1e-2, RhoL=10.0, RhoV=1.0, radius=8.0)),
+    # Non-equilibrium extrapolation walls (_Wall_3_BCs_NEE, Ark/Cpp/Boundary.cpp:140-184)
+    # instead of bounce-back: the Rayleigh-Taylor box and a droplet between walls.
+    'nee_rt': dict(model='D2Q9HCZ', nx=16, ny=64, walls=True, init='ac_rt', wall='NEE',
+                   consts=dict(Mu0=0.01, M_Phi=0.05, W=4.0, Sigma=1e-4, RhoL=3.0, RhoV=1.0, Gy=1e-4)),
+    'nee_ac': dict(model='D2Q9AC', nx=24, ny=24, walls=True, init='ac_drop_inside', wall='NEE',
+                   consts=dict(Mu0=0.01, W=4.0, Sigma=1e-3, RhoL=1.0, RhoV=0.1, radius=6.0)),
 }

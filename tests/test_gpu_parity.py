@@ -20,7 +20,7 @@ pytestmark = pytest.mark.gpu
 
 TOL = 1e-12
 UV_ABS = 1e-13
-SMALL = ['ac_small', 'hcz_drop', 'hcz_rt', 'pp_drop', 'uw_small', 'uw_hcz']
+SMALL = ['ac_small', 'hcz_drop', 'hcz_rt', 'pp_drop', 'uw_small', 'uw_hcz', 'nee_rt', 'nee_ac']
 PRECISIONS = ['fp64', 'fp64fma']
 MODEL = {'D2Q9AC': 'AC', 'D2Q9HCZ': 'HCZ', 'D2Q9PP': 'PP9'}
 CASE_KEYS = ('Mu0', 'M_Phi', 'W', 'Sigma', 'RhoL', 'RhoV', 'Gy', 'Tr', 'aCS', 'Tc_CS')
@@ -30,8 +30,8 @@ def gpu_from_variant(v, precision='fp64'):
     from mpdugks_gb300 import capi
     c = v['consts']
     kw = {k: c[k] for k in CASE_KEYS if k in c}
-    gc = capi.GpuCase(capi.make_case(MODEL[v['model']], precision, scheme=v.get('scheme', 'CD'), **kw), v['nx'],
-                      v['ny'], v['walls'])
+    gc = capi.GpuCase(capi.make_case(MODEL[v['model']], precision, scheme=v.get('scheme', 'CD'),
+                                     wall=v.get('wall', 'BB'), **kw), v['nx'], v['ny'], v['walls'])
     if v['init'] in ('ac_drop', 'ac_drop_inside'):
         gc.init(v['init'], [c.get('radius', -1.0)])
     elif v['init'] == 'scmp_drop':
@@ -83,7 +83,7 @@ def test_init_matches_reference(golden, name):
 # after ~150 steps (a 1e-14 perturbation of one distribution grows to 5e-7 in
 # one jump in the CPU restatement), so only the bit-exact variant can follow
 # that case to 300 steps; the FMA variant is checked on it for 100 steps.
-FMA_FLIPS = {'hcz_rt'}
+FMA_FLIPS = {'hcz_rt', 'nee_rt'}
 
 
 @pytest.mark.parametrize('precision', PRECISIONS)
