@@ -380,7 +380,7 @@ def pseudopotential_bench(steps: int = 100) -> dict:
         'fp32_error_vs_fp64': {'steps': steps + 3, 'fields': errs},
         'note': 'the restated D2V16 model diverges within a few hundred steps in FP64 as well at every '
                 'tested setting (including T = 0.7 Tc with a = 0.5 and rho = rho_c), so the comparison '
-                'covers the first 103 steps',
+                f'covers the first {steps + 3} steps',
     }
 
 
