@@ -384,6 +384,36 @@ def pseudopotential_bench(steps: int = 100) -> dict:
     }
 
 
+# ---------------------------------------------------------------- scheme variants
+
+def scheme_variants_bench(steps: int = 20) -> dict:
+    """The reference's alternative face reconstruction (UW) and wall treatment (NEE)
+    on the plain FP64 path, beside the defaults (CD, bounce-back) on the same grid:
+    a 1024x1024 periodic HCZ droplet (CD / UW) and the 512x2048 Rayleigh-Taylor box
+    with walls (BB / NEE); MLUPS over `steps` steps after 3 warm-up steps."""
+    import torch
+    from mpdugks_gb300 import capi
+    st = torch.cuda.Stream()
+    out = {}
+    drop = dict(Mu0=0.02, M_Phi=0.02, W=4.0, Sigma=1e-3, RhoL=10.0, RhoV=1.0)
+    rt = WORKLOADS['rt512x2048']
+    runs = [('cd', 'HCZ', drop, 1024, 1024, False, 'ac_drop_inside', [200.0], {}),
+            ('uw', 'HCZ', drop, 1024, 1024, False, 'ac_drop_inside', [200.0], dict(scheme='UW')),
+            ('bb', 'HCZ', case_kw(rt), rt['nx'], rt['ny'], True, 'ac_rt', rt['init'], {}),
+            ('nee', 'HCZ', case_kw(rt), rt['nx'], rt['ny'], True, 'ac_rt', rt['init'], dict(wall='NEE'))]
+    for tag, model, kw, nx, ny, walls, init, params, extra in runs:
+        g = capi.GpuCase(capi.make_case(model, 'fp64', **kw, **extra), nx, ny, walls)
+        g.init(init, params)
+        g.step(3, st.cuda_stream)
+        ms, launches, _ = timed_steps(g, steps, st)
+        out[tag] = {'grid': f'{nx}x{ny}', 'mlups': round(nx * ny * steps / (ms * 1e-3) / 1e6, 2),
+                    'ms_per_step': round(ms / steps, 4), 'launches_per_step': launches // steps}
+        del g
+    return {'precision': 'fp64 (reference-exact rounding)', 'steps': steps,
+            'droplet_1024x1024': {'cd': out['cd'], 'uw': out['uw']},
+            'rayleigh_taylor_512x2048': {'bounce_back': out['bb'], 'nee': out['nee']}}
+
+
 # ---------------------------------------------------------------- GPU arms
 
 def field_errors(a, b):
@@ -558,6 +588,9 @@ def run_ours(args, wl, rank, world, local):
     pseudo = None
     if rank == 0 and not args.no_pseudopotential:
         pseudo = pseudopotential_bench(args.pp_steps)
+    variants = None
+    if rank == 0 and not args.no_fp64:
+        variants = scheme_variants_bench()
 
     if rank == 0:
         cpu = None
@@ -581,6 +614,7 @@ def run_ours(args, wl, rank, world, local):
                            'reductions, download 5 fields'},
             'serving': serving,
             'pseudopotential_d2v16': pseudo,
+            'fp64_scheme_variants': variants,
             'gpu_launches': int(launches),
             'clocks': clocks,
             'state_finite': finite,

@@ -59,4 +59,7 @@ VARIANTS = {
                    consts=dict(Mu0=0.01, M_Phi=0.05, W=4.0, Sigma=1e-4, RhoL=3.0, RhoV=1.0, Gy=1e-4)),
     'nee_ac': dict(model='D2Q9AC', nx=24, ny=24, walls=True, init='ac_drop_inside', wall='NEE',
                    consts=dict(Mu0=0.01, W=4.0, Sigma=1e-3, RhoL=1.0, RhoV=0.1, radius=6.0)),
+    # ac_ff with the UW flux scheme: golden Case.ark ("UW = Flux Scheme") and FlowField files
+    'uw_ff': dict(model='D2Q9AC', nx=32, ny=24, walls=False, init='ac_drop', scheme='UW',
+                  consts=dict(Mu0=0.02, W=4.0, Sigma=1e-3, RhoL=1.0, RhoV=0.1, radius=7.0)),
 }

@@ -3,8 +3,9 @@
 OutputCase (Ark/Cpp/Output.cpp:65-141) and Output_Flowfield
 (Ark/Cpp/Output.cpp:541-606) run inside the reference driver
 (oracle/ref/ref_driver.cpp, with REF_FLOWFIELD set) for a few steps of two
-small cases: the reference's AC_Drop init on a 32x24 periodic grid (ac_ff)
-and a 16x64 Rayleigh-Taylor box with walls (hcz_rt).  The files land in
+small cases: the reference's AC_Drop init on a 32x24 periodic grid (ac_ff, and
+uw_ff with the UW flux scheme) and a 16x64 Rayleigh-Taylor box with walls
+(hcz_rt, and nee_rt with NEE walls).  The files land in
 tests/golden/flowfield/<case>/ (FlowField .dat files gzip-compressed).
 Needs the reference sources, so it runs only where they are present:
 
@@ -20,11 +21,13 @@ sys.path.insert(0, str(ROOT / 'oracle' / 'ref'))
 
 import build_ref  # noqa: E402
 
-STEPS = {'ac_ff': 20, 'hcz_rt': 20}
+STEPS = {'ac_ff': 20, 'hcz_rt': 20, 'uw_ff': 20, 'nee_rt': 20}
 
 
-def main() -> None:
+def main(names=None) -> None:
     for name, steps in STEPS.items():
+        if names and name not in names:
+            continue
         build_ref.build(name)
         vdir = build_ref.OUT / name
         ff = vdir / 'FlowField'
@@ -42,4 +45,4 @@ def main() -> None:
 
 
 if __name__ == '__main__':
-    main()
+    main(sys.argv[1:] or None)

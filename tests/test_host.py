@@ -10,7 +10,7 @@ import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
 GOLD = ROOT / 'tests' / 'golden' / 'flowfield'
-CASES = ['ac_ff', 'hcz_rt']
+CASES = ['ac_ff', 'hcz_rt', 'uw_ff', 'nee_rt']
 
 
 def runner() -> Path:
@@ -63,6 +63,9 @@ def test_case_ark_decodes_the_reference_constants():
     assert kv['init'] == '0' and float(kv['param']) == 7.0
     assert float(kv['Mu0']) == 0.02 and float(kv['Sigma']) == 1e-3 and float(kv['RhoV']) == 0.1
     assert kv['flux'] == '0'  # "CD = Flux Scheme"
+    out = subprocess.run([runner(), 'show-config', GOLD / 'uw_ff' / 'Case.ark'], check=True, capture_output=True,
+                         text=True).stdout.split()
+    assert dict(zip(out[0::2], out[1::2]))['flux'] == '1'  # "UW = Flux Scheme"
     # the Rayleigh-Taylor box: walls from the mesh name; no case name, so an init entry is required
     r = subprocess.run([runner(), 'show-config', GOLD / 'hcz_rt' / 'Case.ark'], capture_output=True, text=True)
     assert r.returncode == 1 and "give an 'init' entry" in r.stderr
@@ -88,7 +91,10 @@ def test_flowfield_sections_hold_the_reference_fields_in_cell_order():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize('case,extra', [('ac_ff', []),
-                                        ('hcz_rt', ['--set', 'init=ac_rt', '--set', 'gravity=0.0001'])])
+                                        ('hcz_rt', ['--set', 'init=ac_rt', '--set', 'gravity=0.0001']),
+                                        ('uw_ff', []),
+                                        ('nee_rt', ['--set', 'init=ac_rt', '--set', 'gravity=0.0001',
+                                                    '--set', 'wall scheme=NEE'])])
 def test_driver_output_equals_the_reference_files(case, extra, tmp_path):
     """dugks_run on the reference's Case.ark, plain FP64 path: Case.ark and the
     FlowField files at steps 0 and 20 are byte-identical to the reference's."""
