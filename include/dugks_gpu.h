@@ -182,6 +182,21 @@ int64_t dugks_gpu_launch_count(const dugks_handle_t *h);
 
 int dugks_gpu_destroy(dugks_handle_t *h);
 
+/* Checkpoint / restart (no reference counterpart: its FlowField files hold the
+ * macroscopic fields only, Ark/Cpp/Output.cpp:537-606, so a reference run
+ * cannot restart).  dugks_gpu_checkpoint writes the handle's whole device state
+ * (distributions, macroscopic and auxiliary fields, ping-pong orientation,
+ * step counter and the constants an upload derives) into buf, which must hold
+ * dugks_gpu_checkpoint_bytes(h) bytes; it synchronises the handle's stream.
+ * dugks_gpu_restore loads such a buffer into a handle created with the same
+ * case and grid (DUGKS_EINVAL otherwise); the handle then continues bit for bit
+ * as the saved one would have. */
+int dugks_gpu_checkpoint_bytes(const dugks_handle_t *h, size_t *bytes);
+/* Steps done since the upload (after a restore: since the saved run's upload). */
+int dugks_gpu_step_count(const dugks_handle_t *h, int64_t *steps);
+int dugks_gpu_checkpoint(dugks_handle_t *h, void *buf, size_t len);
+int dugks_gpu_restore(dugks_handle_t *h, const void *buf, size_t len);
+
 /* No counterpart in the reference.  For callers that must not allocate
  * device memory themselves or through this library -- a host that hands out
  * a fixed memory budget or its own pool, a plugin running inside another

@@ -93,6 +93,10 @@ SIGNATURES = {
     'dugks_gpu_last_error': (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     'dugks_gpu_launch_count': (C.c_int64, [C.c_void_p]),
     'dugks_gpu_destroy': (C.c_int, [C.c_void_p]),
+    'dugks_gpu_checkpoint_bytes': (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t)]),
+    'dugks_gpu_step_count': (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    'dugks_gpu_checkpoint': (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    'dugks_gpu_restore': (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     'dugks_gpu_step_noalloc': (C.c_int, [C.POINTER(CaseT), C.POINTER(GridT), C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.c_int, C.c_void_p]),
     'dugks_srv_create': (C.c_int, [C.POINTER(SrvConfigT), C.POINTER(C.c_void_p)]),
@@ -228,6 +232,18 @@ class GpuCase:
         out = np.empty((self.Q, self.ny, self.nx), dtype=np.float64)
         self._check(self.lib.dugks_gpu_get_dist(self.h, 0 if which == 'f' else 1, out.ctypes.data))
         return out
+
+    def checkpoint(self) -> np.ndarray:
+        """The whole device state as a byte array (dugks_gpu_checkpoint)."""
+        n = C.c_size_t()
+        self._check(self.lib.dugks_gpu_checkpoint_bytes(self.h, C.byref(n)))
+        buf = np.empty(n.value, dtype=np.uint8)
+        self._check(self.lib.dugks_gpu_checkpoint(self.h, buf.ctypes.data, n.value))
+        return buf
+
+    def restore(self, buf: np.ndarray) -> None:
+        buf = np.ascontiguousarray(buf, dtype=np.uint8)
+        self._check(self.lib.dugks_gpu_restore(self.h, buf.ctypes.data, buf.nbytes))
 
     def check_finite(self) -> int:
         return self.lib.dugks_gpu_check_finite(self.h)

@@ -945,6 +945,97 @@ extern "C" int dugks_gpu_last_error(const dugks_handle_t *h, char *buf, size_t l
 
 extern "C" int64_t dugks_gpu_launch_count(const dugks_handle_t *h) { return h ? h->launches : 0; }
 
+// ---- checkpoint / restart
+namespace {
+struct CkptHeader {
+    char magic[8];
+    uint32_t version, header_bytes;
+    dugks_case_t cs;
+    dugks_grid_t grid;
+    int32_t pad0;
+    uint64_t arena_bytes;
+    int64_t steps;
+    int32_t pending, gcur, first, pp_pending, orient, pad1;
+    f32::PPP ppc;
+};
+const char CKPT_MAGIC[8] = {'D', 'U', 'G', 'K', 'S', 'C', 'K', '1'};
+
+// orientation of the fused path's ping-pong views: 0 as created, 1 swapped
+int fused_orient(const dugks_handle *h) {
+    if (!h->fp32) return 0;
+    const void *df = h->fused64 ? static_cast<const void *>(h->S64f.df) : static_cast<const void *>(h->S32.df);
+    return df == static_cast<const void *>(h->arena) ? 0 : 1;
+}
+}  // namespace
+
+extern "C" int dugks_gpu_checkpoint_bytes(const dugks_handle_t *h, size_t *bytes) {
+    if (!h || !bytes) return DUGKS_EINVAL;
+    *bytes = sizeof(CkptHeader) + h->arena_bytes;
+    return DUGKS_OK;
+}
+
+extern "C" int dugks_gpu_step_count(const dugks_handle_t *h, int64_t *steps) {
+    if (!h || !steps) return DUGKS_EINVAL;
+    *steps = h->steps;
+    return DUGKS_OK;
+}
+
+extern "C" int dugks_gpu_checkpoint(dugks_handle_t *h, void *buf, size_t len) {
+    if (!h || !buf) return fail(h, DUGKS_EINVAL, "null argument");
+    if (len < sizeof(CkptHeader) + h->arena_bytes) return fail(h, DUGKS_EINVAL, "checkpoint buffer too small");
+    int rc = sync_last(h);
+    if (rc) return rc;
+    CkptHeader hd{};
+    std::memcpy(hd.magic, CKPT_MAGIC, sizeof hd.magic);
+    hd.version = 1;
+    hd.header_bytes = sizeof(CkptHeader);
+    hd.cs = h->cs;
+    hd.grid = h->grid;
+    hd.arena_bytes = h->arena_bytes;
+    hd.steps = h->steps;
+    hd.pending = h->pending;
+    hd.gcur = h->gcur;
+    hd.first = h->first;
+    hd.pp_pending = h->pp_pending;
+    hd.orient = fused_orient(h);
+    hd.ppc = h->PPc;
+    std::memcpy(buf, &hd, sizeof hd);
+    cudaError_t e = cudaMemcpy(static_cast<char *>(buf) + sizeof hd, h->arena, h->arena_bytes, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(h, e, "checkpoint copy");
+    return DUGKS_OK;
+}
+
+extern "C" int dugks_gpu_restore(dugks_handle_t *h, const void *buf, size_t len) {
+    if (!h || !buf) return fail(h, DUGKS_EINVAL, "null argument");
+    CkptHeader hd;
+    if (len < sizeof hd) return fail(h, DUGKS_EINVAL, "checkpoint buffer too small");
+    std::memcpy(&hd, buf, sizeof hd);
+    if (std::memcmp(hd.magic, CKPT_MAGIC, sizeof hd.magic) != 0 || hd.version != 1 ||
+        hd.header_bytes != sizeof(CkptHeader))
+        return fail(h, DUGKS_EINVAL, "not a checkpoint of this library version");
+    if (std::memcmp(&hd.cs, &h->cs, sizeof hd.cs) != 0 || std::memcmp(&hd.grid, &h->grid, sizeof hd.grid) != 0 ||
+        hd.arena_bytes != h->arena_bytes)
+        return fail(h, DUGKS_EINVAL, "checkpoint of a different case or grid");
+    if (len < sizeof hd + hd.arena_bytes) return fail(h, DUGKS_EINVAL, "truncated checkpoint");
+    int rc = sync_last(h);
+    if (rc) return rc;
+    cudaError_t e =
+        cudaMemcpy(h->arena, static_cast<const char *>(buf) + sizeof hd, h->arena_bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(h, e, "restore copy");
+    h->steps = hd.steps;
+    h->pending = hd.pending;
+    h->gcur = hd.gcur;
+    h->first = hd.first;
+    h->pp_pending = hd.pp_pending;
+    if (h->pp32) h->PPc = hd.ppc;
+    if (fused_orient(h) != hd.orient) {
+        if (h->fused64) f32::swap_io(h->S64f);
+        else f32::swap_io(h->S32);
+    }
+    h->macros_fresh = false;
+    return DUGKS_OK;
+}
+
 extern "C" int dugks_gpu_destroy(dugks_handle_t *h) {
     if (!h) return DUGKS_OK;
     cudaStreamSynchronize(h->last_stream);

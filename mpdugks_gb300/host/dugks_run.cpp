@@ -3,7 +3,8 @@
 // (Ark/Cpp/main.cpp:134, Ark/Cpp/DUGKS2DSolver.cpp:148-337).
 //
 //   dugks_run run <Case.ark> [--out DIR] [--precision P] [--steps N]
-//                 [--mesh FILE.cas] [--set key=value ...]
+//                 [--mesh FILE.cas] [--checkpoint FILE] [--resume FILE]
+//                 [--set key=value ...]
 //       Reads the case from a Case.ark (the reference's OutputCase layout),
 //       initialises it on the GPU, writes DIR/Case.ark and the FlowField at
 //       step 0, then steps until End_Step (or --steps) or until the density
@@ -12,6 +13,9 @@
 //       (DIR/global/, the reference's names and layout).  With --mesh the
 //       grid comes from a .cas mesh file, as in the reference's
 //       MeshConstruct, and the FlowField cells follow the mesh's cell order.
+//       --checkpoint writes the whole GPU state (dugks_gpu_checkpoint) to FILE
+//       at every FlowField output point and at the end; --resume restores
+//       such a file after the initialisation and continues from its step.
 //   dugks_run rewrite-ark <in> <out>        parse a Case.ark and write it back
 //   dugks_run rewrite-flowfield <in> <out>  parse a FlowField file and write it back
 //   dugks_run mesh-info <FILE.cas>          nx ny y_walls, then the grid
@@ -69,10 +73,39 @@ void output(dugks_handle_t *h, const RunConfig &c, const CartesianMap *mesh, con
     write_flowfield(path, fields(h, c, mesh));
 }
 
+// the whole GPU state to a file (written to FILE.tmp, then renamed)
+void checkpoint_file(dugks_handle_t *h, const std::string &path) {
+    size_t n = 0;
+    check(h, dugks_gpu_checkpoint_bytes(h, &n), "checkpoint size");
+    std::vector<char> buf(n);
+    check(h, dugks_gpu_checkpoint(h, buf.data(), n), "checkpoint");
+    const std::string tmp = path + ".tmp";
+    std::FILE *f = std::fopen(tmp.c_str(), "wb");
+    if (!f) throw std::runtime_error("cannot write " + tmp);
+    const size_t w = std::fwrite(buf.data(), 1, n, f);
+    if (std::fclose(f) != 0 || w != n) throw std::runtime_error("write failed: " + tmp);
+    if (std::rename(tmp.c_str(), path.c_str()) != 0) throw std::runtime_error("cannot rename " + tmp);
+}
+
+// restore a checkpoint file; returns its step
+int64_t restore_file(dugks_handle_t *h, const std::string &path) {
+    std::FILE *f = std::fopen(path.c_str(), "rb");
+    if (!f) throw std::runtime_error("cannot open " + path);
+    std::vector<char> buf;
+    char chunk[1 << 16];
+    size_t r;
+    while ((r = std::fread(chunk, 1, sizeof chunk, f)) > 0) buf.insert(buf.end(), chunk, chunk + r);
+    std::fclose(f);
+    check(h, dugks_gpu_restore(h, buf.data(), buf.size()), "restore");
+    int64_t steps = 0;
+    check(h, dugks_gpu_step_count(h, &steps), "step count");
+    return steps;
+}
+
 int run(int argc, char **argv) {
     if (argc < 3) throw std::runtime_error("run: missing Case.ark");
     CaseArk ark = read_case_ark(argv[2]);
-    std::string out = "FlowField", mesh_file;
+    std::string out = "FlowField", mesh_file, ckpt_file, resume_file;
     int64_t steps_override = -1;
     for (int k = 3; k < argc; ++k) {
         const std::string a = argv[k];
@@ -84,6 +117,8 @@ int run(int argc, char **argv) {
         else if (a == "--precision") ark.set("precision", next());
         else if (a == "--steps") steps_override = std::atoll(next().c_str());
         else if (a == "--mesh") mesh_file = next();
+        else if (a == "--checkpoint") ckpt_file = next();
+        else if (a == "--resume") resume_file = next();
         else if (a == "--set") {
             const std::string kv = next();
             const size_t eq = kv.find('=');
@@ -112,10 +147,15 @@ int run(int argc, char **argv) {
         check(h, dugks_gpu_init(h, c.init_kind, c.init_params.empty() ? nullptr : c.init_params.data(),
                                 (int)c.init_params.size(), c.seed),
               "init");
-        output(h, c, pm, out, 0);
+        int64_t step = 0;
+        if (!resume_file.empty()) {
+            step = restore_file(h, resume_file);
+            std::printf("resumed from %s at step %lld\n", resume_file.c_str(), (long long)step);
+        } else {
+            output(h, c, pm, out, 0);
+        }
         std::printf("iteration start    cells : %d x %d    steps : %lld\n", c.grid.nx, c.grid.ny,
                     (long long)c.end_step);
-        int64_t step = 0;
         double residual = 1.0;
         while (step < c.end_step && residual > c.residual_stop) {
             // up to the next residual / output point
@@ -133,9 +173,13 @@ int run(int argc, char **argv) {
                             r.residual);
                 std::fflush(stdout);
             }
-            if (step % c.write_every == 0 && step < c.end_step) output(h, c, pm, out, step);
+            if (step % c.write_every == 0 && step < c.end_step) {
+                output(h, c, pm, out, step);
+                if (!ckpt_file.empty()) checkpoint_file(h, ckpt_file);
+            }
         }
         output(h, c, pm, out, step);
+        if (!ckpt_file.empty()) checkpoint_file(h, ckpt_file);
         std::printf("iteration End    step : %lld\n", (long long)step);
     } catch (...) {
         dugks_gpu_destroy(h);
@@ -177,7 +221,7 @@ int main(int argc, char **argv) {
         }
         std::fprintf(stderr,
                      "usage: dugks_run run <Case.ark> [--out DIR] [--precision P] [--steps N] [--mesh F.cas]\n"
-                     "                     [--set k=v]...\n"
+                     "                     [--checkpoint FILE] [--resume FILE] [--set k=v]...\n"
                      "       dugks_run rewrite-ark <in> <out>\n"
                      "       dugks_run rewrite-flowfield <in> <out>\n"
                      "       dugks_run show-config <Case.ark>\n"
