@@ -30,6 +30,7 @@ DUGKS_DECLARE_FP64(exact)
 DUGKS_DECLARE_FP64(fast)
 }  // namespace dugks
 #include "fp32_state.cuh"
+#include "trace.hpp"
 namespace dugks {
 namespace f32 {
 cudaError_t launch_step32(const P32 &P, const S32 &S, int first, int gin, int gout, cudaStream_t st,
@@ -641,6 +642,7 @@ extern "C" int dugks_gpu_upload(dugks_handle_t *h, const double *f, const double
 }
 
 extern "C" int dugks_gpu_init(dugks_handle_t *h, int kind, const double *params, int nparams, uint64_t seed) {
+    dugks::TraceRange trace("dugks_gpu_init");
     if (!h) return fail(nullptr, DUGKS_EINVAL, "null handle");
     std::vector<double> f, hd, aux;
     int rc = host_init_state(h->P, h->iM, kind, params, nparams, seed, f, hd, aux);
@@ -650,6 +652,7 @@ extern "C" int dugks_gpu_init(dugks_handle_t *h, int kind, const double *params,
 }
 
 extern "C" int dugks_gpu_step(dugks_handle_t *h, int nsteps, void *stream) {
+    dugks::TraceRange trace("dugks_gpu_step");
     if (!h) return fail(nullptr, DUGKS_EINVAL, "null handle");
     if (nsteps < 0) return fail(h, DUGKS_EINVAL, "nsteps < 0");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -761,6 +764,7 @@ static int finalize(dugks_handle *h) {
 }
 
 extern "C" int dugks_gpu_reduce(dugks_handle_t *h, dugks_reductions_t *r) {
+    dugks::TraceRange trace("dugks_gpu_reduce");
     if (!h || !r) return fail(h, DUGKS_EINVAL, "null argument");
     const bool hasH = (h->P.model == AC || h->P.model == HCZ);
     if (h->fp32) {
@@ -897,6 +901,7 @@ extern "C" int dugks_gpu_get_dist(dugks_handle_t *h, int which, double *out) {
 }
 
 extern "C" int dugks_gpu_download(dugks_handle_t *h, double *rho, double *u, double *v, double *phi, double *p) {
+    dugks::TraceRange trace("dugks_gpu_download");
     if (!h) return fail(nullptr, DUGKS_EINVAL, "null handle");
     double *dst[5] = {rho, u, v, phi, p};
     const int fid[5] = {F_RHO, F_U, F_V, F_PHI, F_P};
@@ -981,6 +986,7 @@ extern "C" int dugks_gpu_step_count(const dugks_handle_t *h, int64_t *steps) {
 }
 
 extern "C" int dugks_gpu_checkpoint(dugks_handle_t *h, void *buf, size_t len) {
+    dugks::TraceRange trace("dugks_gpu_checkpoint");
     if (!h || !buf) return fail(h, DUGKS_EINVAL, "null argument");
     if (len < sizeof(CkptHeader) + h->arena_bytes) return fail(h, DUGKS_EINVAL, "checkpoint buffer too small");
     int rc = sync_last(h);
@@ -1006,6 +1012,7 @@ extern "C" int dugks_gpu_checkpoint(dugks_handle_t *h, void *buf, size_t len) {
 }
 
 extern "C" int dugks_gpu_restore(dugks_handle_t *h, const void *buf, size_t len) {
+    dugks::TraceRange trace("dugks_gpu_restore");
     if (!h || !buf) return fail(h, DUGKS_EINVAL, "null argument");
     CkptHeader hd;
     if (len < sizeof hd) return fail(h, DUGKS_EINVAL, "checkpoint buffer too small");

@@ -45,6 +45,7 @@
 #include "../host/flowfield.hpp"
 #include "dugks_device.cuh"
 #include "fp32_state.cuh"
+#include "trace.hpp"
 
 namespace dugks {
 namespace f32 {
@@ -268,6 +269,7 @@ void writer_loop(dugks_srv *s) {
         const size_t n = (size_t)c->grid.nx * c->grid.ny;
         std::string why;
         try {
+            TraceRange trace("srv FlowField write");
             dugks_host::FlowField ff;
             ff.cells = n;
             const double *b = j.buf.p;
@@ -632,8 +634,12 @@ void batch_loop(dugks_srv *s) {
             gi = (int)s->graphs.size() - 1;
         }
         const auto t_chunk = Clock::now();
-        cudaError_t e = cudaGraphLaunch(s->graphs[gi].exec, s->s_batch);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s->s_batch);
+        cudaError_t e;
+        {
+            TraceRange trace("srv batch chunk");
+            e = cudaGraphLaunch(s->graphs[gi].exec, s->s_batch);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->s_batch);
+        }
         {
             std::lock_guard<std::mutex> lk(s->mu);
             s->st.chunks += 1;
@@ -698,8 +704,11 @@ void solo_loop(dugks_srv *s, int lane) {
             const int64_t stop = next_stop(*c, c->steps_done);
             if (c->steps_done < stop) {
                 const int n = (int)std::min<int64_t>(s->chunk, stop - c->steps_done);
-                rc = dugks_gpu_step(c->h, n, st);
-                if (rc == DUGKS_OK && cudaStreamSynchronize(st) != cudaSuccess) rc = DUGKS_ECUDA;
+                {
+                    TraceRange trace("srv solo chunk");
+                    rc = dugks_gpu_step(c->h, n, st);
+                    if (rc == DUGKS_OK && cudaStreamSynchronize(st) != cudaSuccess) rc = DUGKS_ECUDA;
+                }
                 if (rc) break;
                 {
                     std::lock_guard<std::mutex> lk(s->mu);

@@ -25,6 +25,7 @@
 #include "../../include/dugks_gpu.h"
 #include "dugks_device.cuh"
 #include "fp32_state.cuh"
+#include "trace.hpp"
 
 namespace dugks {
 void derive_params(const dugks_case_t &cs, const dugks_grid_t &g, Params &P);
@@ -281,6 +282,7 @@ extern "C" int dugks_slabs_init(dugks_slabs_t *s, int kind, const double *params
 }
 
 extern "C" int dugks_slabs_step(dugks_slabs_t *s, int nsteps) {
+    dugks::TraceRange trace("dugks_slabs_step");
     if (!s || nsteps < 0) return fail("bad argument");
     for (int k = 0; k < nsteps; ++k) {
         const uint32_t sn = (uint32_t)s->steps;
