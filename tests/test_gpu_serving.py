@@ -127,6 +127,8 @@ def test_cancel_and_oversized_submit():
 @pytest.mark.parametrize('item', [
     (lambda: ac_case(), 560, 3300, False, 'ac_drop_inside', [200.0], 37),
     (lambda: rt_case(), 560, 3300, True, 'ac_rt', [3.0, 0.1, 1e-4], 41),
+    # ragged: a last strip of 25 columns, a last segment of 27 rows
+    (lambda: rt_case(), 1117, 1531, True, 'ac_rt', [0.7, 0.1, 1e-4], 23),
 ])
 def test_streaming_kernel_equals_the_tile_kernel(item):
     """Single-case FP32 steps on a grid of more strip segments than resident warps
