@@ -1047,6 +1047,21 @@ double orc_const(const orc_state *s, const char *name) {
     return NAN;
 }
 
+int orc_velocities(const orc_state *s, double *xi_u, double *xi_v, double *xi2) {
+    for (int q = 0; q < s->Q; ++q) {
+        xi_u[q] = s->xi_u[q];
+        xi_v[q] = s->xi_v[q];
+        xi2[q] = s->xi2[q];
+    }
+    return s->Q;
+}
+
+int orc_d2v16_equilibrium(const orc_state *s, double rho, double u, double v, double *eq) {
+    if (s->in.model != ORC_PP16) return -1;
+    orc_d2v16_eq(s, rho, u, v, eq);
+    return 0;
+}
+
 void orc_sums(const orc_state *s, double *sum_rho, double *sum_phi) {
     double a = 0, b = 0;
     for (int j = 0; j < s->ny; ++j)

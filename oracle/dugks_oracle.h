@@ -52,6 +52,10 @@ int orc_set(orc_state *s, const char *name, const double *in);
 double orc_const(const orc_state *s, const char *name);
 /* sums in cell order j-major: sum rho, sum phi */
 void orc_sums(const orc_state *s, double *sum_rho, double *sum_phi);
+/* the model's discrete velocities and |xi|^2 + eta^2 (D2V16: eta^2 on the first four) */
+int orc_velocities(const orc_state *s, double *xi_u, double *xi_v, double *xi2);
+/* D2V16 equilibrium (Macro16 x inverse moment matrix) at (rho, u, v); -1 for other models */
+int orc_d2v16_equilibrium(const orc_state *s, double rho, double u, double v, double *eq);
 
 #ifdef __cplusplus
 }

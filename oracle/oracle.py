@@ -51,6 +51,10 @@ def lib():
         L.orc_sums.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.orc_steps_done.argtypes = [C.c_void_p]
         L.orc_steps_done.restype = C.c_long
+        L.orc_velocities.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_velocities.restype = C.c_int
+        L.orc_d2v16_equilibrium.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_void_p]
+        L.orc_d2v16_equilibrium.restype = C.c_int
         _lib = L
     return _lib
 
@@ -96,6 +100,18 @@ class Oracle:
     @property
     def steps_done(self) -> int:
         return lib().orc_steps_done(self._h)
+
+    def velocities(self):
+        """(xi_u, xi_v, |xi|^2 + eta^2) of the model's discrete velocities."""
+        a = [np.empty(self.Q) for _ in range(3)]
+        lib().orc_velocities(self._h, *[x.ctypes.data for x in a])
+        return tuple(a)
+
+    def d2v16_equilibrium(self, rho: float, u: float, v: float) -> np.ndarray:
+        eq = np.empty(16)
+        if lib().orc_d2v16_equilibrium(self._h, rho, u, v, eq.ctypes.data) != 0:
+            raise ValueError('not a D2V16 model')
+        return eq
 
     def get(self, name: str) -> np.ndarray:
         out = np.empty((self.ny, self.nx), dtype=np.float64)
