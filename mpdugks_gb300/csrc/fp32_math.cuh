@@ -153,27 +153,47 @@ __device__ __forceinline__ T sym8p(const T *a) {
     return add2(add2(add2(a[1], a[5]), add2(a[3], a[7])), add2(add2(a[2], a[6]), add2(a[4], a[8])));
 }
 
-// Stochastic rounding of the pair a + b into storage.  The exact sum is
-// s + err (two-sum); each lane moves to its neighbour toward err with
-// probability |err| / spacing, drawn from 16 random bits.  Without it a state
-// that is nearly steady repeats the same FP32 rounding every step and the
-// error grows linearly with the step count; with it the rounding errors are
-// unbiased and uncorrelated (random-walk growth).
-__device__ __forceinline__ float sr_lane(float s, float err, uint32_t bits16) {
-    if (err == 0.f) return s;
-    // neighbour of s toward err (s != 0 here: a + b == 0 is exact)
-    const int away = ((err > 0.f) == (s > 0.f)) ? 1 : -1;
-    const float nb = __int_as_float(__float_as_int(s) + away);
-    const float u = __int_as_float(0x3F800000u | (bits16 << 7)) - 1.0f;  // [0, 1)
-    return (u * fabsf(nb - s) < fabsf(err)) ? nb : s;
+// Stochastic rounding into storage.  The exact sum a + b is s + err (two-sum,
+// |err| <= ulp(s)/2); it is rounded to the neighbour of s toward err with
+// probability |err| / ulp(s) and to s otherwise, so the expected stored value is
+// the exact sum.  Without it a state that is nearly steady repeats the same FP32
+// rounding every step and the error grows linearly with the step count; with it
+// the rounding errors are unbiased and uncorrelated (random-walk growth).
+// Branch-free form (dithered rounding): RN(s + (err + d)) with d uniform on one
+// ulp of s, centred on zero, rounds up past s + ulp/2 with probability err/ulp
+// (err > 0; likewise down).  d = (u - c) ulp(s): u = 1 + k/2^16 from 16 random bits
+// and c = 1.5 - 2^-17, so d takes the 2^16 values ((k + 1/2)/2^16 - 1/2) ulp,
+// symmetric about zero; ulp(s) = 2^-23 times the power of two of s's exponent
+// field (0 for zero and subnormal s, which round to nearest).  Where s is exactly a
+// power of two the spacing below it is half an ulp and the rounding there is off
+// (a value in 2^23).
+constexpr float SR_K23 = 1.1920928955078125e-07f;                  // 2^-23
+constexpr float SR_CK23 = 1.1920928955078125e-07f * 1.5f - 9.094947017729282e-13f;  // (1.5 - 2^-17) 2^-23
+__device__ __forceinline__ float sr_expo(float s) { return __uint_as_float(__float_as_uint(s) & 0x7F800000u); }
+// Random bits of one stored value: the top 16 bits of the cell's hash times an odd
+// multiplier of its own (a bijection whose top bits depend on every bit of the
+// hash); f_q takes SR_KEY[q], h_q SR_KEY[16 + q].
+__device__ constexpr uint32_t SR_KEY[32] = {
+    0x80FC0BC5U, 0x50DC981BU, 0x948370BDU, 0x6F00BBEFU, 0x6921FE53U, 0xACF1E17FU, 0x529BE043U, 0xD424EA1FU,
+    0x4410E049U, 0x3DF351F1U, 0x79059AD3U, 0xC9E412E1U, 0x3D12F7E1U, 0xB72B606FU, 0xCAA9EBCFU, 0xED92F735U,
+    0x2BA2AE99U, 0x9E7EEAA5U, 0x2B6A852DU, 0xB2A328A7U, 0x6C59C00FU, 0x8140B75FU, 0xABCF5FADU, 0x69A981B9U,
+    0x4BE2AC07U, 0xEB7B9DAFU, 0xF51F1E29U, 0x21348DABU, 0x4606377DU, 0xC35C9E73U, 0x31187EB1U, 0xCE316DA3U};
+// u = 1 + k/2^16 from the top 16 bits of a 32-bit word
+__device__ __forceinline__ float sr_unit(uint32_t bits) { return __uint_as_float(0x3F800000u | ((bits >> 9) & 0x7FFF80u)); }
+__device__ __forceinline__ float sr_round(float s, float err, uint32_t bits) {
+    const float u = sr_unit(bits);
+    const float w = __fmaf_rn(u, SR_K23, -SR_CK23);
+    return __fadd_rn(s, __fmaf_rn(w, sr_expo(s), err));
 }
-__device__ __forceinline__ float2 add_sr2(float2 a, float2 b, uint32_t bits) {
+__device__ __forceinline__ float2 add_sr2(float2 a, float2 b, uint32_t bits_f, uint32_t bits_h) {
     const float2 s = add2(a, b);
     const float2 bb = sub2(s, a);
     const float2 err = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
-    return make_float2(sr_lane(s.x, err.x, bits & 0xFFFFu), sr_lane(s.y, err.y, bits >> 16));
+    const float2 u = make_float2(sr_unit(bits_f), sr_unit(bits_h));
+    const float2 w = fma2(u, mk2(SR_K23, SR_K23), mk2(-SR_CK23, -SR_CK23));
+    return add2(s, fma2(w, mk2(sr_expo(s.x), sr_expo(s.y)), err));
 }
-__device__ __forceinline__ double2 add_sr2(double2 a, double2 b, uint32_t) { return add2(a, b); }
+__device__ __forceinline__ double2 add_sr2(double2 a, double2 b, uint32_t, uint32_t) { return add2(a, b); }
 
 __device__ __forceinline__ float rcp(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
@@ -487,7 +507,7 @@ __device__ __forceinline__ void update_cell(const PR<R> &P, const typename Pair<
         else if (ys >= 0) s = sub2(FS[ys], FN[ys]);
         // old value plus one small increment, rounded stochastically into storage
         const T incr = (xs >= 0 || ys >= 0) ? fma2(dtv, s, fma2(btp, inc[q], inc[q])) : fma2(btp, inc[q], inc[q]);
-        dn[q] = add_sr2(Pq[q], incr, h0 * (2u * q + 1u) + (uint32_t)q * 0x632BE5ABU);
+        dn[q] = add_sr2(Pq[q], incr, h0 * SR_KEY[q], h0 * SR_KEY[16 + q]);
     }
 }
 

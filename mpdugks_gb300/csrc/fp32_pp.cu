@@ -150,11 +150,11 @@ __device__ __forceinline__ void cs_psi(const PPP &P, FF rho, FF p, float &scg, f
 }
 __device__ __forceinline__ double ff_to_double(FF a) { return (double)a.hi + (double)a.lo; }
 
-__device__ __forceinline__ float sr1(float a, float b, uint32_t bits16) {
+__device__ __forceinline__ float sr1(float a, float b, uint32_t bits) {
     const float s = a + b;
     const float bb = s - a;
     const float err = (a - (s - bb)) + (b - bb);
-    return sr_lane(s, err, bits16);
+    return sr_round(s, err, bits);
 }
 
 // 8-neighbour isotropic gradient of a periodic field (Ark/Lib/GradSchemeBasic.h:153-208)
@@ -318,8 +318,7 @@ __global__ void __launch_bounds__(256) k_pp32_update(PPP P, PPS S, uint32_t step
         s += S.xfl[o + c];
         s += S.yfl[o + c];
         const float d = S.df[o + c];
-        const uint32_t bits = h0 * (2u * q + 1u) + (uint32_t)q * 0x632BE5ABU;
-        const float dn = sr1(d, P.aTP * (S.bf[o + c] - d) + P.dtV * s, bits & 0xFFFFu);
+        const float dn = sr1(d, P.aTP * (S.bf[o + c] - d) + P.dtV * s, h0 * SR_KEY[q]);
         S.df[o + c] = dn;
         ff_acc(sR, dn);
         ff_acc_prod(su, dn, P.xi_u[q]);
