@@ -3,6 +3,7 @@
 // Host side of the drop-in: derives the case constants with the reference's
 // header formulas, allocates the resident device state, runs the reference's
 // initialisation functions on the host, and drives the step kernels.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -42,7 +43,8 @@ cudaError_t launch_step64f(const PR<double> &P, const SR<double> &S, int first, 
 void launch_macros64f(const PR<double> &P, const SR<double> &S, double *rho, double *u, double *v, double *p,
                       double *phi, int opitch, cudaStream_t st, int64_t *launches);
 cudaError_t launch_stream32(const P32 &P, const S32 &S, int first, int gin, int gout, cudaStream_t st,
-                            int64_t *launches, uint32_t step);
+                            int64_t *launches, uint32_t step, const void *tmap, int zin, int *err);
+cudaError_t stream_tensor_map(void *map_out, float *base, int nx, int ny, int pitch, size_t qs);
 cudaError_t launch_pp32_step(const PPP &P, const PPS &S, int do_msrc, cudaStream_t st, int64_t *launches,
                              uint32_t step);
 cudaError_t launch_pp32_force(const PPP &P, const PPS &S, cudaStream_t st, int64_t *launches);
@@ -106,6 +108,12 @@ struct dugks_handle {
     f32::PR<double> P64f{};
     f32::SR<double> S64f{};
     int first = 1;            // next step is the first after an upload
+    // TMA staging of the streaming FP32 step: a tensor map over both state copies
+    // (from tmap_base, the arena's first plane) and the error word of its staged loads
+    CUtensorMap tmap{};
+    bool has_tmap = false;
+    const float *tmap_base = nullptr;
+    int *kerr = nullptr;
     bool macros_fresh = false;
     double *out3 = nullptr;   // tau, Fx, Fy for output (allocated on first request)
     // FP32 storage of the pseudopotential models
@@ -416,7 +424,16 @@ static int create_fp32(dugks_handle *h, dugks_handle_t **out) {
         h->fused64 = true;
         return create_fused<double>(h, out, h->P64f, h->S64f);
     }
-    return create_fused<float>(h, out, h->P32, h->S32);
+    int rc = create_fused<float>(h, out, h->P32, h->S32);
+    if (rc) return rc;
+    // the streaming step's stage loads go through TMA where a tensor map can describe
+    // the state (any grid of at least 32 columns); otherwise they are per-lane copies
+    h->kerr = h->flag + 32;  // a spare word of the zeroed 256-byte flag block
+    if (f32::stream_tensor_map(&h->tmap, h->S32.df, h->P.nx, h->P.ny, h->P.pitch, h->S32.qs) == cudaSuccess) {
+        h->has_tmap = true;
+        h->tmap_base = h->S32.df;
+    }
+    return DUGKS_OK;
 }
 
 // FP64 [Q][ny][nx] state -> deviations and first-step planes on the device.
@@ -477,6 +494,16 @@ static int macros_fp32(dugks_handle *h) {
     if (e != cudaSuccess) return cuda_fail(h, e, "macros launch");
     h->macros_fresh = true;
     return DUGKS_OK;
+}
+
+// the streaming step's staged loads all completed (read after a synchronisation of
+// the handle's stream); DUGKS_ETIMEOUT once one did not
+static int stage_loads_ok(dugks_handle *h) {
+    if (!h->kerr) return DUGKS_OK;
+    int v = 0;
+    cudaError_t e = cudaMemcpy(&v, h->kerr, sizeof v, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(h, e, "stage-load status");
+    return v ? fail(h, DUGKS_ETIMEOUT, "a TMA stage load of the streaming step did not complete") : DUGKS_OK;
 }
 
 extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, dugks_handle_t **out) {
@@ -681,7 +708,8 @@ extern "C" int dugks_gpu_step(dugks_handle_t *h, int nsteps, void *stream) {
             cudaError_t e = h->fused64 ? f32::launch_stepX(h->P64f, h->S64f, h->first, h->gcur, h->gcur ^ 1, st,
                                                            &h->launches, sn)
                                        : f32::launch_stream32(h->P32, h->S32, h->first, h->gcur, h->gcur ^ 1, st,
-                                                              &h->launches, sn);
+                                                              &h->launches, sn, h->has_tmap ? &h->tmap : nullptr,
+                                                              h->S32.df == h->tmap_base ? 0 : 24, h->kerr);
             if (e != cudaSuccess) return cuda_fail(h, e, "fp32 step launch");
             if (h->fused64) f32::swap_io(h->S64f);
             else f32::swap_io(h->S32);
@@ -777,6 +805,7 @@ extern "C" int dugks_gpu_reduce(dugks_handle_t *h, dugks_reductions_t *r) {
     cudaError_t e = cudaMemcpyAsync(o, h->out4, sizeof o, cudaMemcpyDeviceToHost, h->last_stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->last_stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "reduce");
+    if (int rc = stage_loads_ok(h)) return rc;
     r->sum_rho = o[0];
     r->sum_phi = o[1];
     r->residual = std::sqrt(o[2] / (o[3] + 1.0E-30));
@@ -938,6 +967,7 @@ extern "C" int dugks_gpu_check_finite(dugks_handle_t *h) {
     cudaError_t e = cudaMemcpyAsync(&flag, h->flag, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(h, e, "check_finite");
+    if (int rc = stage_loads_ok(h)) return rc;
     return flag ? fail(h, DUGKS_ENAN, "non-finite value in the state") : DUGKS_OK;
 }
 

@@ -404,7 +404,6 @@ __device__ __forceinline__ void face_flux(const PR<R> &P, FO &&O, FN &&N, FD &&D
                                           typename Pair<R>::T (&F)[6]) {
     using T = typename Pair<R>::T;
     const T half = mk2(R(0.5), R(0.5));
-    const T hdt = mk2(P.hDt, P.hDt);
     T bh[9];
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
@@ -416,22 +415,23 @@ __device__ __forceinline__ void face_flux(const PR<R> &P, FO &&O, FN &&N, FD &&D
             bh[q] = avg;
             continue;
         }
-        // xi.grad as the sum of the normal part (o - n)/(-d) and the tangential
-        // central difference averaged over the two cells of the face
-        T g = mk2(R(0.), R(0.));
-        bool have = false;
+        // avg - hDt xi.grad: the normal part (o - n)/(-d) is folded into the two
+        // cells' weights 1/2 -+ hDt sn/(-d) (0.25 and 0.75 on unit cells, exact),
+        // the tangential central difference, averaged over the two cells of the
+        // face, enters with the weight -hDt st/(4 d_t)
+        T b = avg;
         if (sn != 0) {
             const R rn = XF ? P.r_ndx : P.r_ndy;
-            g = mul2(sub2(o, n), mk2(sn * rn, sn * rn));
-            have = true;
+            const R cn = P.hDt * ((R)sn * rn);
+            b = fma2(n, mk2(R(0.5) + cn, R(0.5) + cn), mul2(o, mk2(R(0.5) - cn, R(0.5) - cn)));
         }
         if (st != 0) {
             const T d = D(q);
             const R rt = XF ? P.r_2dy : P.r_n2dx;
-            const R k = R(0.5) * (R)st * rt;
-            g = have ? fma2(d, mk2(k, k), g) : mul2(d, mk2(k, k));
+            const R k = -(P.hDt * (R(0.5) * (R)st * rt));
+            b = fma2(d, mk2(k, k), b);
         }
-        bh[q] = sub2(avg, mul2(hdt, g));
+        bh[q] = b;
     }
     // face moments (sum f, sum h) with the mirror-symmetric association
     const T z = add2(mk2(MODEL == AC ? R(0.) : bh[0].x, bh[0].y), sym8p(bh));

@@ -24,9 +24,11 @@
 // back, as in the tile kernel.  The per-cell arithmetic is the tile kernel's
 // (fp32_math.cuh) with the same random bits, so the two kernels give
 // bit-identical results.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 
 #include "dugks_device.cuh"
 #include "fp32_math.cuh"
@@ -39,38 +41,144 @@ constexpr int SW = 28;   // interior columns of a strip
 constexpr int SEG_MAX = 128;  // rows of a segment: 128, 64 or 32 (enough segments per warp)
 constexpr int WPB = 2;   // warps per block
 constexpr int NSTG = 4;  // stage ring: rows k .. k+3
-constexpr int NPL = 18;  // staged planes per row: f and h deviations (aux is read directly)
-// per-warp shared memory (floats): stage ring [NSTG][18][32], f-bar-plus ring
-// [3][9][32] pairs, averaged-field ring [3][6][32]
-constexpr int STG_F = NSTG * NPL * 32;
-constexpr int BR_F = 3 * 9 * 32 * 2;
-constexpr int AR_F = 3 * 6 * 32;
+// per-warp shared memory, in floats:
+//   stage ring [NSTG][18][32]: the raw deviation planes (9 f, then 9 h) of rows
+//     k .. k+3, 32 columns each -- the box one TMA load writes;
+//   f-bar-plus ring, per row slot: [4][32] float4 holding the pairs of directions
+//     (1,2), (3,4), (5,6), (7,8), then [32] float2 holding direction 0;
+//   averaged-field ring, per row slot: [32] float4 (srcx, srcy, rhox, rhoy), then
+//     [32] float2 (fx, fy).
+// 8- and 16-byte entries make one shared-memory instruction move two or four values.
+// After the warps' regions: 4 mbarriers per warp (one per stage slot).
+constexpr int STG_SLOT = 18 * 32;    // floats per stage slot
+constexpr int STG_F = NSTG * STG_SLOT;
+constexpr int BR_SLOT = 9 * 32 * 2;  // floats per row slot of the f-bar-plus ring
+constexpr int BR_F = 3 * BR_SLOT;
+constexpr int AR_SLOT = 6 * 32;      // floats per row slot of the averaged-field ring
+constexpr int AR_F = 3 * AR_SLOT;
 constexpr int WARP_F = STG_F + BR_F + AR_F;
-constexpr size_t STREAM_SMEM = (size_t)WPB * WARP_F * sizeof(float);
+constexpr size_t STREAM_SMEM = (size_t)WPB * WARP_F * sizeof(float) + (size_t)WPB * NSTG * 8;
+static_assert((STG_SLOT * 4) % 128 == 0 && (WARP_F * 4) % 128 == 0, "TMA destinations are 128-byte aligned");
+static_assert((BR_SLOT * 4) % 16 == 0 && (AR_SLOT * 4) % 16 == 0, "16-byte aligned ring slots");
+constexpr unsigned STG_TX_BYTES = STG_SLOT * 4;   // bytes one TMA row load delivers
+constexpr int TMA_WAIT_LIMIT = 1 << 22;           // try_wait polls before a staged load is given up
 
 __device__ __forceinline__ int m3(int j) { return (j + 6) % 3; }  // j >= -6
 __device__ __forceinline__ int m4(int j) { return (j + 8) & 3; }  // j >= -8
 __device__ __forceinline__ int wrap_any(int j, int n) { return ((j % n) + n) % n; }
 
-template <int MODEL, bool WALLS>
+// ---- TMA row loads completed through an mbarrier (inline PTX)
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait for the phase of the given parity; true when it completed
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+    for (int it = 0; it < TMA_WAIT_LIMIT; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// one box {32 columns, 1 row, 18 planes} at (x, y, z) of a 3-D tensor map into shared memory
+__device__ __forceinline__ void tma_load_row(unsigned dst, const CUtensorMap *map, int x, int y, int z, unsigned bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::
+            "r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
+// one row slot of the f-bar-plus ring (see above); l is a lane (column of the strip)
+struct BRow {
+    float *base;
+    __device__ __forceinline__ float4 *quad() const { return reinterpret_cast<float4 *>(base); }
+    __device__ __forceinline__ float2 *rest() const { return reinterpret_cast<float2 *>(base + 4 * 32 * 4); }
+    __device__ __forceinline__ float2 get(int q, int l) const {
+        if (q == 0) return rest()[l];
+        const float4 v = quad()[((q - 1) >> 1) * 32 + l];
+        return ((q - 1) & 1) ? make_float2(v.z, v.w) : make_float2(v.x, v.y);
+    }
+    __device__ __forceinline__ void put(const float2 (&b)[9], int l) const {
+#pragma unroll
+        for (int g = 0; g < 4; ++g)
+            quad()[g * 32 + l] = make_float4(b[2 * g + 1].x, b[2 * g + 1].y, b[2 * g + 2].x, b[2 * g + 2].y);
+        rest()[l] = b[0];
+    }
+};
+// one row slot of the averaged-field ring: {srcx, srcy, rhox, rhoy, fx, fy}
+struct ARow {
+    float *base;
+    __device__ __forceinline__ float4 *quad() const { return reinterpret_cast<float4 *>(base); }
+    __device__ __forceinline__ float2 *pair() const { return reinterpret_cast<float2 *>(base + 32 * 4); }
+    __device__ __forceinline__ void get(float (&a)[6], int l) const {
+        const float4 v = quad()[l];
+        const float2 w = pair()[l];
+        a[0] = v.x, a[1] = v.y, a[2] = v.z, a[3] = v.w, a[4] = w.x, a[5] = w.y;
+    }
+    __device__ __forceinline__ void put(const float (&a)[6], int l) const {
+        quad()[l] = make_float4(a[0], a[1], a[2], a[3]);
+        pair()[l] = make_float2(a[4], a[5]);
+    }
+};
+
+// first: the first step after an initialisation (the collision takes the state the
+// initialisation left instead of the macroscopic quantities of the deviations).  A
+// runtime flag, as in the tile kernels, so that both compile the per-cell stages alike
+// (the same multiply-add contractions) and give bit-identical results.
+// TMA: the stage ring is filled by TMA row loads from `tmap`, a 3-D map (columns,
+// rows, planes) over both state copies, the copy a step reads starting at plane
+// zin; strips whose window wraps around the periodic x boundary, and slab
+// partitions, load per lane with cp.async.  A load not complete within
+// TMA_WAIT_LIMIT polls sets *err and ends the warp.
+template <int MODEL, bool WALLS, bool TMA>
 __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, int gin, int gout, uint32_t step,
-                                                       int nstrips, int nsegs, int seg_rows) {
+                                                       int nstrips, int nsegs, int seg_rows,
+                                                       const __grid_constant__ CUtensorMap tmap, int zin, int *err) {
     using T = float2;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     float *wbase = reinterpret_cast<float *>(smem_raw) + (size_t)wib * WARP_F;
-    float *stg = wbase;                                   // [NSTG][NPL][32]
-    T *bring = reinterpret_cast<T *>(wbase + STG_F);      // [3][9][32]
-    float *aring = wbase + STG_F + BR_F;                  // [3][6][32]
-    auto STG = [&](int slot, int p) -> float & { return stg[(slot * NPL + p) * 32 + lane]; };
+    float *stg = wbase;                                   // [NSTG][18][32]
+    float *bring = wbase + STG_F;                         // [3] row slots
+    float *aring = wbase + STG_F + BR_F;                  // [3] row slots
+    auto STG = [&](int slot, int q) -> T {
+        return mk2(stg[slot * STG_SLOT + q * 32 + lane], stg[slot * STG_SLOT + (9 + q) * 32 + lane]);
+    };
+    // mbarriers of this warp's stage slots; their phase parities (bit s: slot s)
+    const unsigned bar0 = smem_u32(smem_raw + (size_t)WPB * WARP_F * sizeof(float) + (size_t)wib * NSTG * 8);
+    const bool tma_ok = TMA && (smem_u32(smem_raw) & 127u) == 0 && !(P.halo_lo || P.halo_hi);
+    uint32_t phases = 0;
+    if (TMA) {
+        if (lane == 0) {
+#pragma unroll
+            for (int s = 0; s < NSTG; ++s) mbar_init(bar0 + 8 * s);
+            asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        }
+        __syncwarp();
+    }
 
     const int nx = P.nx, ny = P.ny, pitch = P.pitch;
     const int gw = blockIdx.x * WPB + wib, nw = gridDim.x * WPB;
     for (int item = gw; item < nstrips * nsegs; item += nw) {
         const int strip = item % nstrips, seg = item / nstrips;
-        const int x0 = strip * SW, w = min(SW, nx - x0);
+        // the strip's window is columns hs .. hs+31 (a multiple of 4: 16-byte TMA
+        // coordinates); its interior columns x0 .. x0+w-1 run over 2 .. nx+1, the
+        // last strip's wrapping around the periodic x boundary
+        const int hs = strip * SW, x0 = hs + 2, w = min(SW, nx + 2 - x0);
         const int y0 = seg * seg_rows, y1 = min(y0 + seg_rows, ny);
-        const int gi = wrap_any(x0 - 2 + lane, nx);
+        const int gi = wrap_any(hs + lane, nx);
+        const bool use_tma = tma_ok && hs + 32 <= nx;
         const bool interior = lane >= 2 && lane < 2 + w;
         const bool colL = lane >= 1 && lane <= 2 + w;  // lanes whose f-bar-plus is needed
         const bool xfL = lane >= 2 && lane <= 2 + w;   // lanes whose west x-face is needed
@@ -81,23 +189,35 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
         auto row_ok = [&](int j) {
             return WALLS ? ((j >= 0 || (hlo && j >= -SLAB_HALO)) && (j < ny || (hhi && j < ny + SLAB_HALO))) : true;
         };
+        auto row_of = [&](int j) { return WALLS ? j : (j < 0 ? j + ny : (j >= ny ? j - ny : j)); };
         auto cell = [&](int j) -> long long {  // signed: halo rows lie below row 0
-            const int jj = WALLS ? j : (j < 0 ? j + ny : (j >= ny ? j - ny : j));
-            return (long long)jj * pitch + gi;
+            return (long long)row_of(j) * pitch + gi;
         };
         // wall sides (no halo)
         const bool wlo = WALLS && !hlo, whi = WALLS && !hhi;
+        auto loaded = [&](int j) { return j <= y1 + 1 && row_ok(j); };
         auto prefetch = [&](int j) {
-            if (j <= y1 + 1 && row_ok(j)) {
-                const long long c = cell(j);
-                float *d = stg + m4(j) * NPL * 32 + lane;
+            if (loaded(j)) {
+                if (use_tma) {
+                    if (lane == 0) {
+                        const unsigned bar = bar0 + 8 * m4(j);
+                        // the slot's previous row was read by every lane (generic proxy)
+                        // before this warp's last __syncwarp
+                        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                        mbar_expect_tx(bar, STG_TX_BYTES);
+                        tma_load_row(smem_u32(stg + m4(j) * STG_SLOT), &tmap, hs, row_of(j), zin, bar);
+                    }
+                } else {
+                    const long long c = cell(j);
+                    float *d = stg + m4(j) * STG_SLOT + lane;
 #pragma unroll
-                for (int q = 0; q < 9; ++q) {
-                    cp_async(d + q * 32, S.df + (size_t)q * S.qs + c);
-                    cp_async(d + (9 + q) * 32, S.dh + (size_t)q * S.qs + c);
+                    for (int q = 0; q < 9; ++q) {
+                        cp_async(d + q * 32, S.df + (size_t)q * S.qs + c);
+                        cp_async(d + (9 + q) * 32, S.dh + (size_t)q * S.qs + c);
+                    }
                 }
             }
-            cp_async_commit();
+            if (!use_tma) cp_async_commit();
         };
         __syncwarp();  // the previous item is done with this warp's buffers
         prefetch(y0 - 2);
@@ -114,9 +234,8 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
         for (int s = 0; s < 6; ++s) FS[s] = mk2(0.f, 0.f);
         for (int k = y0 - 4; k < y1; ++k) {
             // this row's ring slots: f-bar-plus and averaged fields of rows k-1, k, k+1
-            T *const Bm = bring + m3(k - 1) * 288, *const B0 = bring + m3(k) * 288, *const Bp = bring + m3(k + 1) * 288;
-            float *const Am = aring + m3(k - 1) * 192, *const A0 = aring + m3(k) * 192,
-                         *const Ap = aring + m3(k + 1) * 192;
+            const BRow Bm{bring + m3(k - 1) * BR_SLOT}, B0{bring + m3(k) * BR_SLOT}, Bp{bring + m3(k + 1) * BR_SLOT};
+            const ARow Am{aring + m3(k - 1) * AR_SLOT}, A0{aring + m3(k) * AR_SLOT}, Ap{aring + m3(k + 1) * AR_SLOT};
             // aux of row k+2, read directly one row ahead of its collision
             const bool coll = k + 1 >= y0 - 1 && row_ok(k + 1) && colL;
             float a6n[A_N];
@@ -125,7 +244,21 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
 #pragma unroll
                 for (int a = 0; a < A_N; ++a) a6n[a] = __ldg(S.aux + (size_t)a * S.qs + c2);
             }
-            cp_async_wait_all();
+            // row k+2's raw deviations (issued one row ago) have landed
+            if (use_tma) {
+                if (loaded(k + 2)) {
+                    const int s = m4(k + 2);
+                    const bool ok = __all_sync(0xffffffffu, mbar_wait(bar0 + 8 * s, (phases >> s) & 1u));
+                    if (!ok) {
+                        if (lane == 0 && err) atomicExch(err, 1);
+                        mbar_wait(bar0 + 8 * s, (phases >> s) & 1u);  // the copy in flight, once more
+                        return;
+                    }
+                    phases ^= 1u << s;
+                }
+            } else {
+                cp_async_wait_all();
+            }
             __syncwarp();
             // ---- phi of row k+2
             float sfz2 = 0.f, dph2 = 0.f;
@@ -135,9 +268,9 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
                 if (row_ok(j)) {
                     const int sl = m4(j);
                     T za[9];
-                    za[0] = mk2(MODEL == AC ? 0.f : STG(sl, 0), STG(sl, 9));
 #pragma unroll
-                    for (int q = 1; q < 9; ++q) za[q] = mk2(STG(sl, q), STG(sl, 9 + q));
+                    for (int q = 0; q < 9; ++q) za[q] = STG(sl, q);
+                    if (MODEL == AC) za[0].x = 0.f;
                     const T z = ff_sum9(za);
                     sfz2 = z.x;
                     dph2 = z.y;
@@ -164,15 +297,16 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
                     const int sl = m4(j);
                     T Pq[9];
 #pragma unroll
-                    for (int q = 0; q < 9; ++q) Pq[q] = mk2(STG(sl, q), STG(sl, 9 + q));
+                    for (int q = 0; q < 9; ++q) Pq[q] = STG(sl, q);
                     const float ph[8] = {E, W, ph2, ph0, NE, NW, SE, SWv};
                     const long long c = cell(j);
                     float src[6], phi, U, V;
                     collide_cell<MODEL, float>(P, S, c, first, Pq, sfz1, dph1, a6c, ph, inc_nx, src, phi, U, V);
+                    T bp[9];
 #pragma unroll
-                    for (int q = 0; q < 9; ++q) Bp[q * 32 + lane] = add2(Pq[q], inc_nx[q]);
-#pragma unroll
-                    for (int a = 0; a < 6; ++a) Ap[a * 32 + lane] = src[a];
+                    for (int q = 0; q < 9; ++q) bp[q] = add2(Pq[q], inc_nx[q]);
+                    Bp.put(bp, lane);
+                    Ap.put(src, lane);
                     if (j >= y0 && j < y1 && interior) {
                         if (MODEL != AC) {
                             S.oaux[A_FX * S.qs + c] = src[4];
@@ -193,25 +327,33 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
             if (((wlo && k == 0) || (whi && k == ny - 1)) && colL) {
                 // bottom: row -1 (slot of k-1) from rows 0 (k), 1 (k+1); top: row ny (slot of
                 // k+1) from rows ny-1 (k), ny-2 (k-1)
-                T *const Bg = k == 0 ? Bm : Bp, *const B1 = k == 0 ? Bp : Bm;
-                float *const Ag = k == 0 ? Am : Ap, *const A1 = k == 0 ? Ap : Am;
+                const BRow &Bg = k == 0 ? Bm : Bp, &B1 = k == 0 ? Bp : Bm;
+                const ARow &Ag = k == 0 ? Am : Ap, &A1 = k == 0 ? Ap : Am;
                 const T two = mk2(2.f, 2.f);
+                T g[9];
 #pragma unroll
-                for (int q = 0; q < 9; ++q) Bg[q * 32 + lane] = sub2(mul2(two, B0[q * 32 + lane]), B1[q * 32 + lane]);
+                for (int q = 0; q < 9; ++q) g[q] = sub2(mul2(two, B0.get(q, lane)), B1.get(q, lane));
+                float a0[6], a1[6], ag[6];
+                A0.get(a0, lane);
+                A1.get(a1, lane);
 #pragma unroll
-                for (int a = 0; a < 6; ++a) Ag[a * 32 + lane] = 2.f * A0[a * 32 + lane] - A1[a * 32 + lane];
+                for (int a = 0; a < 6; ++a) ag[a] = 2.f * a0[a] - a1[a];
+                Bg.put(g, lane);
+                Ag.put(ag, lane);
             }
             __syncwarp();
             // ---- y-face between rows k-1 and k at the bottom wall (row 0's south face)
             if (wlo && k == 0 && interior) {
-                float av[6];
+                float av[6], am[6], a0[6];
+                Am.get(am, lane);
+                A0.get(a0, lane);
 #pragma unroll
-                for (int a = 0; a < 6; ++a) av[a] = 0.5f * (Am[a * 32 + lane] + A0[a * 32 + lane]);
+                for (int a = 0; a < 6; ++a) av[a] = 0.5f * (am[a] + a0[a]);
                 face_flux<MODEL, false, float>(
-                    P, [&](int q) { return Bm[q * 32 + lane]; }, [&](int q) { return B0[q * 32 + lane]; },
+                    P, [&](int q) { return Bm.get(q, lane); }, [&](int q) { return B0.get(q, lane); },
                     [&](int q) {
-                        return add2(sub2(B0[q * 32 + lane - 1], B0[q * 32 + lane + 1]),
-                                    sub2(Bm[q * 32 + lane - 1], Bm[q * 32 + lane + 1]));
+                        return add2(sub2(B0.get(q, lane - 1), B0.get(q, lane + 1)),
+                                    sub2(Bm.get(q, lane - 1), Bm.get(q, lane + 1)));
                     },
                     av, 1, FS);
             }
@@ -222,15 +364,17 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
             const bool top_wall = whi && k == ny - 1;
             const bool yface = k >= y0 - 1 && ((row_ok(k) && row_ok(k + 1)) || top_wall);
             if (yface && interior) {
-                float av[6];
+                float av[6], a0[6], ap[6];
+                A0.get(a0, lane);
+                Ap.get(ap, lane);
 #pragma unroll
-                for (int a = 0; a < 6; ++a) av[a] = 0.5f * (A0[a * 32 + lane] + Ap[a * 32 + lane]);
+                for (int a = 0; a < 6; ++a) av[a] = 0.5f * (a0[a] + ap[a]);
                 const int wall = top_wall ? 2 : 0;
                 face_flux<MODEL, false, float>(
-                    P, [&](int q) { return B0[q * 32 + lane]; }, [&](int q) { return Bp[q * 32 + lane]; },
+                    P, [&](int q) { return B0.get(q, lane); }, [&](int q) { return Bp.get(q, lane); },
                     [&](int q) {
-                        return add2(sub2(Bp[q * 32 + lane - 1], Bp[q * 32 + lane + 1]),
-                                    sub2(B0[q * 32 + lane - 1], B0[q * 32 + lane + 1]));
+                        return add2(sub2(Bp.get(q, lane - 1), Bp.get(q, lane + 1)),
+                                    sub2(B0.get(q, lane - 1), B0.get(q, lane + 1)));
                     },
                     av, wall, FN);
             }
@@ -240,14 +384,15 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
 #pragma unroll
             for (int s = 0; s < 6; ++s) FW[s] = mk2(0.f, 0.f);
             if (upd && xfL) {
-                float av[6];
+                float av[6], aw[6], a0[6];
+                A0.get(aw, lane - 1);
+                A0.get(a0, lane);
 #pragma unroll
-                for (int a = 0; a < 6; ++a) av[a] = 0.5f * (A0[a * 32 + lane - 1] + A0[a * 32 + lane]);
+                for (int a = 0; a < 6; ++a) av[a] = 0.5f * (aw[a] + a0[a]);
                 face_flux<MODEL, true, float>(
-                    P, [&](int q) { return B0[q * 32 + lane - 1]; }, [&](int q) { return B0[q * 32 + lane]; },
+                    P, [&](int q) { return B0.get(q, lane - 1); }, [&](int q) { return B0.get(q, lane); },
                     [&](int q) {
-                        return add2(sub2(Bp[q * 32 + lane], Bm[q * 32 + lane]),
-                                    sub2(Bp[q * 32 + lane - 1], Bm[q * 32 + lane - 1]));
+                        return add2(sub2(Bp.get(q, lane), Bm.get(q, lane)), sub2(Bp.get(q, lane - 1), Bm.get(q, lane - 1)));
                     },
                     av, 0, FW);
             }
@@ -260,7 +405,7 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
                 const int sl = m4(k);
                 T Pq[9], dn[9];
 #pragma unroll
-                for (int q = 0; q < 9; ++q) Pq[q] = mk2(STG(sl, q), STG(sl, 9 + q));
+                for (int q = 0; q < 9; ++q) Pq[q] = STG(sl, q);
                 const long long c = cell(k);
                 update_cell<float>(P, Pq, inc_cur, FW, FE, FS, FN, sr_bits(P, k, gi, step), dn);
 #pragma unroll
@@ -289,13 +434,13 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
 
 static int g_stream_nsm = 0, g_stream_blocks = 0;
 
-template <int MODEL, bool WALLS>
+template <int MODEL, bool WALLS, bool TMA>
 static cudaError_t stream_prepare() {
-    cudaError_t e = cudaFuncSetAttribute(k_stream32<MODEL, WALLS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_stream32<MODEL, WALLS, TMA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)STREAM_SMEM);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stream32<MODEL, WALLS>, WPB * 32, STREAM_SMEM);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stream32<MODEL, WALLS, TMA>, WPB * 32, STREAM_SMEM);
     if (e != cudaSuccess) return e;
     if (per_sm <= 0) return cudaErrorInvalidConfiguration;
     g_stream_blocks = g_stream_blocks ? min(g_stream_blocks, per_sm) : per_sm;
@@ -304,11 +449,12 @@ static cudaError_t stream_prepare() {
 
 template <int MODEL, bool WALLS>
 static cudaError_t launch_stream_t(const P32 &P, const S32 &S, int first, int gin, int gout, cudaStream_t st,
-                                   uint32_t step, bool *fallback) {
+                                   uint32_t step, const CUtensorMap *tmap, int zin, int *err, bool *fallback) {
     static bool ready = false;
     if (!ready) {
-        cudaError_t e = stream_prepare<MODEL, WALLS>();
+        cudaError_t e = stream_prepare<MODEL, WALLS, false>();
         if (e != cudaSuccess) return e;
+        if ((e = stream_prepare<MODEL, WALLS, true>()) != cudaSuccess) return e;
         int dev = 0;
         if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
         if ((e = cudaDeviceGetAttribute(&g_stream_nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
@@ -329,31 +475,73 @@ static cudaError_t launch_stream_t(const P32 &P, const S32 &S, int first, int gi
     const int nsegs = (P.ny + seg - 1) / seg;
     const int items = nstrips * nsegs;
     const int blocks = min((items + WPB - 1) / WPB, g_stream_nsm * g_stream_blocks);
-    k_stream32<MODEL, WALLS><<<blocks, WPB * 32, STREAM_SMEM, st>>>(P, S, first, gin, gout, step, nstrips, nsegs,
-                                                                     seg);
+    if (tmap) {
+        k_stream32<MODEL, WALLS, true><<<blocks, WPB * 32, STREAM_SMEM, st>>>(P, S, first, gin, gout, step, nstrips,
+                                                                            nsegs, seg, *tmap, zin, err);
+    } else {
+        CUtensorMap none;
+        memset(&none, 0, sizeof none);
+        k_stream32<MODEL, WALLS, false><<<blocks, WPB * 32, STREAM_SMEM, st>>>(P, S, first, gin, gout, step, nstrips,
+                                                                             nsegs, seg, none, 0, err);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_step32(const P32 &P, const S32 &S, int first, int gin, int gout, cudaStream_t st,
                           int64_t *launches, uint32_t step);
 
+// tmap: null, or the handle's 3-D tensor map over its two state copies (stream_tensor_map);
+// zin: the first plane of the copy this step reads (0 or 24); err: the word a staged
+// load that did not complete sets
 cudaError_t launch_stream32(const P32 &P, const S32 &S, int first, int gin, int gout, cudaStream_t st,
-                            int64_t *launches, uint32_t step) {
+                            int64_t *launches, uint32_t step, const void *tmap, int zin, int *err) {
     // the row window of a segment wraps at most once: grids of fewer than 8 rows
     // run the tile kernel (same arithmetic, same results)
     if (P.ny < 8) return launch_step32(P, S, first, gin, gout, st, launches, step);
+    const CUtensorMap *tm = static_cast<const CUtensorMap *>(tmap);
     cudaError_t e = cudaErrorInvalidValue;
     bool fallback = false;
     switch (P.model * 2 + (P.walls ? 1 : 0)) {
-        case AC * 2 + 0: e = launch_stream_t<AC, false>(P, S, first, gin, gout, st, step, &fallback); break;
-        case AC * 2 + 1: e = launch_stream_t<AC, true>(P, S, first, gin, gout, st, step, &fallback); break;
-        case HCZ * 2 + 0: e = launch_stream_t<HCZ, false>(P, S, first, gin, gout, st, step, &fallback); break;
-        case HCZ * 2 + 1: e = launch_stream_t<HCZ, true>(P, S, first, gin, gout, st, step, &fallback); break;
+        case AC * 2 + 0: e = launch_stream_t<AC, false>(P, S, first, gin, gout, st, step, tm, zin, err, &fallback); break;
+        case AC * 2 + 1: e = launch_stream_t<AC, true>(P, S, first, gin, gout, st, step, tm, zin, err, &fallback); break;
+        case HCZ * 2 + 0:
+            e = launch_stream_t<HCZ, false>(P, S, first, gin, gout, st, step, tm, zin, err, &fallback);
+            break;
+        case HCZ * 2 + 1:
+            e = launch_stream_t<HCZ, true>(P, S, first, gin, gout, st, step, tm, zin, err, &fallback);
+            break;
         default: break;
     }
     if (e == cudaSuccess && fallback) return launch_step32(P, S, first, gin, gout, st, launches, step);
     if (e == cudaSuccess) *launches += 1;
     return e;
+}
+
+// A 3-D tensor map (x: nx columns, y: ny rows, z: 48 planes) over the two state
+// copies of a single-case FP32 handle: 9 f, 9 h and 6 aux planes each, one plane
+// every qs floats from `base`; box {32, 1, 18} (the stage slot of one row).
+cudaError_t stream_tensor_map(void *map_out, float *base, int nx, int ny, int pitch, size_t qs) {
+    using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static EncodeFn encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess) return e;
+        if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorSymbolNotFound;
+        encode = reinterpret_cast<EncodeFn>(fn);
+    }
+    if (nx < 32 || ((uintptr_t)base & 15) || ((size_t)pitch * 4) % 16 || (qs * 4) % 16) return cudaErrorInvalidValue;
+    const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, 48};
+    const cuuint64_t strides[2] = {(cuuint64_t)pitch * 4, (cuuint64_t)qs * 4};
+    const cuuint32_t box[3] = {32, 1, 18};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = encode(static_cast<CUtensorMap *>(map_out), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims,
+                              strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
 }  // namespace f32

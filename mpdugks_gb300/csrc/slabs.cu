@@ -39,7 +39,7 @@ double rest_h(const Params &P, int q);
 }  // namespace internal
 namespace f32 {
 cudaError_t launch_stream32(const P32 &P, const S32 &S, int first, int gin, int gout, cudaStream_t st,
-                            int64_t *launches, uint32_t step);
+                            int64_t *launches, uint32_t step, const void *tmap, int zin, int *err);
 void launch_macros32(const P32 &P, const S32 &S, double *rho, double *u, double *v, double *p, double *phi,
                      int opitch, cudaStream_t st, int64_t *launches);
 template <typename R>
@@ -288,7 +288,8 @@ extern "C" int dugks_slabs_step(dugks_slabs_t *s, int nsteps) {
         const uint32_t sn = (uint32_t)s->steps;
         for (auto &q : s->parts) {
             cudaSetDevice(q.device);
-            cudaError_t e = f32::launch_stream32(q.P, q.S, s->first, s->gcur, s->gcur ^ 1, q.st, &s->launches, sn);
+            cudaError_t e = f32::launch_stream32(q.P, q.S, s->first, s->gcur, s->gcur ^ 1, q.st, &s->launches, sn,
+                                                 nullptr, 0, nullptr);
             if (e != cudaSuccess) return cuda_fail(e, "partition step");
         }
         if (s->multi_device) {  // every partition's step is done before its rows are copied
