@@ -160,7 +160,9 @@ int dugks_gpu_step(dugks_handle_t *h, int nsteps, void *stream);
  * the benchmark to time the dominant kernel live; synchronises the stream. */
 int dugks_gpu_step_profiled(dugks_handle_t *h, int nsteps, void *stream, double *ms_per_phase, int *nphases);
 
-/* Sum of rho, sum of phi and the density residual (FP64 device reductions). */
+/* Sum of rho, sum of phi and the density residual (FP64 device reductions).
+ * DUGKS_ETIMEOUT: a step of a DUGKS_FP32_DEV handle had a TMA row load that did
+ * not complete within its bounded wait (the state is then not valid). */
 int dugks_gpu_reduce(dugks_handle_t *h, dugks_reductions_t *r);
 
 /* Download the macroscopic fields (any pointer may be NULL): [ny][nx] each. */
@@ -171,7 +173,8 @@ int dugks_gpu_get_field(dugks_handle_t *h, int field, double *out);
 int dugks_gpu_set_field(dugks_handle_t *h, int field, const double *in);
 int dugks_gpu_get_dist(dugks_handle_t *h, int which, double *out);
 
-/* Scan the state for NaN/Inf: DUGKS_OK or DUGKS_ENAN. */
+/* Scan the state for NaN/Inf: DUGKS_OK or DUGKS_ENAN (DUGKS_ETIMEOUT as for
+ * dugks_gpu_reduce). */
 int dugks_gpu_check_finite(dugks_handle_t *h);
 
 /* Last error message of the handle (or of the last failed create if h is NULL). */
