@@ -41,9 +41,9 @@ RHO_H, RHO_L = 3.0, 1.0         # Atwood (3-1)/(3+1) = 0.5
 
 WORKLOADS = {
     'rt8192': dict(nx=8192, ny=8192, re=10000.0, init=[0.5, 0.05, 1e-4], precision='fp32dev',
-                   name='rayleigh_taylor_8192x8192_hcz_walls'),
+                   name='rayleigh_taylor_8192x8192_hcz_walls', full_steps=10000, yc=0.5),
     'rt512x2048': dict(nx=512, ny=2048, re=3000.0, init=[], precision='fp64',
-                       name='rayleigh_taylor_512x2048_hcz_walls'),
+                       name='rayleigh_taylor_512x2048_hcz_walls', full_steps=20000, yc=2.0),
 }
 
 # algorithmic HBM bytes per cell and step (state read once + written once)
@@ -448,6 +448,59 @@ def developed_flow_errors(steps: int = 300) -> dict:
             'fp64fma_vs_fp64': field_errors(runs['fp64fma'], runs['fp64'])}
 
 
+def rt_fronts(phi, nx: int, yc: float) -> dict:
+    """Rayleigh-Taylor fronts of a phi field [ny][nx] (heavy phase phi = 1 above the
+    interface): spike tip = lowest row with phi > 1/2 somewhere, bubble tip = highest row
+    with phi < 1/2 somewhere, both relative to the initial mean height yc*L in units of
+    L = nx; mixing zone = rows whose x-mean of phi lies in (0.01, 0.99), in units of L."""
+    import numpy as np
+    heavy = np.nonzero((phi > 0.5).any(axis=1))[0]
+    light = np.nonzero((phi < 0.5).any(axis=1))[0]
+    mean = phi.mean(axis=1)
+    mix = np.nonzero((mean > 0.01) & (mean < 0.99))[0]
+    c = yc * nx
+    return {'spike': round((float(heavy.min()) + 0.5 - c) / nx, 5) if heavy.size else None,
+            'bubble': round((float(light.max()) + 0.5 - c) / nx, 5) if light.size else None,
+            'mixing_zone': round(float(mix.size) / nx, 5)}
+
+
+def full_run(args, wl) -> dict:
+    """The configuration run to its full step count: time per 1000 steps (CUDA events),
+    mass and phase-field drift, density residual, finiteness and the fronts of the
+    instability every 1000 steps."""
+    import torch
+    from mpdugks_gb300 import capi
+    prec = args.precision or wl['precision']
+    nx, ny, n = wl['nx'], wl['ny'], args.full_steps or wl['full_steps']
+    kw = case_kw(wl)
+    stream = torch.cuda.Stream()
+    gc = capi.GpuCase(capi.make_case('HCZ', prec, **kw), nx, ny, True)
+    gc.init('ac_rt', wl['init'])
+    r0 = gc.reduce()
+    T = (nx / (kw['Gy'] * 0.5)) ** 0.5  # T = sqrt(L / (g At)), At = 0.5
+    dt = 0.5                            # CFL dx / max|xi| of the reference (Ark/Constant/ZeroNamespace.h)
+    rows, total_ms, done = [], 0.0, 0
+    while done < n:
+        k = min(1000, n - done)
+        ms, _, _ = timed_steps(gc, k, stream)
+        total_ms += ms
+        done += k
+        r = gc.reduce()
+        fin = gc.check_finite() == 0
+        row = {'steps': done, 't_over_T': round(done * dt / T, 4), 'ms_per_step': round(ms / k, 4),
+               'sum_rho_rel_drift': (r.sum_rho - r0.sum_rho) / r0.sum_rho,
+               'sum_phi_rel_drift': (r.sum_phi - r0.sum_phi) / r0.sum_phi,
+               'residual': r.residual, 'finite': fin}
+        row.update(rt_fronts(gc.get('phi').reshape(ny, nx), nx, wl['yc']))
+        rows.append(row)
+        if not fin:
+            break
+    cells = nx * ny
+    return {'workload': wl['name'], 'precision': prec, 'steps': done, 'seconds': round(total_ms / 1e3, 3),
+            'mlups': round(cells * done / (total_ms * 1e-3) / 1e6, 3), 'T_steps': round(T / dt, 1),
+            'history': rows}
+
+
 def timed_steps(gc, n: int, stream, clocks_idx=None):
     """n steps on `stream` bracketed by CUDA events on that stream; (ms, launches, clocks)."""
     import torch
@@ -653,6 +706,10 @@ def main():
     ap.add_argument('--profile-steps', type=int, default=0,
                     help='only run this many steps of the workload (for ncu) and exit')
     ap.add_argument('--grid', default=None, help='NXxNY override of the grid (profiling runs only)')
+    ap.add_argument('--full-run', action='store_true',
+                    help='run the workload for its configured step count (10000 at 8192^2, 20000 at 512x2048) '
+                         'and print its history (timing, conservation, residual, instability fronts)')
+    ap.add_argument('--full-steps', type=int, default=0, help='step count of --full-run (0: the configured one)')
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -675,6 +732,11 @@ def main():
         ap.error('--grid is for --profile-steps runs only')
     if args.impl == 'reference':
         return run_reference(args, wl, rank, world)
+    if args.full_run:
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps({'full_run': full_run(args, wl)}), flush=True)
+        return 0
     if args.serving_only:
         import torch
         torch.cuda.set_device(local)

@@ -122,6 +122,10 @@ def test_a_rank_that_leaves_is_reported_not_waited_for():
     ('HCZ', True, 48, 100, 3, 'ac_rt', [1.0, 0.1, 1e-4], dict(Mu0=0.01, M_Phi=0.05, W=4.0, Sigma=1e-4, RhoL=3.0,
                                                                RhoV=1.0, Gy=1e-4)),
     ('HCZ', False, 50, 300, 2, 'ac_drop_inside', [15.0], dict(Mu0=0.02, W=4.0, Sigma=1e-2, RhoL=10.0, RhoV=1.0)),
+    # large enough for the undivided case to take the streaming kernel with TMA row loads,
+    # against partitions whose rows (halo rows included) are loaded per lane
+    ('HCZ', True, 1120, 1664, 2, 'ac_rt', [0.75, 0.1, 1e-4], dict(Mu0=0.01, M_Phi=0.05, W=4.0, Sigma=1e-4,
+                                                                   RhoL=3.0, RhoV=1.0, Gy=1e-4)),
 ])
 def test_partitioned_run_equals_the_undivided_case(model, walls, nx, ny, n, init, params, kw):
     from mpdugks_gb300 import capi
