@@ -27,6 +27,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 
@@ -38,7 +39,7 @@ namespace dugks {
 namespace f32 {
 
 constexpr int SW = 28;   // interior columns of a strip
-constexpr int SEG_MAX = 128;  // rows of a segment: 128, 64 or 32 (enough segments per warp)
+constexpr int SEG_MAX = 128;  // longest first-choice segment (rows)
 constexpr int WPB = 2;   // warps per block
 constexpr int NSTG = 4;  // stage ring: rows k .. k+3
 // per-warp shared memory, in floats:
@@ -434,6 +435,32 @@ __global__ void __launch_bounds__(WPB * 32) k_stream32(P32 P, S32 S, int first, 
 
 static int g_stream_nsm = 0, g_stream_blocks = 0;
 
+// Rows of a strip segment.  The persistent warps take the (strip, segment) items in
+// turn, so a step lasts as long as the warps with the most items.  First choice: the
+// longest of 128, 64, 32 rows that still gives every resident warp about 4 items (a long
+// segment costs fewer warm-up rows).  Where that leaves fewer than 8 rounds of items,
+// the last, partly filled round is a large share of the step (measured: 2048^2 in 32-row
+// segments, 1.3 rounds, takes 1.28x the time of the best length), and the length is
+// searched instead: the fill of the last round, (items / warps) / ceil(items / warps),
+// times the share of a segment that is not warm-up, len / (len + 4), is maximised.
+int stream_segment_rows(int nstrips, int ny, int warps) {
+    int seg = SEG_MAX;
+    while (seg > 32 && (long long)nstrips * ((ny + seg - 1) / seg) < 4LL * warps) seg /= 2;
+    if ((double)nstrips * ((ny + seg - 1) / seg) >= 8.0 * warps) return seg;
+    int best = seg;
+    double best_eff = -1.0;
+    for (int len = 16; len <= ny; ++len) {
+        const int n = (ny + len - 1) / len;
+        const double waves = (double)nstrips * n / warps;
+        const double eff = waves / std::ceil(waves) * ((double)ny / n / ((double)ny / n + 4.0));
+        if (eff > best_eff + 1e-9) {
+            best_eff = eff;
+            best = len;
+        }
+    }
+    return best;
+}
+
 template <int MODEL, bool WALLS, bool TMA>
 static cudaError_t stream_prepare() {
     cudaError_t e = cudaFuncSetAttribute(k_stream32<MODEL, WALLS, TMA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -470,8 +497,7 @@ static cudaError_t launch_stream_t(const P32 &P, const S32 &S, int first, int gi
         *fallback = true;
         return cudaSuccess;
     }
-    int seg = SEG_MAX;
-    while (seg > 32 && (long long)nstrips * ((P.ny + seg - 1) / seg) < 4LL * warps) seg /= 2;
+    const int seg = stream_segment_rows(nstrips, P.ny, warps);
     const int nsegs = (P.ny + seg - 1) / seg;
     const int items = nstrips * nsegs;
     const int blocks = min((items + WPB - 1) / WPB, g_stream_nsm * g_stream_blocks);
