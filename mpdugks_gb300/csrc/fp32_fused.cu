@@ -33,6 +33,11 @@
 #include "dugks_device.cuh"
 #include "fp32_state.cuh"
 #include "fp32_math.cuh"
+#include "fp32_stream.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
 
 namespace dugks {
 namespace f32 {
@@ -388,6 +393,31 @@ __global__ void __launch_bounds__(BX *BY, 1) k_batch32(const int2 *__restrict__ 
     }
 }
 
+// The same in the streaming form: items (case slot, strip, first row, end row) of the
+// cases of one model and wall kind, each run by one warp with stream_item and its
+// case's constants, state and step number (per-lane row loads: no tensor map per case).
+// Items of a case whose step number reached case_stop are skipped.
+template <int MODEL, bool WALLS>
+__global__ void __launch_bounds__(WPB * 32) k_streamb32(const int4 *__restrict__ items, int nitems, int kstep,
+                                                        const int *__restrict__ case_base,
+                                                        const int *__restrict__ case_stop) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    float *wbase = reinterpret_cast<float *>(smem_raw) + (size_t)wib * WARP_F;
+    float *stg = wbase, *bring = wbase + STG_F, *aring = wbase + STG_F + BR_F;
+    uint32_t phases = 0;
+    const int gw = blockIdx.x * WPB + wib, nw = gridDim.x * WPB;
+    for (int it = gw; it < nitems; it += nw) {
+        const int4 t = items[it];
+        const int sn = case_base[t.x] + kstep;
+        if (sn >= case_stop[t.x]) continue;
+        const BatchCase &B = c_batch[t.x];
+        const int par = sn & 1;
+        stream_item<MODEL, WALLS, false>(B.P, B.S[par], sn == 0, par, par ^ 1, (uint32_t)sn, t.y, t.z, t.w, false,
+                                         nullptr, 0, nullptr, stg, bring, aring, 0u, phases, lane);
+    }
+}
+
 // case_base[slots[k]] += n for the k < count slots of a launch sequence
 __global__ void k_batch_advance(int *case_base, const int *slots, int count, int n) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -417,6 +447,21 @@ static cudaError_t batch_attr() {
                                 (int)(smem_elems<float>() * sizeof(float)));
 }
 
+static int g_streamb_blocks = 0;  // resident blocks of k_streamb32 per SM, set by batch_prepare
+
+template <int MODEL, bool WALLS>
+static cudaError_t streamb_attr() {
+    cudaError_t e = cudaFuncSetAttribute(k_streamb32<MODEL, WALLS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)STREAM_SMEM);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_streamb32<MODEL, WALLS>, WPB * 32, STREAM_SMEM);
+    if (e != cudaSuccess) return e;
+    if (per_sm <= 0) return cudaErrorInvalidConfiguration;
+    g_streamb_blocks = g_streamb_blocks ? std::min(g_streamb_blocks, per_sm) : per_sm;
+    return cudaSuccess;
+}
+
 // kernel attributes of the batched launches; called before any stream capture
 cudaError_t batch_prepare() {
     cudaError_t e;
@@ -424,6 +469,10 @@ cudaError_t batch_prepare() {
     if ((e = batch_attr<AC, true>()) != cudaSuccess) return e;
     if ((e = batch_attr<HCZ, false>()) != cudaSuccess) return e;
     if ((e = batch_attr<HCZ, true>()) != cudaSuccess) return e;
+    if ((e = streamb_attr<AC, false>()) != cudaSuccess) return e;
+    if ((e = streamb_attr<AC, true>()) != cudaSuccess) return e;
+    if ((e = streamb_attr<HCZ, false>()) != cudaSuccess) return e;
+    if ((e = streamb_attr<HCZ, true>()) != cudaSuccess) return e;
     int dev = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     return cudaDeviceGetAttribute(&g_batch_nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -448,6 +497,64 @@ cudaError_t launch_batch32(int model, int walls, const int2 *tiles, int ntiles, 
         case AC * 2 + 1: e = launch_batch_t<AC, true>(tiles, ntiles, kstep, case_base, case_stop, st); break;
         case HCZ * 2 + 0: e = launch_batch_t<HCZ, false>(tiles, ntiles, kstep, case_base, case_stop, st); break;
         case HCZ * 2 + 1: e = launch_batch_t<HCZ, true>(tiles, ntiles, kstep, case_base, case_stop, st); break;
+        default: break;
+    }
+    if (e == cudaSuccess) *launches += 1;
+    return e;
+}
+
+// Items of one k_streamb32 launch over the cases (slot, nx, ny), each with ny >= 8:
+// every case in strips of SW columns and row segments of one common length, chosen
+// like the single-case step's (stream_segment_rows): the fill of the last round of
+// items over the resident warps times the share of the rows that are not warm-up.
+void stream_batch_items(const std::vector<int3> &cases, std::vector<int4> &items) {
+    items.clear();
+    if (cases.empty()) return;
+    const double warps = (double)std::max(1, g_batch_nsm * g_streamb_blocks * WPB);
+    int maxny = 0;
+    for (const int3 &c : cases) maxny = std::max(maxny, c.z);
+    int best = std::min(32, maxny);
+    double best_eff = -1.0;
+    for (int len = std::min(16, maxny); len <= maxny; ++len) {
+        double n = 0.0, rows = 0.0, warm = 0.0;
+        for (const int3 &c : cases) {
+            const int strips = (c.y + SW - 1) / SW, segs = (c.z + len - 1) / len;
+            n += (double)strips * segs;
+            rows += (double)strips * c.z;
+            warm += 4.0 * strips * segs;
+        }
+        const double waves = n / warps;
+        const double eff = waves / std::ceil(waves) * (rows / (rows + warm));
+        if (eff > best_eff + 1e-9) {
+            best_eff = eff;
+            best = len;
+        }
+    }
+    for (const int3 &c : cases) {
+        const int strips = (c.y + SW - 1) / SW;
+        for (int y0 = 0; y0 < c.z; y0 += best)
+            for (int st = 0; st < strips; ++st) items.push_back(make_int4(c.x, st, y0, std::min(y0 + best, c.z)));
+    }
+}
+
+template <int MODEL, bool WALLS>
+static cudaError_t launch_streamb_t(const int4 *items, int nitems, int kstep, const int *case_base,
+                                    const int *case_stop, cudaStream_t st) {
+    if (g_batch_nsm <= 0 || g_streamb_blocks <= 0) return cudaErrorNotReady;
+    const int blocks = std::min((nitems + WPB - 1) / WPB, g_batch_nsm * g_streamb_blocks);
+    k_streamb32<MODEL, WALLS><<<blocks, WPB * 32, STREAM_SMEM, st>>>(items, nitems, kstep, case_base, case_stop);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_streamb32(int model, int walls, const int4 *items, int nitems, int kstep, const int *case_base,
+                             const int *case_stop, cudaStream_t st, int64_t *launches) {
+    if (nitems <= 0) return cudaSuccess;
+    cudaError_t e = cudaErrorInvalidValue;
+    switch (model * 2 + (walls ? 1 : 0)) {
+        case AC * 2 + 0: e = launch_streamb_t<AC, false>(items, nitems, kstep, case_base, case_stop, st); break;
+        case AC * 2 + 1: e = launch_streamb_t<AC, true>(items, nitems, kstep, case_base, case_stop, st); break;
+        case HCZ * 2 + 0: e = launch_streamb_t<HCZ, false>(items, nitems, kstep, case_base, case_stop, st); break;
+        case HCZ * 2 + 1: e = launch_streamb_t<HCZ, true>(items, nitems, kstep, case_base, case_stop, st); break;
         default: break;
     }
     if (e == cudaSuccess) *launches += 1;

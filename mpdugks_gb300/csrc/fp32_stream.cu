@@ -1,29 +1,10 @@
-// FP32 deviation-storage DUGKS step, streaming form: one warp per strip of
-// 28 columns (plus a two-column halo on each side, 32 lanes), marching along
-// y through a segment of rows.  No block-wide barrier: the y-neighbours of a
-// row are in the warp's own rolling buffers (shared memory), the
-// x-neighbours are the adjacent lanes' entries of the same buffers (or a
-// shuffle), so every warp runs independently of the others and of its block.
-//
-// Per row k the warp does, in order:
-//   phi of row k+2 (float-float sum of its h deviations, staged in shared
-//     memory); cp.async of row k+3's deviations into the stage ring (the
-//     aux of a row is read directly into registers one row ahead of its
-//     collision);
-//   collision of row k+1 (macros, MacroSource on the 3x3 phi stencil from
-//     the phi of rows k..k+2 and the adjacent lanes, f-bar-plus) into the
-//     f-bar-plus ring;
-//   the y-face between rows k and k+1 (its flux is row k's north face and,
-//     carried to the next row, row k+1's south face);
-//   the x-faces of row k (west face per lane, east face from the next lane);
-//   the update of row k.
-// A segment starts four rows early (phi of rows y0-2 and y0-1, collision of
-// row y0-1, the face below row y0); those rows' results are not written.
-// Bounce-back walls: ghost rows -1 and ny of f-bar-plus and of the averaged
-// fields are extrapolated (2 a0 - a1) into the rings and the wall faces bounce
-// back, as in the tile kernel.  The per-cell arithmetic is the tile kernel's
-// (fp32_math.cuh) with the same random bits, so the two kernels give
-// bit-identical results.
+// FP32 deviation-storage DUGKS step, streaming form, single case: the kernel
+// k_stream32 over the (strip, row segment) items of one grid, its launcher, and the
+// tensor map of its TMA row loads.  What a warp does per item is described in
+// fp32_stream.cuh; k_stream32 keeps its own copy of that item body, written out in
+// the kernel (the shared stream_item, inlined here, gave 4 more registers and a 1.4 %
+// slower step on 8192^2 cells), so a change to the per-item steps is made in both:
+// tests/test_gpu_serving.py checks the two bit for bit.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -31,107 +12,11 @@
 #include <cstdint>
 #include <cstring>
 
-#include "dugks_device.cuh"
-#include "fp32_math.cuh"
-#include "fp32_state.cuh"
+// constants, ring layouts, TMA helpers shared with the batched streaming kernel
+#include "fp32_stream.cuh"
 
 namespace dugks {
 namespace f32 {
-
-constexpr int SW = 28;   // interior columns of a strip
-constexpr int SEG_MAX = 128;  // longest first-choice segment (rows)
-constexpr int WPB = 2;   // warps per block
-constexpr int NSTG = 4;  // stage ring: rows k .. k+3
-// per-warp shared memory, in floats:
-//   stage ring [NSTG][18][32]: the raw deviation planes (9 f, then 9 h) of rows
-//     k .. k+3, 32 columns each -- the box one TMA load writes;
-//   f-bar-plus ring, per row slot: [4][32] float4 holding the pairs of directions
-//     (1,2), (3,4), (5,6), (7,8), then [32] float2 holding direction 0;
-//   averaged-field ring, per row slot: [32] float4 (srcx, srcy, rhox, rhoy), then
-//     [32] float2 (fx, fy).
-// 8- and 16-byte entries make one shared-memory instruction move two or four values.
-// After the warps' regions: 4 mbarriers per warp (one per stage slot).
-constexpr int STG_SLOT = 18 * 32;    // floats per stage slot
-constexpr int STG_F = NSTG * STG_SLOT;
-constexpr int BR_SLOT = 9 * 32 * 2;  // floats per row slot of the f-bar-plus ring
-constexpr int BR_F = 3 * BR_SLOT;
-constexpr int AR_SLOT = 6 * 32;      // floats per row slot of the averaged-field ring
-constexpr int AR_F = 3 * AR_SLOT;
-constexpr int WARP_F = STG_F + BR_F + AR_F;
-constexpr size_t STREAM_SMEM = (size_t)WPB * WARP_F * sizeof(float) + (size_t)WPB * NSTG * 8;
-static_assert((STG_SLOT * 4) % 128 == 0 && (WARP_F * 4) % 128 == 0, "TMA destinations are 128-byte aligned");
-static_assert((BR_SLOT * 4) % 16 == 0 && (AR_SLOT * 4) % 16 == 0, "16-byte aligned ring slots");
-constexpr unsigned STG_TX_BYTES = STG_SLOT * 4;   // bytes one TMA row load delivers
-constexpr int TMA_WAIT_LIMIT = 1 << 22;           // try_wait polls before a staged load is given up
-
-__device__ __forceinline__ int m3(int j) { return (j + 6) % 3; }  // j >= -6
-__device__ __forceinline__ int m4(int j) { return (j + 8) & 3; }  // j >= -8
-__device__ __forceinline__ int wrap_any(int j, int n) { return ((j % n) + n) % n; }
-
-// ---- TMA row loads completed through an mbarrier (inline PTX)
-__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(unsigned bar) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
-    unsigned ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// bounded wait for the phase of the given parity; true when it completed
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
-    for (int it = 0; it < TMA_WAIT_LIMIT; ++it)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-// one box {32 columns, 1 row, 18 planes} at (x, y, z) of a 3-D tensor map into shared memory
-__device__ __forceinline__ void tma_load_row(unsigned dst, const CUtensorMap *map, int x, int y, int z, unsigned bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::
-            "r"(dst),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
-        : "memory");
-}
-
-// one row slot of the f-bar-plus ring (see above); l is a lane (column of the strip)
-struct BRow {
-    float *base;
-    __device__ __forceinline__ float4 *quad() const { return reinterpret_cast<float4 *>(base); }
-    __device__ __forceinline__ float2 *rest() const { return reinterpret_cast<float2 *>(base + 4 * 32 * 4); }
-    __device__ __forceinline__ float2 get(int q, int l) const {
-        if (q == 0) return rest()[l];
-        const float4 v = quad()[((q - 1) >> 1) * 32 + l];
-        return ((q - 1) & 1) ? make_float2(v.z, v.w) : make_float2(v.x, v.y);
-    }
-    __device__ __forceinline__ void put(const float2 (&b)[9], int l) const {
-#pragma unroll
-        for (int g = 0; g < 4; ++g)
-            quad()[g * 32 + l] = make_float4(b[2 * g + 1].x, b[2 * g + 1].y, b[2 * g + 2].x, b[2 * g + 2].y);
-        rest()[l] = b[0];
-    }
-};
-// one row slot of the averaged-field ring: {srcx, srcy, rhox, rhoy, fx, fy}
-struct ARow {
-    float *base;
-    __device__ __forceinline__ float4 *quad() const { return reinterpret_cast<float4 *>(base); }
-    __device__ __forceinline__ float2 *pair() const { return reinterpret_cast<float2 *>(base + 32 * 4); }
-    __device__ __forceinline__ void get(float (&a)[6], int l) const {
-        const float4 v = quad()[l];
-        const float2 w = pair()[l];
-        a[0] = v.x, a[1] = v.y, a[2] = v.z, a[3] = v.w, a[4] = w.x, a[5] = w.y;
-    }
-    __device__ __forceinline__ void put(const float (&a)[6], int l) const {
-        quad()[l] = make_float4(a[0], a[1], a[2], a[3]);
-        pair()[l] = make_float2(a[4], a[5]);
-    }
-};
 
 // first: the first step after an initialisation (the collision takes the state the
 // initialisation left instead of the macroscopic quantities of the deviations).  A

@@ -1,0 +1,411 @@
+// The streaming form of the FP32 deviation-storage step: its constants, shared-memory
+// ring layout and TMA helpers (used by the single-case kernel k_stream32,
+// fp32_stream.cu, and the batched serving kernel k_streamb32, fp32_fused.cu), and the
+// per-warp work on one (strip, row segment) item, stream_item (k_streamb32; k_stream32
+// has the same steps written out in the kernel).
+//
+// A warp marches a strip of 28 columns (plus a two-column halo on each side, 32
+// lanes) along y through a segment of rows.  No block-wide barrier: the
+// y-neighbours of a row are in the warp's own rolling buffers (shared memory), the
+// x-neighbours are the adjacent lanes' entries of the same buffers (or a shuffle),
+// so every warp runs independently of the others and of its block.
+//
+// Per row k the warp does, in order:
+//   phi of row k+2 (float-float sum of its h deviations, staged in shared
+//     memory); the load of row k+3's deviations into the stage ring (the aux of a
+//     row is read directly into registers one row ahead of its collision);
+//   collision of row k+1 (macros, MacroSource on the 3x3 phi stencil from the phi
+//     of rows k..k+2 and the adjacent lanes, f-bar-plus) into the f-bar-plus ring;
+//   the y-face between rows k and k+1 (its flux is row k's north face and,
+//     carried to the next row, row k+1's south face);
+//   the x-faces of row k (west face per lane, east face from the next lane);
+//   the update of row k.
+// A segment starts four rows early (phi of rows y0-2 and y0-1, collision of row
+// y0-1, the face below row y0); those rows' results are not written.  Bounce-back
+// walls: ghost rows -1 and ny of f-bar-plus and of the averaged fields are
+// extrapolated (2 a0 - a1) into the rings and the wall faces bounce back, as in
+// the tile kernel.  The per-cell arithmetic is the tile kernel's (fp32_math.cuh)
+// with the same random bits, so the kernels give bit-identical results.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "dugks_device.cuh"
+#include "fp32_math.cuh"
+#include "fp32_state.cuh"
+
+namespace dugks {
+namespace f32 {
+
+constexpr int SW = 28;   // interior columns of a strip
+constexpr int SEG_MAX = 128;  // longest first-choice segment (rows)
+constexpr int WPB = 2;   // warps per block
+constexpr int NSTG = 4;  // stage ring: rows k .. k+3
+// per-warp shared memory, in floats:
+//   stage ring [NSTG][18][32]: the raw deviation planes (9 f, then 9 h) of rows
+//     k .. k+3, 32 columns each -- the box one TMA load writes;
+//   f-bar-plus ring, per row slot: [4][32] float4 holding the pairs of directions
+//     (1,2), (3,4), (5,6), (7,8), then [32] float2 holding direction 0;
+//   averaged-field ring, per row slot: [32] float4 (srcx, srcy, rhox, rhoy), then
+//     [32] float2 (fx, fy).
+// 8- and 16-byte entries make one shared-memory instruction move two or four values.
+// After the warps' regions: 4 mbarriers per warp (one per stage slot).
+constexpr int STG_SLOT = 18 * 32;    // floats per stage slot
+constexpr int STG_F = NSTG * STG_SLOT;
+constexpr int BR_SLOT = 9 * 32 * 2;  // floats per row slot of the f-bar-plus ring
+constexpr int BR_F = 3 * BR_SLOT;
+constexpr int AR_SLOT = 6 * 32;      // floats per row slot of the averaged-field ring
+constexpr int AR_F = 3 * AR_SLOT;
+constexpr int WARP_F = STG_F + BR_F + AR_F;
+constexpr size_t STREAM_SMEM = (size_t)WPB * WARP_F * sizeof(float) + (size_t)WPB * NSTG * 8;
+static_assert((STG_SLOT * 4) % 128 == 0 && (WARP_F * 4) % 128 == 0, "TMA destinations are 128-byte aligned");
+static_assert((BR_SLOT * 4) % 16 == 0 && (AR_SLOT * 4) % 16 == 0, "16-byte aligned ring slots");
+constexpr unsigned STG_TX_BYTES = STG_SLOT * 4;   // bytes one TMA row load delivers
+constexpr int TMA_WAIT_LIMIT = 1 << 22;           // try_wait polls before a staged load is given up
+
+__device__ __forceinline__ int m3(int j) { return (j + 6) % 3; }  // j >= -6
+__device__ __forceinline__ int m4(int j) { return (j + 8) & 3; }  // j >= -8
+__device__ __forceinline__ int wrap_any(int j, int n) { return ((j % n) + n) % n; }
+
+// ---- TMA row loads completed through an mbarrier (inline PTX)
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait for the phase of the given parity; true when it completed
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+    for (int it = 0; it < TMA_WAIT_LIMIT; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// one box {32 columns, 1 row, 18 planes} at (x, y, z) of a 3-D tensor map into shared memory
+__device__ __forceinline__ void tma_load_row(unsigned dst, const CUtensorMap *map, int x, int y, int z, unsigned bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::
+            "r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
+// one row slot of the f-bar-plus ring (see above); l is a lane (column of the strip)
+struct BRow {
+    float *base;
+    __device__ __forceinline__ float4 *quad() const { return reinterpret_cast<float4 *>(base); }
+    __device__ __forceinline__ float2 *rest() const { return reinterpret_cast<float2 *>(base + 4 * 32 * 4); }
+    __device__ __forceinline__ float2 get(int q, int l) const {
+        if (q == 0) return rest()[l];
+        const float4 v = quad()[((q - 1) >> 1) * 32 + l];
+        return ((q - 1) & 1) ? make_float2(v.z, v.w) : make_float2(v.x, v.y);
+    }
+    __device__ __forceinline__ void put(const float2 (&b)[9], int l) const {
+#pragma unroll
+        for (int g = 0; g < 4; ++g)
+            quad()[g * 32 + l] = make_float4(b[2 * g + 1].x, b[2 * g + 1].y, b[2 * g + 2].x, b[2 * g + 2].y);
+        rest()[l] = b[0];
+    }
+};
+// one row slot of the averaged-field ring: {srcx, srcy, rhox, rhoy, fx, fy}
+struct ARow {
+    float *base;
+    __device__ __forceinline__ float4 *quad() const { return reinterpret_cast<float4 *>(base); }
+    __device__ __forceinline__ float2 *pair() const { return reinterpret_cast<float2 *>(base + 32 * 4); }
+    __device__ __forceinline__ void get(float (&a)[6], int l) const {
+        const float4 v = quad()[l];
+        const float2 w = pair()[l];
+        a[0] = v.x, a[1] = v.y, a[2] = v.z, a[3] = v.w, a[4] = w.x, a[5] = w.y;
+    }
+    __device__ __forceinline__ void put(const float (&a)[6], int l) const {
+        quad()[l] = make_float4(a[0], a[1], a[2], a[3]);
+        pair()[l] = make_float2(a[4], a[5]);
+    }
+};
+
+// One (strip, rows y0 .. y1-1) item of a step of one case.  stg, bring, aring: the
+// warp's shared-memory rings; bar0, phases: its stage-slot mbarriers and their phase
+// parities (TMA instances).  use of TMA for the item: tma_ok and a window that does not
+// wrap around x.  Returns false when a TMA load did not complete (the warp must end).
+template <int MODEL, bool WALLS, bool TMA>
+__device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int first, int gin, int gout, uint32_t step,
+                                            int strip, int y0, int y1, bool tma_ok, const CUtensorMap *tmap_p,
+                                            int zin, int *err, float *stg, float *bring, float *aring,
+                                            unsigned bar0, uint32_t &phases, int lane) {
+    using T = float2;
+    auto STG = [&](int slot, int q) -> T {
+        return mk2(stg[slot * STG_SLOT + q * 32 + lane], stg[slot * STG_SLOT + (9 + q) * 32 + lane]);
+    };
+    const int nx = P.nx, ny = P.ny, pitch = P.pitch;
+    // the strip's window is columns hs .. hs+31 (a multiple of 4: 16-byte TMA
+    // coordinates); its interior columns x0 .. x0+w-1 run over 2 .. nx+1, the
+    // last strip's wrapping around the periodic x boundary
+    const int hs = strip * SW, x0 = hs + 2, w = min(SW, nx + 2 - x0);
+    const int gi = wrap_any(hs + lane, nx);
+    const bool use_tma = tma_ok && hs + 32 <= nx;
+    const bool interior = lane >= 2 && lane < 2 + w;
+    const bool colL = lane >= 1 && lane <= 2 + w;  // lanes whose f-bar-plus is needed
+    const bool xfL = lane >= 2 && lane <= 2 + w;   // lanes whose west x-face is needed
+    // rows of the window lie in [y0-4, y1+3] (the launcher ensures ny >= 8).  A
+    // slab partition (WALLS instance) reads rows below 0 / from ny up from its
+    // halo rows where halo_lo / halo_hi is set; elsewhere they are walls.
+    const bool hlo = WALLS && P.halo_lo, hhi = WALLS && P.halo_hi;
+    auto row_ok = [&](int j) {
+        return WALLS ? ((j >= 0 || (hlo && j >= -SLAB_HALO)) && (j < ny || (hhi && j < ny + SLAB_HALO))) : true;
+    };
+    auto row_of = [&](int j) { return WALLS ? j : (j < 0 ? j + ny : (j >= ny ? j - ny : j)); };
+    auto cell = [&](int j) -> long long {  // signed: halo rows lie below row 0
+        return (long long)row_of(j) * pitch + gi;
+    };
+    // wall sides (no halo)
+    const bool wlo = WALLS && !hlo, whi = WALLS && !hhi;
+    auto loaded = [&](int j) { return j <= y1 + 1 && row_ok(j); };
+    auto prefetch = [&](int j) {
+        if (loaded(j)) {
+            if (use_tma) {
+                if (lane == 0) {
+                    const unsigned bar = bar0 + 8 * m4(j);
+                    // the slot's previous row was read by every lane (generic proxy)
+                    // before this warp's last __syncwarp
+                    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                    mbar_expect_tx(bar, STG_TX_BYTES);
+                    tma_load_row(smem_u32(stg + m4(j) * STG_SLOT), tmap_p, hs, row_of(j), zin, bar);
+                }
+            } else {
+                const long long c = cell(j);
+                float *d = stg + m4(j) * STG_SLOT + lane;
+#pragma unroll
+                for (int q = 0; q < 9; ++q) {
+                    cp_async(d + q * 32, S.df + (size_t)q * S.qs + c);
+                    cp_async(d + (9 + q) * 32, S.dh + (size_t)q * S.qs + c);
+                }
+            }
+        }
+        if (!use_tma) cp_async_commit();
+    };
+    __syncwarp();  // the previous item is done with this warp's buffers
+    prefetch(y0 - 2);
+    // rolling per-lane state: phi of rows k, k+1, k+2; the (sum f, sum h)
+    // deviation sums of rows k+1, k+2; row k's collision increments and
+    // south-face flux
+    float ph0 = 0.f, ph1 = 0.f, ph2 = 0.f;
+    float sfz1 = 0.f, dph1 = 0.f;
+    float a6c[A_N];  // aux of row k+1 (loaded at the previous row)
+    T inc_cur[9], FS[6];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) inc_cur[q] = mk2(0.f, 0.f);
+#pragma unroll
+    for (int s = 0; s < 6; ++s) FS[s] = mk2(0.f, 0.f);
+    for (int k = y0 - 4; k < y1; ++k) {
+        // this row's ring slots: f-bar-plus and averaged fields of rows k-1, k, k+1
+        const BRow Bm{bring + m3(k - 1) * BR_SLOT}, B0{bring + m3(k) * BR_SLOT}, Bp{bring + m3(k + 1) * BR_SLOT};
+        const ARow Am{aring + m3(k - 1) * AR_SLOT}, A0{aring + m3(k) * AR_SLOT}, Ap{aring + m3(k + 1) * AR_SLOT};
+        // aux of row k+2, read directly one row ahead of its collision
+        const bool coll = k + 1 >= y0 - 1 && row_ok(k + 1) && colL;
+        float a6n[A_N];
+        if (MODEL != AC && !first && k + 2 >= y0 - 1 && row_ok(k + 2) && colL) {
+            const long long c2 = cell(k + 2);
+#pragma unroll
+            for (int a = 0; a < A_N; ++a) a6n[a] = __ldg(S.aux + (size_t)a * S.qs + c2);
+        }
+        // row k+2's raw deviations (issued one row ago) have landed
+        if (use_tma) {
+            if (loaded(k + 2)) {
+                const int s = m4(k + 2);
+                const bool ok = __all_sync(0xffffffffu, mbar_wait(bar0 + 8 * s, (phases >> s) & 1u));
+                if (!ok) {
+                    if (lane == 0 && err) atomicExch(err, 1);
+                    mbar_wait(bar0 + 8 * s, (phases >> s) & 1u);  // the copy in flight, once more
+                    return false;
+                }
+                phases ^= 1u << s;
+            }
+        } else {
+            cp_async_wait_all();
+        }
+        __syncwarp();
+        // ---- phi of row k+2
+        float sfz2 = 0.f, dph2 = 0.f;
+        {
+            const int j = k + 2;
+            float phv = 0.f;
+            if (row_ok(j)) {
+                const int sl = m4(j);
+                T za[9];
+#pragma unroll
+                for (int q = 0; q < 9; ++q) za[q] = STG(sl, q);
+                if (MODEL == AC) za[0].x = 0.f;
+                const T z = ff_sum9(za);
+                sfz2 = z.x;
+                dph2 = z.y;
+                phv = P.phi0 + dph2;
+            } else if ((wlo && j == -1) || (whi && j == ny)) {
+                // ghost phi: the previous step's extrapolation (Ark/Cpp/Boundary.cpp:38-63)
+                phv = S.gphi[(size_t)(gin * 2 + (j < 0 ? 0 : 1)) * pitch + gi];
+            }
+            ph2 = phv;
+        }
+        __syncwarp();  // every lane has read slot k+2 (slot k+3 = slot k-1 is refilled next)
+        prefetch(k + 3);
+        // ---- collision of row k+1
+        T inc_nx[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) inc_nx[q] = mk2(0.f, 0.f);
+        {
+            const int j = k + 1;
+            // 3x3 phi stencil: rows k (S), k+1, k+2 (N); lanes +-1 (E/W)
+            const float E = __shfl_down_sync(0xffffffffu, ph1, 1), W = __shfl_up_sync(0xffffffffu, ph1, 1);
+            const float NE = __shfl_down_sync(0xffffffffu, ph2, 1), NW = __shfl_up_sync(0xffffffffu, ph2, 1);
+            const float SE = __shfl_down_sync(0xffffffffu, ph0, 1), SWv = __shfl_up_sync(0xffffffffu, ph0, 1);
+            if (coll) {
+                const int sl = m4(j);
+                T Pq[9];
+#pragma unroll
+                for (int q = 0; q < 9; ++q) Pq[q] = STG(sl, q);
+                const float ph[8] = {E, W, ph2, ph0, NE, NW, SE, SWv};
+                const long long c = cell(j);
+                float src[6], phi, U, V;
+                collide_cell<MODEL, float>(P, S, c, first, Pq, sfz1, dph1, a6c, ph, inc_nx, src, phi, U, V);
+                T bp[9];
+#pragma unroll
+                for (int q = 0; q < 9; ++q) bp[q] = add2(Pq[q], inc_nx[q]);
+                Bp.put(bp, lane);
+                Ap.put(src, lane);
+                if (j >= y0 && j < y1 && interior) {
+                    if (MODEL != AC) {
+                        S.oaux[A_FX * S.qs + c] = src[4];
+                        S.oaux[A_FY * S.qs + c] = src[5];
+                        S.oaux[A_RHOX * S.qs + c] = src[2];
+                        S.oaux[A_RHOY * S.qs + c] = src[3];
+                        S.oaux[A_PPU * S.qs + c] = phi * U;
+                        S.oaux[A_PPV * S.qs + c] = phi * V;
+                    }
+                    // ghost phi for the next step's MacroSource
+                    if (wlo && j == 0) S.gphi[(size_t)(gout * 2 + 0) * pitch + gi] = 2.f * phi - ph2;
+                    if (whi && j == ny - 1) S.gphi[(size_t)(gout * 2 + 1) * pitch + gi] = 2.f * phi - ph0;
+                }
+            }
+        }
+        __syncwarp();
+        // ---- wall ghost rows of f-bar-plus and of the averaged fields (2 a0 - a1)
+        if (((wlo && k == 0) || (whi && k == ny - 1)) && colL) {
+            // bottom: row -1 (slot of k-1) from rows 0 (k), 1 (k+1); top: row ny (slot of
+            // k+1) from rows ny-1 (k), ny-2 (k-1)
+            const BRow &Bg = k == 0 ? Bm : Bp, &B1 = k == 0 ? Bp : Bm;
+            const ARow &Ag = k == 0 ? Am : Ap, &A1 = k == 0 ? Ap : Am;
+            const T two = mk2(2.f, 2.f);
+            T g[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) g[q] = sub2(mul2(two, B0.get(q, lane)), B1.get(q, lane));
+            float a0[6], a1[6], ag[6];
+            A0.get(a0, lane);
+            A1.get(a1, lane);
+#pragma unroll
+            for (int a = 0; a < 6; ++a) ag[a] = 2.f * a0[a] - a1[a];
+            Bg.put(g, lane);
+            Ag.put(ag, lane);
+        }
+        __syncwarp();
+        // ---- y-face between rows k-1 and k at the bottom wall (row 0's south face)
+        if (wlo && k == 0 && interior) {
+            float av[6], am[6], a0[6];
+            Am.get(am, lane);
+            A0.get(a0, lane);
+#pragma unroll
+            for (int a = 0; a < 6; ++a) av[a] = 0.5f * (am[a] + a0[a]);
+            face_flux<MODEL, false, float>(
+                P, [&](int q) { return Bm.get(q, lane); }, [&](int q) { return B0.get(q, lane); },
+                [&](int q) {
+                    return add2(sub2(B0.get(q, lane - 1), B0.get(q, lane + 1)),
+                                sub2(Bm.get(q, lane - 1), Bm.get(q, lane + 1)));
+                },
+                av, 1, FS);
+        }
+        // ---- y-face between rows k and k+1 (row k's north face)
+        T FN[6];
+#pragma unroll
+        for (int s = 0; s < 6; ++s) FN[s] = mk2(0.f, 0.f);
+        const bool top_wall = whi && k == ny - 1;
+        const bool yface = k >= y0 - 1 && ((row_ok(k) && row_ok(k + 1)) || top_wall);
+        if (yface && interior) {
+            float av[6], a0[6], ap[6];
+            A0.get(a0, lane);
+            Ap.get(ap, lane);
+#pragma unroll
+            for (int a = 0; a < 6; ++a) av[a] = 0.5f * (a0[a] + ap[a]);
+            const int wall = top_wall ? 2 : 0;
+            face_flux<MODEL, false, float>(
+                P, [&](int q) { return B0.get(q, lane); }, [&](int q) { return Bp.get(q, lane); },
+                [&](int q) {
+                    return add2(sub2(Bp.get(q, lane - 1), Bp.get(q, lane + 1)),
+                                sub2(B0.get(q, lane - 1), B0.get(q, lane + 1)));
+                },
+                av, wall, FN);
+        }
+        // ---- x-faces of row k: the west face of every lane, the east face from the next lane
+        const bool upd = k >= y0 && row_ok(k);
+        T FW[6];
+#pragma unroll
+        for (int s = 0; s < 6; ++s) FW[s] = mk2(0.f, 0.f);
+        if (upd && xfL) {
+            float av[6], aw[6], a0[6];
+            A0.get(aw, lane - 1);
+            A0.get(a0, lane);
+#pragma unroll
+            for (int a = 0; a < 6; ++a) av[a] = 0.5f * (aw[a] + a0[a]);
+            face_flux<MODEL, true, float>(
+                P, [&](int q) { return B0.get(q, lane - 1); }, [&](int q) { return B0.get(q, lane); },
+                [&](int q) {
+                    return add2(sub2(Bp.get(q, lane), Bm.get(q, lane)), sub2(Bp.get(q, lane - 1), Bm.get(q, lane - 1)));
+                },
+                av, 0, FW);
+        }
+        T FE[6];
+#pragma unroll
+        for (int s = 0; s < 6; ++s)
+            FE[s] = mk2(__shfl_down_sync(0xffffffffu, FW[s].x, 1), __shfl_down_sync(0xffffffffu, FW[s].y, 1));
+        // ---- update of row k
+        if (upd && interior) {
+            const int sl = m4(k);
+            T Pq[9], dn[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) Pq[q] = STG(sl, q);
+            const long long c = cell(k);
+            update_cell<float>(P, Pq, inc_cur, FW, FE, FS, FN, sr_bits(P, k, gi, step), dn);
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                S.odf[(size_t)q * S.qs + c] = dn[q].x;
+                S.odh[(size_t)q * S.qs + c] = dn[q].y;
+            }
+        }
+        // ---- roll the per-lane state one row up
+#pragma unroll
+        for (int q = 0; q < 9; ++q) inc_cur[q] = inc_nx[q];
+#pragma unroll
+        for (int s = 0; s < 6; ++s) FS[s] = FN[s];
+        ph0 = ph1;
+        ph1 = ph2;
+        sfz1 = sfz2;
+        dph1 = dph2;
+        if (MODEL != AC) {
+#pragma unroll
+            for (int a = 0; a < A_N; ++a) a6c[a] = a6n[a];
+        }
+    }
+    cp_async_wait_all();  // nothing in flight into this warp's buffers
+    return true;
+}
+
+}  // namespace f32
+}  // namespace dugks

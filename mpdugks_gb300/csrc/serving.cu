@@ -53,6 +53,9 @@ cudaError_t batch_set_case(int slot, const P32 &P, const S32 &S, int64_t step, c
 int batch_tiles_of(int nx, int ny);
 cudaError_t launch_batch32(int model, int walls, const int2 *tiles, int ntiles, int kstep, const int *case_base,
                            const int *case_stop, cudaStream_t st, int64_t *launches);
+cudaError_t launch_streamb32(int model, int walls, const int4 *items, int nitems, int kstep, const int *case_base,
+                             const int *case_stop, cudaStream_t st, int64_t *launches);
+void stream_batch_items(const std::vector<int3> &cases, std::vector<int4> &items);
 cudaError_t launch_batch_advance(int *case_base, const int *slots, int count, int n, cudaStream_t st,
                                  int64_t *launches);
 cudaError_t batch_prepare();
@@ -494,29 +497,54 @@ void admit_loop(dugks_srv *s) {
 
 // ---- batch lane
 cudaError_t capture_chunk(dugks_srv *s, const std::vector<std::shared_ptr<SrvCase>> &act, Chunk &ch) {
-    // group the cases by (model, walls); tile table per group, slot list at the end
-    std::map<std::pair<int, int>, std::vector<int2>> groups;
+    // group the cases by (model, walls); per group the streaming kernel's items (cases of
+    // at least 8 rows) and the tile kernel's tiles (the rest); slot list at the end
+    struct Group {
+        std::vector<int3> cases;  // (slot, nx, ny) of the streaming kernel
+        std::vector<int4> items;
+        std::vector<int2> tiles;
+    };
+    std::map<std::pair<int, int>, Group> groups;
     std::vector<int> slots;
     for (const auto &c : act) {
         const int m = internal::model_of(c->h), w = internal::walls_of(c->h);
-        auto &tb = groups[{m, w}];
-        const int nt = f32::batch_tiles_of(c->grid.nx, c->grid.ny);
-        for (int t = 0; t < nt; ++t) tb.push_back(make_int2(c->slot, t));
+        Group &g = groups[{m, w}];
+        if (c->grid.ny >= 8) {
+            g.cases.push_back(make_int3(c->slot, c->grid.nx, c->grid.ny));
+        } else {
+            const int nt = f32::batch_tiles_of(c->grid.nx, c->grid.ny);
+            for (int t = 0; t < nt; ++t) g.tiles.push_back(make_int2(c->slot, t));
+        }
         slots.push_back(c->slot);
     }
     size_t total = 0;
-    for (auto &g : groups) total += g.second.size() * sizeof(int2);
-    const size_t slot_off = (total + 255) & ~(size_t)255;
+    for (auto &kv : groups) {
+        f32::stream_batch_items(kv.second.cases, kv.second.items);
+        total += ((kv.second.items.size() * sizeof(int4) + 255) & ~(size_t)255) +
+                 ((kv.second.tiles.size() * sizeof(int2) + 255) & ~(size_t)255);
+    }
+    const size_t slot_off = total;
     total = slot_off + slots.size() * sizeof(int);
     cudaError_t e = cudaMalloc(&ch.dev, total);
     if (e != cudaSuccess) return e;
     std::vector<char> host(total);
+    struct Where {
+        int model, walls;
+        size_t items_off;
+        int nitems;
+        size_t tiles_off;
+        int ntiles;
+    };
+    std::vector<Where> where;
     size_t off = 0;
-    std::vector<std::pair<std::pair<int, int>, std::pair<size_t, int>>> where;  // group -> (offset, count)
-    for (auto &g : groups) {
-        std::memcpy(host.data() + off, g.second.data(), g.second.size() * sizeof(int2));
-        where.push_back({g.first, {off, (int)g.second.size()}});
-        off += g.second.size() * sizeof(int2);
+    for (auto &kv : groups) {
+        Where w{kv.first.first, kv.first.second, off, (int)kv.second.items.size(), 0, (int)kv.second.tiles.size()};
+        std::memcpy(host.data() + off, kv.second.items.data(), kv.second.items.size() * sizeof(int4));
+        off += (kv.second.items.size() * sizeof(int4) + 255) & ~(size_t)255;
+        w.tiles_off = off;
+        std::memcpy(host.data() + off, kv.second.tiles.data(), kv.second.tiles.size() * sizeof(int2));
+        off += (kv.second.tiles.size() * sizeof(int2) + 255) & ~(size_t)255;
+        where.push_back(w);
     }
     std::memcpy(host.data() + slot_off, slots.data(), slots.size() * sizeof(int));
     if ((e = cudaMemcpy(ch.dev, host.data(), total, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
@@ -525,9 +553,12 @@ cudaError_t capture_chunk(dugks_srv *s, const std::vector<std::shared_ptr<SrvCas
     if ((e = cudaStreamBeginCapture(s->s_batch, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
     cudaError_t le = cudaSuccess;
     for (int k = 0; k < s->chunk && le == cudaSuccess; ++k)
-        for (auto &g : where) {
-            le = f32::launch_batch32(g.first.first, g.first.second, reinterpret_cast<const int2 *>(base + g.second.first),
-                                     g.second.second, k, s->d_base, s->d_stop, s->s_batch, &launches);
+        for (const Where &g : where) {
+            le = f32::launch_streamb32(g.model, g.walls, reinterpret_cast<const int4 *>(base + g.items_off), g.nitems,
+                                       k, s->d_base, s->d_stop, s->s_batch, &launches);
+            if (le == cudaSuccess)
+                le = f32::launch_batch32(g.model, g.walls, reinterpret_cast<const int2 *>(base + g.tiles_off),
+                                         g.ntiles, k, s->d_base, s->d_stop, s->s_batch, &launches);
             if (le != cudaSuccess) break;
         }
     if (le == cudaSuccess)
