@@ -340,6 +340,46 @@ __device__ __forceinline__ double face_bh(const Params &P, const double *__restr
     return 0.5 * (o + n) - P.hDt * (gx * xu + gy * xv);
 }
 
+// The same for a D2Q9 velocity xi = (xu, xv), components in {-1, 0, 1} known at compile
+// time after unrolling: a gradient a zero component multiplies is not formed (the
+// product with 0 and its sum with the other term only decide the sign of a zero
+// result), and a product with +-1 is the operand or its negation (exact); the
+// nonzero terms keep the reference's order and rounding.
+template <bool XF, bool WALLS>
+__device__ __forceinline__ double face_bh9(const Params &P, const double *__restrict__ B, int i, int im, int ip,
+                                           int j, int xu, int xv) {
+    const int ny = P.ny, pitch = P.pitch;
+    double o, n, gx = 0.0, gy = 0.0;
+    if (XF) {
+        o = cellv<WALLS>(B, ny, pitch, j, im);
+        n = cellv<WALLS>(B, ny, pitch, j, i);
+        if (xv != 0) {
+            const double SL = cellv<WALLS>(B, ny, pitch, j - 1, im), SR = cellv<WALLS>(B, ny, pitch, j - 1, i);
+            const double NL = cellv<WALLS>(B, ny, pitch, j + 1, im), NR = cellv<WALLS>(B, ny, pitch, j + 1, i);
+            gy = P.grad_mul ? (0.5 * ((NR - SR) + (NL - SL))) * P.r_2dy
+                            : (0.5 * (NR - SR) + 0.5 * (NL - SL)) / (2 * P.dy);
+        }
+        if (xu != 0) gx = P.grad_mul ? (o - n) * P.r_ndx : (o - n) / (-P.dx);
+    } else {
+        o = cellv<WALLS>(B, ny, pitch, j - 1, i);
+        n = cellv<WALLS>(B, ny, pitch, j, i);
+        if (xu != 0) {
+            const double WB = cellv<WALLS>(B, ny, pitch, j - 1, im), EB = cellv<WALLS>(B, ny, pitch, j - 1, ip);
+            const double WT = cellv<WALLS>(B, ny, pitch, j, im), ET = cellv<WALLS>(B, ny, pitch, j, ip);
+            gx = P.grad_mul ? (0.5 * ((WT - ET) + (WB - EB))) * P.r_n2dx
+                            : (0.5 * (WT - ET) + 0.5 * (WB - EB)) / (2 * (-P.dx));
+        }
+        if (xv != 0) gy = P.grad_mul ? (o - n) * P.r_ndy : (o - n) / (-P.dy);
+    }
+    const double avg = 0.5 * (o + n);
+    if (xu == 0 && xv == 0) return avg;
+    double g;
+    if (xu != 0 && xv != 0) g = sx(xu, gx) + sx(xv, gy);
+    else if (xu != 0) g = sx(xu, gx);
+    else g = sx(xv, gy);
+    return avg - P.hDt * g;
+}
+
 // ---------------------------------------------------------------------------
 // UW flux scheme (_FLUX_SCHEME_UW_ARK), periodic grids.
 //
@@ -452,11 +492,11 @@ __global__ void __launch_bounds__(256) k_faces_ac(Params P, State S) {
                 bh[q] = face_uw<false>(P, S.bh + qo, S.ghx + qo, S.ghy + qo, co, cn, xu, xv, lo);
             }
         } else if (xf) {
-            bf[q] = face_bh<true, WALLS>(P, S.bf + (size_t)q * S.qs, i, im, ip, j, xu, xv);
-            bh[q] = face_bh<true, WALLS>(P, S.bh + (size_t)q * S.qs, i, im, ip, j, xu, xv);
+            bf[q] = face_bh9<true, WALLS>(P, S.bf + (size_t)q * S.qs, i, im, ip, j, d2q9_xu(q), d2q9_xv(q));
+            bh[q] = face_bh9<true, WALLS>(P, S.bh + (size_t)q * S.qs, i, im, ip, j, d2q9_xu(q), d2q9_xv(q));
         } else {
-            bf[q] = face_bh<false, WALLS>(P, S.bf + (size_t)q * S.qs, i, im, ip, j, xu, xv);
-            bh[q] = face_bh<false, WALLS>(P, S.bh + (size_t)q * S.qs, i, im, ip, j, xu, xv);
+            bf[q] = face_bh9<false, WALLS>(P, S.bf + (size_t)q * S.qs, i, im, ip, j, d2q9_xu(q), d2q9_xv(q));
+            bh[q] = face_bh9<false, WALLS>(P, S.bh + (size_t)q * S.qs, i, im, ip, j, d2q9_xu(q), d2q9_xv(q));
         }
     }
     double Phi = 0, sumf = 0;
@@ -473,11 +513,14 @@ __global__ void __launch_bounds__(256) k_faces_ac(Params P, State S) {
         p = (sumf - bf[0]) * P.Kp;  // the u-dependent terms vanish with u = 0
         Mu = Rho * P.RT * P.Tau0;
     } else {
+        // first moments over the directions with a nonzero component (the others add +-0)
         double su = 0, sv = 0;
 #pragma unroll
-        for (int q = 0; q < 9; ++q) su += sx(d2q9_xu(q), bf[q]);
+        for (int q = 0; q < 9; ++q)
+            if (d2q9_xu(q) != 0) su += sx(d2q9_xu(q), bf[q]);
 #pragma unroll
-        for (int q = 0; q < 9; ++q) sv += sx(d2q9_xv(q), bf[q]);
+        for (int q = 0; q < 9; ++q)
+            if (d2q9_xv(q) != 0) sv += sx(d2q9_xv(q), bf[q]);
         const double inv = 1.0 / (Rho * P.RT);
         U = RDIV(su, Rho * P.RT, inv);
         V = RDIV(sv, Rho * P.RT, inv);
@@ -697,24 +740,52 @@ __global__ void __launch_bounds__(256) k_update(Params P, State S) {
     const bool xlo = P.uw && i == 0, ylo = P.uw && j == 0;
     for (int q = 0; q < Q; ++q) {
         const size_t oq = (size_t)q * S.qs, oy = (size_t)q * S.qsy;
+        // net flux E, N, W, S in the reference's order.  D2Q9 Allen-Cahn: the faces
+        // a direction runs along carry exactly 0 (k_faces_ac writes sx(0, .) = 0), so
+        // only the crossing faces are added (the zeros only decide the sign of a zero
+        // sum) and the rest direction has no flux term
+        const bool cx = !HASH || d2q9_xu(q) != 0, cy = !HASH || d2q9_xv(q) != 0;
         double s = 0.0;
-        s += -S.xff[oq + cE];
-        s += -S.yff[oy + cN];
-        s += xlo ? S.xlo_f[(size_t)q * P.ny + j] : S.xff[oq + c];
-        s += ylo ? S.ylo_f[(size_t)q * pitch + i] : S.yff[oy + c];
-        const double fn = P.aTP * S.bf[oq + c] - P.bTP * S.f[oq + c] + P.dtV * s;
+        if (cx && cy) {
+            s = -S.xff[oq + cE];
+            s += -S.yff[oy + cN];
+            s += xlo ? S.xlo_f[(size_t)q * P.ny + j] : S.xff[oq + c];
+            s += ylo ? S.ylo_f[(size_t)q * pitch + i] : S.yff[oy + c];
+        } else if (cx) {
+            s = -S.xff[oq + cE];
+            s += xlo ? S.xlo_f[(size_t)q * P.ny + j] : S.xff[oq + c];
+        } else if (cy) {
+            s = -S.yff[oy + cN];
+            s += ylo ? S.ylo_f[(size_t)q * pitch + i] : S.yff[oy + c];
+        }
+        const double fn = (cx || cy) ? P.aTP * S.bf[oq + c] - P.bTP * S.f[oq + c] + P.dtV * s
+                                     : P.aTP * S.bf[oq + c] - P.bTP * S.f[oq + c];
         S.f[oq + c] = fn;
         sumf += fn;
         if (q == 0) f0 = fn;
-        su += (MODEL == PP16) ? fn * P.xi_u[q] : sx(d2q9_xu(q), fn);
-        sv += (MODEL == PP16) ? fn * P.xi_v[q] : sx(d2q9_xv(q), fn);
+        if (MODEL == PP16) {
+            su += fn * P.xi_u[q];
+            sv += fn * P.xi_v[q];
+        } else {
+            if (!HASH || d2q9_xu(q) != 0) su += sx(d2q9_xu(q), fn);
+            if (!HASH || d2q9_xv(q) != 0) sv += sx(d2q9_xv(q), fn);
+        }
         if (HASH) {
             double t = 0.0;
-            t += -S.xfh[oq + cE];
-            t += -S.yfh[oy + cN];
-            t += xlo ? S.xlo_h[(size_t)q * P.ny + j] : S.xfh[oq + c];
-            t += ylo ? S.ylo_h[(size_t)q * pitch + i] : S.yfh[oy + c];
-            const double hn = P.aTP * S.bh[oq + c] - P.bTP * S.h[oq + c] + P.dtV * t;
+            if (cx && cy) {
+                t = -S.xfh[oq + cE];
+                t += -S.yfh[oy + cN];
+                t += xlo ? S.xlo_h[(size_t)q * P.ny + j] : S.xfh[oq + c];
+                t += ylo ? S.ylo_h[(size_t)q * pitch + i] : S.yfh[oy + c];
+            } else if (cx) {
+                t = -S.xfh[oq + cE];
+                t += xlo ? S.xlo_h[(size_t)q * P.ny + j] : S.xfh[oq + c];
+            } else if (cy) {
+                t = -S.yfh[oy + cN];
+                t += ylo ? S.ylo_h[(size_t)q * pitch + i] : S.yfh[oy + c];
+            }
+            const double hn = (cx || cy) ? P.aTP * S.bh[oq + c] - P.bTP * S.h[oq + c] + P.dtV * t
+                                         : P.aTP * S.bh[oq + c] - P.bTP * S.h[oq + c];
             S.h[oq + c] = hn;
             Phi += hn;
         }
