@@ -39,6 +39,9 @@ struct Params {
     // Reconstruction denominators as multipliers: -1/dx, -1/dy, 1/(2dy), 1/(-2dx).
     // grad_mul = 1 when dx and dy are powers of two, so x/d == x*(1/d) exactly.
     double r_ndx, r_ndy, r_2dy, r_n2dx;
+    // reciprocals RN(1/d) of divisors fixed per case, for the correctly rounded quotient
+    // qdiv_rn: 1/RT, 1/(6 2dx), 1/(6 2dy), 1/(6 MinL MinL), 1/(W (PhiL - PhiV)), 1/(RT dt)
+    double r_RT, r_g6x, r_g6y, r_lap, r_wI, r_RTdt;
     int grad_mul, uw;                              // uw: upwind face reconstruction (DUGKS_FLUX_UW)
     double c16;                                    // D2V16 lattice speed
     double xi_u[16], xi_v[16], omega[16];

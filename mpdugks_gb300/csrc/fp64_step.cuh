@@ -130,7 +130,7 @@ __device__ __forceinline__ void d2v16_eq(const Params &P, double rho, double u, 
 // D2Q9PP equilibrium (Ark/Lib/D2Q9PP.cpp:51-62).
 __device__ __forceinline__ void d2q9pp_eq(const Params &P, double rho, double U, double V, double *eq) {
     const double uu = U * U + V * V;
-    const double invRT = 1.0 / P.RT;
+    const double invRT = P.r_RT;
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
         const int xu = d2q9_xu(q), xv = d2q9_xv(q);
@@ -159,11 +159,14 @@ __device__ __forceinline__ void calc_psi(const Params &P, double rho, double p, 
 }
 
 // 8-neighbour isotropic gradient (Ark/Lib/GradSchemeBasic.h:153-208).
-__device__ __forceinline__ double iso_gx(double E, double W, double NE, double NW, double SE, double SW, double d2) {
-    return (4 * (E - W) + 1 * (NE - NW + SE - SW)) / (d2 * 6);
+// r: RN(1/(d2 6)) (Params r_g6x / r_g6y)
+__device__ __forceinline__ double iso_gx(double E, double W, double NE, double NW, double SE, double SW, double d2,
+                                         double r) {
+    return QDIV(4 * (E - W) + 1 * (NE - NW + SE - SW), d2 * 6, r);
 }
-__device__ __forceinline__ double iso_gy(double N, double S, double NE, double NW, double SE, double SW, double d2) {
-    return (4 * (N - S) + 1 * (NE - SE + NW - SW)) / (d2 * 6);
+__device__ __forceinline__ double iso_gy(double N, double S, double NE, double NW, double SE, double SW, double d2,
+                                         double r) {
+    return QDIV(4 * (N - S) + 1 * (NE - SE + NW - SW), d2 * 6, r);
 }
 
 // ---------------------------------------------------------------------------
@@ -185,9 +188,9 @@ __device__ __forceinline__ void macro_source(const Params &P, const State &S, in
     };
     const double E = at(j, ip), W = at(j, im), N = at(j + 1, i), Sd = at(j - 1, i);
     const double NE = at(j + 1, ip), NW = at(j + 1, im), SW = at(j - 1, im), SE = at(j - 1, ip);
-    double Phi_x = iso_gx(E, W, NE, NW, SE, SW, P._2dx);
-    double Phi_y = iso_gy(N, Sd, NE, NW, SE, SW, P._2dy);
-    const double lap = (4 * (E + N + W + Sd) + (NE + NW + SW + SE) - 20 * phi) / (6 * P.MinL * P.MinL);
+    double Phi_x = iso_gx(E, W, NE, NW, SE, SW, P._2dx, P.r_g6x);
+    double Phi_y = iso_gy(N, Sd, NE, NW, SE, SW, P._2dy, P.r_g6y);
+    const double lap = QDIV(4 * (E + N + W + Sd) + (NE + NW + SW + SE) - 20 * phi, 6 * P.MinL * P.MinL, P.r_lap);
     SetZero(Phi_x);
     SetZero(Phi_y);
     const double F = 2 * P.Beta * (phi - P.PhiL) * (phi - P.PhiV) * (2 * phi - P.PhiL - P.PhiV) - P.Kappa * lap;
@@ -199,12 +202,13 @@ __device__ __forceinline__ void macro_source(const Params &P, const State &S, in
     const double L = sqrt(Phi_x * Phi_x + Phi_y * Phi_y);
     const double dU = phi * U - ppu_old, dV = phi * V - ppv_old;
     if (L != 0) {
-        const double tmp = -4 * (phi - P.PhiL) * (phi - P.PhiV) / (P.wI * (P.PhiL - P.PhiV));
-        srcx = Phi_x * tmp / L + dU / (P.RT * P.dt);
-        srcy = Phi_y * tmp / L + dV / (P.RT * P.dt);
+        const double tmp = QDIV(-4 * (phi - P.PhiL) * (phi - P.PhiV), P.wI * (P.PhiL - P.PhiV), P.r_wI);
+        const double rL = 1.0 / L;
+        srcx = QDIV(Phi_x * tmp, L, rL) + QDIV(dU, P.RT * P.dt, P.r_RTdt);
+        srcy = QDIV(Phi_y * tmp, L, rL) + QDIV(dV, P.RT * P.dt, P.r_RTdt);
     } else {
-        srcx = dU / (P.RT * P.dt);
-        srcy = dV / (P.RT * P.dt);
+        srcx = QDIV(dU, P.RT * P.dt, P.r_RTdt);
+        srcy = QDIV(dV, P.RT * P.dt, P.r_RTdt);
     }
 }
 
@@ -248,7 +252,7 @@ __global__ void __launch_bounds__(256) k_collide(Params P, State S, int do_msrc,
             if (j == 0) S.gphi[(size_t)(gout * 2 + 0) * pitch + i] = 2.0 * phi - S.fld[F_PHI][c + pitch];
             if (j == P.ny - 1) S.gphi[(size_t)(gout * 2 + 1) * pitch + i] = 2.0 * phi - S.fld[F_PHI][c - pitch];
         }
-        const double invRT = 1.0 / P.RT;
+        const double invRT = P.r_RT;
         const double pRT = QDIV(p, P.RT, invRT);
         const double uu = U * U + V * V;
         // (xi.a)/RT for xi in {0,+-1}^2 takes 4 distinct magnitudes; (-x)/RT == -(x/RT)
@@ -292,8 +296,8 @@ __global__ void __launch_bounds__(256) k_collide(Params P, State S, int do_msrc,
             const int im = wrapi(i - 1, nx), ip = wrapi(i + 1, nx), jm = wrapi(j - 1, ny), jp = wrapi(j + 1, ny);
             const double *__restrict__ PS = S.fld[F_PSI];
             auto at = [&](int jj, int ii) { return PS[(size_t)jj * pitch + ii]; };
-            const double gx = iso_gx(at(j, ip), at(j, im), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dx);
-            const double gy = iso_gy(at(jp, i), at(jm, i), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dy);
+            const double gx = iso_gx(at(j, ip), at(j, im), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dx, P.r_g6x);
+            const double gy = iso_gy(at(jp, i), at(jm, i), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dy, P.r_g6y);
             const double k = -S.fld[F_SCG][c] * at(j, i);
             fx = gx * k;
             fy = gy * k;
@@ -523,13 +527,14 @@ __global__ void __launch_bounds__(256) k_faces_ac(Params P, State S) {
 #pragma unroll
     for (int q = 0; q < 9; ++q) sumf += bf[q];
     const double Rho = P.aPhi * Phi + P.bPhi;
-    const double invRT = 1.0 / P.RT;
-    double U, V, p, Mu;
+    const double invRT = P.r_RT;
+    double U, V, p, Mu, tauh;
     if (MODEL == AC) {
         U = 0.0;
         V = 0.0;
         p = (sumf - bf[0]) * P.Kp;  // the u-dependent terms vanish with u = 0
         Mu = Rho * P.RT * P.Tau0;
+        tauh = Mu / (Rho * P.RT);
     } else {
         // first moments over the directions with a nonzero component (the others add +-0)
         double su = 0, sv = 0;
@@ -547,8 +552,8 @@ __global__ void __launch_bounds__(256) k_faces_ac(Params P, State S) {
         p = sumf + 0.5 * P.hDt * P.RT * (Rho_x * U + Rho_y * V);
         Mu = P.NuV + (Phi - P.PhiV) * (P.NuL - P.NuV);
         Mu *= Rho;
+        tauh = QDIV(Mu, Rho * P.RT, inv);
     }
-    const double tauh = Mu / (Rho * P.RT);
     const double ah = 2.0 * tauh / (2.0 * tauh + P.hDt), bh_ = 1.0 - ah, ch = tauh * bh_;
     const double uu = U * U + V * V;
     const double pRT = QDIV(p, P.RT, invRT);
@@ -713,8 +718,8 @@ __global__ void __launch_bounds__(256) k_faces_pp2(Params P, State S) {
     const size_t c = (size_t)j * pitch + i;
     const double *__restrict__ PS = xf ? S.xpsi : S.ypsi;
     auto at = [&](int jj, int ii) { return PS[(size_t)jj * pitch + ii]; };
-    const double gx = iso_gx(at(j, ip), at(j, im), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dx);
-    const double gy = iso_gy(at(jp, i), at(jm, i), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dy);
+    const double gx = iso_gx(at(j, ip), at(j, im), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dx, P.r_g6x);
+    const double gy = iso_gy(at(jp, i), at(jm, i), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dy, P.r_g6y);
     const double k = -(xf ? S.xscg : S.yscg)[c] * at(j, i);
     const double Fx = gx * k, Fy = gy * k;
     (xf ? S.xfFx : S.yfFx)[c] = Fx;
@@ -810,12 +815,13 @@ __global__ void __launch_bounds__(256) k_update(Params P, State S) {
     }
     if (MODEL == AC || MODEL == HCZ) {
         const double Rho = P.aPhi * Phi + P.bPhi;
-        double U, V, p, Mu;
+        double U, V, p, Mu, tau;
         if (MODEL == AC) {
             U = 0.0;
             V = 0.0;
             p = (sumf - f0) * P.Kp;  // (hDt rho_x.u - rho w0 |u|^2 lambda) vanishes with u = 0
             Mu = Rho * P.RT * P.Tau0;
+            tau = Mu / (Rho * P.RT);
         } else {
             const double inv = 1.0 / (Rho * P.RT);
             U = QDIV(su, Rho * P.RT, inv);
@@ -825,18 +831,20 @@ __global__ void __launch_bounds__(256) k_update(Params P, State S) {
             p = sumf + P.hDt * (S.fld[F_RHOX][c] * U + S.fld[F_RHOY][c] * V) * P.RT;
             Mu = P.NuV + (Phi - P.PhiV) * (P.NuL - P.NuV);
             Mu *= Rho;
+            tau = QDIV(Mu, Rho * P.RT, inv);
         }
         S.fld[F_PHI][c] = Phi;
         S.fld[F_RHO][c] = Rho;
         S.fld[F_U][c] = U;
         S.fld[F_V][c] = V;
         S.fld[F_P][c] = p;
-        S.fld[F_TAU][c] = Mu / (Rho * P.RT);
+        S.fld[F_TAU][c] = tau;
     } else {
         const double Rho = sumf;
-        double U = su / Rho, V = sv / Rho;
-        U += P.hDt * S.fld[F_FX][c] / Rho;
-        V += P.hDt * S.fld[F_FY][c] / Rho;
+        const double invR = 1.0 / Rho;
+        double U = QDIV(su, Rho, invR), V = QDIV(sv, Rho, invR);
+        U += QDIV(P.hDt * S.fld[F_FX][c], Rho, invR);
+        V += QDIV(P.hDt * S.fld[F_FY][c], Rho, invR);
         const double p = 1.0 * cs_pressure(P, Rho);
         double scg, psi;
         calc_psi(P, Rho, p, scg, psi);
@@ -875,8 +883,8 @@ __global__ void __launch_bounds__(256) k_finalize(Params P, State S, int gin) {
         const int im = wrapi(i - 1, nx), ip = wrapi(i + 1, nx), jm = wrapi(j - 1, ny), jp = wrapi(j + 1, ny);
         const double *__restrict__ PS = S.fld[F_PSI];
         auto at = [&](int jj, int ii) { return PS[(size_t)jj * pitch + ii]; };
-        const double gx = iso_gx(at(j, ip), at(j, im), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dx);
-        const double gy = iso_gy(at(jp, i), at(jm, i), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dy);
+        const double gx = iso_gx(at(j, ip), at(j, im), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dx, P.r_g6x);
+        const double gy = iso_gy(at(jp, i), at(jm, i), at(jp, ip), at(jp, im), at(jm, ip), at(jm, im), P._2dy, P.r_g6y);
         const double k = -S.fld[F_SCG][c] * at(j, i);
         S.fld[F_FX][c] = gx * k;
         S.fld[F_FY][c] = gy * k;

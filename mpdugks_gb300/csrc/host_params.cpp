@@ -89,6 +89,15 @@ void derive_params(const dugks_case_t &cs, const dugks_grid_t &g, Params &P) {
         P.r_2dy = 1.0 / (2 * P.dy);
         P.r_n2dx = 1.0 / (2 * (-P.dx));
     }
+    {   // reciprocals of the divisors the device forms with the same expressions (IEEE
+        // double here and there, so the same divisors and the same reciprocals)
+        P.r_RT = 1.0 / P.RT;
+        P.r_g6x = 1.0 / (P._2dx * 6);
+        P.r_g6y = 1.0 / (P._2dy * 6);
+        P.r_lap = 1.0 / (6 * P.MinL * P.MinL);
+        P.r_wI = 1.0 / (P.wI * (P.PhiL - P.PhiV));
+        P.r_RTdt = 1.0 / (P.RT * P.dt);
+    }
     P.uw = cs.flux_scheme == DUGKS_FLUX_UW ? 1 : 0;
     P.nee = (cs.wall_scheme == DUGKS_WALL_NEE && g.y_walls) ? 1 : 0;
     P.T_CS = cs.Tr * cs.Tc_CS;
