@@ -500,8 +500,9 @@ static int macros_fp32(dugks_handle *h) {
 // the handle's stream); DUGKS_ETIMEOUT once one did not
 static int stage_loads_ok(dugks_handle *h) {
     if (!h->kerr) return DUGKS_OK;
-    int v = 0;
-    cudaError_t e = cudaMemcpy(&v, h->kerr, sizeof v, cudaMemcpyDeviceToHost);
+    int v = 0;  // on the handle's stream (the callers have just synchronised it)
+    cudaError_t e = cudaMemcpyAsync(&v, h->kerr, sizeof v, cudaMemcpyDeviceToHost, h->last_stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->last_stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "stage-load status");
     return v ? fail(h, DUGKS_ETIMEOUT, "a TMA stage load of the streaming step did not complete") : DUGKS_OK;
 }
