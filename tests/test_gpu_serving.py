@@ -28,6 +28,8 @@ MIX = [
     (lambda: ac_case(Sigma=5e-3, RhoV=0.5), 130, 70, False, 'ac_drop', [15.0], 61),
     (lambda: ac_case('fp64'), 48, 48, False, 'ac_drop_inside', [10.0], 40),
     (lambda: ac_case(RhoV=0.02), 200, 40, False, 'ac_drop_inside', [12.0], 203),
+    # under 8 rows: the batch lane's tile kernel, in the same model group as streaming items
+    (lambda: ac_case(), 40, 6, False, 'ac_drop_inside', [2.0], 45),
     # pseudopotential FP32 cases: solo lanes, concurrently
     (lambda: pp_case('PP16'), 40, 40, False, 'scmp_drop', [], 80),
     (lambda: pp_case('PP9'), 48, 48, False, 'pp_noise', [0.2, 0.01], 90),
@@ -129,12 +131,17 @@ def test_cancel_and_oversized_submit():
     (lambda: rt_case(), 560, 3300, True, 'ac_rt', [3.0, 0.1, 1e-4], 41),
     # ragged: a last strip of 25 columns, a last segment of 27 rows
     (lambda: rt_case(), 1117, 1531, True, 'ac_rt', [0.7, 0.1, 1e-4], 23),
+    # small: the single-case step runs the tile kernel, the server the batched streaming kernel
+    (lambda: rt_case(), 64, 128, True, 'ac_rt', [1.0, 0.1, 1e-4], 29),
+    # under 8 rows: the tile kernel on both sides (batched in the server)
+    (lambda: ac_case(), 40, 6, False, 'ac_drop_inside', [2.0], 31),
 ])
 def test_streaming_kernel_equals_the_tile_kernel(item):
-    """Single-case FP32 steps on a grid of more strip segments than resident warps
-    run the streaming kernel (warps marching 28-column strips through row
-    segments); the server runs the tile kernel.  With walls and without, they
-    agree bit for bit."""
+    """A case solved by the server (batched streaming kernel k_streamb32; the batched
+    tile kernel for cases under 8 rows) against the same case stepped alone (the
+    streaming kernel k_stream32, with TMA row loads, where the grid has more strip
+    segments than resident warps; the tile kernel otherwise).  With walls and
+    without, they agree bit for bit."""
     from mpdugks_gb300 import capi
     f, nx, ny, w, init, params, n = item
     srv = capi.Server(chunk_steps=16)
