@@ -443,15 +443,20 @@ def scheme_variants_bench(steps: int = 20) -> dict:
 # ---------------------------------------------------------------- GPU arms
 
 def field_errors(a, b):
-    """Per-field max-norm and L2 error of case a against case b, relative to b."""
+    """Per-field max-norm and L2 error of case a against case b, relative to b (linf, l2),
+    and the max-norm difference in lattice units (linf_abs) beside the field's max-norm
+    (max_abs): a velocity that starts from rest is tiny after a few steps, and its
+    relative error says little on its own."""
     import numpy as np
     out = {}
     for k in ('rho', 'u', 'v', 'p', 'phi'):
         x, y = a.get(k), b.get(k)
         d = x - y
         ny = float(np.max(np.abs(y)))
-        out[k] = {'linf': float(np.max(np.abs(d))) / ny if ny else float(np.max(np.abs(d))),
-                  'l2': float(np.linalg.norm(d) / np.linalg.norm(y)) if ny else 0.0}
+        dmax = float(np.max(np.abs(d)))
+        out[k] = {'linf': dmax / ny if ny else dmax,
+                  'l2': float(np.linalg.norm(d) / np.linalg.norm(y)) if ny else 0.0,
+                  'linf_abs': dmax, 'max_abs': ny}
     return out
 
 
