@@ -272,12 +272,13 @@ __global__ void __launch_bounds__(256) k_collide(Params P, State S, int do_msrc,
             } else {
                 const double u1 = ur.get(xu, xv);
                 const double G = u1 + 0.5 * u1 * u1 - uu * P.Lambda0;
-                const double cu = (double)xu - U, cv = (double)xv - V;
+                const double cu = xu == 0 ? -U : (double)xu - U, cv = xv == 0 ? -V : (double)xv - V;  // 0 - U as -U
                 hEq = w * (1.0 + u1) * phi;
                 fEq = w * (p + rho * G * P.RT);
                 fSo = w * ((1 + G) * (cu * fx + cv * fy) + G * P.RT * (cu * rhox + cv * rhoy));
             }
-            const double hSo = (sx(xu, srcx) + sx(xv, srcy)) * w;
+            const double hSo = (xu != 0 && xv != 0 ? sx(xu, srcx) + sx(xv, srcy)
+                                                : (xu != 0 ? sx(xu, srcx) : sx(xv, srcy))) * w;
             const size_t o = (size_t)q * S.qs + c;
             if (WALLS && P.nee && (j == 0 || j == P.ny - 1)) {  // kept for the NEE wall faces
                 const size_t wq = ((size_t)(j == 0 ? 0 : 1) * 9 + q) * pitch + i, ws = (size_t)2 * 9 * pitch;
@@ -574,12 +575,13 @@ __global__ void __launch_bounds__(256) k_faces_ac(Params P, State S) {
         } else {
             const double u1 = ur.get(xu, xv);
             const double G = u1 + 0.5 * u1 * u1 - uu * P.Lambda0;
-            const double cu = (double)xu - U, cv = (double)xv - V;
+            const double cu = xu == 0 ? -U : (double)xu - U, cv = xv == 0 ? -V : (double)xv - V;  // 0 - U as -U
             hEq = w * Phi * (1.0 + u1);
             fEq = w * (p + Rho * P.RT * G);
             fSo = w * ((1 + G) * (cu * Fx + cv * Fy) + G * P.RT * (cu * Rho_x + cv * Rho_y));
         }
-        const double hSo = (sx(xu, Phi_x) + sx(xv, Phi_y)) * w;
+        const double hSo = (xu != 0 && xv != 0 ? sx(xu, Phi_x) + sx(xv, Phi_y)
+                                                : (xu != 0 ? sx(xu, Phi_x) : sx(xv, Phi_y))) * w;
         hh[q] = P.h_ah * bh[q] + P.h_bh * hEq + P.h_ch * hSo;
         hf[q] = ah * bf[q] + bh_ * fEq + ch * fSo;
     }
@@ -602,6 +604,7 @@ __global__ void __launch_bounds__(256) k_faces_ac(Params P, State S) {
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
         const int s = xf ? d2q9_xu(q) : d2q9_xv(q);
+        if (s == 0) continue;  // no flux along the face: the update does not read these slots
         outf[(size_t)q * qs + c] = sx(s, hf[q]);
         outh[(size_t)q * qs + c] = sx(s, hh[q]);
     }
@@ -764,9 +767,9 @@ __global__ void __launch_bounds__(256) k_update(Params P, State S) {
     for (int q = 0; q < Q; ++q) {
         const size_t oq = (size_t)q * S.qs, oy = (size_t)q * S.qsy;
         // net flux E, N, W, S in the reference's order.  D2Q9 Allen-Cahn: the faces
-        // a direction runs along carry exactly 0 (k_faces_ac writes sx(0, .) = 0), so
-        // only the crossing faces are added (the zeros only decide the sign of a zero
-        // sum) and the rest direction has no flux term
+        // a direction runs along carry no flux (xi.n = 0: the reference adds exact zeros,
+        // which only decide the sign of a zero sum; k_faces_ac does not store them), so
+        // only the crossing faces are added and the rest direction has no flux term
         const bool cx = !HASH || d2q9_xu(q) != 0, cy = !HASH || d2q9_xv(q) != 0;
         double s = 0.0;
         if (cx && cy) {
