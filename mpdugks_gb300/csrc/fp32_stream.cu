@@ -4,7 +4,8 @@
 // fp32_stream.cuh; k_stream32 keeps its own copy of that item body, written out in
 // the kernel (the shared stream_item, inlined here, gave 4 more registers and a 1.4 %
 // slower step on 8192^2 cells), so a change to the per-item steps is made in both:
-// tests/test_gpu_serving.py checks the two bit for bit.
+// tests/test_gpu_serving.py checks the two bit for bit, tests/test_stream_item_copies.py
+// that the two texts differ only where they must.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
