@@ -19,7 +19,6 @@
 namespace dugks {
 #define DUGKS_DECLARE_FP64(NS)                                                                                  \
     namespace NS {                                                                                              \
-    void set_d2v16_matrix(const double *m256, cudaStream_t st);                                                 \
     void launch_fp64_step(const Params &P, const State &S, int do_msrc, int gin, int gout, cudaStream_t st,     \
                           int64_t *launches, cudaEvent_t *ev);                                                  \
     void launch_fp64_finalize(const Params &P, const State &S, int gin, cudaStream_t st, int64_t *launches);   \
@@ -48,7 +47,6 @@ cudaError_t stream_tensor_map(void *map_out, float *base, int nx, int ny, int pi
 cudaError_t launch_pp32_step(const PPP &P, const PPS &S, int do_msrc, cudaStream_t st, int64_t *launches,
                              uint32_t step);
 cudaError_t launch_pp32_force(const PPP &P, const PPS &S, cudaStream_t st, int64_t *launches);
-void set_d2v16_matrix_f32(const double *m256, cudaStream_t st);
 template <typename R>
 cudaError_t launch_plane_from_f64(R *dst, int dpitch, const double *src, int nx, int ny, double sub,
                                   cudaStream_t st, int64_t *launches);
@@ -208,6 +206,7 @@ static size_t fp64_arena_bytes(const Params &P) {
         total += 4 * Q * cellb + 2 * align256(sizeof(double) * Q * P.ny) + 2 * Q * rowb;
     total += cellb;                               // rho_last
     total += align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 256 + 256;
+    if (P.model == PP16) total += align256(sizeof(double) * 256);  // the case's D2V16 inverse moment matrix
     return total;
 }
 
@@ -217,7 +216,8 @@ static cudaError_t to_dev(const dugks_handle *h, double *d, const double *src, i
 static size_t pp32_arena_bytes(const Params &P) {
     const size_t cf = align256((size_t)P.pitch * P.ny * sizeof(float));
     const size_t cd = align256((size_t)P.pitch * P.ny * sizeof(double));
-    return (6 * (size_t)P.Q + 18) * cf + 6 * cd + align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 512;
+    return (6 * (size_t)P.Q + 18) * cf + 6 * cd + align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 512 +
+           (P.model == PP16 ? align256(sizeof(float) * 256) : 0);
 }
 
 // a double as the unevaluated float sum hi + lo (about 48 significant bits)
@@ -305,7 +305,20 @@ static int create_pp32(dugks_handle *h, dugks_handle_t **out) {
         C.xi_v[q] = (float)P.xi_v[q];
     }
     for (int q = 0; q < 9; ++q) C.w9[q] = (float)P.omega[q];
-    if (P.model == PP16) f32::set_d2v16_matrix_f32(&h->iM[0][0], nullptr);
+    C.iM16 = nullptr;
+    if (P.model == PP16) {
+        // this case's inverse moment matrix, in FP32, after the flag word
+        float m[256];
+        for (int k = 0; k < 256; ++k) m[k] = (float)(&h->iM[0][0])[k];
+        float *dm = reinterpret_cast<float *>(cur + 256);
+        e = cudaMemcpy(dm, m, sizeof m, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(h->arena);
+            delete h;
+            return fail(nullptr, DUGKS_ECUDA, std::string("device setup failed: ") + cudaGetErrorString(e));
+        }
+        C.iM16 = dm;
+    }
     e = cudaStreamSynchronize(nullptr);
     if (e != cudaSuccess) {
         cudaFree(h->arena);
@@ -602,9 +615,16 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
     h->partial = take(align256(sizeof(double) * 4 * h->nblocks));
     h->out4 = take(256);
     h->flag = reinterpret_cast<int *>(take(256));
+    P.iM16 = nullptr;
     if (P.model == PP16) {
-        exact::set_d2v16_matrix(&h->iM[0][0], nullptr);
-        fast::set_d2v16_matrix(&h->iM[0][0], nullptr);
+        double *dm = take(align256(sizeof(double) * 256));
+        e = cudaMemcpy(dm, &h->iM[0][0], sizeof(double) * 256, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(h->arena);
+            delete h;
+            return fail(nullptr, DUGKS_ECUDA, std::string("device setup failed: ") + cudaGetErrorString(e));
+        }
+        P.iM16 = dm;
     }
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {

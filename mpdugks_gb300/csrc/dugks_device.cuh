@@ -44,6 +44,9 @@ struct Params {
     double r_RT, r_g6x, r_g6y, r_lap, r_wI, r_RTdt;
     int grad_mul, uw;                              // uw: upwind face reconstruction (DUGKS_FLUX_UW)
     double c16;                                    // D2V16 lattice speed
+    // D2V16 inverse moment matrix of this case, [16][16] in the case's device memory
+    // (Ark/Lib/D2V16.cpp:34-52): each case holds its own
+    const double *iM16;
     double xi_u[16], xi_v[16], omega[16];
     int bb[16];
 };

@@ -30,21 +30,14 @@
 namespace dugks {
 namespace f32 {
 
-__constant__ float c_iM16f[16][16];  // D2V16 inverse moment matrix (Ark/Lib/D2V16.cpp:34-52), FP32
-
-void set_d2v16_matrix_f32(const double *m256, cudaStream_t st) {
-    float m[256];
-    for (int k = 0; k < 256; ++k) m[k] = (float)m256[k];
-    cudaMemcpyToSymbolAsync(c_iM16f, m, sizeof(m), 0, cudaMemcpyHostToDevice, st);
-    cudaStreamSynchronize(st);  // m is on the stack
-}
-
 // Equilibrium deviations de_q = eq_q(rho, u, v) - f_rest_q.
 template <int MODEL>
 __device__ __forceinline__ void pp_deq(const PPP &P, float dr, float rho, float u, float v, float *de) {
     if (MODEL == PP16) {
         // Macro16 (Ark/Lib/D2V16.cpp:125-145) at T = T0, p = rho RT, minus its value at
-        // (rho_ref, 0, 0): linear in rho at rest
+        // (rho_ref, 0, 0): linear in rho at rest; times the case's inverse moment matrix
+        // (Ark/Lib/D2V16.cpp:34-52), read through the read-only path (every lane of a warp
+        // reads the same entry)
         const float RT = P.RT, u2 = u * u, v2 = v * v, s2 = u2 + v2;
         float M[16];
         M[0] = dr;
@@ -67,7 +60,7 @@ __device__ __forceinline__ void pp_deq(const PPP &P, float dr, float rho, float 
         for (int j = 0; j < 16; ++j) {
             float s = 0.f;
 #pragma unroll
-            for (int k = 0; k < 16; ++k) s = fmaf(c_iM16f[j][k], M[k], s);
+            for (int k = 0; k < 16; ++k) s = fmaf(__ldg(P.iM16 + j * 16 + k), M[k], s);
             de[j] = s;
         }
     } else {
@@ -220,8 +213,10 @@ __global__ void __launch_bounds__(256) k_pp32_faces1(PPP P, PPS S) {
     const int nx = P.nx, ny = P.ny, pitch = P.pitch;
     const int im = wrapi(i - 1, nx), ip = wrapi(i + 1, nx), jm = wrapi(j - 1, ny), jp = wrapi(j + 1, ny);
     const size_t c = (size_t)j * pitch + i;
-    FF sR{0.f, 0.f};
-    float su = 0.f, sv = 0.f;
+    // face moments as float-float sums: the first moments are small differences of the
+    // large deviations of opposite directions (liquid cells lie far from rho_ref), so a
+    // plain FP32 sum loses most of the face velocity's digits
+    FF sR{0.f, 0.f}, su{0.f, 0.f}, sv{0.f, 0.f};
     float *B = xf ? S.xb : S.yb;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -242,13 +237,13 @@ __global__ void __launch_bounds__(256) k_pp32_faces1(PPP P, PPS S) {
         const float b = 0.5f * (o + n) - P.hDt * (gx * P.xi_u[q] + gy * P.xi_v[q]);
         B[(size_t)q * S.qs + c] = b;
         ff_acc(sR, b);
-        su += b * P.xi_u[q];
-        sv += b * P.xi_v[q];
+        ff_acc_prod(su, b, P.xi_u[q]);
+        ff_acc_prod(sv, b, P.xi_v[q]);
     }
     sR = ff_norm(sR);
     const FF R = ff_add(FF{P.rref_hi, P.rref_lo}, sR);
     const float Rf = R.hi;
-    float U = su / Rf, V = sv / Rf;
+    float U = __fadd_rn(su.hi, su.lo) / Rf, V = __fadd_rn(sv.hi, sv.lo) / Rf;
     U += 0.5f * P.hDt * (xf ? S.xFx : S.yFx)[c] / Rf;
     V += 0.5f * P.hDt * (xf ? S.xFy : S.yFy)[c] / Rf;
     const FF p = cs_p(P, R);

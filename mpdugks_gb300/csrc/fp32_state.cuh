@@ -66,6 +66,9 @@ struct PPP {
     // rho_ref, R0 T_CS, aCS, RT
     float rref_hi, rref_lo, rtcs_hi, rtcs_lo, acs_hi, acs_lo, rt_hi, rt_lo;
     float xi_u[16], xi_v[16], w9[9], frest[16];
+    // D2V16 inverse moment matrix of this case ([16][16], in the case's device memory):
+    // each case holds its own, so cases of different lattice speed run side by side
+    const float *iM16;
 };
 // State: f deviations and the step's scratch in FP32, the density (and the
 // pressure for output) in FP64.

@@ -39,7 +39,6 @@
 namespace dugks {
 namespace DUGKS_KNS {
 
-__constant__ double c_iM16[16][16];  // D2V16 inverse moment matrix (Ark/Lib/D2V16.cpp:34-52)
 
 // x / d rounded to nearest, from y = RN(1/d): q0 = RN(x y) lies within an ulp of x / d,
 // the residual r = x - d q0 is exact in one fused multiply-add, and RN(q0 + r y) is the
@@ -122,7 +121,7 @@ __device__ __forceinline__ void d2v16_eq(const Params &P, double rho, double u, 
     for (int j = 0; j < 16; ++j) {
         double s = 0;
 #pragma unroll
-        for (int k = 0; k < 16; ++k) s += c_iM16[j][k] * M[k];
+        for (int k = 0; k < 16; ++k) s += __ldg(P.iM16 + j * 16 + k) * M[k];
         eq[j] = s;
     }
 }
@@ -954,9 +953,6 @@ __global__ void k_check_finite(const double *__restrict__ a, size_t n, int *flag
 
 // ---------------------------------------------------------------------------
 // Host-side launch helpers (called from capi.cu).
-void set_d2v16_matrix(const double *m256, cudaStream_t st) {
-    cudaMemcpyToSymbolAsync(c_iM16, m256, sizeof(double) * 256, 0, cudaMemcpyHostToDevice, st);
-}
 
 template <int MODEL, bool WALLS>
 static void launch_step_t(const Params &P, const State &S, int do_msrc, int gin, int gout, cudaStream_t st,

@@ -74,3 +74,27 @@ def test_fp32_pseudopotential_fields_and_distributions():
     for k in ('fx', 'fy', 'psi'):
         x, y = a.get(k), b.get(k)
         assert np.max(np.abs(x - y)) <= 1e-4 * np.max(np.abs(y)), k
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'fp32dev'])
+def test_d2v16_cases_of_different_lattice_speed_side_by_side(precision):
+    """Each D2V16 case holds its own inverse moment matrix: two live cases with lattice
+    speeds 0.5 and 0.6, stepped alternately, give what each gives alone."""
+    from mpdugks_gb300 import capi
+
+    def case(c):
+        g = capi.GpuCase(capi.make_case('PP16', precision, d2v16_c=c), 32, 32, False)
+        g.init('pp_noise', [0.2, 0.01], seed=5)
+        return g
+    alone = {}
+    for c in (0.5, 0.6):
+        g = case(c)
+        g.step(20)
+        alone[c] = {k: g.get(k) for k in ('rho', 'u', 'v')}
+    a, b = case(0.5), case(0.6)
+    for _ in range(10):
+        a.step(2)
+        b.step(2)
+    for c, g in ((0.5, a), (0.6, b)):
+        for k in ('rho', 'u', 'v'):
+            assert np.array_equal(g.get(k), alone[c][k]), (c, k)
