@@ -51,6 +51,9 @@ template <typename R>
 cudaError_t launch_plane_from_f64(R *dst, int dpitch, const double *src, int nx, int ny, double sub,
                                   cudaStream_t st, int64_t *launches);
 template <typename R>
+cudaError_t launch_phase_from_f64(R *g, R *phi, size_t qs, int pitch, const double *h, int nx, int ny,
+                                  cudaStream_t st, int64_t *launches);
+template <typename R>
 void launch_out_forces(const PR<R> &P, const SR<R> &S, const double *phi, const double *rho, int opitch, int first,
                        double *tau, double *fx, double *fy, cudaStream_t st, int64_t *launches);
 inline cudaError_t launch_stepX(const P32 &P, const S32 &S, int a, int b, int c, cudaStream_t st, int64_t *l,
@@ -175,7 +178,6 @@ static double f_rest(const Params &P, int q) {
     if (P.model == AC) return P.omega[q] * p0 / P.RT - (q == 0 ? p0 / P.RT : 0.0);
     return P.omega[q] * p0;
 }
-static double h_rest(const Params &P, int q) { return P.omega[q] * DUGKS_F32_PHI0; }
 
 constexpr int REDUCE_BLOCKS = 152 * 4;
 
@@ -184,7 +186,7 @@ static size_t fused_arena_bytes(const Params &P, size_t rsize) {
     const size_t rowf = (size_t)P.pitch * rsize;
     const size_t cellf = align256(rowf * P.ny);
     const size_t celld = align256((size_t)P.pitch * sizeof(double) * P.ny);
-    return 2 * (18 + f32::A_N) * cellf + f32::I_N * cellf + align256(4 * rowf) +
+    return 2 * f32::PL_N * cellf + f32::I_N * cellf + align256(f32::GPHI_ROWS * rowf) +
            6 * celld /* rho u v p phi + rho_last */ + align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 512;
 }
 
@@ -408,14 +410,12 @@ static int create_fused(dugks_handle *h, dugks_handle_t **out, f32::PR<R> &PQ, f
     auto takef = [&](size_t b) { R *p = reinterpret_cast<R *>(cur); cur += b; return p; };
     auto taked = [&](size_t b) { double *p = reinterpret_cast<double *>(cur); cur += b; return p; };
     S.qs = cellf / sizeof(R);
-    S.df = takef(9 * cellf);
-    S.dh = takef(9 * cellf);
-    S.aux = takef(f32::A_N * cellf);
-    S.odf = takef(9 * cellf);
-    S.odh = takef(9 * cellf);
-    S.oaux = takef(f32::A_N * cellf);
+    // two state copies of PL_N planes each (f, g, the phi pair, aux; fp32_state.cuh)
+    R *copy0 = takef(f32::PL_N * cellf), *copy1 = takef(f32::PL_N * cellf);
+    f32::set_copy(copy0, S.qs, S.df, S.dg, S.phi, S.aux);
+    f32::set_copy(copy1, S.qs, S.odf, S.odg, S.ophi, S.oaux);
     S.init = takef(f32::I_N * cellf);
-    S.gphi = takef(align256(4 * rowf));
+    S.gphi = takef(align256(f32::GPHI_ROWS * rowf));
     const int fids[5] = {F_RHO, F_U, F_V, F_P, F_PHI};
     for (int k : fids) h->S.fld[k] = taked(celld);
     h->rho_last = taked(celld);
@@ -465,9 +465,18 @@ static int upload_fused(dugks_handle *h, f32::SR<R> &S, const double *f, const d
         if (r != cudaSuccess) return r;
         return f32::launch_plane_from_f64<R>(dst, P.pitch, stage, nx, ny, sub, st, &h->launches);
     };
-    for (int q = 0; q < 9; ++q) {
+    for (int q = 0; q < 9; ++q)
         if ((e = put(S.df + q * S.qs, f + q * n, f_rest(P, q))) != cudaSuccess) return cuda_fail(h, e, "upload f");
-        if ((e = put(S.dh + q * S.qs, hd + q * n, h_rest(P, q))) != cudaSuccess) return cuda_fail(h, e, "upload h");
+    // the phase field: the nine FP64 h planes go to the copy the next step writes (free
+    // until then: 9 n doubles fit in its PL_N planes), then phi = sum_q h_q as a pair and
+    // g_q = h_q - w_q phi into the copy it reads
+    {
+        double *hst = reinterpret_cast<double *>(S.odf);
+        if ((e = cudaMemcpyAsync(hst, hd, 9 * n * sizeof(double), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+            return cuda_fail(h, e, "upload h");
+        if ((e = f32::launch_phase_from_f64<R>(S.dg, S.phi, S.qs, P.pitch, hst, nx, ny, st, &h->launches)) !=
+            cudaSuccess)
+            return cuda_fail(h, e, "upload h");
     }
     const int src[f32::I_N] = {F_PHI, F_RHO, F_U, F_V, F_P, F_TAU, F_PHIX, F_PHIY, F_RHOX, F_RHOY, F_FX, F_FY};
     for (int k = 0; k < f32::I_N; ++k) {
@@ -730,7 +739,7 @@ extern "C" int dugks_gpu_step(dugks_handle_t *h, int nsteps, void *stream) {
                                                            &h->launches, sn)
                                        : f32::launch_stream32(h->P32, h->S32, h->first, h->gcur, h->gcur ^ 1, st,
                                                               &h->launches, sn, h->has_tmap ? &h->tmap : nullptr,
-                                                              h->S32.df == h->tmap_base ? 0 : 24, h->kerr);
+                                                              h->S32.df == h->tmap_base ? 0 : f32::PL_N, h->kerr);
             if (e != cudaSuccess) return cuda_fail(h, e, "fp32 step launch");
             if (h->fused64) f32::swap_io(h->S64f);
             else f32::swap_io(h->S32);
@@ -929,18 +938,45 @@ extern "C" int dugks_gpu_get_dist(dugks_handle_t *h, int which, double *out) {
     }
     if (h->fp32) {
         const size_t es = h->fused64 ? sizeof(double) : sizeof(float);
+        const char *base = h->fused64 ? reinterpret_cast<const char *>(h->S64f.df)
+                                      : reinterpret_cast<const char *>(h->S32.df);
+        const size_t qs = h->fused64 ? h->S64f.qs : h->S32.qs;
         std::vector<unsigned char> tmp(n * es);
-        for (int q = 0; q < 9; ++q) {
-            const void *src = h->fused64 ? (const void *)((which ? h->S64f.dh : h->S64f.df) + q * h->S64f.qs)
-                                         : (const void *)((which ? h->S32.dh : h->S32.df) + q * h->S32.qs);
-            cudaError_t e = cudaMemcpy2D(tmp.data(), (size_t)h->P.nx * es, src, (size_t)h->P.pitch * es,
-                                         (size_t)h->P.nx * es, h->P.ny, cudaMemcpyDeviceToHost);
+        // plane k of the copy the next step reads, as doubles
+        auto plane = [&](int k, double *dst) -> int {
+            cudaError_t e = cudaMemcpy2D(tmp.data(), (size_t)h->P.nx * es, base + (size_t)k * qs * es,
+                                         (size_t)h->P.pitch * es, (size_t)h->P.nx * es, h->P.ny, cudaMemcpyDeviceToHost);
             if (e != cudaSuccess) return cuda_fail(h, e, "download distribution");
-            const double r0 = which ? h_rest(h->P, q) : f_rest(h->P, q);
-            for (size_t k = 0; k < n; ++k)
-                out[q * n + k] = r0 + (h->fused64 ? reinterpret_cast<const double *>(tmp.data())[k]
-                                                  : (double)reinterpret_cast<const float *>(tmp.data())[k]);
+            for (size_t i = 0; i < n; ++i)
+                dst[i] = h->fused64 ? reinterpret_cast<const double *>(tmp.data())[i]
+                                    : (double)reinterpret_cast<const float *>(tmp.data())[i];
+            return DUGKS_OK;
+        };
+        if (which == 0) {
+            for (int q = 0; q < 9; ++q) {
+                int rc2 = plane(f32::PL_F + q, out + q * n);
+                if (rc2) return rc2;
+                const double r0 = f_rest(h->P, q);
+                for (size_t k = 0; k < n; ++k) out[q * n + k] += r0;
+            }
+            return DUGKS_OK;
         }
+        // h_q = w_q phi + g_q, h_0 = w_0 phi - sum_{q>0} g_q
+        std::vector<double> phi(n), lo(n);
+        int rc2 = plane(f32::PL_PHI, phi.data());
+        if (!rc2) rc2 = plane(f32::PL_PHI + 1, lo.data());
+        if (rc2) return rc2;
+        for (size_t k = 0; k < n; ++k) phi[k] += lo[k];
+        std::vector<double> gsum(n, 0.0);
+        for (int q = 1; q < 9; ++q) {
+            if ((rc2 = plane(f32::PL_G + q - 1, out + q * n))) return rc2;
+            const double wq = h->P.omega[q];
+            for (size_t k = 0; k < n; ++k) {
+                gsum[k] += out[q * n + k];
+                out[q * n + k] += wq * phi[k];
+            }
+        }
+        for (size_t k = 0; k < n; ++k) out[k] = h->P.omega[0] * phi[k] - gsum[k];
         return DUGKS_OK;
     }
     for (int q = 0; q < h->P.Q; ++q) {
@@ -1014,7 +1050,7 @@ struct CkptHeader {
     int32_t pending, gcur, first, pp_pending, orient, pad1;
     f32::PPP ppc;
 };
-const char CKPT_MAGIC[8] = {'D', 'U', 'G', 'K', 'S', 'C', 'K', '1'};
+const char CKPT_MAGIC[8] = {'D', 'U', 'G', 'K', 'S', 'C', 'K', '2'};
 
 // orientation of the fused path's ping-pong views: 0 as created, 1 swapped
 int fused_orient(const dugks_handle *h) {
@@ -1147,7 +1183,6 @@ void set_stream(dugks_handle_t *h, cudaStream_t st) { h->last_stream = st; }
 // for the slab decomposition (slabs.cu)
 void derive_fp32(const Params &P, f32::P32 *Q) { derive_p32<float>(P, *Q); }
 double rest_f(const Params &P, int q) { return f_rest(P, q); }
-double rest_h(const Params &P, int q) { return h_rest(P, q); }
 
 }  // namespace internal
 }  // namespace dugks

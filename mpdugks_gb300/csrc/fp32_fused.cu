@@ -1,15 +1,19 @@
 // FP32 deviation-storage DUGKS step: one fused kernel per time step.
 //
-// Storage: f~ and h~ as FP32 deviations from fixed rest equilibria,
-//   HCZ: f0_q = w_q p0;  AC: f0_q = w_q p0/RT - [q=0] p0/RT;  h0_q = w_q phi0,
-// (p0 = 1, phi0 = 1/2).  Every step relation of the reference is affine with
-// coefficients that sum to one (aBP + bBP = 1, ah + bh = 1, 4/3 - 1/3 = 1)
-// and the rest parts of the four face fluxes of a cell cancel (sum of
-// +-xi.n = 0, bounce-back maps q to a direction of equal weight), so the step
-// is carried out on the deviations directly; the rest moments enter only the
-// macroscopic quantities (p = p0 + dp, phi = phi0 + dphi).  Cell moment sums
-// (phi, rho u, rho v, p) are float-float (Knuth two-sum) sums of the FP32
-// deviations; the domain sums and residual are FP64 reductions.
+// Storage (fp32_state.cuh): f~ as FP32 deviations from fixed rest equilibria,
+//   HCZ: f0_q = w_q p0;  AC: f0_q = w_q p0/RT - [q=0] p0/RT  (p0 = 1);
+// h~ as the phase field phi (a float-float pair) and the remainders
+// g_q = h_q - w_q phi (q = 1..8) in FP32.  Every step relation of the reference
+// is affine with coefficients that sum to one (aBP + bBP = 1, ah + bh = 1,
+// 4/3 - 1/3 = 1) and the rest parts of the four face fluxes of a cell cancel
+// (sum of +-xi.n = 0, bounce-back maps q to a direction of equal weight), so the
+// step is carried out on the deviations directly; the rest moments enter only the
+// macroscopic quantities (p = p0 + dp).  The phase field's w_q phi part is carried
+// through the step in closed form (fp32_math.cuh): the faces work relative to
+// w_q times the face average of phi, phi changes by the sum of the small face
+// fluxes, and the g_q by small increments.  Cell moment sums (rho u, rho v, p)
+// are float-float (Knuth two-sum) sums of the FP32 deviations; the domain sums
+// and residual are FP64 reductions.
 //
 // One CTA = 32 x 16 threads over a 30 x 14 tile of cells plus a one-cell
 // halo ring: every thread owns one cell of the (w+2) x (h+2) region, computes
@@ -46,12 +50,13 @@ constexpr int TW = 30, TH = 14;  // interior tile
 constexpr int BX = 32, BY = 16;  // threads = tile + halo ring
 
 
-constexpr size_t SMEM_ELEMS = (size_t)(BY + 2) * (BX + 2) + (18 + 6 + 12) * BY * BX;
+// phi pairs (halo 2), f-bar-plus pairs, south-face flux pairs, averaged fields
+constexpr size_t SMEM_ELEMS = (size_t)2 * (BY + 2) * (BX + 2) + (18 + 6 + 12) * BY * BX;
 // Prefetch staging (storage type float only): the next tile's own-cell planes
-// (9 f, 9 h, 6 aux) and the h planes of its phi ring, copied asynchronously
-// (cp.async) while the current tile computes.
+// (the PL_N planes of a state copy) and the phi pairs of its phi ring, copied
+// asynchronously (cp.async) while the current tile computes.
 constexpr int RING_MAX = 2 * (TW + 4) + 2 * (TH + 2);  // ring cells of a full tile
-constexpr size_t STG_ELEMS = (size_t)24 * BY * BX + 9 * RING_MAX;
+constexpr size_t STG_ELEMS = (size_t)PL_N * BY * BX + 2 * RING_MAX;
 template <typename R>
 constexpr bool prefetched() { return sizeof(R) == 4; }
 template <typename R>
@@ -102,15 +107,10 @@ __device__ __forceinline__ void prefetch_tile(const PR<float> &P, const SR<float
     if (g.real) {
         float *d = stg + r * BX + e;
         constexpr int BS = BY * BX;
+        // f, g, phi; the aux planes only for the flow-solving model (AC: u = 0)
+        constexpr int NPL = MODEL == AC ? PL_AUX : PL_N;
 #pragma unroll
-        for (int q = 0; q < 9; ++q) {
-            cp_async(d + q * BS, S.df + (size_t)q * S.qs + g.c);
-            cp_async(d + (9 + q) * BS, S.dh + (size_t)q * S.qs + g.c);
-        }
-        if (MODEL != AC) {
-#pragma unroll
-            for (int k = 0; k < A_N; ++k) cp_async(d + (18 + k) * BS, S.aux + (size_t)k * S.qs + g.c);
-        }
+        for (int k = 0; k < NPL; ++k) cp_async(d + k * BS, S.df + (size_t)k * S.qs + g.c);
     }
     const int nr = g.nring();
     for (int k = tid; k < nr; k += BX * BY) {
@@ -120,8 +120,8 @@ __device__ __forceinline__ void prefetch_tile(const PR<float> &P, const SR<float
         if (WALLS && (rj < 0 || rj >= P.ny)) continue;  // ghost phi or unused
         if (!WALLS) rj = wrapi(rj, P.ny);
         const size_t cc = (size_t)rj * P.pitch + wrapi(g.x0 + re - 1, P.nx);
-#pragma unroll
-        for (int q = 0; q < 9; ++q) cp_async(stg_ring + q * RING_MAX + k, S.dh + (size_t)q * S.qs + cc);
+        cp_async(stg_ring + k, S.phi + cc);
+        cp_async(stg_ring + RING_MAX + k, S.phi + S.qs + cc);
     }
     cp_async_commit();
 }
@@ -133,17 +133,17 @@ struct Views {
     T (*sB)[BY][BX];       // f-bar-plus pairs
     T (*sFS)[BY][BX];      // south-face flux pairs (6 slots)
     R (*sA)[BY][BX];       // srcx srcy rhox rhoy fx fy
-    R (*sphi)[BX + 2];     // phi, halo 2
-    R *stg;                // [24][BY][BX] staged own-cell inputs (prefetch)
-    R *stg_ring;           // [9][RING_MAX] staged ring h (prefetch)
+    T (*sphi)[BX + 2];     // phi pairs (head, tail), halo 2
+    R *stg;                // [PL_N][BY][BX] staged own-cell inputs (prefetch)
+    R *stg_ring;           // [2][RING_MAX] staged ring phi pairs (prefetch)
     __device__ __forceinline__ explicit Views(unsigned char *raw) {
         R *smem = reinterpret_cast<R *>(raw);
         sB = reinterpret_cast<T(*)[BY][BX]>(smem);
         sFS = sB + 9;
         sA = reinterpret_cast<R(*)[BY][BX]>(sFS + 6);
-        sphi = reinterpret_cast<R(*)[BX + 2]>(smem + (18 + 12 + 6) * BY * BX);
+        sphi = reinterpret_cast<T(*)[BX + 2]>(smem + (18 + 12 + 6) * BY * BX);
         stg = smem + SMEM_ELEMS;
-        stg_ring = stg + 24 * BY * BX;
+        stg_ring = stg + PL_N * BY * BX;
     }
 };
 
@@ -167,27 +167,25 @@ __device__ __forceinline__ void tile_step(const PR<R> &P, const SR<R> &S, int fi
     const bool act = g.act, ghost = g.ghost, real = g.real;
     const size_t c = g.c;
 
-    // ---- stage 0: own deviations (f, h pairs), phi of the halo-2 region
+    // ---- stage 0: own deviations (f, g pairs), phi pairs of the halo-2 region
     T Pq[9];
-    R dphi = R(0.), sfz = R(0.);
+    R sfz = R(0.);
     if (real) {
-        if (staged) {
+        auto plane = [&](int k) -> R { return staged ? stg[(k * BY + r) * BX + e] : S.df[(size_t)k * S.qs + c]; };
+        Pq[0] = mk2(plane(PL_F), R(0.));
 #pragma unroll
-            for (int q = 0; q < 9; ++q) Pq[q] = mk2(stg[(q * BY + r) * BX + e], stg[((9 + q) * BY + r) * BX + e]);
-        } else {
-#pragma unroll
-            for (int q = 0; q < 9; ++q) Pq[q] = mk2(S.df[(size_t)q * S.qs + c], S.dh[(size_t)q * S.qs + c]);
-        }
-        // (sum f, sum h) as a float-float pair; the Allen-Cahn pressure omits f_0
-        const T za[9] = {mk2(MODEL == AC ? R(0.) : Pq[0].x, Pq[0].y), Pq[1], Pq[2], Pq[3], Pq[4],
+        for (int q = 1; q < 9; ++q) Pq[q] = mk2(plane(PL_F + q), plane(PL_G + q - 1));
+        // (sum f, sum g) as a float-float pair; the Allen-Cahn pressure omits f_0
+        const T za[9] = {mk2(MODEL == AC ? R(0.) : Pq[0].x, R(0.)), Pq[1], Pq[2], Pq[3], Pq[4],
                          Pq[5], Pq[6], Pq[7], Pq[8]};
         const T z = ff_sum9(za);
         sfz = z.x;
-        dphi = z.y;
-        sphi[r + 1][e + 1] = P.phi0 + dphi;
+        Pq[0].y = -z.y;  // g_0 = -sum_{q>0} g_q
+        sphi[r + 1][e + 1] = mk2(plane(PL_PHI), plane(PL_PHI + 1));
     } else if (act && WALLS) {
         // ghost phi: the previous step's extrapolation (Ark/Cpp/Boundary.cpp:38-63)
-        sphi[r + 1][e + 1] = S.gphi[(size_t)(gin * 2 + (gj < 0 ? 0 : 1)) * pitch + gi];
+        const size_t gr = gphi_row(gin, gj < 0 ? 0 : 1);
+        sphi[r + 1][e + 1] = mk2(S.gphi[gr * pitch + gi], S.gphi[(gr + 1) * pitch + gi]);
     }
     {   // ring of the phi region
         const int nr = g.nring();
@@ -196,18 +194,16 @@ __device__ __forceinline__ void tile_step(const PR<R> &P, const SR<R> &S, int fi
             g.ring(k, re, rr);
             const int ri = wrapi(x0 + re - 1, nx);
             int rj = y0 + rr - 1;
-            R v = R(0.);
+            T v = mk2(R(0.), R(0.));
             if (WALLS && (rj < -1 || rj > ny)) {
-                v = R(0.);  // never read: no real cell of this tile reaches it
+                v = mk2(R(0.), R(0.));  // never read: no real cell of this tile reaches it
             } else if (WALLS && (rj == -1 || rj == ny)) {
-                v = S.gphi[(size_t)(gin * 2 + (rj < 0 ? 0 : 1)) * pitch + ri];
+                const size_t gr = gphi_row(gin, rj < 0 ? 0 : 1);
+                v = mk2(S.gphi[gr * pitch + ri], S.gphi[(gr + 1) * pitch + ri]);
             } else {
                 if (!WALLS) rj = wrapi(rj, ny);
                 const size_t cc = (size_t)rj * pitch + ri;
-                R ha[9];
-#pragma unroll
-                for (int q = 0; q < 9; ++q) ha[q] = staged ? stg_ring[q * RING_MAX + k] : S.dh[(size_t)q * S.qs + cc];
-                v = P.phi0 + ff_sum9(ha);
+                v = staged ? mk2(stg_ring[k], stg_ring[RING_MAX + k]) : mk2(S.phi[cc], S.phi[S.qs + cc]);
             }
             sphi[rr + 1][re + 1] = v;
         }
@@ -215,7 +211,7 @@ __device__ __forceinline__ void tile_step(const PR<R> &P, const SR<R> &S, int fi
     __syncthreads();
 
     // ---- stage 1: macros, MacroSource, f-bar-plus of every real cell of the region
-    R phi = P.phi0 + dphi, U = R(0.), V = R(0.);
+    R phi = R(0.), U = R(0.), V = R(0.);
     T inc[9];  // collision increments B - T of this cell
     R src[6];
     if (real) {
@@ -223,12 +219,12 @@ __device__ __forceinline__ void tile_step(const PR<R> &P, const SR<R> &S, int fi
         if (MODEL != AC && !first) {
 #pragma unroll
             for (int k = 0; k < A_N; ++k)
-                a6[k] = staged ? stg[((18 + k) * BY + r) * BX + e] : S.aux[(size_t)k * S.qs + c];
+                a6[k] = staged ? stg[((PL_AUX + k) * BY + r) * BX + e] : S.aux[(size_t)k * S.qs + c];
         }
         // sphi[r+1][e+1] is this cell
-        const R ph[8] = {sphi[r + 1][e + 2], sphi[r + 1][e], sphi[r + 2][e + 1], sphi[r][e + 1],
+        const T ph[8] = {sphi[r + 1][e + 2], sphi[r + 1][e], sphi[r + 2][e + 1], sphi[r][e + 1],
                          sphi[r + 2][e + 2], sphi[r + 2][e], sphi[r][e + 2], sphi[r][e]};
-        collide_cell<MODEL, R>(P, S, c, first, Pq, sfz, dphi, a6, ph, inc, src, phi, U, V);
+        collide_cell<MODEL, R>(P, S, c, first, Pq, sfz, a6, sphi[r + 1][e + 1], ph, inc, src, phi, U, V);
 #pragma unroll
         for (int q = 0; q < 9; ++q) sB[q][r][e] = add2(Pq[q], inc[q]);
 #pragma unroll
@@ -247,13 +243,29 @@ __device__ __forceinline__ void tile_step(const PR<R> &P, const SR<R> &S, int fi
         }
         // ghost phi for the next step's MacroSource, written by the tile owning the row
         if (real && e >= 1 && e <= w && r >= 1 && r <= hh) {
-            if (gj == 0) S.gphi[(size_t)(gout * 2 + 0) * pitch + gi] = R(2.) * phi - sphi[r + 2][e + 1];
-            if (gj == ny - 1) S.gphi[(size_t)(gout * 2 + 1) * pitch + gi] = R(2.) * phi - sphi[r][e + 1];
+            if (gj == 0 || gj == ny - 1) {
+                const int side = gj == 0 ? 0 : 1;
+                const T gv = ghost_pair(sphi[r + 1][e + 1], side == 0 ? sphi[r + 2][e + 1] : sphi[r][e + 1]);
+                const size_t gr = gphi_row(gout, side);
+                S.gphi[gr * pitch + gi] = gv.x;
+                S.gphi[(gr + 1) * pitch + gi] = gv.y;
+            }
         }
     }
     __syncthreads();
     hook();  // every read of the staged inputs of this tile is done
 
+    // phi pair of the region cell (rr, ee) as the faces and the update see it: at a
+    // wall the ghost row of f-bar-plus is 2 B_0 - B_1 of this step, so its phi is
+    // 2 phi_0 - phi_1 of this step (not the previous step's ghost MacroSource reads)
+    auto phiB = [&](int rr, int ee) -> T {
+        if (WALLS) {
+            const int jj = y0 + rr - 1;
+            if (jj == -1) return ghost_pair(sphi[rr + 2][ee + 1], sphi[rr + 3][ee + 1]);
+            if (jj == ny) return ghost_pair(sphi[rr][ee + 1], sphi[rr - 1][ee + 1]);
+        }
+        return sphi[rr + 1][ee + 1];
+    };
     // ---- stage 2: west x-face and south y-face of this thread's cell
     T FW[6], FSo[6];
     const bool do_x = act && e >= 1 && r >= 1 && r <= hh;           // faces x0-1|x0 .. x0+w-1|x0+w
@@ -262,24 +274,28 @@ __device__ __forceinline__ void tile_step(const PR<R> &P, const SR<R> &S, int fi
         R av[6];
 #pragma unroll
         for (int k = 0; k < 6; ++k) av[k] = R(0.5) * (sA[k][r][e - 1] + sA[k][r][e]);
+        const FacePhi<R> fp =
+            face_phi_x(phiB(r, e - 1), phiB(r, e), phiB(r + 1, e), phiB(r - 1, e), phiB(r + 1, e - 1), phiB(r - 1, e - 1));
         face_flux<MODEL, true, R>(
             P, [&](int q) { return sB[q][r][e - 1]; }, [&](int q) { return sB[q][r][e]; },
             [&](int q) {
                 return add2(sub2(sB[q][r + 1][e], sB[q][r - 1][e]), sub2(sB[q][r + 1][e - 1], sB[q][r - 1][e - 1]));
             },
-            av, 0, FW);
+            av, fp, 0, FW);
     }
     if (do_y) {
         R av[6];
 #pragma unroll
         for (int k = 0; k < 6; ++k) av[k] = R(0.5) * (sA[k][r - 1][e] + sA[k][r][e]);
         const int wall = (WALLS && gj == 0) ? 1 : ((WALLS && gj == ny) ? 2 : 0);
+        const FacePhi<R> fp =
+            face_phi_y(phiB(r - 1, e), phiB(r, e), phiB(r, e - 1), phiB(r, e + 1), phiB(r - 1, e - 1), phiB(r - 1, e + 1));
         face_flux<MODEL, false, R>(
             P, [&](int q) { return sB[q][r - 1][e]; }, [&](int q) { return sB[q][r][e]; },
             [&](int q) {
                 return add2(sub2(sB[q][r][e - 1], sB[q][r][e + 1]), sub2(sB[q][r - 1][e - 1], sB[q][r - 1][e + 1]));
             },
-            av, wall, FSo);
+            av, fp, wall, FSo);
     }
     if (do_y) {
 #pragma unroll
@@ -299,12 +315,20 @@ __device__ __forceinline__ void tile_step(const PR<R> &P, const SR<R> &S, int fi
         T FN[6], dn[9];
 #pragma unroll
         for (int s = 0; s < 6; ++s) FN[s] = sFS[s][r + 1][e];
-        update_cell<R>(P, Pq, inc, FW, FE, FSo, FN, sr_bits(P, gj, gi, step), dn);
+        const R half_dtv = R(0.5) * P.dtV;
+        const R px = half_dtv * pdiff(phiB(r, e - 1), phiB(r, e + 1));
+        const R py = half_dtv * pdiff(phiB(r - 1, e), phiB(r + 1, e));
+        R dphi;
+        update_cell<R>(P, Pq, inc, FW, FE, FSo, FN, px, py, sr_bits(P, gj, gi, step), dn, dphi);
+        S.odf[c] = dn[0].x;
 #pragma unroll
-        for (int q = 0; q < 9; ++q) {
+        for (int q = 1; q < 9; ++q) {
             S.odf[(size_t)q * S.qs + c] = dn[q].x;
-            S.odh[(size_t)q * S.qs + c] = dn[q].y;
+            S.odg[(size_t)(q - 1) * S.qs + c] = dn[q].y;
         }
+        const T pn = phi_add(sphi[r + 1][e + 1], dphi);
+        S.ophi[c] = pn.x;
+        S.ophi[S.qs + c] = pn.y;
         if (MODEL != AC) {  // AC: u = 0, the next step needs no previous force, gradient or phi*u
             S.oaux[A_FX * S.qs + c] = src[4];
             S.oaux[A_FY * S.qs + c] = src[5];
@@ -398,7 +422,7 @@ __global__ void __launch_bounds__(BX *BY, 1) k_batch32(const int2 *__restrict__ 
 // case's constants, state and step number (per-lane row loads: no tensor map per case).
 // Items of a case whose step number reached case_stop are skipped.
 template <int MODEL, bool WALLS>
-__global__ void __launch_bounds__(WPB * 32) k_streamb32(const int4 *__restrict__ items, int nitems, int kstep,
+__global__ void __launch_bounds__(WPB * 32, STREAM_MIN_BLOCKS) k_streamb32(const int4 *__restrict__ items, int nitems, int kstep,
                                                         const int *__restrict__ case_base,
                                                         const int *__restrict__ case_stop) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -577,24 +601,23 @@ __global__ void __launch_bounds__(256) k_macros32(PR<R> P, SR<R> S, double *rho_
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= P.nx || j >= P.ny) return;
     const size_t c = (size_t)j * P.pitch + i;
-    R df[9], dh[9];
+    R df[9];
 #pragma unroll
-    for (int q = 0; q < 9; ++q) {
-        df[q] = S.df[(size_t)q * S.qs + c];
-        dh[q] = S.dh[(size_t)q * S.qs + c];
-    }
-    R dphi, rho, U, V, dp;
+    for (int q = 0; q < 9; ++q) df[q] = S.df[(size_t)q * S.qs + c];
+    const double phid = (double)S.phi[c] + (double)S.phi[S.qs + c];
+    const R phi = (R)phid;
+    R rho, U, V, dp;
     if (MODEL == AC)
-        cell_macros<MODEL, R>(P, df, dh, R(0), R(0), R(0), R(0), dphi, rho, U, V, dp);
+        cell_macros<MODEL, R>(P, df, phi, R(0), R(0), R(0), R(0), rho, U, V, dp);
     else
-        cell_macros<MODEL, R>(P, df, dh, S.aux[A_FX * S.qs + c], S.aux[A_FY * S.qs + c], S.aux[A_RHOX * S.qs + c],
-                           S.aux[A_RHOY * S.qs + c], dphi, rho, U, V, dp);
+        cell_macros<MODEL, R>(P, df, phi, S.aux[A_FX * S.qs + c], S.aux[A_FY * S.qs + c], S.aux[A_RHOX * S.qs + c],
+                              S.aux[A_RHOY * S.qs + c], rho, U, V, dp);
     const size_t o = (size_t)j * opitch + i;
-    rho_o[o] = (double)P.aPhi * ((double)P.phi0 + (double)dphi) + (double)P.bPhi;
+    rho_o[o] = (double)P.aPhi * phid + (double)P.bPhi;
     u_o[o] = U;
     v_o[o] = V;
     p_o[o] = (double)P.p0 + (double)dp;
-    phi_o[o] = (double)P.phi0 + (double)dphi;
+    phi_o[o] = phid;
 }
 
 // One FP64 plane (dense [ny][nx], as the C ABI passes it) to the storage type,
@@ -619,6 +642,41 @@ template cudaError_t launch_plane_from_f64<float>(float *, int, const double *, 
                                                   int64_t *);
 template cudaError_t launch_plane_from_f64<double>(double *, int, const double *, int, int, double, cudaStream_t,
                                                    int64_t *);
+
+// The phase field of an FP64 state h [9][ny][nx] (dense, as the C ABI passes it) in
+// the storage layout: phi = sum_q h_q as a pair (head, tail) and g_q = h_q - w_q phi
+// for q = 1..8, one plane every qs elements from g and phi.
+template <typename R>
+__global__ void __launch_bounds__(256) k_phase_from_f64(R *g, R *phi, size_t qs, int pitch,
+                                                        const double *__restrict__ h, int nx, int ny) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= nx || j >= ny) return;
+    const size_t n = (size_t)nx * ny, sidx = (size_t)j * nx + i, d = (size_t)j * pitch + i;
+    double hq[9], ph = 0.0;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        hq[q] = h[q * n + sidx];
+        ph += hq[q];
+    }
+    const R hi = (R)ph;
+    phi[d] = hi;
+    phi[qs + d] = (R)(ph - (double)hi);
+#pragma unroll
+    for (int q = 1; q < 9; ++q) g[(size_t)(q - 1) * qs + d] = (R)(hq[q] - d2q9_w(q) * ph);
+}
+
+template <typename R>
+cudaError_t launch_phase_from_f64(R *g, R *phi, size_t qs, int pitch, const double *h, int nx, int ny,
+                                  cudaStream_t st, int64_t *launches) {
+    const dim3 grd((nx + 255) / 256, ny);
+    k_phase_from_f64<R><<<grd, 256, 0, st>>>(g, phi, qs, pitch, h, nx, ny);
+    *launches += 1;
+    return cudaGetLastError();
+}
+template cudaError_t launch_phase_from_f64<float>(float *, float *, size_t, int, const double *, int, int,
+                                                  cudaStream_t, int64_t *);
+template cudaError_t launch_phase_from_f64<double>(double *, double *, size_t, int, const double *, int, int,
+                                                   cudaStream_t, int64_t *);
 
 // tau, Fx, Fy of a deviation-storage case in FP64, for output: tau is Tau0
 // after the first step (before it, the initialisation's, in the init planes);

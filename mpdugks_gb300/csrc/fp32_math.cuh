@@ -33,8 +33,9 @@ __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >
 // pairs of opposite directions first, ((E+W) + (N+S)) + ((NE+SW) + (NW+SE)),
 // then the rest direction; a Knuth two-sum at every node and the node errors
 // summed in the same tree (depth 4, where a running sum is a chain of 8).
+// Returns the head (the rounded tree sum) and, in tail, the summed node errors.
 template <typename V, typename Add, typename Sub>
-__device__ __forceinline__ V ff_tree9(const V (&a)[9], Add add, Sub sub) {
+__device__ __forceinline__ V ff_tree9(const V (&a)[9], Add add, Sub sub, V &tail) {
     auto ts = [&](V x, V y, V &e) {
         const V s = add(x, y);
         const V bb = sub(s, x);
@@ -47,25 +48,22 @@ __device__ __forceinline__ V ff_tree9(const V (&a)[9], Add add, Sub sub) {
     const V sA = ts(s15, s37, eA), sB = ts(s26, s48, eB);
     const V sC = ts(sA, sB, eC);
     const V sD = ts(sC, a[0], eD);
-    const V err = add(add(add(add(e15, e37), eA), add(add(e26, e48), eB)), add(eC, eD));
-    return add(sD, err);
+    tail = add(add(add(add(e15, e37), eA), add(add(e26, e48), eB)), add(eC, eD));
+    return sD;
 }
+// the same sum as one value (head + tail rounded once)
 template <typename V>
 __device__ __forceinline__ V ff_sum9(const V (&a)[9]) {
-    return ff_tree9(a, [](V x, V y) { return x + y; }, [](V x, V y) { return x - y; });
+    V tail;
+    const V head = ff_tree9(a, [](V x, V y) { return x + y; }, [](V x, V y) { return x - y; }, tail);
+    return head + tail;
 }
 // Macroscopic state of one cell after the update of the previous step
-// (Update_MacroVar), from its deviations; HCZ needs the previous force and
-// density gradient (aux), AC has u = 0.
+// (Update_MacroVar) from its flow deviations and its phase field phi; HCZ needs
+// the previous force and density gradient (aux), AC has u = 0.
 template <int MODEL, typename R>
-__device__ __forceinline__ void cell_macros(const PR<R> &P, const R *df, const R *dh, R fx_old,
-                                            R fy_old, R rx_old, R ry_old, R &dphi, R &rho,
-                                            R &U, R &V, R &dp) {
-    R ha[9];
-#pragma unroll
-    for (int q = 0; q < 9; ++q) ha[q] = dh[q];
-    dphi = ff_sum9(ha);
-    const R phi = P.phi0 + dphi;
+__device__ __forceinline__ void cell_macros(const PR<R> &P, const R *df, R phi, R fx_old, R fy_old, R rx_old,
+                                            R ry_old, R &rho, R &U, R &V, R &dp) {
     rho = P.aPhi * phi + P.bPhi;
     if (MODEL == AC) {
         const R fa[9] = {R(0.), df[1], df[2], df[3], df[4], df[5], df[6], df[7], df[8]};
@@ -88,15 +86,25 @@ __device__ __forceinline__ void cell_macros(const PR<R> &P, const R *df, const R
     }
 }
 
-// MacroSource (Ark/Cpp/SourceM.cpp:35-62) from the 3x3 phi stencil of the cell
-template <typename R>
-__device__ __forceinline__ void macro_source9(const PR<R> &P, R phi, R E, R W, R N, R S, R NE, R NW, R SE, R SW,
-                                              R rho, R U, R V, R ppu, R ppv, R &srcx, R &srcy, R &rhox, R &rhoy,
-                                              R &fx, R &fy) {
+// MacroSource (Ark/Cpp/SourceM.cpp:35-62) from the 3x3 phi stencil of the cell.
+// The stencil's phi values are float-float pairs (x: head, y: tail; the tails are
+// zero in FP64) and enter as differences to the centre cell, d = (X - C), each
+// formed head with head and tail with tail: a difference of nearby values is then
+// correct to the working precision of the difference itself.  Formed from FP32
+// values of phi instead, the Laplacian's sum 4 sum(axis) + sum(diag) - 20 phi keeps
+// the rounding of numbers near 20 on a result that the bulk term of the chemical
+// potential nearly cancels.  ph = {E, W, N, S, NE, NW, SE, SW}.
+template <typename R, typename T>
+__device__ __forceinline__ void macro_source9(const PR<R> &P, R phi, T C, const T (&ph)[8], R rho, R U, R V, R ppu,
+                                              R ppv, R &srcx, R &srcy, R &rhox, R &rhoy, R &fx, R &fy) {
+    R d[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) d[k] = (ph[k].x - C.x) + (ph[k].y - C.y);
+    const R E = d[0], W = d[1], N = d[2], S = d[3], NE = d[4], NW = d[5], SE = d[6], SW = d[7];
     // mirror-symmetric association: x -> -x maps every sum onto its exact negation
     R gx = (R(4.) * (E - W) + ((NE - NW) + (SE - SW))) * P.inv_12dx;
     R gy = (R(4.) * (N - S) + ((NE - SE) + (NW - SW))) * P.inv_12dy;
-    const R lap = (R(4.) * ((E + W) + (N + S)) + ((NE + SW) + (NW + SE)) - R(20.) * phi) * P.inv_6dd;
+    const R lap = (R(4.) * ((E + W) + (N + S)) + ((NE + SW) + (NW + SE))) * P.inv_6dd;
     if (fabs(gx) < R(DUGKS_F32_GCLAMP)) gx = R(0.);
     if (fabs(gy) < R(DUGKS_F32_GCLAMP)) gy = R(0.);
     const R F = R(2.) * P.Beta * (phi - P.PhiL) * (phi - P.PhiV) * (R(2.) * phi - P.PhiL - P.PhiV) - P.Kappa * lap;
@@ -139,11 +147,47 @@ __device__ __forceinline__ double2 fma2(double2 a, double2 b, double2 c) {
 }
 template <typename T> __device__ __forceinline__ T neg2(T a) { return mk2(-a.x, -a.y); }
 
+template <typename T>
+__device__ __forceinline__ T ff_sum9_ht(const T (&a)[9], T &tail) {
+    return ff_tree9(a, [](T x, T y) { return add2(x, y); }, [](T x, T y) { return sub2(x, y); }, tail);
+}
 __device__ __forceinline__ float2 ff_sum9(const float2 (&a)[9]) {
-    return ff_tree9(a, [](float2 x, float2 y) { return add2(x, y); }, [](float2 x, float2 y) { return sub2(x, y); });
+    float2 tail;
+    const float2 head = ff_sum9_ht(a, tail);
+    return add2(head, tail);
 }
 __device__ __forceinline__ double2 ff_sum9(const double2 (&a)[9]) {
-    return ff_tree9(a, [](double2 x, double2 y) { return add2(x, y); }, [](double2 x, double2 y) { return sub2(x, y); });
+    double2 tail;
+    const double2 head = ff_sum9_ht(a, tail);
+    return add2(head, tail);
+}
+
+// ---- the phase field phi as a float-float pair (x: head, y: tail; the tail is zero
+// in FP64).  Differences of neighbouring values are formed head with head and tail
+// with tail, which is exact for the heads of nearby values.
+template <typename T>
+__device__ __forceinline__ auto pdiff(T a, T b) -> decltype(a.x) {
+    return (a.x - b.x) + (a.y - b.y);
+}
+// phi + d as a pair, d small (Knuth two-sum of the heads, the tails added, renormalised)
+template <typename T, typename R>
+__device__ __forceinline__ T phi_add(T a, R d) {
+    const R s = a.x + d;
+    const R bb = s - a.x;
+    const R e = (a.x - (s - bb)) + (d - bb);
+    const R lo = e + a.y;
+    const R hi = s + lo;
+    return mk2(hi, lo - (hi - s));
+}
+// Wall ghost value 2 a - b of two phi pairs (Ark/Cpp/Boundary.cpp:38-63), the head's
+// rounding error moved into the tail.
+template <typename T>
+__device__ __forceinline__ T ghost_pair(T a, T b) {
+    const auto two_a = a.x + a.x, nb = -b.x;
+    const auto s = two_a + nb;
+    const auto bb = s - two_a;
+    const auto e = (two_a - (s - bb)) + (nb - bb);
+    return mk2(s, e + ((a.y + a.y) - b.y));
 }
 
 // mirror-symmetric sum of directions 1..8: ((E+W)+(N+S)) + ((NE+SW)+(NW+SE)), which
@@ -289,16 +333,18 @@ __device__ __forceinline__ void eq_pair(const PR<R> &P, const EqSite<R> &e, type
 
 // Stage 1 of one cell: macroscopic state (from the deviations, or on the first
 // step after an initialisation from the state it left), MacroSource on the 3x3
-// phi stencil ph = {E, W, N, S, NE, NW, SE, SW}, and the collision increment
-// inc = B - T of every direction (f, h pairs).  src = {srcx, srcy, rhox, rhoy,
+// stencil of phi pairs, centre pc and ph = {E, W, N, S, NE, NW, SE, SW}, and the
+// collision increment inc = B - T of every direction.  Pq and inc are (f, h) pairs
+// whose h part is relative to w_q phi of this cell: Pq[q].y = g_q, and the h
+// equilibrium enters as h_eq - w_q phi = w_q phi u1.  src = {srcx, srcy, rhox, rhoy,
 // fx, fy}; phi_o, U_o, V_o for the caller's outputs.
 template <int MODEL, typename R>
 __device__ __forceinline__ void collide_cell(const PR<R> &P, const SR<R> &S, long long c, int first,
-                                             const typename Pair<R>::T (&Pq)[9], R sfz, R dphi, const R (&a6)[A_N],
-                                             const R (&ph)[8], typename Pair<R>::T (&inc)[9], R (&src)[6], R &phi_o,
-                                             R &U_o, R &V_o) {
+                                             const typename Pair<R>::T (&Pq)[9], R sfz, const R (&a6)[A_N],
+                                             typename Pair<R>::T pc, const typename Pair<R>::T (&ph)[8],
+                                             typename Pair<R>::T (&inc)[9], R (&src)[6], R &phi_o, R &U_o, R &V_o) {
     using T = typename Pair<R>::T;
-    R phi = P.phi0 + dphi, rho = R(0.), U = R(0.), V = R(0.), dp = R(0.);
+    R phi = pc.x + pc.y, rho = R(0.), U = R(0.), V = R(0.), dp = R(0.);
     R srcx = R(0.), srcy = R(0.), rhox = R(0.), rhoy = R(0.), fx = R(0.), fy = R(0.);
     R aBP, cBP, rxo = R(0.), ryo = R(0.);
     if (first) {
@@ -306,7 +352,6 @@ __device__ __forceinline__ void collide_cell(const PR<R> &P, const SR<R> &S, lon
         // initialisation left (p0, zero forces, tau from Mu0), as uploaded
         const R *I = S.init;
         const long long ps = (long long)S.qs;
-        phi = P.phi0 + I[I_DPHI * ps + c];
         rho = I[I_RHO * ps + c];
         U = I[I_U * ps + c];
         V = I[I_V * ps + c];
@@ -341,25 +386,22 @@ __device__ __forceinline__ void collide_cell(const PR<R> &P, const SR<R> &S, lon
             V = mv.y * inv + P.hDt * fyo * inv;
             dp = sfz + P.hDt * (rxo * U + ryo * V) * P.RT;
         }
-        macro_source9(P, phi, ph[0], ph[1], ph[2], ph[3], ph[4], ph[5], ph[6], ph[7], rho, U, V, ppu, ppv, srcx,
-                      srcy, rhox, rhoy, fx, fy);
+        macro_source9(P, phi, pc, ph, rho, U, V, ppu, ppv, srcx, srcy, rhox, rhoy, fx, fy);
         aBP = P.aBP_f;  // tau is constant after the first step (nu_L = nu_V)
         cBP = P.tauf * (R(1.) - aBP);
     }
     const R bBP = R(1.) - aBP;
     const R uu = U * U + V * V;
-    // dphi itself, not (phi0 + dphi) - phi0: one rounding less in the zeroth moment
-    const R dphi_c = first ? phi - P.phi0 : dphi;
     // equilibria of q != 0; q = 0 from the exact zeroth moment (sum dEq = dp for
-    // HCZ, 0 for AC; sum dhEq = dphi), so FP32 weights cannot leak mass
+    // HCZ, 0 for AC; sum (h_eq - w phi) = 0), so FP32 weights cannot leak mass
     T Eq[9], So[9];
-    const EqSite<R> es = eq_site<MODEL, R>(P, U, V, uu, rho, phi, dp, dphi_c, fx, fy, rhox, rhoy, srcx, srcy);
+    const EqSite<R> es = eq_site<MODEL, R>(P, U, V, uu, rho, phi, dp, R(0.), fx, fy, rhox, rhoy, srcx, srcy);
     eq_pair<MODEL, 1>(P, es, Eq[1], So[1], Eq[5], So[5]);
     eq_pair<MODEL, 2>(P, es, Eq[2], So[2], Eq[6], So[6]);
     eq_pair<MODEL, 3>(P, es, Eq[3], So[3], Eq[7], So[7]);
     eq_pair<MODEL, 4>(P, es, Eq[4], So[4], Eq[8], So[8]);
     const T sEq = sym8p(Eq);
-    Eq[0] = sub2(mk2(MODEL == AC ? R(0.) : dp, dphi_c), sEq);
+    Eq[0] = sub2(mk2(MODEL == AC ? R(0.) : dp, R(0.)), sEq);
     if (MODEL == AC) {
         So[0] = mk2(R(0.), R(0.));
     } else {
@@ -390,6 +432,26 @@ __device__ __forceinline__ void collide_cell(const PR<R> &P, const SR<R> &S, lon
     V_o = V;
 }
 
+// Phase-field inputs of one face: avg = (phi_o + phi_n)/2 (the face's h reference is
+// w_q avg), dn = phi_n - phi_o, dt = the tangential difference of phi summed over the
+// two cells (the same combination D(q) forms of the f-bar-plus values), all from pairs.
+template <typename R>
+struct FacePhi {
+    R avg, dn, dt;
+};
+// x-face between o (west) and n (east); u / d: the cells above / below each
+template <typename T>
+__device__ __forceinline__ FacePhi<decltype(T::x)> face_phi_x(T o, T n, T nu, T nd, T ou, T od) {
+    using R = decltype(T::x);
+    return {R(0.5) * (o.x + n.x), pdiff(n, o), pdiff(nu, nd) + pdiff(ou, od)};
+}
+// y-face between o (below) and n (above); w / e: the cells west / east of each
+template <typename T>
+__device__ __forceinline__ FacePhi<decltype(T::x)> face_phi_y(T o, T n, T nw, T ne, T ow, T oe) {
+    using R = decltype(T::x);
+    return {R(0.5) * (o.x + n.x), pdiff(n, o), pdiff(nw, ne) + pdiff(ow, oe)};
+}
+
 // Stage 2 of one face: half-step reconstruction at the face midpoint, face
 // moments, equilibria of the six directions crossing the face and their
 // fluxes xi.n (f, h pairs, slot order xslot / yslot).  XF: an x-face (normal
@@ -399,9 +461,13 @@ __device__ __forceinline__ void collide_cell(const PR<R> &P, const SR<R> &S, lon
 // ((n+t) - (n-t)) + ((o+t) - (o-t)) with t the tangential neighbour offset
 // (x-face: +y; y-face: -x); av = face averages of {srcx, srcy, rhox, rhoy, fx,
 // fy}; wall: 0, or 1 / 2 for the bottom / top wall face (bounce-back).
+// The h parts are relative to w_q phi of their cell; the face works relative to
+// w_q fp.avg: the reconstruction of w_q phi adds w_q (L_q(phi) - avg) from fp, and
+// the fluxes F[q].y returned are those of h_q - w_q fp.avg (the w_q avg parts of a
+// cell's four faces are added by the update from the phi differences).
 template <int MODEL, bool XF, typename R, typename FO, typename FN, typename FD>
-__device__ __forceinline__ void face_flux(const PR<R> &P, FO &&O, FN &&N, FD &&D, const R (&av)[6], int wall,
-                                          typename Pair<R>::T (&F)[6]) {
+__device__ __forceinline__ void face_flux(const PR<R> &P, FO &&O, FN &&N, FD &&D, const R (&av)[6],
+                                          const FacePhi<R> &fp, int wall, typename Pair<R>::T (&F)[6]) {
     using T = typename Pair<R>::T;
     const T half = mk2(R(0.5), R(0.5));
     T bh[9];
@@ -418,27 +484,33 @@ __device__ __forceinline__ void face_flux(const PR<R> &P, FO &&O, FN &&N, FD &&D
         // avg - hDt xi.grad: the normal part (o - n)/(-d) is folded into the two
         // cells' weights 1/2 -+ hDt sn/(-d) (0.25 and 0.75 on unit cells, exact),
         // the tangential central difference, averaged over the two cells of the
-        // face, enters with the weight -hDt st/(4 d_t)
+        // face, enters with the weight -hDt st/(4 d_t); the phase field's w_q phi
+        // part takes the same weights on phi: w_q (cn (phi_n - phi_o) + k dt)
         T b = avg;
+        R wphi = R(0.);
         if (sn != 0) {
             const R rn = XF ? P.r_ndx : P.r_ndy;
             const R cn = P.hDt * ((R)sn * rn);
             b = fma2(n, mk2(R(0.5) + cn, R(0.5) + cn), mul2(o, mk2(R(0.5) - cn, R(0.5) - cn)));
+            wphi = cn * fp.dn;
         }
         if (st != 0) {
             const T d = D(q);
             const R rt = XF ? P.r_2dy : P.r_n2dx;
             const R k = -(P.hDt * (R(0.5) * (R)st * rt));
             b = fma2(d, mk2(k, k), b);
+            wphi = fma(k, fp.dt, wphi);
         }
+        b.y = fma((R)d2q9_w(q), wphi, b.y);
         bh[q] = b;
     }
     // face moments (sum f, sum h) with the mirror-symmetric association
     const T z = add2(mk2(MODEL == AC ? R(0.) : bh[0].x, bh[0].y), sym8p(bh));
+    // dphif: the face phi relative to fp.avg
     const R sf = z.x, dphif = z.y;
     const R su = (bh[1].x - bh[5].x) + ((bh[2].x - bh[6].x) + (bh[8].x - bh[4].x));
     const R sv = (bh[3].x - bh[7].x) + ((bh[2].x - bh[6].x) + (bh[4].x - bh[8].x));
-    const R phif = P.phi0 + dphif;
+    const R phif = fp.avg + dphif;
     const R rhof = P.aPhi * phif + P.bPhi;
     R Uf, Vf, dpf;
     if (MODEL == AC) {
@@ -488,25 +560,42 @@ __device__ __forceinline__ void face_flux(const PR<R> &P, FO &&O, FN &&N, FD &&D
 
 // Stage 3 of one cell: the finite-volume update (Update_phi_T) of the
 // deviations, 4/3 B - 1/3 T = T + (4/3)(B - T) + dt/V sum(F), rounded
-// stochastically into storage with the cell's random bits h0.
+// stochastically into storage with the cell's random bits h0.  The h parts: the
+// face fluxes carry h_q - w_q avg(phi) of their face, so
+//   phi_new = phi + dphi,  dphi = dt/V sum_q (sum of the cell's h fluxes of q)
+// (the w_q avg(phi) parts cancel: sum_q w_q xi_q = 0, and sum_q (B - T) = 0), and
+//   g_q,new = g_q + (4/3) inc_q + dt/V (h flux sum of q)
+//             + w_q (xi_q,x px + xi_q,y py) - w_q dphi   (q = 1..8),
+// px = dt/V (phi_W - phi_E)/2, py = dt/V (phi_S - phi_N)/2: the w_q avg(phi) flux
+// divergence on unit cells.  dn[q].y (q >= 1) is g_q,new; dn[0].y is not used.
 template <typename R>
 __device__ __forceinline__ void update_cell(const PR<R> &P, const typename Pair<R>::T (&Pq)[9],
                                             const typename Pair<R>::T (&inc)[9], const typename Pair<R>::T (&FW)[6],
                                             const typename Pair<R>::T (&FE)[6], const typename Pair<R>::T (&FS)[6],
-                                            const typename Pair<R>::T (&FN)[6], uint32_t h0,
-                                            typename Pair<R>::T (&dn)[9]) {
+                                            const typename Pair<R>::T (&FN)[6], R px, R py, uint32_t h0,
+                                            typename Pair<R>::T (&dn)[9], R &dphi) {
     using T = typename Pair<R>::T;
     const T btp = mk2(P.bTP, P.bTP), dtv = mk2(P.dtV, P.dtV);
+    T s[9];
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
         // net flux (W - E) + (S - N) with the mirror-symmetric association
-        T s = mk2(R(0.), R(0.));
+        s[q] = mk2(R(0.), R(0.));
         const int xs = xslot(q), ys = yslot(q);
-        if (xs >= 0 && ys >= 0) s = add2(sub2(FW[xs], FE[xs]), sub2(FS[ys], FN[ys]));
-        else if (xs >= 0) s = sub2(FW[xs], FE[xs]);
-        else if (ys >= 0) s = sub2(FS[ys], FN[ys]);
+        if (xs >= 0 && ys >= 0) s[q] = add2(sub2(FW[xs], FE[xs]), sub2(FS[ys], FN[ys]));
+        else if (xs >= 0) s[q] = sub2(FW[xs], FE[xs]);
+        else if (ys >= 0) s[q] = sub2(FS[ys], FN[ys]);
+    }
+    dphi = P.dtV * sym8p(s).y;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const int xs = xslot(q), ys = yslot(q);
         // old value plus one small increment, rounded stochastically into storage
-        const T incr = (xs >= 0 || ys >= 0) ? fma2(dtv, s, fma2(btp, inc[q], inc[q])) : fma2(btp, inc[q], inc[q]);
+        T incr = (xs >= 0 || ys >= 0) ? fma2(dtv, s[q], fma2(btp, inc[q], inc[q])) : fma2(btp, inc[q], inc[q]);
+        if (q > 0) {
+            const R wq = (R)d2q9_w(q);
+            incr.y = fma(wq, (sxf(d2q9_xu(q), px) + sxf(d2q9_xv(q), py)) - dphi, incr.y);
+        }
         dn[q] = add_sr2(Pq[q], incr, h0 * SR_KEY[q], h0 * SR_KEY[16 + q]);
     }
 }

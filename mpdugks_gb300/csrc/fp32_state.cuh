@@ -41,16 +41,41 @@ enum { I_DPHI = 0, I_RHO, I_U, I_V, I_DP, I_TAU, I_SRCX, I_SRCY, I_RHOX, I_RHOY,
 // aux planes: previous MacroSource outputs read by the next step
 enum { A_FX = 0, A_FY, A_RHOX, A_RHOY, A_PPU, A_PPV, A_N };
 
+// One copy of the state is PL_N planes [ny][pitch], one every qs elements:
+//   f: the nine flow deviations f_q - f0_q;
+//   g: the phase field's remainders g_q = h_q - w_q phi of the eight moving
+//      directions q = 1..8 (h_0 follows from sum_q h_q = phi: g_0 = -sum g_q);
+//   phi: the phase field itself as a float-float pair (head, tail);
+//   aux: the previous MacroSource outputs.
+// h_q - h0_q spans w_q/2 across an interface, and its FP32 rounding noise in phi (about
+// 1e-8 per step) drove the velocity of a resting drop; the pair carries phi to ~1e-14
+// and the remainders g_q are small, so what FP32 rounds is small.
+constexpr int PL_F = 0, PL_G = 9, PL_PHI = 17, PL_AUX = 19, PL_N = PL_AUX + A_N;
+
 template <typename R>
 struct SR {
-    R *df, *dh;   // deviations [9][ny][pitch]: the state a step reads
-    R *aux;       // [A_N][ny][pitch]
-    R *odf, *odh, *oaux;  // the state a step writes (swapped with the above after each step)
+    R *df, *dg, *phi, *aux;      // the copy a step reads: planes PL_F, PL_G, PL_PHI, PL_AUX
+    R *odf, *odg, *ophi, *oaux;  // the copy it writes (swapped with the above after each step)
     R *init;      // [I_N][ny][pitch]
-    R *gphi;      // ghost phi rows [2 buffers][bottom, top][pitch]
-    size_t qs;    // ny * pitch
+    R *gphi;      // ghost phi rows [2 buffers][bottom, top][head, tail][pitch]
+    size_t qs;    // plane stride (>= ny * pitch)
 };
 using S32 = SR<float>;
+
+// the four plane groups of a copy that starts at base
+template <typename R>
+inline void set_copy(R *base, size_t qs, R *&f, R *&g, R *&phi, R *&aux) {
+    f = base + PL_F * qs;
+    g = base + PL_G * qs;
+    phi = base + PL_PHI * qs;
+    aux = base + PL_AUX * qs;
+}
+
+// Wall ghost rows of phi (the previous step's extrapolation 2 phi_0 - phi_1 below row 0
+// and above row ny-1): phi as a float-float pair, head and tail rows.
+constexpr int GPHI_ROWS = 8;
+// first of the two rows (head, then tail) of buffer buf (0, 1) and side (0 bottom, 1 top)
+__host__ __device__ __forceinline__ size_t gphi_row(int buf, int side) { return (size_t)(buf * 2 + side) * 2; }
 
 // ---- FP32 deviation storage of the pseudopotential models (D2Q9PP, D2V16)
 // Constants: FP32 step coefficients, the velocity set, the rest equilibrium
@@ -92,7 +117,8 @@ constexpr int BATCH_MAX_CASES = 64;
 template <typename R>
 inline void swap_io(SR<R> &S) {
     R *t = S.df; S.df = S.odf; S.odf = t;
-    t = S.dh; S.dh = S.odh; S.odh = t;
+    t = S.dg; S.dg = S.odg; S.odg = t;
+    t = S.phi; S.phi = S.ophi; S.ophi = t;
     t = S.aux; S.aux = S.oaux; S.oaux = t;
 }
 

@@ -1,8 +1,7 @@
 // The streaming form of the FP32 deviation-storage step: its constants, shared-memory
 // ring layout and TMA helpers (used by the single-case kernel k_stream32,
 // fp32_stream.cu, and the batched serving kernel k_streamb32, fp32_fused.cu), and the
-// per-warp work on one (strip, row segment) item, stream_item (k_streamb32; k_stream32
-// has the same steps written out in the kernel).
+// per-warp work on one (strip, row segment) item, stream_item (run by both kernels).
 //
 // A warp marches a strip of 28 columns (plus a two-column halo on each side, 32
 // lanes) along y through a segment of rows.  No block-wide barrier: the
@@ -11,9 +10,9 @@
 // so every warp runs independently of the others and of its block.
 //
 // Per row k the warp does, in order:
-//   phi of row k+2 (float-float sum of its h deviations, staged in shared
-//     memory); the load of row k+3's deviations into the stage ring (the aux of a
-//     row is read directly into registers one row ahead of its collision);
+//   the sums of row k+2's staged deviations (sum f, sum g); the load of row k+3's
+//     deviations into the stage ring (the phase field phi and the aux of a row are
+//     read directly into registers one row ahead of their use);
 //   collision of row k+1 (macros, MacroSource on the 3x3 phi stencil from the phi
 //     of rows k..k+2 and the adjacent lanes, f-bar-plus) into the f-bar-plus ring;
 //   the y-face between rows k and k+1 (its flux is row k's north face and,
@@ -43,8 +42,11 @@ constexpr int SW = 28;   // interior columns of a strip
 constexpr int SEG_MAX = 128;  // longest first-choice segment (rows)
 constexpr int WPB = 2;   // warps per block
 constexpr int NSTG = 4;  // stage ring: rows k .. k+3
+// resident blocks per SM the streaming kernels are compiled for: 6 blocks of 2 warps
+// fill the shared memory (6 x 2 warp rings) and cap a thread at 168 registers
+constexpr int STREAM_MIN_BLOCKS = 6;
 // per-warp shared memory, in floats:
-//   stage ring [NSTG][18][32]: the raw deviation planes (9 f, then 9 h) of rows
+//   stage ring [NSTG][17][32]: the raw planes (9 f, then g_1 .. g_8) of rows
 //     k .. k+3, 32 columns each -- the box one TMA load writes;
 //   f-bar-plus ring, per row slot: [4][32] float4 holding the pairs of directions
 //     (1,2), (3,4), (5,6), (7,8), then [32] float2 holding direction 0;
@@ -52,7 +54,8 @@ constexpr int NSTG = 4;  // stage ring: rows k .. k+3
 //     [32] float2 (fx, fy).
 // 8- and 16-byte entries make one shared-memory instruction move two or four values.
 // After the warps' regions: 4 mbarriers per warp (one per stage slot).
-constexpr int STG_SLOT = 18 * 32;    // floats per stage slot
+constexpr int STG_PLANES = PL_PHI;   // the planes a row load stages: 9 f, 8 g
+constexpr int STG_SLOT = STG_PLANES * 32;  // floats per stage slot
 constexpr int STG_F = NSTG * STG_SLOT;
 constexpr int BR_SLOT = 9 * 32 * 2;  // floats per row slot of the f-bar-plus ring
 constexpr int BR_F = 3 * BR_SLOT;
@@ -92,7 +95,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
-// one box {32 columns, 1 row, 18 planes} at (x, y, z) of a 3-D tensor map into shared memory
+// one box {32 columns, 1 row, STG_PLANES planes} at (x, y, z) of a 3-D tensor map into shared memory
 __device__ __forceinline__ void tma_load_row(unsigned dst, const CUtensorMap *map, int x, int y, int z, unsigned bar) {
     asm volatile(
         "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::
@@ -144,8 +147,9 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
                                             int zin, int *err, float *stg, float *bring, float *aring,
                                             unsigned bar0, uint32_t &phases, int lane) {
     using T = float2;
+    // (f_q, g_q) of a staged row; g_0 is -sum_{q>0} g_q and is filled in by the caller
     auto STG = [&](int slot, int q) -> T {
-        return mk2(stg[slot * STG_SLOT + q * 32 + lane], stg[slot * STG_SLOT + (9 + q) * 32 + lane]);
+        return mk2(stg[slot * STG_SLOT + q * 32 + lane], q ? stg[slot * STG_SLOT + (8 + q) * 32 + lane] : 0.f);
     };
     const int nx = P.nx, ny = P.ny, pitch = P.pitch;
     // the strip's window is columns hs .. hs+31 (a multiple of 4: 16-byte TMA
@@ -186,21 +190,39 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
                 const long long c = cell(j);
                 float *d = stg + m4(j) * STG_SLOT + lane;
 #pragma unroll
-                for (int q = 0; q < 9; ++q) {
-                    cp_async(d + q * 32, S.df + (size_t)q * S.qs + c);
-                    cp_async(d + (9 + q) * 32, S.dh + (size_t)q * S.qs + c);
-                }
+                for (int q = 0; q < STG_PLANES; ++q) cp_async(d + q * 32, S.df + (size_t)q * S.qs + c);
             }
         }
         if (!use_tma) cp_async_commit();
     };
+    // phi of row j as a pair: a stored row, the wall ghost row (the previous step's
+    // extrapolation, Ark/Cpp/Boundary.cpp:38-63, read by MacroSource only), or unused
+    auto load_phi = [&](int j) -> T {
+        if (j <= y1 + 1 && row_ok(j)) {
+            const long long c = cell(j);
+            return mk2(__ldg(S.phi + c), __ldg(S.phi + S.qs + c));
+        }
+        if ((wlo && j == -1) || (whi && j == ny)) {
+            const size_t gr = gphi_row(gin, j < 0 ? 0 : 1);
+            return mk2(S.gphi[gr * pitch + gi], S.gphi[(gr + 1) * pitch + gi]);
+        }
+        return mk2(0.f, 0.f);
+    };
+    auto from_east = [](T v) {
+        return mk2(__shfl_down_sync(0xffffffffu, v.x, 1), __shfl_down_sync(0xffffffffu, v.y, 1));
+    };
+    auto from_west = [](T v) {
+        return mk2(__shfl_up_sync(0xffffffffu, v.x, 1), __shfl_up_sync(0xffffffffu, v.y, 1));
+    };
     __syncwarp();  // the previous item is done with this warp's buffers
     prefetch(y0 - 2);
-    // rolling per-lane state: phi of rows k, k+1, k+2; the (sum f, sum h)
-    // deviation sums of rows k+1, k+2; row k's collision increments and
-    // south-face flux
-    float ph0 = 0.f, ph1 = 0.f, ph2 = 0.f;
-    float sfz1 = 0.f, dph1 = 0.f;
+    // rolling per-lane state: the phi pairs of rows k-1 .. k+2 (ph_m, ph0, ph1, ph2),
+    // of row k+3 (ph_n, loaded one row ahead) and of row k-1 in the west lane
+    // (ph_mw); the (sum f, sum g) of the staged rows k+1, k+2; row k's collision
+    // increments and south-face flux
+    T ph_m = mk2(0.f, 0.f), ph_mw = mk2(0.f, 0.f), ph0 = mk2(0.f, 0.f), ph1 = mk2(0.f, 0.f);
+    T ph2 = mk2(0.f, 0.f), ph_n = load_phi(y0 - 2);
+    float sfz1 = 0.f, sg1 = 0.f;
     float a6c[A_N];  // aux of row k+1 (loaded at the previous row)
     T inc_cur[9], FS[6];
 #pragma unroll
@@ -211,7 +233,7 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
         // this row's ring slots: f-bar-plus and averaged fields of rows k-1, k, k+1
         const BRow Bm{bring + m3(k - 1) * BR_SLOT}, B0{bring + m3(k) * BR_SLOT}, Bp{bring + m3(k + 1) * BR_SLOT};
         const ARow Am{aring + m3(k - 1) * AR_SLOT}, A0{aring + m3(k) * AR_SLOT}, Ap{aring + m3(k + 1) * AR_SLOT};
-        // aux of row k+2, read directly one row ahead of its collision
+        // aux of row k+2 and phi of row k+3, read directly one row ahead of their use
         const bool coll = k + 1 >= y0 - 1 && row_ok(k + 1) && colL;
         float a6n[A_N];
         if (MODEL != AC && !first && k + 2 >= y0 - 1 && row_ok(k + 2) && colL) {
@@ -219,14 +241,20 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
 #pragma unroll
             for (int a = 0; a < A_N; ++a) a6n[a] = __ldg(S.aux + (size_t)a * S.qs + c2);
         }
+        ph2 = ph_n;
+        ph_n = load_phi(k + 3);
         // row k+2's raw deviations (issued one row ago) have landed
         if (use_tma) {
             if (loaded(k + 2)) {
                 const int s = m4(k + 2);
                 const bool ok = __all_sync(0xffffffffu, mbar_wait(bar0 + 8 * s, (phases >> s) & 1u));
                 if (!ok) {
+                    // a warp has one row load in flight at a time (row k+3 is issued only
+                    // after row k+2 has landed), so this slot's copy is the only one that
+                    // can still write the warp's shared memory: wait for it once more
+                    // (bounded), then end the warp
                     if (lane == 0 && err) atomicExch(err, 1);
-                    mbar_wait(bar0 + 8 * s, (phases >> s) & 1u);  // the copy in flight, once more
+                    mbar_wait(bar0 + 8 * s, (phases >> s) & 1u);
                     return false;
                 }
                 phases ^= 1u << s;
@@ -235,26 +263,17 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
             cp_async_wait_all();
         }
         __syncwarp();
-        // ---- phi of row k+2
-        float sfz2 = 0.f, dph2 = 0.f;
-        {
-            const int j = k + 2;
-            float phv = 0.f;
-            if (row_ok(j)) {
-                const int sl = m4(j);
-                T za[9];
+        // ---- (sum f, sum g) of row k+2
+        float sfz2 = 0.f, sg2 = 0.f;
+        if (row_ok(k + 2)) {
+            const int sl = m4(k + 2);
+            T za[9];
 #pragma unroll
-                for (int q = 0; q < 9; ++q) za[q] = STG(sl, q);
-                if (MODEL == AC) za[0].x = 0.f;
-                const T z = ff_sum9(za);
-                sfz2 = z.x;
-                dph2 = z.y;
-                phv = P.phi0 + dph2;
-            } else if ((wlo && j == -1) || (whi && j == ny)) {
-                // ghost phi: the previous step's extrapolation (Ark/Cpp/Boundary.cpp:38-63)
-                phv = S.gphi[(size_t)(gin * 2 + (j < 0 ? 0 : 1)) * pitch + gi];
-            }
-            ph2 = phv;
+            for (int q = 0; q < 9; ++q) za[q] = STG(sl, q);
+            if (MODEL == AC) za[0].x = 0.f;
+            const T z = ff_sum9(za);
+            sfz2 = z.x;
+            sg2 = z.y;
         }
         __syncwarp();  // every lane has read slot k+2 (slot k+3 = slot k-1 is refilled next)
         prefetch(k + 3);
@@ -262,21 +281,22 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
         T inc_nx[9];
 #pragma unroll
         for (int q = 0; q < 9; ++q) inc_nx[q] = mk2(0.f, 0.f);
+        // 3x3 phi stencil of row k+1: rows k (S), k+1, k+2 (N); lanes +-1 (E/W)
+        const T E = from_east(ph1), W = from_west(ph1);
+        const T NE = from_east(ph2), NW = from_west(ph2);
+        const T SE = from_east(ph0), SWv = from_west(ph0);
         {
             const int j = k + 1;
-            // 3x3 phi stencil: rows k (S), k+1, k+2 (N); lanes +-1 (E/W)
-            const float E = __shfl_down_sync(0xffffffffu, ph1, 1), W = __shfl_up_sync(0xffffffffu, ph1, 1);
-            const float NE = __shfl_down_sync(0xffffffffu, ph2, 1), NW = __shfl_up_sync(0xffffffffu, ph2, 1);
-            const float SE = __shfl_down_sync(0xffffffffu, ph0, 1), SWv = __shfl_up_sync(0xffffffffu, ph0, 1);
             if (coll) {
                 const int sl = m4(j);
                 T Pq[9];
 #pragma unroll
                 for (int q = 0; q < 9; ++q) Pq[q] = STG(sl, q);
-                const float ph[8] = {E, W, ph2, ph0, NE, NW, SE, SWv};
+                Pq[0].y = -sg1;
+                const T ph[8] = {E, W, ph2, ph0, NE, NW, SE, SWv};
                 const long long c = cell(j);
                 float src[6], phi, U, V;
-                collide_cell<MODEL, float>(P, S, c, first, Pq, sfz1, dph1, a6c, ph, inc_nx, src, phi, U, V);
+                collide_cell<MODEL, float>(P, S, c, first, Pq, sfz1, a6c, ph1, ph, inc_nx, src, phi, U, V);
                 T bp[9];
 #pragma unroll
                 for (int q = 0; q < 9; ++q) bp[q] = add2(Pq[q], inc_nx[q]);
@@ -292,8 +312,13 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
                         S.oaux[A_PPV * S.qs + c] = phi * V;
                     }
                     // ghost phi for the next step's MacroSource
-                    if (wlo && j == 0) S.gphi[(size_t)(gout * 2 + 0) * pitch + gi] = 2.f * phi - ph2;
-                    if (whi && j == ny - 1) S.gphi[(size_t)(gout * 2 + 1) * pitch + gi] = 2.f * phi - ph0;
+                    auto put_ghost = [&](int side, T v) {
+                        const size_t gr = gphi_row(gout, side);
+                        S.gphi[gr * pitch + gi] = v.x;
+                        S.gphi[(gr + 1) * pitch + gi] = v.y;
+                    };
+                    if (wlo && j == 0) put_ghost(0, ghost_pair(ph1, ph2));
+                    if (whi && j == ny - 1) put_ghost(1, ghost_pair(ph1, ph0));
                 }
             }
         }
@@ -317,41 +342,57 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
             Ag.put(ag, lane);
         }
         __syncwarp();
+        // phi pairs of rows k-1 and k+1 as the faces and the update of row k see them: at
+        // a wall the ghost row of f-bar-plus is 2 B_0 - B_1 of this step, so its phi is
+        // 2 phi_0 - phi_1 of this step (not the previous step's ghost MacroSource reads)
+        const bool bot = wlo && k == 0, top = whi && k == ny - 1;
+        T dn_c = ph_m, dn_w = ph_mw, up_c = ph1, up_w = W, up_e = E;
+        if (bot) {
+            dn_c = ghost_pair(ph0, ph1);
+            dn_w = ghost_pair(SWv, W);
+        }
+        if (top) {
+            const T mE = from_east(ph_m);
+            up_c = ghost_pair(ph0, ph_m);
+            up_w = ghost_pair(SWv, ph_mw);
+            up_e = ghost_pair(SE, mE);
+        }
         // ---- y-face between rows k-1 and k at the bottom wall (row 0's south face)
-        if (wlo && k == 0 && interior) {
+        if (bot && interior) {
             float av[6], am[6], a0[6];
             Am.get(am, lane);
             A0.get(a0, lane);
 #pragma unroll
             for (int a = 0; a < 6; ++a) av[a] = 0.5f * (am[a] + a0[a]);
+            const FacePhi<float> fp = face_phi_y(dn_c, ph0, SWv, SE, dn_w, ghost_pair(SE, E));
             face_flux<MODEL, false, float>(
                 P, [&](int q) { return Bm.get(q, lane); }, [&](int q) { return B0.get(q, lane); },
                 [&](int q) {
                     return add2(sub2(B0.get(q, lane - 1), B0.get(q, lane + 1)),
                                 sub2(Bm.get(q, lane - 1), Bm.get(q, lane + 1)));
                 },
-                av, 1, FS);
+                av, fp, 1, FS);
         }
         // ---- y-face between rows k and k+1 (row k's north face)
         T FN[6];
 #pragma unroll
         for (int s = 0; s < 6; ++s) FN[s] = mk2(0.f, 0.f);
-        const bool top_wall = whi && k == ny - 1;
-        const bool yface = k >= y0 - 1 && ((row_ok(k) && row_ok(k + 1)) || top_wall);
+        const bool yface = k >= y0 - 1 && ((row_ok(k) && row_ok(k + 1)) || top);
         if (yface && interior) {
             float av[6], a0[6], ap[6];
             A0.get(a0, lane);
             Ap.get(ap, lane);
 #pragma unroll
             for (int a = 0; a < 6; ++a) av[a] = 0.5f * (a0[a] + ap[a]);
-            const int wall = top_wall ? 2 : 0;
+            const int wall = top ? 2 : 0;
+            const FacePhi<float> fp = face_phi_y(ph0, up_c, up_w, up_e, SWv, SE);
             face_flux<MODEL, false, float>(
                 P, [&](int q) { return B0.get(q, lane); }, [&](int q) { return Bp.get(q, lane); },
                 [&](int q) {
                     return add2(sub2(Bp.get(q, lane - 1), Bp.get(q, lane + 1)),
                                 sub2(B0.get(q, lane - 1), B0.get(q, lane + 1)));
                 },
-                av, wall, FN);
+                av, fp, wall, FN);
         }
         // ---- x-faces of row k: the west face of every lane, the east face from the next lane
         const bool upd = k >= y0 && row_ok(k);
@@ -364,12 +405,13 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
             A0.get(a0, lane);
 #pragma unroll
             for (int a = 0; a < 6; ++a) av[a] = 0.5f * (aw[a] + a0[a]);
+            const FacePhi<float> fp = face_phi_x(SWv, ph0, up_c, dn_c, up_w, dn_w);
             face_flux<MODEL, true, float>(
                 P, [&](int q) { return B0.get(q, lane - 1); }, [&](int q) { return B0.get(q, lane); },
                 [&](int q) {
                     return add2(sub2(Bp.get(q, lane), Bm.get(q, lane)), sub2(Bp.get(q, lane - 1), Bm.get(q, lane - 1)));
                 },
-                av, 0, FW);
+                av, fp, 0, FW);
         }
         T FE[6];
 #pragma unroll
@@ -382,22 +424,31 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
 #pragma unroll
             for (int q = 0; q < 9; ++q) Pq[q] = STG(sl, q);
             const long long c = cell(k);
-            update_cell<float>(P, Pq, inc_cur, FW, FE, FS, FN, sr_bits(P, k, gi, step), dn);
+            const float half_dtv = 0.5f * P.dtV;
+            const float px = half_dtv * pdiff(SWv, SE), py = half_dtv * pdiff(dn_c, up_c);
+            float dphi;
+            update_cell<float>(P, Pq, inc_cur, FW, FE, FS, FN, px, py, sr_bits(P, k, gi, step), dn, dphi);
+            S.odf[c] = dn[0].x;
 #pragma unroll
-            for (int q = 0; q < 9; ++q) {
+            for (int q = 1; q < 9; ++q) {
                 S.odf[(size_t)q * S.qs + c] = dn[q].x;
-                S.odh[(size_t)q * S.qs + c] = dn[q].y;
+                S.odg[(size_t)(q - 1) * S.qs + c] = dn[q].y;
             }
+            const T pn = phi_add(ph0, dphi);
+            S.ophi[c] = pn.x;
+            S.ophi[S.qs + c] = pn.y;
         }
         // ---- roll the per-lane state one row up
 #pragma unroll
         for (int q = 0; q < 9; ++q) inc_cur[q] = inc_nx[q];
 #pragma unroll
         for (int s = 0; s < 6; ++s) FS[s] = FN[s];
+        ph_m = ph0;
+        ph_mw = SWv;
         ph0 = ph1;
         ph1 = ph2;
         sfz1 = sfz2;
-        dph1 = dph2;
+        sg1 = sg2;
         if (MODEL != AC) {
 #pragma unroll
             for (int a = 0; a < A_N; ++a) a6c[a] = a6n[a];

@@ -7,9 +7,9 @@
 // a halo filled from the neighbouring partition (periodic grids wrap from
 // the last partition to the first).  Every step each partition runs the
 // streaming kernel on its rows (halo rows are read, never written), then the
-// two boundary rows of all 24 state planes (9 f, 9 h deviations, 6 aux) are
-// copied into the neighbours' halo rows: one strided copy per neighbour and
-// side.  The stochastic-rounding bits use global cell numbers, so the
+// two boundary rows of all PL_N state planes (9 f deviations, 8 phase-field
+// remainders g, the phi pair, 6 aux) are copied into the neighbours' halo rows: one
+// strided copy per neighbour and side.  The stochastic-rounding bits use global cell numbers, so the
 // decomposed run is bit-identical to the undivided one.
 //
 // The reference has no counterpart (one OpenMP process per case).  Only one
@@ -35,7 +35,6 @@ int host_init_state(const Params &P, const double iM[16][16], int kind, const do
 namespace internal {
 void derive_fp32(const Params &P, f32::P32 *Q);
 double rest_f(const Params &P, int q);
-double rest_h(const Params &P, int q);
 }  // namespace internal
 namespace f32 {
 cudaError_t launch_stream32(const P32 &P, const S32 &S, int first, int gin, int gout, cudaStream_t st,
@@ -105,10 +104,10 @@ int cuda_fail(cudaError_t e, const char *what) {
     return fail(std::string(what) + ": " + cudaGetErrorString(e), DUGKS_ECUDA);
 }
 
-// rows [0, n) of 24 planes of `src` (stride sp floats) -> rows of `dst` (stride dp)
+// rows [0, n) of the PL_N planes of `src` (stride sp floats) -> rows of `dst` (stride dp)
 cudaError_t copy_rows(float *dst, size_t dp, const float *src, size_t sp, int pitch, int n, cudaStream_t st) {
-    return cudaMemcpy2DAsync(dst, dp * sizeof(float), src, sp * sizeof(float), (size_t)n * pitch * sizeof(float), 24,
-                             cudaMemcpyDefault, st);
+    return cudaMemcpy2DAsync(dst, dp * sizeof(float), src, sp * sizeof(float), (size_t)n * pitch * sizeof(float),
+                             f32::PL_N, cudaMemcpyDefault, st);
 }
 
 // halo exchange into the current state of every partition
@@ -194,8 +193,8 @@ extern "C" int dugks_slabs_create(const dugks_case_t *c, const dugks_grid_t *g, 
         q.P.halo_hi = q.hi >= 0;
         const int pitch = s->P.pitch;
         q.plane = (size_t)(q.nrows + 2 * H) * pitch;
-        // two state sets of 24 planes, 12 first-step planes, ghost phi rows
-        const size_t floats = 2 * 24 * q.plane + f32::I_N * q.plane + 4 * (size_t)pitch;
+        // two state sets of PL_N planes, 12 first-step planes, ghost phi rows
+        const size_t floats = 2 * f32::PL_N * q.plane + f32::I_N * q.plane + f32::GPHI_ROWS * (size_t)pitch;
         cudaError_t e = cudaSetDevice(q.device);
         // one stream per device: the partitions of a device, their halo copies and
         // the next step are ordered on it
@@ -214,14 +213,10 @@ extern "C" int dugks_slabs_create(const dugks_case_t *c, const dugks_grid_t *g, 
         }
         float *a = q.arena + (size_t)H * pitch;  // row 0 of plane 0
         q.S.qs = q.plane;
-        q.S.df = a;
-        q.S.dh = a + 9 * q.plane;
-        q.S.aux = a + 18 * q.plane;
-        q.S.odf = a + 24 * q.plane;
-        q.S.odh = a + 33 * q.plane;
-        q.S.oaux = a + 42 * q.plane;
-        q.S.init = a + 48 * q.plane;
-        q.S.gphi = q.arena + (2 * 24 + f32::I_N) * q.plane;
+        f32::set_copy(a, q.plane, q.S.df, q.S.dg, q.S.phi, q.S.aux);
+        f32::set_copy(a + f32::PL_N * q.plane, q.plane, q.S.odf, q.S.odg, q.S.ophi, q.S.oaux);
+        q.S.init = a + 2 * f32::PL_N * q.plane;
+        q.S.gphi = q.arena + (2 * f32::PL_N + f32::I_N) * q.plane;
     }
     cudaSetDevice(dev0);
     *out = s;
@@ -236,6 +231,17 @@ extern "C" int dugks_slabs_init(dugks_slabs_t *s, int kind, const double *params
         return fail("unknown init kind for this model");
     const int nx = s->grid.nx, ny = s->grid.ny, pitch = s->P.pitch;
     const size_t n = (size_t)nx * ny;
+    // the phase field in the storage layout: g_q = h_q - w_q phi (q = 1..8) and phi
+    // = sum_q h_q as the pair (head, tail) of its FP32 rounding
+    std::vector<double> g(8 * n), phi2(2 * n);
+    for (size_t c = 0; c < n; ++c) {
+        double ph = 0.0;
+        for (int q = 0; q < 9; ++q) ph += h[(size_t)q * n + c];
+        for (int q = 1; q < 9; ++q) g[(size_t)(q - 1) * n + c] = h[(size_t)q * n + c] - d2q9_w(q) * ph;
+        const double hi = (double)(float)ph;
+        phi2[c] = hi;
+        phi2[n + c] = ph - hi;
+    }
     const int isrc[f32::I_N] = {F_PHI, F_RHO, F_U, F_V, F_P, F_TAU, F_PHIX, F_PHIY, F_RHOX, F_RHOY, F_FX, F_FY};
     const int asrc[f32::A_N] = {F_FX, F_FY, F_RHOX, F_RHOY, F_PPU, F_PPV};
     for (auto &q : s->parts) {
@@ -262,10 +268,11 @@ extern "C" int dugks_slabs_init(dugks_slabs_t *s, int kind, const double *params
             if (r != cudaSuccess) return r;
             return cudaStreamSynchronize(q.st);  // tmp is reused
         };
-        for (int k = 0; k < 9 && e == cudaSuccess; ++k) {
+        for (int k = 0; k < 9 && e == cudaSuccess; ++k)
             e = put(q.S.df + (size_t)k * q.plane, f.data() + (size_t)k * n, internal::rest_f(s->P, k));
-            if (e == cudaSuccess) e = put(q.S.dh + (size_t)k * q.plane, h.data() + (size_t)k * n, internal::rest_h(s->P, k));
-        }
+        for (int k = 0; k < 8 && e == cudaSuccess; ++k) e = put(q.S.dg + (size_t)k * q.plane, g.data() + (size_t)k * n, 0.0);
+        for (int k = 0; k < 2 && e == cudaSuccess; ++k)
+            e = put(q.S.phi + (size_t)k * q.plane, phi2.data() + (size_t)k * n, 0.0);
         for (int k = 0; k < f32::I_N && e == cudaSuccess; ++k) {
             const double sub = k == f32::I_DPHI ? DUGKS_F32_PHI0 : (k == f32::I_DP ? 1.0 : 0.0);
             e = put(q.S.init + (size_t)k * q.plane, aux.data() + (size_t)isrc[k] * n, sub);
