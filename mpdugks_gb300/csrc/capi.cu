@@ -47,6 +47,8 @@ cudaError_t stream_tensor_map(void *map_out, float *base, int nx, int ny, int pi
 cudaError_t launch_pp32_step(const PPP &P, const PPS &S, int do_msrc, cudaStream_t st, int64_t *launches,
                              uint32_t step);
 cudaError_t launch_pp32_force(const PPP &P, const PPS &S, cudaStream_t st, int64_t *launches);
+cudaError_t launch_pp_g_from_f64(float *g, int pitch, const double *f, const double *rho, int nx, int ny, double e,
+                                 cudaStream_t st, int64_t *launches);
 template <typename R>
 cudaError_t launch_plane_from_f64(R *dst, int dpitch, const double *src, int nx, int ny, double sub,
                                   cudaStream_t st, int64_t *launches);
@@ -122,6 +124,7 @@ struct dugks_handle {
     f32::PPP PPc{};
     f32::PPS PPs{};
     int pp_pending = 0;       // the next collision computes the cell force from psi
+    const double *pp_rho0 = nullptr;  // the density plane the step reads as created (checkpoint orientation)
 };
 
 static std::string g_create_err;
@@ -218,7 +221,7 @@ static cudaError_t to_dev(const dugks_handle *h, double *d, const double *src, i
 static size_t pp32_arena_bytes(const Params &P) {
     const size_t cf = align256((size_t)P.pitch * P.ny * sizeof(float));
     const size_t cd = align256((size_t)P.pitch * P.ny * sizeof(double));
-    return (6 * (size_t)P.Q + 18) * cf + 6 * cd + align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 512 +
+    return (6 * (size_t)P.Q + 18) * cf + 7 * cd + align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 512 +
            (P.model == PP16 ? align256(sizeof(float) * 256) : 0);
 }
 
@@ -259,6 +262,8 @@ static int create_pp32(dugks_handle *h, dugks_handle_t **out) {
                       &S.xFx, &S.xFy, &S.yFx, &S.yFy, &S.psi, &S.scg, &S.Fx, &S.Fy};
     for (auto p : scal) *p = tf(1);
     S.rho = td();
+    S.rho_o = td();
+    h->pp_rho0 = S.rho;
     S.p = td();
     S.U = td();
     S.V = td();
@@ -307,6 +312,11 @@ static int create_pp32(dugks_handle *h, dugks_handle_t **out) {
         C.xi_v[q] = (float)P.xi_v[q];
     }
     for (int q = 0; q < 9; ++q) C.w9[q] = (float)P.omega[q];
+    {   // the rest equilibrium per unit density, e_q = eq_q(1, 0, 0)
+        double rest[16];
+        pp_rest_eq(P, h->iM, 1.0, rest);
+        for (int q = 0; q < Q; ++q) C.erest[q] = (float)rest[q];
+    }
     C.iM16 = nullptr;
     if (P.model == PP16) {
         // this case's inverse moment matrix, in FP32, after the flag word
@@ -339,32 +349,32 @@ static int upload_pp32(dugks_handle *h, const double *f, const double *aux) {
     cudaStream_t st = h->last_stream;
     f32::PPP &C = h->PPc;
     f32::PPS &S = h->PPs;
-    double mean = 0.0;
-    for (size_t k = 0; k < n; ++k) mean += aux[(size_t)F_RHO * n + k];
-    C.rho_ref = mean / (double)n;
-    split_ff(C.rho_ref, C.rref_hi, C.rref_lo);
-    double rest[16];
-    pp_rest_eq(P, h->iM, C.rho_ref, rest);
-    for (int q = 0; q < P.Q; ++q) C.frest[q] = (float)rest[q];
-    double *stage = nullptr;
-    cudaError_t e = cudaMalloc(&stage, n * sizeof(double));
-    if (e != cudaSuccess) return cuda_fail(h, e, "upload staging");
-    auto put = [&](float *dst, const double *src, double sub) -> cudaError_t {
-        cudaError_t r = cudaMemcpyAsync(stage, src, n * sizeof(double), cudaMemcpyHostToDevice, st);
-        if (r != cudaSuccess) return r;
-        return f32::launch_plane_from_f64<float>(dst, P.pitch, stage, nx, ny, sub, st, &h->launches);
-    };
-    for (int q = 0; q < P.Q && e == cudaSuccess; ++q)
-        e = put(S.df + (size_t)q * S.qs, f + (size_t)q * n, (double)C.frest[q]);
-    if (e == cudaSuccess) e = put(S.Fx, aux + (size_t)F_FX * n, 0.0);
-    if (e == cudaSuccess) e = put(S.Fy, aux + (size_t)F_FY * n, 0.0);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    cudaFree(stage);
-    if (e != cudaSuccess) return cuda_fail(h, e, "upload");
-    // the FP64 planes of the state as uploaded; face forces and psi restart
+    cudaError_t e;
+    // the FP64 planes of the state as uploaded (the density first: the remainders are
+    // taken against it); face forces and psi restart
     const int fid[4] = {F_RHO, F_U, F_V, F_P};
     for (int k : fid)
         if ((e = to_dev(h, h->S.fld[k], aux + (size_t)k * n)) != cudaSuccess) return cuda_fail(h, e, "upload");
+    double *stage = nullptr;
+    e = cudaMalloc(&stage, n * sizeof(double));
+    if (e != cudaSuccess) return cuda_fail(h, e, "upload staging");
+    // g_q = f_q - e_q rho
+    for (int q = 0; q < P.Q && e == cudaSuccess; ++q) {
+        e = cudaMemcpyAsync(stage, f + (size_t)q * n, n * sizeof(double), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = f32::launch_pp_g_from_f64(S.df + (size_t)q * S.qs, P.pitch, stage, S.rho, nx, ny, (double)C.erest[q],
+                                          st, &h->launches);
+    }
+    auto put = [&](float *dst, const double *src) -> cudaError_t {
+        cudaError_t r = cudaMemcpyAsync(stage, src, n * sizeof(double), cudaMemcpyHostToDevice, st);
+        if (r != cudaSuccess) return r;
+        return f32::launch_plane_from_f64<float>(dst, P.pitch, stage, nx, ny, 0.0, st, &h->launches);
+    };
+    if (e == cudaSuccess) e = put(S.Fx, aux + (size_t)F_FX * n);
+    if (e == cudaSuccess) e = put(S.Fy, aux + (size_t)F_FY * n);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(stage);
+    if (e != cudaSuccess) return cuda_fail(h, e, "upload");
     float *zero[] = {S.xFx, S.xFy, S.yFx, S.yFy, S.psi, S.scg};
     for (auto z : zero) cudaMemsetAsync(z, 0, S.qs * sizeof(float), st);
     cudaMemsetAsync(h->rho_last, 0, (size_t)P.pitch * ny * sizeof(double), st);
@@ -725,6 +735,8 @@ extern "C" int dugks_gpu_step(dugks_handle_t *h, int nsteps, void *stream) {
                                                   (uint32_t)(h->steps + s));
             if (e != cudaSuccess) return cuda_fail(h, e, "fp32 pseudopotential step launch");
             h->pp_pending = 1;
+            std::swap(h->PPs.rho, h->PPs.rho_o);  // the density the update wrote is the state's
+            h->S.fld[F_RHO] = h->PPs.rho;
         }
         h->steps += nsteps;
         cudaError_t e = cudaGetLastError();
@@ -928,11 +940,15 @@ extern "C" int dugks_gpu_get_dist(dugks_handle_t *h, int which, double *out) {
     if (rc) return rc;
     const size_t n = (size_t)h->P.nx * h->P.ny;
     if (h->pp32) {
+        // f_q = e_q rho + g_q
+        std::vector<double> rho(n);
+        cudaError_t e = to_host(h, rho.data(), h->PPs.rho);
+        if (e != cudaSuccess) return cuda_fail(h, e, "download density");
         for (int q = 0; q < h->P.Q; ++q) {
             int rc2 = pp32_plane_to_host(h, h->PPs.df + (size_t)q * h->PPs.qs, out + q * n);
             if (rc2) return rc2;
-            const double r0 = h->PPc.frest[q];
-            for (size_t k = 0; k < n; ++k) out[q * n + k] += r0;
+            const double eq = h->PPc.erest[q];
+            for (size_t k = 0; k < n; ++k) out[q * n + k] += eq * rho[k];
         }
         return DUGKS_OK;
     }
@@ -1054,6 +1070,7 @@ const char CKPT_MAGIC[8] = {'D', 'U', 'G', 'K', 'S', 'C', 'K', '2'};
 
 // orientation of the fused path's ping-pong views: 0 as created, 1 swapped
 int fused_orient(const dugks_handle *h) {
+    if (h->pp32) return h->PPs.rho == h->pp_rho0 ? 0 : 1;
     if (!h->fp32) return 0;
     const void *df = h->fused64 ? static_cast<const void *>(h->S64f.df) : static_cast<const void *>(h->S32.df);
     return df == static_cast<const void *>(h->arena) ? 0 : 1;
@@ -1123,8 +1140,14 @@ extern "C" int dugks_gpu_restore(dugks_handle_t *h, const void *buf, size_t len)
     h->pp_pending = hd.pp_pending;
     if (h->pp32) h->PPc = hd.ppc;
     if (fused_orient(h) != hd.orient) {
-        if (h->fused64) f32::swap_io(h->S64f);
-        else f32::swap_io(h->S32);
+        if (h->pp32) {
+            std::swap(h->PPs.rho, h->PPs.rho_o);
+            h->S.fld[F_RHO] = h->PPs.rho;
+        } else if (h->fused64) {
+            f32::swap_io(h->S64f);
+        } else {
+            f32::swap_io(h->S32);
+        }
     }
     h->macros_fresh = false;
     return DUGKS_OK;

@@ -661,8 +661,10 @@ __global__ void __launch_bounds__(256) k_phase_from_f64(R *g, R *phi, size_t qs,
     const R hi = (R)ph;
     phi[d] = hi;
     phi[qs + d] = (R)(ph - (double)hi);
+    // separately rounded product and difference (no contraction): the same doubles as
+    // the host-side split of a slab partition's initial state
 #pragma unroll
-    for (int q = 1; q < 9; ++q) g[(size_t)(q - 1) * qs + d] = (R)(hq[q] - d2q9_w(q) * ph);
+    for (int q = 1; q < 9; ++q) g[(size_t)(q - 1) * qs + d] = (R)__dsub_rn(hq[q], __dmul_rn(d2q9_w(q), ph));
 }
 
 template <typename R>

@@ -8,17 +8,19 @@
 // force, equilibrium, He-Shan-Doolen source, flux) and the update (with the
 // cell macros, pressure and psi).
 //
-// Storage: f as FP32 deviations from the rest equilibrium f_rest =
-// eq(rho_ref, 0, 0); the step's scratch in FP32; the density in FP64.  Every
-// relation of the step is affine with coefficients summing to one and the rest
-// parts of a cell's four face fluxes cancel, so the step runs on deviations.
-// Equilibria are evaluated as deviations directly: eq(rho, u) - f_rest =
-// iM (M(rho, u) - M(rho_ref, 0)) with d rho = rho - rho_ref exact, so nothing
-// cancels.  Moment sums and the equation of state are float-float (below);
-// stores are stochastically rounded as in the Allen-Cahn path.  (Fusing face
-// pass 2 with the update, the fluxes of a tile in shared memory and the face
-// reconstruction recomputed instead of stored, ran slower: 0.55 against
-// 0.46 ms per D2V16 step at 1024^2, 128 registers and two blocks per SM.)
+// Storage: the density rho in FP64 and f as the FP32 remainders g_q = f_q - e_q rho,
+// e_q = eq_q(1, 0, 0) the rest equilibrium per unit density.  At rest f = e rho, so
+// the g_q are small (the equilibrium's velocity part and the non-equilibrium part)
+// where deviations from one global rest state would span the liquid-vapour density
+// difference.  The step carries the e_q rho part in closed form: the collision keeps
+// it (sum_q (B - f) = 0), the faces reconstruct it from the FP64 density and work
+// relative to e_q times the face average of rho, and the update changes rho by the
+// sum of the small face fluxes (the e_q avg(rho) parts cancel: sum_q e_q xi_q = 0)
+// and each g_q by small increments.  Moment sums and the equation of state are
+// float-float (below); stores are stochastically rounded as in the Allen-Cahn path.
+// (Fusing face pass 2 with the update, the fluxes of a tile in shared memory and the
+// face reconstruction recomputed instead of stored, ran slower: 0.55 against 0.46 ms
+// per D2V16 step at 1024^2, 128 registers and two blocks per SM.)
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -30,23 +32,23 @@
 namespace dugks {
 namespace f32 {
 
-// Equilibrium deviations de_q = eq_q(rho, u, v) - f_rest_q.
+// Equilibrium parts de_q = eq_q(rho, u, v) - e_q rho (zero at rest).
 template <int MODEL>
-__device__ __forceinline__ void pp_deq(const PPP &P, float dr, float rho, float u, float v, float *de) {
+__device__ __forceinline__ void pp_deq(const PPP &P, float rho, float u, float v, float *de) {
     if (MODEL == PP16) {
         // Macro16 (Ark/Lib/D2V16.cpp:125-145) at T = T0, p = rho RT, minus its value at
-        // (rho_ref, 0, 0): linear in rho at rest; times the case's inverse moment matrix
-        // (Ark/Lib/D2V16.cpp:34-52), read through the read-only path (every lane of a warp
-        // reads the same entry)
+        // (rho, 0, 0) (at rest the moments are linear in rho); times the case's inverse
+        // moment matrix (Ark/Lib/D2V16.cpp:34-52), read through the read-only path (every
+        // lane of a warp reads the same entry)
         const float RT = P.RT, u2 = u * u, v2 = v * v, s2 = u2 + v2;
         float M[16];
-        M[0] = dr;
+        M[0] = 0.f;
         M[1] = rho * u;
         M[2] = rho * v;
-        M[3] = 3.f * RT * dr + rho * s2;
+        M[3] = rho * s2;
         M[4] = M[1] * v;
-        M[5] = RT * dr + rho * u2;
-        M[6] = RT * dr + rho * v2;
+        M[5] = rho * u2;
+        M[6] = rho * v2;
         M[7] = M[1] * (5.f * RT + s2);
         M[8] = M[2] * (5.f * RT + s2);
         M[9] = M[1] * (3.f * RT + u2);
@@ -54,22 +56,22 @@ __device__ __forceinline__ void pp_deq(const PPP &P, float dr, float rho, float 
         M[11] = M[2] * (RT + u2);
         M[12] = M[1] * (RT + v2);
         M[13] = (7.f * RT + s2) * M[4];
-        M[14] = 5.f * RT * RT * dr + rho * RT * (8.f * u2 + v2) + rho * u2 * s2;
-        M[15] = 5.f * RT * RT * dr + rho * RT * (8.f * v2 + u2) + rho * v2 * s2;
+        M[14] = rho * RT * (8.f * u2 + v2) + rho * u2 * s2;
+        M[15] = rho * RT * (8.f * v2 + u2) + rho * v2 * s2;
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
             float s = 0.f;
 #pragma unroll
-            for (int k = 0; k < 16; ++k) s = fmaf(__ldg(P.iM16 + j * 16 + k), M[k], s);
+            for (int k = 1; k < 16; ++k) s = fmaf(__ldg(P.iM16 + j * 16 + k), M[k], s);
             de[j] = s;
         }
     } else {
-        // D2Q9PP (Ark/Lib/D2Q9PP.cpp:51-62): w rho (1 + u1 + u1^2/2 - |u|^2 lambda)
+        // D2Q9PP (Ark/Lib/D2Q9PP.cpp:51-62): w rho (1 + u1 + u1^2/2 - |u|^2 lambda) - w rho
         const float uu = u * u + v * v;
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
             const float u1 = (sxf(d2q9_xu(q), u) + sxf(d2q9_xv(q), v)) * P.invRT;
-            de[q] = P.w9[q] * (dr + rho * (u1 + 0.5f * u1 * u1 - uu * P.Lambda0));
+            de[q] = P.w9[q] * (rho * (u1 + 0.5f * u1 * u1 - uu * P.Lambda0));
         }
     }
 }
@@ -163,7 +165,8 @@ __device__ __forceinline__ void iso_grad(const PPP &P, const float *__restrict__
 }
 
 // Collision pre-step: cell force F = -G psi grad psi (Ark/Cpp/PseudoP.cpp:31-38, from the
-// previous update's psi) when do_msrc, equilibrium, source, f-bar-plus deviations.
+// previous update's psi) when do_msrc, equilibrium, source; f-bar-plus as the remainder
+// B_q - e_q rho = g_q + (1 - a)(de_q - g_q) + c S_q.
 template <int MODEL>
 __global__ void __launch_bounds__(256) k_pp32_collide(PPP P, PPS S, int do_msrc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -183,27 +186,29 @@ __global__ void __launch_bounds__(256) k_pp32_collide(PPP P, PPS S, int do_msrc)
         fx = S.Fx[c];
         fy = S.Fy[c];
     }
-    const double rhod = S.rho[c];
-    const float rho = (float)rhod, dr = (float)(rhod - P.rho_ref);
+    const float rho = (float)S.rho[c];
     const float U = (float)S.U[c], V = (float)S.V[c];
     float de[Q];
-    pp_deq<MODEL>(P, dr, rho, U, V, de);
+    pp_deq<MODEL>(P, rho, U, V, de);
     const float tau = P.Tau0;
     const float aBP = (2.f * tau - P.hDt) / (2.f * tau + P.dt), bBP = 1.f - aBP, cBP = tau * bBP;
     const float inv = 1.f / (rho * P.RT);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-        const float eq = P.frest[q] + de[q];
+        const float eq = fmaf(P.erest[q], rho, de[q]);
         const float So = (fx * (P.xi_u[q] - U) + fy * (P.xi_v[q] - V)) * eq * inv;
         const size_t o = (size_t)q * S.qs + c;
-        const float d = S.df[o];
-        S.bf[o] = d + (bBP * (de[q] - d) + cBP * So);
+        const float g = S.df[o];
+        S.bf[o] = g + (bBP * (de[q] - g) + cBP * So);
     }
 }
 
 // Face pass 1 (x faces: blockIdx.z = 0, y faces: 1): half-step reconstruction,
 // face moments with the previous face force, face pressure and psi
-// (Ark/Lib/D2Q9PP.cpp:110-136, Ark/Cpp/PseudoP.cpp:23-30).
+// (Ark/Lib/D2Q9PP.cpp:110-136, Ark/Cpp/PseudoP.cpp:23-30).  The face values are
+// stored relative to e_q times the face average of rho: the reconstruction of the
+// remainders plus e_q (L_q(rho) - avg), L_q(rho) the same reconstruction applied to the
+// FP64 density.
 template <int MODEL>
 __global__ void __launch_bounds__(256) k_pp32_faces1(PPP P, PPS S) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -213,9 +218,20 @@ __global__ void __launch_bounds__(256) k_pp32_faces1(PPP P, PPS S) {
     const int nx = P.nx, ny = P.ny, pitch = P.pitch;
     const int im = wrapi(i - 1, nx), ip = wrapi(i + 1, nx), jm = wrapi(j - 1, ny), jp = wrapi(j + 1, ny);
     const size_t c = (size_t)j * pitch + i;
-    // face moments as float-float sums: the first moments are small differences of the
-    // large deviations of opposite directions (liquid cells lie far from rho_ref), so a
-    // plain FP32 sum loses most of the face velocity's digits
+    auto rh = [&](int jj, int ii) { return S.rho[(size_t)jj * pitch + ii]; };
+    // the density's reconstruction: face average and hDt times its gradient
+    double ravg, hgx, hgy;
+    if (xf) {
+        ravg = 0.5 * (rh(j, im) + rh(j, i));
+        hgx = (double)P.hDt * ((rh(j, im) - rh(j, i)) * (double)P.r_ndx);
+        hgy = (double)P.hDt * ((0.5 * ((rh(jp, i) - rh(jm, i)) + (rh(jp, im) - rh(jm, im)))) * (double)P.r_2dy);
+    } else {
+        ravg = 0.5 * (rh(jm, i) + rh(j, i));
+        hgx = (double)P.hDt * ((0.5 * ((rh(j, im) - rh(j, ip)) + (rh(jm, im) - rh(jm, ip)))) * (double)P.r_n2dx);
+        hgy = (double)P.hDt * ((rh(jm, i) - rh(j, i)) * (double)P.r_ndy);
+    }
+    const float hgxf = (float)hgx, hgyf = (float)hgy;
+    // face moments as float-float sums
     FF sR{0.f, 0.f}, su{0.f, 0.f}, sv{0.f, 0.f};
     float *B = xf ? S.xb : S.yb;
 #pragma unroll
@@ -234,14 +250,16 @@ __global__ void __launch_bounds__(256) k_pp32_faces1(PPP P, PPS S) {
             gx = (0.5f * ((at(j, im) - at(j, ip)) + (at(jm, im) - at(jm, ip)))) * P.r_n2dx;
             gy = (o - n) * P.r_ndy;
         }
-        const float b = 0.5f * (o + n) - P.hDt * (gx * P.xi_u[q] + gy * P.xi_v[q]);
+        float b = 0.5f * (o + n) - P.hDt * (gx * P.xi_u[q] + gy * P.xi_v[q]);
+        b = fmaf(-P.erest[q], hgxf * P.xi_u[q] + hgyf * P.xi_v[q], b);
         B[(size_t)q * S.qs + c] = b;
         ff_acc(sR, b);
         ff_acc_prod(su, b, P.xi_u[q]);
         ff_acc_prod(sv, b, P.xi_v[q]);
     }
     sR = ff_norm(sR);
-    const FF R = ff_add(FF{P.rref_hi, P.rref_lo}, sR);
+    const float rah = (float)ravg;
+    const FF R = ff_add(FF{rah, (float)(ravg - (double)rah)}, sR);
     const float Rf = R.hi;
     float U = __fadd_rn(su.hi, su.lo) / Rf, V = __fadd_rn(sv.hi, sv.lo) / Rf;
     U += 0.5f * P.hDt * (xf ? S.xFx : S.yFx)[c] / Rf;
@@ -249,7 +267,7 @@ __global__ void __launch_bounds__(256) k_pp32_faces1(PPP P, PPS S) {
     const FF p = cs_p(P, R);
     float scg, psi;
     cs_psi(P, R, p, scg, psi);
-    (xf ? S.xr : S.yr)[c] = sR.hi;
+    (xf ? S.xr : S.yr)[c] = __fadd_rn(sR.hi, sR.lo);  // face rho - avg(rho)
     (xf ? S.xu : S.yu)[c] = U;
     (xf ? S.xv : S.yv)[c] = V;
     (xf ? S.xg : S.yg)[c] = scg;
@@ -257,7 +275,8 @@ __global__ void __launch_bounds__(256) k_pp32_faces1(PPP P, PPS S) {
 }
 
 // Face pass 2: face force from the face-psi stencil (Ark/Cpp/PseudoP.cpp:39-46,
-// Ark/Lib/GradSchemeBasic.h:181-208), equilibrium, source and flux xi.n.
+// Ark/Lib/GradSchemeBasic.h:181-208), equilibrium, source and flux xi.n of the face
+// values relative to e_q avg(rho).
 template <int MODEL>
 __global__ void __launch_bounds__(256) k_pp32_faces2(PPP P, PPS S) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -272,10 +291,11 @@ __global__ void __launch_bounds__(256) k_pp32_faces2(PPP P, PPS S) {
     (xf ? S.xFx : S.yFx)[c] = Fx;
     (xf ? S.xFy : S.yFy)[c] = Fy;
     const float dr = (xf ? S.xr : S.yr)[c];
-    const float R = ff_add(FF{P.rref_hi, P.rref_lo}, FF{dr, 0.f}).hi;
+    const size_t co = xf ? (size_t)j * P.pitch + wrapi(i - 1, P.nx) : (size_t)wrapi(j - 1, P.ny) * P.pitch + i;
+    const float R = (float)(0.5 * (S.rho[co] + S.rho[c]) + (double)dr);
     const float U = (xf ? S.xu : S.yu)[c], V = (xf ? S.xv : S.yv)[c];
     float de[Q];
-    pp_deq<MODEL>(P, dr, R, U, V, de);
+    pp_deq<MODEL>(P, R, U, V, de);
     const float tauh = P.Tau0;
     const float ah = 2.f * tauh / (2.f * tauh + P.hDt), bh = 1.f - ah, ch = tauh * bh;
     const float inv = 1.f / (R * P.RT);
@@ -283,27 +303,36 @@ __global__ void __launch_bounds__(256) k_pp32_faces2(PPP P, PPS S) {
     float *out = xf ? S.xfl : S.yfl;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-        const float eq = P.frest[q] + de[q];
+        const float eq = fmaf(P.erest[q], R, de[q]);
         const float So = (Fx * (P.xi_u[q] - U) + Fy * (P.xi_v[q] - V)) * eq * inv;
+        const float heq = fmaf(P.erest[q], dr, de[q]);  // eq - e_q avg(rho)
         const float b = B[(size_t)q * S.qs + c];
-        const float t = de[q] + ah * (b - de[q]) + ch * So;
+        const float t = heq + ah * (b - heq) + ch * So;
         out[(size_t)q * S.qs + c] = t * (xf ? P.xi_u[q] : P.xi_v[q]);
     }
 }
 
 // Update (Ark/Cpp/DUGKS2DSolver.cpp:748-792) and cell macros (Ark/Lib/D2Q9PP.cpp:89-109):
-// deviations + 4/3 (f-bar-plus - deviations) + dt/V sum(F), rounded stochastically;
-// rho, U, V, p, psi from float-float sums (rho and p kept in FP64).
+//   rho_new = rho + drho, drho = dt/V sum_q (net face flux of q),
+//   g_q,new = g_q + 4/3 (b_q - g_q) + dt/V (net flux of q)
+//             + e_q (xi_q,x px + xi_q,y py) - e_q drho   (stochastically rounded),
+// px = dt/V (rho_W - rho_E)/2, py = dt/V (rho_S - rho_N)/2 (the e_q avg(rho) flux
+// divergence on unit cells, from the FP64 density); U, V, p, psi from float-float
+// sums, rho in FP64.
 template <int MODEL>
 __global__ void __launch_bounds__(256) k_pp32_update(PPP P, PPS S, uint32_t step) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= P.nx || j >= P.ny) return;
     constexpr int Q = MODEL == PP16 ? 16 : 9;
     const int pitch = P.pitch;
-    const int ip = wrapi(i + 1, P.nx), jn = wrapi(j + 1, P.ny);
+    const int ip = wrapi(i + 1, P.nx), im = wrapi(i - 1, P.nx), jn = wrapi(j + 1, P.ny), js = wrapi(j - 1, P.ny);
     const size_t c = (size_t)j * pitch + i, cE = (size_t)j * pitch + ip, cN = (size_t)jn * pitch + i;
     const uint32_t h0 = mix32((uint32_t)c * 0x9E3779B1U ^ step * 0x85EBCA77U);
-    FF sR{0.f, 0.f}, su{0.f, 0.f}, sv{0.f, 0.f};
+    const double rho = S.rho[c];
+    const float px = (float)(0.5 * (double)P.dtV * (S.rho[(size_t)j * pitch + im] - S.rho[cE]));
+    const float py = (float)(0.5 * (double)P.dtV * (S.rho[(size_t)js * pitch + i] - S.rho[cN]));
+    float sq[Q];
+    FF sd{0.f, 0.f};
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         const size_t o = (size_t)q * S.qs;
@@ -312,30 +341,56 @@ __global__ void __launch_bounds__(256) k_pp32_update(PPP P, PPS S, uint32_t step
         s += -S.yfl[o + cN];
         s += S.xfl[o + c];
         s += S.yfl[o + c];
-        const float d = S.df[o + c];
-        const float dn = sr1(d, P.aTP * (S.bf[o + c] - d) + P.dtV * s, h0 * SR_KEY[q]);
-        S.df[o + c] = dn;
-        ff_acc(sR, dn);
-        ff_acc_prod(su, dn, P.xi_u[q]);
-        ff_acc_prod(sv, dn, P.xi_v[q]);
+        sq[q] = s;
+        ff_acc(sd, s);
     }
-    const FF R = ff_add(FF{P.rref_hi, P.rref_lo}, ff_norm(sR));
-    const float Rf = R.hi;
-    float U = __fadd_rn(su.hi, su.lo) / Rf, V = __fadd_rn(sv.hi, sv.lo) / Rf;
-    U += P.hDt * S.Fx[c] / Rf;
-    V += P.hDt * S.Fy[c] / Rf;
+    const double drho = (double)P.dtV * ((double)sd.hi + (double)sd.lo);
+    const float drf = (float)drho;
+    const double rho_n = rho + drho;
+    FF su{0.f, 0.f}, sv{0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const size_t o = (size_t)q * S.qs;
+        const float g = S.df[o + c];
+        float inc = fmaf(P.aTP, S.bf[o + c] - g, P.dtV * sq[q]);
+        inc = fmaf(P.erest[q], (P.xi_u[q] * px + P.xi_v[q] * py) - drf, inc);
+        const float gn = sr1(g, inc, h0 * SR_KEY[q]);
+        S.df[o + c] = gn;
+        ff_acc_prod(su, gn, P.xi_u[q]);
+        ff_acc_prod(sv, gn, P.xi_v[q]);
+    }
+    const float rh = (float)rho_n;
+    const FF R{rh, (float)(rho_n - (double)rh)};
+    float U = __fadd_rn(su.hi, su.lo) / rh, V = __fadd_rn(sv.hi, sv.lo) / rh;
+    U += P.hDt * S.Fx[c] / rh;
+    V += P.hDt * S.Fy[c] / rh;
     const FF p = cs_p(P, R);
     float scg, psi;
     cs_psi(P, R, p, scg, psi);
-    // rho_ref + the sum in FP64: the next collision takes rho - rho_ref as the
-    // deviations' sum, and a representation offset of rho_ref (even of 1e-16, as
-    // in the float-float R) made the mass drift steadily
-    S.rho[c] = P.rho_ref + ff_to_double(ff_norm(sR));
+    S.rho_o[c] = rho_n;
     S.U[c] = U;
     S.V[c] = V;
     S.p[c] = ff_to_double(p);
     S.scg[c] = scg;
     S.psi[c] = psi;
+}
+
+// One FP64 distribution plane f_q [ny][nx] (dense, as the C ABI passes it) as the
+// stored remainder g_q = f_q - e_q rho, rho the FP64 density [ny][pitch]
+__global__ void __launch_bounds__(256) k_pp_g_from_f64(float *g, int pitch, const double *__restrict__ f,
+                                                       const double *__restrict__ rho, int nx, int ny, double e) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= nx || j >= ny) return;
+    const size_t d = (size_t)j * pitch + i;
+    g[d] = (float)__dsub_rn(f[(size_t)j * nx + i], __dmul_rn(e, rho[d]));
+}
+
+cudaError_t launch_pp_g_from_f64(float *g, int pitch, const double *f, const double *rho, int nx, int ny, double e,
+                                 cudaStream_t st, int64_t *launches) {
+    const dim3 grd((nx + 255) / 256, ny);
+    k_pp_g_from_f64<<<grd, 256, 0, st>>>(g, pitch, f, rho, nx, ny, e);
+    *launches += 1;
+    return cudaGetLastError();
 }
 
 // the cell force of the current psi (the state the reference holds after a step)

@@ -77,32 +77,34 @@ constexpr int GPHI_ROWS = 8;
 // first of the two rows (head, then tail) of buffer buf (0, 1) and side (0 bottom, 1 top)
 __host__ __device__ __forceinline__ size_t gphi_row(int buf, int side) { return (size_t)(buf * 2 + side) * 2; }
 
-// ---- FP32 deviation storage of the pseudopotential models (D2Q9PP, D2V16)
-// Constants: FP32 step coefficients, the velocity set, the rest equilibrium
-// f_rest = eq(rho_ref, 0, 0) the deviations are taken from, and the
+// ---- FP32 storage of the pseudopotential models (D2Q9PP, D2V16)
+// Constants: FP32 step coefficients, the velocity set, the rest equilibrium per
+// unit density e_q = eq_q(1, 0, 0) (the state holds f_q - e_q rho), and the
 // Carnahan-Starling constants in FP64 (the pressure and psi are evaluated from
 // the FP64 density).
 struct PPP {
     int nx, ny, pitch, model, Q;
     float hDt, dt, RT, invRT, Lambda0, Tau0, aTP, bTP, dtV;
     float r_2dy, r_ndx, r_n2dx, r_ndy, inv_6_2dx, inv_6_2dy;
-    double rho_ref, R0, T_CS, aCS, RTd;
+    double R0, T_CS, aCS, RTd;
     // the same constants as float-float pairs (hi + lo) for the device arithmetic:
-    // rho_ref, R0 T_CS, aCS, RT
-    float rref_hi, rref_lo, rtcs_hi, rtcs_lo, acs_hi, acs_lo, rt_hi, rt_lo;
-    float xi_u[16], xi_v[16], w9[9], frest[16];
+    // R0 T_CS, aCS, RT
+    float rtcs_hi, rtcs_lo, acs_hi, acs_lo, rt_hi, rt_lo;
+    float xi_u[16], xi_v[16], w9[9], erest[16];
     // D2V16 inverse moment matrix of this case ([16][16], in the case's device memory):
     // each case holds its own, so cases of different lattice speed run side by side
     const float *iM16;
 };
-// State: f deviations and the step's scratch in FP32, the density (and the
-// pressure for output) in FP64.
+// State: the remainders g_q = f_q - e_q rho and the step's scratch in FP32, the
+// density (and the pressure for output) in FP64; the density in two planes: the
+// update reads its neighbours' density while it writes its own into rho_o, and the
+// two swap after each step.
 struct PPS {
-    float *df, *bf;                  // [Q][ny][pitch]
+    float *df, *bf;                  // g and the collision's remainders B_q - e_q rho [Q][ny][pitch]
     float *xb, *yb, *xfl, *yfl;      // face reconstructions and fluxes [Q][ny][pitch]
     float *xr, *yr, *xu, *yu, *xv, *yv, *xg, *yg, *xps, *yps;  // face rho, U, V, G, psi
     float *xFx, *xFy, *yFx, *yFy;    // face forces (kept for the next step's face velocity)
-    double *rho, *p, *U, *V;         // cell density, pressure and velocity
+    double *rho, *rho_o, *p, *U, *V; // cell density (read / written by the update), pressure, velocity
     float *psi, *scg, *Fx, *Fy;
     size_t qs;
 };
