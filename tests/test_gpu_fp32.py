@@ -56,26 +56,20 @@ def test_fp32_first_step_matches_fp64():
 # hcz_rt is checked over 50 steps: after 50-100 steps the reference's own
 # discontinuous |grad phi| < 1e-14 clamp flips on rounding-level differences
 # (even the FMA-contracted FP64 variant departs there).
-# Velocity of the static HCZ drop is the spurious current (max |u| ~5e-4), the
-# residual of the surface-tension / pressure balance, and follows the interface
-# shape; the stochastically rounded FP32 state random-walks that shape, so the
-# velocity error grows ~sqrt(steps): 4e-6 at 200 steps, 8e-6 at 1000, 1.1e-5 at
-# 2000 (L2).  The target 1e-5 is asserted on velocity at 1000 steps and 2e-5 at 2000.
-@pytest.mark.parametrize('name,steps,utol', [('ac_c1', 2000, TARGET), ('hcz_drop', 1000, TARGET),
-                                             ('hcz_drop', 2000, 2 * TARGET), ('hcz_rt', 50, TARGET)])
-def test_fp32_error_vs_fp64(name, steps, utol):
+# Every field, velocity included, is held to the target in the max-norm relative to
+# the field's largest value.  The static drop's velocity is its spurious current
+# (max |u| ~5e-4): the phase field is stored as phi (float-float) plus small
+# remainders, so its rounding no longer moves the interface that drives that current.
+@pytest.mark.parametrize('name,steps', [('ac_c1', 2000), ('hcz_drop', 1000), ('hcz_drop', 2000), ('hcz_rt', 50)])
+def test_fp32_error_vs_fp64(name, steps):
     v = VARIANTS[name]
     a, b = make(v, 'fp32dev'), make(v, 'fp64')
     a.step(steps)
     b.step(steps)
     errs = field_errors(a, b)
     print(name, steps, {k: f'Linf {e[0]:.2e} L2 {e[1]:.2e}' for k, e in errs.items()})
-    for k in ('rho', 'p', 'phi'):
+    for k in ('rho', 'p', 'phi', 'u', 'v'):
         assert errs[k][0] <= TARGET, (k, errs[k])
-
-    if MODEL[v['model']] == 'HCZ':
-        for k in ('u', 'v'):
-            assert errs[k][1] <= utol, (k, errs[k])
     assert a.check_finite() == 0
 
 
@@ -117,7 +111,6 @@ def test_fp32_many_tiles_vs_fp64():
     for k in ('rho', 'u', 'v', 'p', 'phi'):
         assert np.array_equal(runs[0].get(k), runs[1].get(k)), k
     errs = field_errors(runs[0], runs[2])
-    for k in ('rho', 'p', 'phi'):
+    print({k: f'Linf {e[0]:.2e} L2 {e[1]:.2e}' for k, e in errs.items()})
+    for k in ('rho', 'p', 'phi', 'u', 'v'):
         assert errs[k][0] <= TARGET, (k, errs[k])
-    for k in ('u', 'v'):
-        assert errs[k][1] <= TARGET, (k, errs[k])

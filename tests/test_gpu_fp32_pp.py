@@ -1,14 +1,14 @@
-"""FP32 deviation storage of the pseudopotential models (D2Q9PP, D2V16) against
-the plain FP64 path.
+"""FP32 storage of the pseudopotential models (D2Q9PP, D2V16) against the plain FP64
+path.
 
-Errors per field: max-norm and L2 ratios ||a - b|| / ||b|| over the grid.
-Horizons: the D2Q9PP droplet is stable (2000 steps).  The D2V16 model (the
-reference's D2V16 does not build; this is its restatement) diverges within a
-few hundred steps in FP64 as well, at every tested setting (CPU restatement:
-SCMP_Drop and seeded noise, T/Tc 0.7-0.85), so its comparison stops at 100
-steps, before the divergence.  Phase separation from seeded noise amplifies
-any perturbation (FP64 variants differ as well), so noise cases are compared
-over 100 steps.
+Errors per field: max-norm and L2 ratios ||a - b|| / ||b|| over the grid.  The
+resting droplets are held to 1e-5 in the max-norm on every field over 2000 steps.
+D2V16 runs at the lattice speed c = 0.5: at the reference's c = 1.2 (T0 = 1/3) the
+rest equilibrium of the 2c axis ring is -0.36 rho and the linearised step is unstable
+for relaxation times above ~0.3 (tests/test_d2v16_stability.py), so a droplet there
+diverges within a few hundred steps in FP64 as well.  Phase separation from seeded
+noise amplifies any perturbation, rounding included: those cases are compared
+against the spread that two FP64 evaluations (plain and FMA-contracted) already show.
 """
 import numpy as np
 import pytest
@@ -16,13 +16,14 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def pair(model, n, init, params):
+def pair(model, n, init, params, precisions=('fp32dev', 'fp64'), **kw):
     from mpdugks_gb300 import capi
-    a = capi.GpuCase(capi.make_case(model, 'fp32dev'), n, n, False)
-    b = capi.GpuCase(capi.make_case(model, 'fp64'), n, n, False)
-    a.init(init, params, seed=7)
-    b.init(init, params, seed=7)
-    return a, b
+    out = []
+    for prec in precisions:
+        g = capi.GpuCase(capi.make_case(model, prec, **kw), n, n, False)
+        g.init(init, params, seed=7)
+        out.append(g)
+    return out
 
 
 def errors(a, b):
@@ -34,23 +35,33 @@ def errors(a, b):
     return out
 
 
-@pytest.mark.parametrize('model,n,init,params,steps,tol', [
-    # (rho max-norm, p max-norm, u/v L2)
-    ('PP9', 32, 'scmp_drop', [], 2000, (1e-5, 5e-5, 5e-5)),
-    ('PP9', 64, 'pp_noise', [0.2, 0.01], 100, (1e-5, 1e-5, 1e-4)),
-    ('PP16', 32, 'scmp_drop', [], 100, (1e-5, 5e-5, 1e-4)),
-    ('PP16', 64, 'pp_noise', [0.2, 0.01], 100, (1e-5, 1e-5, 1e-4)),
-])
-def test_fp32_pseudopotential_close_to_fp64(model, n, init, params, steps, tol):
-    a, b = pair(model, n, init, params)
-    a.step(steps)
-    b.step(steps)
+@pytest.mark.parametrize('model,kw', [('PP9', {}), ('PP16', dict(d2v16_c=0.5))])
+def test_fp32_pseudopotential_droplet_within_target(model, kw):
+    a, b = pair(model, 32, 'scmp_drop', [], **kw)
+    a.step(2000)
+    b.step(2000)
     e = errors(a, b)
-    print(model, n, init, steps, {k: f'{v[0]:.2e}/{v[1]:.2e}' for k, v in e.items()})
+    print(model, {k: f'{v[0]:.2e}/{v[1]:.2e}' for k, v in e.items()})
     assert a.check_finite() == 0
-    assert e['rho'][0] <= tol[0], e
-    assert e['p'][0] <= tol[1], e
-    assert e['u'][1] <= tol[2] and e['v'][1] <= tol[2], e
+    for k in ('rho', 'p', 'u', 'v'):
+        assert e[k][0] <= 1e-5, (k, e)
+
+
+@pytest.mark.parametrize('model,kw', [('PP9', {}), ('PP16', dict(d2v16_c=0.5))])
+def test_fp32_pseudopotential_noise_within_fp64_spread(model, kw):
+    """Spinodal growth from 1 % density noise (100 steps): FP32 storage against FP64 is
+    within the target on rho and p, and its velocity difference is of the size that the
+    FMA-contracted FP64 variant already shows against plain FP64."""
+    a, b, c = pair(model, 64, 'pp_noise', [0.2, 0.01], ('fp32dev', 'fp64', 'fp64fma'), **kw)
+    for g in (a, b, c):
+        g.step(100)
+    e, efma = errors(a, b), errors(c, b)
+    print(model, {k: f'{v[0]:.2e}/{v[1]:.2e}' for k, v in e.items()},
+          'fma', {k: f'{v[0]:.2e}/{v[1]:.2e}' for k, v in efma.items()})
+    assert a.check_finite() == 0
+    assert e['rho'][0] <= 1e-5 and e['p'][0] <= 1e-5, e
+    for k in ('u', 'v'):
+        assert e[k][0] <= max(1e-5, 10 * efma[k][0]), (k, e, efma)
 
 
 def test_fp32_pseudopotential_conserves_mass():
@@ -64,9 +75,9 @@ def test_fp32_pseudopotential_conserves_mass():
 
 
 def test_fp32_pseudopotential_fields_and_distributions():
-    """Distributions round-trip through the deviation storage; forces and psi are exposed."""
-    from mpdugks_gb300 import capi
-    a, b = pair('PP16', 32, 'scmp_drop', [])
+    """Distributions round-trip through the storage (rho in FP64 plus FP32 remainders);
+    forces and psi are exposed."""
+    a, b = pair('PP16', 32, 'scmp_drop', [], d2v16_c=0.5)
     fa, fb = a.dist('f'), b.dist('f')
     assert np.max(np.abs(fa - fb)) <= 1e-7 * np.max(np.abs(fb))
     a.step(5)
