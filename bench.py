@@ -46,10 +46,14 @@ WORKLOADS = {
                        name='rayleigh_taylor_512x2048_hcz_walls', full_steps=20000, yc=2.0),
 }
 
-# algorithmic HBM bytes per cell and step (state read once + written once)
-#   FP32 storage, HCZ: 18 deviations + 6 aux planes, 4 B each, read and written = 192 B
-#   FP64 (multi-kernel step): 18 distributions + 2 aux planes, 8 B, read and written = 320 B
-ALGO_BYTES = {'fp32dev': 192, 'fp64': 320, 'fp64fma': 320, 'fp64fused': 384}
+# algorithmic HBM bytes per cell and step: the compulsory state, read once and written once
+#   FP32 storage, Allen-Cahn D2Q9: 18 distributions + 2 aux (prev phi u, v), 4 B each = 160 B
+#   FP64 (multi-kernel step): 18 distributions + 2 aux planes, 8 B each = 320 B
+ALGO_BYTES = {'fp32dev': 160, 'fp64': 320, 'fp64fma': 320, 'fp64fused': 320}
+# bytes the FP32 step actually stores per cell and step: a state copy is 25 FP32 planes
+# (9 f, 8 phase-field remainders, the phi pair, 6 aux: the force and density gradient
+# are kept rather than recomputed), read and written
+STORED_BYTES = {'fp32dev': 200, 'fp64': 320, 'fp64fma': 320, 'fp64fused': 400}
 # DRAM bytes per cell and step of the fused FP32 kernel: ncu dram__bytes_read.sum +
 # dram__bytes_write.sum of one k_stream32 launch on 3072x3072 cells, divided by the cells
 # (profiles/k_stream32_rt3072x3072_fp32.md); scaled by the cell count to a full launch
@@ -75,6 +79,43 @@ def load_peaks():
         d = json.loads(p.read_text())
         return float(d.get('hbm_gbs', 6800.0)), 'measured'
     return 6800.0, 'fallback'
+
+
+def fp64_peak_tflops(n: int = 4096, reps: int = 5) -> float:
+    """FP64 throughput this GPU reaches in a library GEMM (torch float64 matmul, cuBLAS
+    DGEMM, 2 n^3 flops), best of `reps`: the denominator of the FP64 path's %FP64."""
+    import torch
+    a = torch.randn(n, n, dtype=torch.float64, device='cuda')
+    b = torch.randn(n, n, dtype=torch.float64, device='cuda')
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = float('inf')
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def fp64_pipe(lups: float) -> dict:
+    """The plain FP64 step against the FP64 rate a library GEMM reaches on this GPU."""
+    peak = fp64_peak_tflops()
+    out = {'peak_tflops': round(peak, 4), 'peak_source': 'measured: torch float64 matmul 4096^3 (cuBLAS DGEMM)'}
+    if FP64_FLOPS_PER_CELL:
+        ach = FP64_FLOPS_PER_CELL * lups / 1e12
+        out.update({'flops_per_cell': FP64_FLOPS_PER_CELL, 'achieved_tflops': round(ach, 4),
+                    'frac': round(ach / peak, 4)})
+    return out
+
+
+# FP64 operations per cell-update of the plain FP64 step (k_collide + k_faces_ac + k_update
+# on the 512x2048 Rayleigh-Taylor case, reference-exact variant): ncu counts of the DADD,
+# DMUL and DFMA thread instructions of one step divided by the cells, a DFMA counted as two
+# (profiles/fp64_step_rt512x2048_fp64_ops.md)
+FP64_FLOPS_PER_CELL = None
 
 
 class ClockSampler:
@@ -241,18 +282,24 @@ def serving_stream(cases: int, steps: int, seed: int):
     return out
 
 
-# Carnahan-Starling with a = 0.5, b = 4, R = 1: Tc = 0.3773 a / b, rho_c = 0.13044 / b
-PP_A, PP_TC, PP_RHO_C = 0.5, 0.3773 * 0.5 / 4.0, 0.13044 / 4.0
-# the pseudopotential cases are checked every 100 steps (the Allen-Cahn cases every
-# 1000, the reference's residual cadence): the restated D2V16 model diverges within a
-# few hundred steps at these settings, and a non-finite case should stop soon
-PP_CHECK_EVERY = 100
+# Carnahan-Starling with a = 0.5, b = 4, R = 1 (the EOS of Ark/Lib/nonidealEoS.h, whose b is 4):
+# Tc = 0.3773 a / (b R), rho_c = 0.5218 / b (eta_c = b rho_c / 4 = 0.13044)
+PP_A, PP_TC, PP_RHO_C = 0.5, 0.3773 * 0.5 / 4.0, 0.13044
+# D2V16 lattice speed and viscosity of the pseudopotential cases.  The reference's
+# c = 1.2 is linearly unstable for relaxation times above ~0.3 (oracle/d2v16_stability.py),
+# which a vapour phase (nu = Mu0 / rho) always reaches; c = 0.5 is stable for nu from
+# 0.01 to 10.  Mu0 is not given by the configurations: 0.3 keeps the spurious currents of
+# the separated phases (~0.1 at T = 0.7 Tc) finite, where 0.03 and 1.0 diverge.
+D2V16_C, PP_MU0 = 0.5, 0.3
+# the pseudopotential cases are checked every 1000 steps, like the Allen-Cahn cases
+# (the reference's residual cadence)
+PP_CHECK_EVERY = 1000
 
 
 def serving_case(c: dict, precision: str):
     from mpdugks_gb300 import capi
     if c['model'] == 'PP16':
-        return capi.make_case('PP16', precision, Tr=c['tr'], aCS=PP_A, Tc_CS=PP_TC)
+        return capi.make_case('PP16', precision, Tr=c['tr'], aCS=PP_A, Tc_CS=PP_TC, d2v16_c=D2V16_C, Mu0=PP_MU0)
     return capi.make_case('AC', precision, Mu0=0.02, M_Phi=0.02, W=4.0, Sigma=c['sigma'], RhoL=1.0,
                           RhoV=c['rho_v'])
 
@@ -315,49 +362,62 @@ def serving_bench(args) -> dict:
     tts, finite, lu, span, stats, pp = serve(True)
     btts, bfinite, blu, bspan, bstats, bpp = serve(False)
     done = len(tts)
-    # one case at a time on a sample of the stream's Allen-Cahn cases (the first ones)
-    sample = ac[:args.serving_sample]
+    # One case at a time, the comparators: a sample of the stream's Allen-Cahn cases that
+    # spans its grid sizes (every k-th case in the order of N), each stepped on its own
+    # for a fraction of its steps; a case's time is its measured per-step time times its
+    # step count, and the stream's time is the sum over the stream's Allen-Cahn cases of
+    # the per-cell-update time of the sample case nearest in N.
+    by_n = sorted(ac, key=lambda c: c['n'])
+    k = max(1, len(by_n) // max(1, args.serving_sample))
+    sample = by_n[k // 2::k][:args.serving_sample]
 
     def one_at_a_time(precision):
-        torch.cuda.synchronize()
-        ta = time.perf_counter()
-        slu = 0
+        rates = []
         for c in sample:
             gc = capi.GpuCase(serving_case(c, precision), c['n'], c['n'], False)
             gc.init(c['init'], c['params'])
-            gc.step(c['steps'])
+            gc.step(2)
+            torch.cuda.synchronize()
+            nst = max(20, c['steps'] // args.serving_fraction)
+            ta = time.perf_counter()
+            gc.step(nst)
             gc.get('rho')
-            slu += c['n'] * c['n'] * c['steps']
+            el = time.perf_counter() - ta
+            rates.append((c['n'], el / (c['n'] * c['n'] * nst)))  # seconds per cell update
             del gc
-        torch.cuda.synchronize()
-        el = time.perf_counter() - ta
-        return {'cases': len(sample), 'seconds': round(el, 3), 'cases_per_s': round(len(sample) / el, 4),
-                'mlups': round(slu / el / 1e6, 2),
-                'stream_cases_per_s_projected': round(done / (lu / (slu / el)), 4) if lu else None}
+        ns = np.array([r[0] for r in rates])
+        total = 0.0
+        for c in ac:
+            sec_per_lu = rates[int(np.argmin(np.abs(ns - c['n'])))][1]
+            total += sec_per_lu * c['n'] * c['n'] * c['steps']
+        return {'sample_cases': len(sample), 'sample_n': [int(x) for x in ns],
+                'steps_timed_per_case': f'max(20, steps / {args.serving_fraction})',
+                'mlups_sample_median': round(float(np.median([1e-6 / r[1] for r in rates])), 2),
+                'stream_seconds_projected': round(total, 3),
+                'stream_cases_per_s_projected': round(len(ac) / total, 4)}
 
     fp64 = one_at_a_time('fp64')
     fp32 = one_at_a_time('fp32dev')
     cps = done / span if span > 0 else 0.0
+    bcps = len(btts) / bspan if bspan > 0 else 0.0
     return {
         'workload': f'{args.serving_cases}-case seeded stream (Poisson 20/s, N lognormal median 256 in '
                     f'[64,1024], {args.serving_steps} steps each, FP32 storage): {len(ac)} Allen-Cahn droplets/'
                     f'bubbles (R=N/5, density ratio U[2,100], sigma U[1e-4,1e-2]) and {len(stream) - len(ac)} '
-                    'D2V16 pseudopotential cases (T/Tc U[0.6,0.85], CS a=0.5 b=4, rho_c(1+0.01U) noise); '
-                    f'checked every 1000 (Allen-Cahn) / {PP_CHECK_EVERY} (D2V16) steps',
+                    f'D2V16 pseudopotential cases (T/Tc U[0.6,0.85], CS a=0.5 b=4, rho_c(1+0.01U) noise, '
+                    f'lattice speed {D2V16_C}, Mu0 {PP_MU0}); checked every 1000 steps',
         'allen_cahn': 'completed, span, cases_per_s, mlups and tts are of the Allen-Cahn cases',
         'completed': done, 'finite': finite, 'span_s': round(span, 3), 'cases_per_s': round(cps, 4),
         'mlups': round(lu / span / 1e6, 2) if span > 0 else None,
         'mlups_all_cases': round(stats.cell_updates / span / 1e6, 2) if span > 0 else None,
         'tts_p50_s': round(float(np.percentile(tts, 50)), 4) if tts else None,
         'tts_p99_s': round(float(np.percentile(tts, 99)), 4) if tts else None,
-        'pseudopotential_d2v16': dict(pp, note='the restated D2V16 model diverges at these settings in FP64 '
-                                               'as well; each such case stops at the first check after it '
-                                               'becomes non-finite'),
+        'pseudopotential_d2v16': pp,
         'max_resident': stats.max_resident, 'graphs_captured': stats.graphs_captured, 'chunks': stats.chunks,
         'bytes_peak': stats.bytes_peak, 'max_bytes': stats.max_bytes, 'solo_steps': stats.solo_steps,
         'burst': {'how': 'the same cases all submitted at once (capacity)', 'completed': len(btts),
                   'finite': bfinite, 'span_s': round(bspan, 3),
-                  'cases_per_s': round(len(btts) / bspan, 4) if bspan > 0 else None,
+                  'cases_per_s': round(bcps, 4) if bspan > 0 else None,
                   'mlups': round(blu / bspan / 1e6, 2) if bspan > 0 else None,
                   'mlups_all_cases': round(bstats.cell_updates / bspan / 1e6, 2) if bspan > 0 else None,
                   'tts_p50_s': round(float(np.percentile(btts, 50)), 4) if btts else None,
@@ -365,27 +425,90 @@ def serving_bench(args) -> dict:
                   'pseudopotential_d2v16': bpp,
                   'max_resident': bstats.max_resident, 'bytes_peak': bstats.bytes_peak},
         'one_at_a_time_fp64': fp64, 'one_at_a_time_fp32': fp32,
-        'vs_one_at_a_time_fp64': round(cps / fp64['stream_cases_per_s_projected'], 2)
-        if fp64['stream_cases_per_s_projected'] else None,
+        # the gain of the server over one case at a time: against the plain FP64 path
+        # (precision and batching together) and against FP32 storage without batching
+        # (batching alone), paced at the stream's arrivals and at capacity
+        'vs_one_at_a_time_fp64': round(cps / fp64['stream_cases_per_s_projected'], 2),
+        'vs_one_at_a_time_fp32': round(cps / fp32['stream_cases_per_s_projected'], 2),
+        'capacity_vs_one_at_a_time_fp64': round(bcps / fp64['stream_cases_per_s_projected'], 2),
+        'capacity_vs_one_at_a_time_fp32': round(bcps / fp32['stream_cases_per_s_projected'], 2),
     }
 
 
 # ---------------------------------------------------------------- pseudopotential D2V16
 
-def pseudopotential_bench(steps: int = 100) -> dict:
-    """The pseudopotential configuration: D2V16, 1024x1024 periodic, seeded density
-    noise rho = 0.2 (1 + 0.01 U(-1, 1)), Carnahan-Starling EOS (the reference's default
-    constants: a = 1, b = 4, T = 0.85 Tc); FP32 deviation storage against the plain FP64
-    path on the same grid, MLUPS and per-field errors after `steps` steps."""
+def cs_pressure(rho, T, a=PP_A):
+    """Carnahan-Starling pressure of Ark/Lib/nonidealEoS.h (R = 1, b = 4: eta = rho)."""
+    return rho * T * (1 + rho + rho ** 2 - rho ** 3) / (1 - rho) ** 3 - a * rho ** 2
+
+
+def maxwell_densities(Tr: float) -> tuple[float, float]:
+    """Coexisting vapour and liquid densities of the Carnahan-Starling EOS at T = Tr Tc by
+    the Maxwell construction: the saturation pressure p_s at which the two branches
+    enclose equal areas, int_{rho_v}^{rho_l} (p - p_s) / rho^2 drho = 0 (equal areas in
+    the specific volume 1/rho); p_s by bisection, the area being monotone in p_s."""
     import numpy as np
-    import torch
+    from scipy.integrate import quad
+    from scipy.optimize import brentq
+    T = Tr * PP_TC
+    grid = np.linspace(1e-5, 0.7, 70001)
+    pr = cs_pressure(grid, T)
+    d = np.diff(pr)
+    i1 = int(np.argmax(d < 0))                  # the vapour-side spinodal (local maximum)
+    i2 = i1 + int(np.argmax(d[i1:] > 0))        # the liquid-side spinodal (local minimum)
+    s1, s2 = grid[i1], grid[i2]
+
+    def branches(ps):
+        return (brentq(lambda r: cs_pressure(r, T) - ps, 1e-12, s1, xtol=1e-15),
+                brentq(lambda r: cs_pressure(r, T) - ps, s2, 0.999, xtol=1e-15))
+
+    def area(ps):
+        rv, rl = branches(ps)
+        return quad(lambda r: (cs_pressure(r, T) - ps) / r ** 2, rv, rl, limit=200, epsabs=1e-14)[0]
+    lo, hi = max(cs_pressure(s2, T), 1e-14), cs_pressure(s1, T)
+    for _ in range(100):
+        mid = 0.5 * (lo + hi)
+        if area(mid) > 0:
+            lo = mid
+        else:
+            hi = mid
+    rv, rl = branches(0.5 * (lo + hi))
+    return float(rv), float(rl)
+
+
+C3 = dict(n=1024, Tr=0.7, steps=50000)
+
+
+def c3_case(precision: str):
     from mpdugks_gb300 import capi
-    n = 1024
+    return capi.make_case('PP16', precision, Tr=C3['Tr'], aCS=PP_A, Tc_CS=PP_TC, d2v16_c=D2V16_C, Mu0=PP_MU0)
+
+
+def phase_densities(rho) -> dict:
+    """Vapour and liquid densities of a separated field: the mean density of the cells
+    below / above the critical density, and the 1st / 99th percentiles."""
+    import numpy as np
+    r = rho.ravel()
+    lo, hi = r[r < PP_RHO_C], r[r >= PP_RHO_C]
+    return {'vapour_mean': float(lo.mean()) if lo.size else None, 'liquid_mean': float(hi.mean()) if hi.size else None,
+            'p1': float(np.percentile(r, 1)), 'p99': float(np.percentile(r, 99)),
+            'liquid_fraction': float(hi.size / r.size)}
+
+
+def pseudopotential_bench(steps: int = 100) -> dict:
+    """The pseudopotential configuration (C3): D2V16, 1024x1024 periodic, Carnahan-Starling
+    a = 0.5, b = 4, R = 1 at T = 0.7 Tc, density rho_c (1 + 0.01 U(-1, 1)) from seed; FP32
+    storage against the plain FP64 path on the same grid: MLUPS, HBM fraction and the
+    per-field errors after `steps` steps, beside the FMA-contracted FP64 variant against
+    plain FP64 (spinodal growth amplifies any difference, rounding included)."""
+    import torch
+    n = C3['n']
     st = torch.cuda.Stream()
     out, cases = {}, {}
-    for prec in ('fp32dev', 'fp64'):
-        g = capi.GpuCase(capi.make_case('PP16', prec), n, n, False)
-        g.init('pp_noise', [0.2, 0.01], seed=2026)
+    for prec in ('fp32dev', 'fp64', 'fp64fma'):
+        from mpdugks_gb300 import capi
+        g = capi.GpuCase(c3_case(prec), n, n, False)
+        g.init('pp_noise', [PP_RHO_C, 0.01], seed=2026)
         g.step(3, st.cuda_stream)
         ms, launches, _ = timed_steps(g, steps, st)
         mlups = n * n * steps / (ms * 1e-3) / 1e6
@@ -397,17 +520,49 @@ def pseudopotential_bench(steps: int = 100) -> dict:
                      'hbm_frac': round(mlups * algo / 1e3 / load_peaks()[0], 4), 'peak': load_peaks()[1]}
         cases[prec] = g
     errs = field_errors(cases['fp32dev'], cases['fp64'])
-    del errs['phi']
+    efma = field_errors(cases['fp64fma'], cases['fp64'])
+    for e in (errs, efma):
+        del e['phi']
     return {
-        'workload': f'D2V16 pseudopotential, {n}x{n} periodic, seeded noise rho = 0.2(1 + 0.01 U(-1,1)), '
-                    'Carnahan-Starling a=1 b=4, T = 0.85 Tc',
-        'fp32': out['fp32dev'], 'fp64': out['fp64'],
+        'workload': f'D2V16 pseudopotential (C3), {n}x{n} periodic, Carnahan-Starling a=0.5 b=4 R=1, '
+                    f'T = {C3["Tr"]} Tc, rho_c(1 + 0.01 U(-1,1)) seeded, lattice speed {D2V16_C}, Mu0 {PP_MU0}',
+        'fp32': out['fp32dev'], 'fp64': out['fp64'], 'fp64fma': out['fp64fma'],
         'fp32_speedup': round(out['fp32dev']['mlups'] / out['fp64']['mlups'], 2),
         'fp32_error_vs_fp64': {'steps': steps + 3, 'fields': errs},
-        'note': 'the restated D2V16 model diverges within a few hundred steps in FP64 as well at every '
-                'tested setting (including T = 0.7 Tc with a = 0.5 and rho = rho_c), so the comparison '
-                f'covers the first {steps + 3} steps',
+        'fp64fma_error_vs_fp64': {'steps': steps + 3, 'fields': efma},
+        'maxwell_densities': maxwell_densities(C3['Tr']),
     }
+
+
+def c3_full(args) -> dict:
+    """C3 to its full step count: density range, phase densities against the Maxwell
+    construction, mass drift and finiteness every 5000 steps, MLUPS."""
+    import torch
+    from mpdugks_gb300 import capi
+    n, total = C3['n'], args.full_steps or C3['steps']
+    prec = args.precision or 'fp32dev'
+    st = torch.cuda.Stream()
+    g = capi.GpuCase(c3_case(prec), n, n, False)
+    g.init('pp_noise', [PP_RHO_C, 0.01], seed=2026)
+    m0 = g.reduce().sum_rho
+    rows, ms_total, done = [], 0.0, 0
+    while done < total:
+        k = min(5000, total - done)
+        ms, _, _ = timed_steps(g, k, st)
+        ms_total += ms
+        done += k
+        rho = g.get('rho')
+        import numpy as np
+        fin = bool(np.isfinite(rho).all())
+        row = {'steps': done, 'ms_per_step': round(ms / k, 4), 'finite': fin,
+               'mass_rel_drift': (float(rho.sum()) - m0) / m0, 'max_abs_u': float(np.max(np.abs(g.get('u'))))}
+        row.update(phase_densities(rho))
+        rows.append(row)
+        if not fin:
+            break
+    return {'workload': 'C3 D2V16 pseudopotential coexistence 1024x1024', 'precision': prec, 'steps': done,
+            'mlups': round(n * n * done / (ms_total * 1e-3) / 1e6, 2), 'maxwell_densities': maxwell_densities(C3['Tr']),
+            'history': rows}
 
 
 # ---------------------------------------------------------------- scheme variants
@@ -609,10 +764,13 @@ def run_ours(args, wl, rank, world, local):
                 'traffic_source': None if traffic is None else 'ncu DRAM bytes of one launch at 3072x3072, '
                                                                'scaled by the cell count',
                 'kernel': kernel, 'algorithmic_bytes_per_cell': algo,
+                'stored_bytes_per_cell': STORED_BYTES[prec],
+                'stored_gbs': round(STORED_BYTES[prec] * cells / (step_ms * 1e-3) / 1e9, 2),
                 'cells_per_launch': cells, 'peak_source': f'{peak_kind} hbm_gbs (copy bandwidth)'}
     if phase:
         roofline['phase_ms'] = phase
-        roofline['note'] = 'FP64 path: bound by the FP64 pipe (1.2 TFLOP/s on GB300), not HBM'
+        roofline['note'] = 'FP64 path: bound by the FP64 pipe, not HBM (fp64_pipe)'
+        roofline['fp64_pipe'] = fp64_pipe(cells * args.steps / (ms * 1e-3))
 
     # ---- the plain FP64 path on the same grid, and the FP32-vs-FP64 field errors
     fp64 = None
@@ -635,6 +793,7 @@ def run_ours(args, wl, rank, world, local):
                 'precision': 'fp64 (reference-exact rounding)',
                 'fp32_speedup': round(mlups_total / world / m64, 2),
                 'fp32_error_vs_fp64': {'steps': n_cmp, 'fields': errs},
+                'fp64_pipe': fp64_pipe(cells * k64 / (ms64 * 1e-3)),
                 'developed_flow': developed_flow_errors()}
         gx = g64
     # ---- end to end through the C ABI with host buffers: upload the FP64 initial
@@ -731,9 +890,14 @@ def main():
     ap.add_argument('--pseudopotential-only', action='store_true',
                     help='run only the D2V16 FP32/FP64 measurement (--pp-steps timed steps)')
     ap.add_argument('--pp-steps', type=int, default=100)
+    ap.add_argument('--c3-full', action='store_true',
+                    help='run the D2V16 coexistence configuration (C3) to its 50000 steps (--precision, --full-steps)')
     ap.add_argument('--serving-cases', type=int, default=SERVING['cases'])
     ap.add_argument('--serving-steps', type=int, default=SERVING['steps'])
-    ap.add_argument('--serving-sample', type=int, default=3, help='cases solved one at a time for comparison')
+    ap.add_argument('--serving-sample', type=int, default=24,
+                    help='Allen-Cahn cases (spanning the grid sizes) solved one at a time for comparison')
+    ap.add_argument('--serving-fraction', type=int, default=10,
+                    help='the one-at-a-time comparators time 1/fraction of each sample case\'s steps')
     ap.add_argument('--profile-steps', type=int, default=0,
                     help='only run this many steps of the workload (for ncu) and exit')
     ap.add_argument('--grid', default=None, help='NXxNY override of the grid (profiling runs only)')
@@ -772,6 +936,11 @@ def main():
         import torch
         torch.cuda.set_device(local)
         print(json.dumps({'serving': serving_bench(args)}), flush=True)
+        return 0
+    if args.c3_full:
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps({'c3_full': c3_full(args)}), flush=True)
         return 0
     if args.pseudopotential_only:
         import torch
