@@ -308,9 +308,9 @@ def serving_bench(args) -> dict:
     """Cases arrive on their schedule and are submitted to the server as they
     arrive; p50/p99 time to solution (submit to result on the host) and the
     aggregate rate.  Every case is checked every 1000 steps (the reference's
-    residual control): a non-finite state stops it.  Beside it: the Allen-Cahn
-    cases solved one at a time (FP64 plain path and FP32 storage, no batching)
-    on a sample, as cases/s."""
+    residual control): a non-finite state stops it.  Beside it: the same work one
+    case at a time (FP64 plain path, and FP32 storage without batching), timed on a
+    sample of each model's cases, as cases/s."""
     import numpy as np
     import torch
     from mpdugks_gb300 import capi
@@ -327,11 +327,12 @@ def serving_bench(args) -> dict:
                 time.sleep(dt)
             ids.append(srv.submit(serving_case(c, 'fp32dev'), c['n'], c['n'], False, c['init'], c['params'],
                                   nsteps=c['steps'], check_every=PP_CHECK_EVERY if c['model'] == 'PP16' else 0))
-        tts, finite, lu = [], 0, 0
+        tts, finite, lu, ran = [], 0, 0, []
         t_first, t_last = None, 0.0
         pp = {'submitted': 0, 'completed': 0, 'diverged': 0, 'failed': 0, 'steps_at_stop': [], 'tts': []}
         for cid, c in zip(ids, stream):
             st = srv.wait(cid, 3600.0)
+            ran.append(int(st.steps_done))
             t_first = st.t_submit if t_first is None else min(t_first, st.t_submit)
             t_last = max(t_last, st.t_done)
             if c['model'] == 'PP16':
@@ -357,49 +358,62 @@ def serving_bench(args) -> dict:
         if steps:
             pp['steps_at_stop_min_max'] = [min(steps), max(steps)]
             pp['tts_p50_s'] = round(float(np.percentile(ptts, 50)), 4)
-        return tts, finite, lu, t_last - (t_first or 0.0), stats, pp
+        return tts, finite, lu, t_last - (t_first or 0.0), stats, pp, ran
 
-    tts, finite, lu, span, stats, pp = serve(True)
-    btts, bfinite, blu, bspan, bstats, bpp = serve(False)
+    tts, finite, lu, span, stats, pp, steps_ran = serve(True)
+    btts, bfinite, blu, bspan, bstats, bpp, _ = serve(False)
     done = len(tts)
-    # One case at a time, the comparators: a sample of the stream's Allen-Cahn cases that
-    # spans its grid sizes (every k-th case in the order of N), each stepped on its own
-    # for a fraction of its steps; a case's time is its measured per-step time times its
-    # step count, and the stream's time is the sum over the stream's Allen-Cahn cases of
-    # the per-cell-update time of the sample case nearest in N.
-    by_n = sorted(ac, key=lambda c: c['n'])
-    k = max(1, len(by_n) // max(1, args.serving_sample))
-    sample = by_n[k // 2::k][:args.serving_sample]
+    # One case at a time, the comparators, on the same work as the server's: a sample
+    # of the stream's cases of each model spanning its grid sizes (every k-th case in the
+    # order of N), each stepped alone for a fraction of its steps; the stream's time is
+    # the sum over all its cases of the per-cell-update time of the sample case of the
+    # same model nearest in N, times the case's cell updates in the server (a case the
+    # server stopped early -- diverged -- counts with the steps it ran there).
+    ran = dict(zip([id(c) for c in stream], steps_ran))
+
+    def strata(cases, m):
+        by_n = sorted(cases, key=lambda c: c['n'])
+        kk = max(1, len(by_n) // max(1, m))
+        return by_n[kk // 2::kk][:m]
+    pp_cases = [c for c in stream if c['model'] == 'PP16']
+    samples = {'AC': strata(ac, args.serving_sample), 'PP16': strata(pp_cases, max(1, args.serving_sample // 2))}
 
     def one_at_a_time(precision):
-        rates = []
-        for c in sample:
-            gc = capi.GpuCase(serving_case(c, precision), c['n'], c['n'], False)
-            gc.init(c['init'], c['params'])
-            gc.step(2)
-            torch.cuda.synchronize()
-            nst = max(20, c['steps'] // args.serving_fraction)
-            ta = time.perf_counter()
-            gc.step(nst)
-            gc.get('rho')
-            el = time.perf_counter() - ta
-            rates.append((c['n'], el / (c['n'] * c['n'] * nst)))  # seconds per cell update
-            del gc
-        ns = np.array([r[0] for r in rates])
+        rates, out = {}, {}
+        for model, sample in samples.items():
+            rates[model] = []
+            for c in sample:
+                gc = capi.GpuCase(serving_case(c, precision), c['n'], c['n'], False)
+                gc.init(c['init'], c['params'])
+                gc.step(2)
+                torch.cuda.synchronize()
+                nst = max(20, min(1000, c['steps']) // args.serving_fraction)
+                ta = time.perf_counter()
+                gc.step(nst)
+                gc.get('rho')
+                el = time.perf_counter() - ta
+                rates[model].append((c['n'], el / (c['n'] * c['n'] * nst)))  # seconds per cell update
+                del gc
         total = 0.0
-        for c in ac:
-            sec_per_lu = rates[int(np.argmin(np.abs(ns - c['n'])))][1]
-            total += sec_per_lu * c['n'] * c['n'] * c['steps']
-        return {'sample_cases': len(sample), 'sample_n': [int(x) for x in ns],
-                'steps_timed_per_case': f'max(20, steps / {args.serving_fraction})',
-                'mlups_sample_median': round(float(np.median([1e-6 / r[1] for r in rates])), 2),
-                'stream_seconds_projected': round(total, 3),
-                'stream_cases_per_s_projected': round(len(ac) / total, 4)}
+        for c in stream:
+            r = rates[c['model']]
+            ns = np.array([x[0] for x in r])
+            total += r[int(np.argmin(np.abs(ns - c['n'])))][1] * c['n'] * c['n'] * ran[id(c)]
+        for model, r in rates.items():
+            out[model] = {'sample_cases': len(r), 'sample_n': [int(x[0]) for x in r],
+                          'mlups_sample_median': round(float(np.median([1e-6 / x[1] for x in r])), 2)}
+        out['steps_timed_per_case'] = f'max(20, min(1000, steps) / {args.serving_fraction})'
+        out['stream_seconds_projected'] = round(total, 3)
+        out['stream_cases_per_s_projected'] = round(len(stream) / total, 4)
+        return out
 
     fp64 = one_at_a_time('fp64')
     fp32 = one_at_a_time('fp32dev')
     cps = done / span if span > 0 else 0.0
     bcps = len(btts) / bspan if bspan > 0 else 0.0
+    # all cases of the stream (Allen-Cahn and D2V16) per second: the server against one
+    # case at a time on the same work
+    all_cps, ball_cps = len(stream) / span, len(stream) / bspan
     return {
         'workload': f'{args.serving_cases}-case seeded stream (Poisson 20/s, N lognormal median 256 in '
                     f'[64,1024], {args.serving_steps} steps each, FP32 storage): {len(ac)} Allen-Cahn droplets/'
@@ -428,10 +442,11 @@ def serving_bench(args) -> dict:
         # the gain of the server over one case at a time: against the plain FP64 path
         # (precision and batching together) and against FP32 storage without batching
         # (batching alone), paced at the stream's arrivals and at capacity
-        'vs_one_at_a_time_fp64': round(cps / fp64['stream_cases_per_s_projected'], 2),
-        'vs_one_at_a_time_fp32': round(cps / fp32['stream_cases_per_s_projected'], 2),
-        'capacity_vs_one_at_a_time_fp64': round(bcps / fp64['stream_cases_per_s_projected'], 2),
-        'capacity_vs_one_at_a_time_fp32': round(bcps / fp32['stream_cases_per_s_projected'], 2),
+        'stream_cases_per_s': round(all_cps, 4), 'capacity_stream_cases_per_s': round(ball_cps, 4),
+        'vs_one_at_a_time_fp64': round(all_cps / fp64['stream_cases_per_s_projected'], 2),
+        'vs_one_at_a_time_fp32': round(all_cps / fp32['stream_cases_per_s_projected'], 2),
+        'capacity_vs_one_at_a_time_fp64': round(ball_cps / fp64['stream_cases_per_s_projected'], 2),
+        'capacity_vs_one_at_a_time_fp32': round(ball_cps / fp32['stream_cases_per_s_projected'], 2),
     }
 
 

@@ -221,7 +221,7 @@ static cudaError_t to_dev(const dugks_handle *h, double *d, const double *src, i
 static size_t pp32_arena_bytes(const Params &P) {
     const size_t cf = align256((size_t)P.pitch * P.ny * sizeof(float));
     const size_t cd = align256((size_t)P.pitch * P.ny * sizeof(double));
-    return (6 * (size_t)P.Q + 18) * cf + 7 * cd + align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 512 +
+    return (6 * (size_t)P.Q + 21) * cf + 7 * cd + align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 512 +
            (P.model == PP16 ? align256(sizeof(float) * 256) : 0);
 }
 
@@ -259,7 +259,8 @@ static int create_pp32(dugks_handle *h, dugks_handle_t **out) {
     S.xfl = tf(Q);
     S.yfl = tf(Q);
     float **scal[] = {&S.xr, &S.yr, &S.xu, &S.yu, &S.xv, &S.yv, &S.xg, &S.yg, &S.xps, &S.yps,
-                      &S.xFx, &S.xFy, &S.yFx, &S.yFy, &S.psi, &S.scg, &S.Fx, &S.Fy};
+                      &S.xFx, &S.xFy, &S.yFx, &S.yFy, &S.psi, &S.scg, &S.Fx, &S.Fy,
+                      &S.psil, &S.xpsl, &S.ypsl};
     for (auto p : scal) *p = tf(1);
     S.rho = td();
     S.rho_o = td();
@@ -375,7 +376,7 @@ static int upload_pp32(dugks_handle *h, const double *f, const double *aux) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     cudaFree(stage);
     if (e != cudaSuccess) return cuda_fail(h, e, "upload");
-    float *zero[] = {S.xFx, S.xFy, S.yFx, S.yFy, S.psi, S.scg};
+    float *zero[] = {S.xFx, S.xFy, S.yFx, S.yFy, S.psi, S.scg, S.psil, S.xpsl, S.ypsl};
     for (auto z : zero) cudaMemsetAsync(z, 0, S.qs * sizeof(float), st);
     cudaMemsetAsync(h->rho_last, 0, (size_t)P.pitch * ny * sizeof(double), st);
     e = cudaStreamSynchronize(st);

@@ -319,7 +319,7 @@ __device__ __forceinline__ void tile_step(const PR<R> &P, const SR<R> &S, int fi
         const R px = half_dtv * pdiff(phiB(r, e - 1), phiB(r, e + 1));
         const R py = half_dtv * pdiff(phiB(r - 1, e), phiB(r + 1, e));
         R dphi;
-        update_cell<R>(P, Pq, inc, FW, FE, FSo, FN, px, py, sr_bits(P, gj, gi, step), dn, dphi);
+        update_cell<R>(P, Pq, inc, FW, FE, FSo, FN, px, py, dn, dphi);
         S.odf[c] = dn[0].x;
 #pragma unroll
         for (int q = 1; q < 9; ++q) {

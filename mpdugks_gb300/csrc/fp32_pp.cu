@@ -17,7 +17,7 @@
 // relative to e_q times the face average of rho, and the update changes rho by the
 // sum of the small face fluxes (the e_q avg(rho) parts cancel: sum_q e_q xi_q = 0)
 // and each g_q by small increments.  Moment sums and the equation of state are
-// float-float (below); stores are stochastically rounded as in the Allen-Cahn path.
+// float-float (below).
 // (Fusing face pass 2 with the update, the fluxes of a tile in shared memory and the
 // face reconstruction recomputed instead of stored, ran slower: 0.55 against 0.46 ms
 // per D2V16 step at 1024^2, 128 registers and two blocks per SM.)
@@ -137,31 +137,34 @@ __device__ __forceinline__ FF cs_p(const PPP &P, FF r) {
                   ff_neg(ff_mul(FF{P.acs_hi, P.acs_lo}, r2)));
 }
 // calcPsi (Ark/Header/Macroscopic.h:64-68): G = sign(p - rho RT), psi = sqrt(2 (p - rho RT) / G)
-__device__ __forceinline__ void cs_psi(const PPP &P, FF rho, FF p, float &scg, float &psi) {
+// psi as a float-float pair (hi, lo): the square root's head and the correction
+// (x - hi^2) / (2 hi) of its residual (hi^2 exactly by fma); the gradient stencil of
+// psi then differences pairs, which matters where grad psi is small against psi
+__device__ __forceinline__ void cs_psi(const PPP &P, FF rho, FF p, float &scg, float &psi, float &psil) {
     const FF g = ff_add(p, ff_neg(ff_mul(rho, FF{P.rt_hi, P.rt_lo})));
     const float G = (float)((g.hi > 0.f) - (g.hi < 0.f));
     scg = G;
-    psi = sqrtf(__fdiv_rn(2.f * g.hi, G));
+    const float xh = 2.f * g.hi * G, xl = 2.f * g.lo * G;  // G = +-1: exact
+    psi = sqrtf(xh);
+    psil = psi > 0.f ? __fdiv_rn(fmaf(-psi, psi, xh) + xl, 2.f * psi) : 0.f;
 }
 __device__ __forceinline__ double ff_to_double(FF a) { return (double)a.hi + (double)a.lo; }
 
-__device__ __forceinline__ float sr1(float a, float b, uint32_t bits) {
-    const float s = a + b;
-    const float bb = s - a;
-    const float err = (a - (s - bb)) + (b - bb);
-    return sr_round(s, err, bits);
-}
 
-// 8-neighbour isotropic gradient of a periodic field (Ark/Lib/GradSchemeBasic.h:153-208)
-__device__ __forceinline__ void iso_grad(const PPP &P, const float *__restrict__ a, int i, int j, float &gx,
-                                         float &gy) {
+// 8-neighbour isotropic gradient of a periodic field given as float-float pairs (hi,
+// lo planes), from pair differences (Ark/Lib/GradSchemeBasic.h:153-208)
+__device__ __forceinline__ void iso_grad(const PPP &P, const float *__restrict__ a, const float *__restrict__ al,
+                                         int i, int j, float &gx, float &gy) {
     const int nx = P.nx, ny = P.ny, pitch = P.pitch;
     const int im = wrapi(i - 1, nx), ip = wrapi(i + 1, nx), jm = wrapi(j - 1, ny), jp = wrapi(j + 1, ny);
-    auto at = [&](int jj, int ii) { return a[(size_t)jj * pitch + ii]; };
-    const float E = at(j, ip), W = at(j, im), N = at(jp, i), S = at(jm, i);
-    const float NE = at(jp, ip), NW = at(jp, im), SE = at(jm, ip), SW = at(jm, im);
-    gx = (4.f * (E - W) + ((NE - NW) + (SE - SW))) * P.inv_6_2dx;
-    gy = (4.f * (N - S) + ((NE - SE) + (NW - SW))) * P.inv_6_2dy;
+    auto at = [&](int jj, int ii) {
+        const size_t o = (size_t)jj * pitch + ii;
+        return make_float2(a[o], al[o]);
+    };
+    const float2 E = at(j, ip), W = at(j, im), N = at(jp, i), S = at(jm, i);
+    const float2 NE = at(jp, ip), NW = at(jp, im), SE = at(jm, ip), SW = at(jm, im);
+    gx = (4.f * pdiff(E, W) + (pdiff(NE, NW) + pdiff(SE, SW))) * P.inv_6_2dx;
+    gy = (4.f * pdiff(N, S) + (pdiff(NE, SE) + pdiff(NW, SW))) * P.inv_6_2dy;
 }
 
 // Collision pre-step: cell force F = -G psi grad psi (Ark/Cpp/PseudoP.cpp:31-38, from the
@@ -176,7 +179,7 @@ __global__ void __launch_bounds__(256) k_pp32_collide(PPP P, PPS S, int do_msrc)
     float fx, fy;
     if (do_msrc) {
         float gx, gy;
-        iso_grad(P, S.psi, i, j, gx, gy);
+        iso_grad(P, S.psi, S.psil, i, j, gx, gy);
         const float k = -S.scg[c] * S.psi[c];
         fx = gx * k;
         fy = gy * k;
@@ -265,8 +268,9 @@ __global__ void __launch_bounds__(256) k_pp32_faces1(PPP P, PPS S) {
     U += 0.5f * P.hDt * (xf ? S.xFx : S.yFx)[c] / Rf;
     V += 0.5f * P.hDt * (xf ? S.xFy : S.yFy)[c] / Rf;
     const FF p = cs_p(P, R);
-    float scg, psi;
-    cs_psi(P, R, p, scg, psi);
+    float scg, psi, psil;
+    cs_psi(P, R, p, scg, psi, psil);
+    (xf ? S.xpsl : S.ypsl)[c] = psil;
     (xf ? S.xr : S.yr)[c] = __fadd_rn(sR.hi, sR.lo);  // face rho - avg(rho)
     (xf ? S.xu : S.yu)[c] = U;
     (xf ? S.xv : S.yv)[c] = V;
@@ -285,7 +289,7 @@ __global__ void __launch_bounds__(256) k_pp32_faces2(PPP P, PPS S) {
     constexpr int Q = MODEL == PP16 ? 16 : 9;
     const size_t c = (size_t)j * P.pitch + i;
     float gx, gy;
-    iso_grad(P, xf ? S.xps : S.yps, i, j, gx, gy);
+    iso_grad(P, xf ? S.xps : S.yps, xf ? S.xpsl : S.ypsl, i, j, gx, gy);
     const float k = -(xf ? S.xg : S.yg)[c] * (xf ? S.xps : S.yps)[c];
     const float Fx = gx * k, Fy = gy * k;
     (xf ? S.xFx : S.yFx)[c] = Fx;
@@ -315,7 +319,7 @@ __global__ void __launch_bounds__(256) k_pp32_faces2(PPP P, PPS S) {
 // Update (Ark/Cpp/DUGKS2DSolver.cpp:748-792) and cell macros (Ark/Lib/D2Q9PP.cpp:89-109):
 //   rho_new = rho + drho, drho = dt/V sum_q (net face flux of q),
 //   g_q,new = g_q + 4/3 (b_q - g_q) + dt/V (net flux of q)
-//             + e_q (xi_q,x px + xi_q,y py) - e_q drho   (stochastically rounded),
+//             + e_q (xi_q,x px + xi_q,y py) - e_q drho,
 // px = dt/V (rho_W - rho_E)/2, py = dt/V (rho_S - rho_N)/2 (the e_q avg(rho) flux
 // divergence on unit cells, from the FP64 density); U, V, p, psi from float-float
 // sums, rho in FP64.
@@ -327,7 +331,6 @@ __global__ void __launch_bounds__(256) k_pp32_update(PPP P, PPS S, uint32_t step
     const int pitch = P.pitch;
     const int ip = wrapi(i + 1, P.nx), im = wrapi(i - 1, P.nx), jn = wrapi(j + 1, P.ny), js = wrapi(j - 1, P.ny);
     const size_t c = (size_t)j * pitch + i, cE = (size_t)j * pitch + ip, cN = (size_t)jn * pitch + i;
-    const uint32_t h0 = mix32((uint32_t)c * 0x9E3779B1U ^ step * 0x85EBCA77U);
     const double rho = S.rho[c];
     const float px = (float)(0.5 * (double)P.dtV * (S.rho[(size_t)j * pitch + im] - S.rho[cE]));
     const float py = (float)(0.5 * (double)P.dtV * (S.rho[(size_t)js * pitch + i] - S.rho[cN]));
@@ -354,7 +357,7 @@ __global__ void __launch_bounds__(256) k_pp32_update(PPP P, PPS S, uint32_t step
         const float g = S.df[o + c];
         float inc = fmaf(P.aTP, S.bf[o + c] - g, P.dtV * sq[q]);
         inc = fmaf(P.erest[q], (P.xi_u[q] * px + P.xi_v[q] * py) - drf, inc);
-        const float gn = sr1(g, inc, h0 * SR_KEY[q]);
+        const float gn = g + inc;
         S.df[o + c] = gn;
         ff_acc_prod(su, gn, P.xi_u[q]);
         ff_acc_prod(sv, gn, P.xi_v[q]);
@@ -365,9 +368,10 @@ __global__ void __launch_bounds__(256) k_pp32_update(PPP P, PPS S, uint32_t step
     U += P.hDt * S.Fx[c] / rh;
     V += P.hDt * S.Fy[c] / rh;
     const FF p = cs_p(P, R);
-    float scg, psi;
-    cs_psi(P, R, p, scg, psi);
+    float scg, psi, psil;
+    cs_psi(P, R, p, scg, psi, psil);
     S.rho_o[c] = rho_n;
+    S.psil[c] = psil;
     S.U[c] = U;
     S.V[c] = V;
     S.p[c] = ff_to_double(p);
@@ -399,7 +403,7 @@ __global__ void __launch_bounds__(256) k_pp32_force(PPP P, PPS S) {
     if (i >= P.nx || j >= P.ny) return;
     const size_t c = (size_t)j * P.pitch + i;
     float gx, gy;
-    iso_grad(P, S.psi, i, j, gx, gy);
+    iso_grad(P, S.psi, S.psil, i, j, gx, gy);
     const float k = -S.scg[c] * S.psi[c];
     S.Fx[c] = gx * k;
     S.Fy[c] = gy * k;

@@ -106,6 +106,7 @@ struct PPS {
     float *xFx, *xFy, *yFx, *yFy;    // face forces (kept for the next step's face velocity)
     double *rho, *rho_o, *p, *U, *V; // cell density (read / written by the update), pressure, velocity
     float *psi, *scg, *Fx, *Fy;
+    float *psil, *xpsl, *ypsl;       // the tails of psi (cell, x faces, y faces) as float-float pairs
     size_t qs;
 };
 

@@ -427,7 +427,7 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
             const float half_dtv = 0.5f * P.dtV;
             const float px = half_dtv * pdiff(SWv, SE), py = half_dtv * pdiff(dn_c, up_c);
             float dphi;
-            update_cell<float>(P, Pq, inc_cur, FW, FE, FS, FN, px, py, sr_bits(P, k, gi, step), dn, dphi);
+            update_cell<float>(P, Pq, inc_cur, FW, FE, FS, FN, px, py, dn, dphi);
             S.odf[c] = dn[0].x;
 #pragma unroll
             for (int q = 1; q < 9; ++q) {

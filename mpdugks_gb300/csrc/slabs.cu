@@ -9,8 +9,9 @@
 // streaming kernel on its rows (halo rows are read, never written), then the
 // two boundary rows of all PL_N state planes (9 f deviations, 8 phase-field
 // remainders g, the phi pair, 6 aux) are copied into the neighbours' halo rows: one
-// strided copy per neighbour and side.  The stochastic-rounding bits use global cell numbers, so the
-// decomposed run is bit-identical to the undivided one.
+// strided copy per neighbour and side.  Every cell computes from the same inputs in
+// the same order as in the undivided case, so the decomposed run is bit-identical to
+// the undivided one.
 //
 // The reference has no counterpart (one OpenMP process per case).  Only one
 // GPU is exercised here: partitions on different devices use peer copies
