@@ -177,6 +177,19 @@ int dugks_gpu_get_dist(dugks_handle_t *h, int which, double *out);
  * dugks_gpu_reduce). */
 int dugks_gpu_check_finite(dugks_handle_t *h);
 
+/* Output quantities of the Allen-Cahn models.
+ * dugks_gpu_drop_l2 replaces AC_Drop_L2Norm (Ark/Cpp/Output.cpp:226-238): the
+ * relative L2 distance sqrt(sum (phi - phi_A)^2 / sum phi_A^2) of the phase field
+ * to the analytic drop profile (Ark/Cpp/Preprocess.cpp:402-438) of the radius and
+ * phase orientation the last dugks_gpu_init (kind 0 or 1) placed, centred at
+ * (nx/2, nx/2), summed on the host in the reference's cell order (the value the
+ * reference prints).  DUGKS_EINVAL for a handle not initialised as a drop.
+ * dugks_gpu_thermo_pressure replaces thermoPressure (Ark/Cpp/Output.cpp:146-163)
+ * for every cell, out [ny][nx]: pZero(phi) - kappa phi lap(phi) + kappa |grad phi|^2 / 2 + p,
+ * from the state the last step's MacroSource saw. */
+int dugks_gpu_drop_l2(dugks_handle_t *h, double *l2);
+int dugks_gpu_thermo_pressure(dugks_handle_t *h, double *out);
+
 /* Last error message of the handle (or of the last failed create if h is NULL). */
 int dugks_gpu_last_error(const dugks_handle_t *h, char *buf, size_t len);
 
@@ -212,9 +225,11 @@ int dugks_gpu_restore(dugks_handle_t *h, const void *buf, size_t len);
  * are complete on return (the last step's MacroSource is applied).  Limits:
  * models DUGKS_MODEL_AC/HCZ, precision DUGKS_FP64 or DUGKS_FP64_FMA,
  * nx*ny <= 4096 cells (larger grids return DUGKS_EINVAL with a message in
- * dugks_gpu_last_error(NULL, ...)).  The first call on each device looks up
- * the array's device address (cudaGetSymbolAddress); make that first call
- * before any stream capture.  All calls share the one array: calls whose
+ * dugks_gpu_last_error(NULL, ...)).  Every call outside a stream capture
+ * looks up the array's device address (cudaGetSymbolAddress), so a device
+ * reset between calls is safe; a call on a capturing stream reuses the address
+ * the last uncaptured call found: make one call before the first capture, and
+ * one again after a device reset before capturing.  All calls share the one array: calls whose
  * work overlaps on the GPU (other streams, other host threads) race on it
  * and must be serialised by the caller.  Asynchronous on `stream`. */
 int dugks_gpu_step_noalloc(const dugks_case_t *c, const dugks_grid_t *g, double *d_f, double *d_h,

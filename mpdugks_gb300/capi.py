@@ -87,6 +87,8 @@ SIGNATURES = {
     'dugks_gpu_reduce': (C.c_int, [C.c_void_p, C.POINTER(ReductionsT)]),
     'dugks_gpu_download': (C.c_int, [C.c_void_p] + [C.c_void_p] * 5),
     'dugks_gpu_get_field': (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    'dugks_gpu_drop_l2': (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    'dugks_gpu_thermo_pressure': (C.c_int, [C.c_void_p, C.c_void_p]),
     'dugks_gpu_set_field': (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     'dugks_gpu_get_dist': (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     'dugks_gpu_check_finite': (C.c_int, [C.c_void_p]),
@@ -218,6 +220,18 @@ class GpuCase:
         r = ReductionsT()
         self._check(self.lib.dugks_gpu_reduce(self.h, C.byref(r)))
         return r
+
+    def drop_l2(self) -> float:
+        """AC_Drop_L2Norm (Ark/Cpp/Output.cpp:226-238) of the current phase field."""
+        v = C.c_double()
+        self._check(self.lib.dugks_gpu_drop_l2(self.h, C.byref(v)))
+        return v.value
+
+    def thermo_pressure(self) -> np.ndarray:
+        """thermoPressure (Ark/Cpp/Output.cpp:146-163) of every cell, [ny][nx]."""
+        out = np.empty((self.ny, self.nx), dtype=np.float64)
+        self._check(self.lib.dugks_gpu_thermo_pressure(self.h, out.ctypes.data))
+        return out
 
     def get(self, name: str) -> np.ndarray:
         out = np.empty((self.ny, self.nx), dtype=np.float64)

@@ -124,6 +124,8 @@ struct dugks_handle {
     f32::PPP PPc{};
     f32::PPS PPs{};
     int pp_pending = 0;       // the next collision computes the cell force from psi
+    int init_kind = -1;       // the last dugks_gpu_init's kind and drop radius (drop L2 norm)
+    double init_radius = 0.0;
     const double *pp_rho0 = nullptr;  // the density plane the step reads as created (checkpoint orientation)
 };
 
@@ -716,6 +718,10 @@ extern "C" int dugks_gpu_init(dugks_handle_t *h, int kind, const double *params,
     int rc = host_init_state(h->P, h->iM, kind, params, nparams, seed, f, hd, aux);
     if (rc) return fail(h, rc, "unknown init kind or bad parameters for this model");
     rc = dugks_gpu_upload(h, f.data(), hd.empty() ? nullptr : hd.data(), aux.data());
+    if (rc == DUGKS_OK) {
+        h->init_kind = kind;
+        h->init_radius = (nparams >= 1 && params && params[0] >= 0) ? params[0] : 0.36 * h->P.nx;
+    }
     return rc;
 }
 
@@ -1000,6 +1006,115 @@ extern "C" int dugks_gpu_get_dist(dugks_handle_t *h, int which, double *out) {
         cudaError_t e = to_host(h, out + q * n, (which ? h->S.h : h->S.f) + q * h->S.qs);
         if (e != cudaSuccess) return cuda_fail(h, e, "download distribution");
     }
+    return DUGKS_OK;
+}
+
+// AC_Drop_L2Norm (Ark/Cpp/Output.cpp:226-238): the phase field downloaded, then the
+// sums in the reference's cell order (CellArray order of a Cartesian mesh is j nx + i)
+// with the drop profile of AnalyticalPhiAC_Drop (Ark/Cpp/Preprocess.cpp:402-438) at
+// the cell centres (i + 1/2, j + 1/2): the same value as the reference's output.
+extern "C" int dugks_gpu_drop_l2(dugks_handle_t *h, double *l2) {
+    if (!h || !l2) return fail(h, DUGKS_EINVAL, "null argument");
+    const Params &P = h->P;
+    if (!(P.model == AC || P.model == HCZ) || !(h->init_kind == 0 || h->init_kind == 1))
+        return fail(h, DUGKS_EINVAL, "the drop L2 norm needs an Allen-Cahn case initialised as a drop");
+    const int nx = P.nx, ny = P.ny;
+    std::vector<double> phi((size_t)nx * ny);
+    int rc = dugks_gpu_get_field(h, F_PHI, phi.data());
+    if (rc) return rc;
+    const double centerX = 0.5 * nx, centerY = 0.5 * nx, radius = h->init_radius;
+    double SumdPhi = 0.0, SumPhi_A = 0.0;
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            const double x = i + 0.5, y = j + 0.5;
+            const double r = std::sqrt((x - centerX) * (x - centerX) + (y - centerY) * (y - centerY));
+            // kind 1 (heavy phase inside) flips the profile's sign
+            const double Phi_A = 0.5 * (P.PhiL + P.PhiV) +
+                                 0.5 * (P.PhiL - P.PhiV) * std::tanh((h->init_kind == 1 ? radius - r : r - radius) * 2 / P.wI);
+            const double dPhi = phi[(size_t)j * nx + i] - Phi_A;
+            SumdPhi += dPhi * dPhi;
+            SumPhi_A += Phi_A * Phi_A;
+        }
+    *l2 = std::sqrt(SumdPhi / SumPhi_A);
+    return DUGKS_OK;
+}
+
+// thermoPressure (Ark/Cpp/Output.cpp:146-163) of every cell, from the state the last
+// step's MacroSource saw (Ark/Cpp/DUGKS2DSolver.cpp:288-295): phi, p, Rho_x, Rho_y and
+// the 9-point Laplacian of phi (Ark/Cpp/GradScheme.cpp:347-376) in the reference's
+// operand order.  Plain FP64 handles take Rho_x, Rho_y and the wall ghost rows from
+// the device's MacroSource; FP32 storage recomputes them from phi on the host (the
+// gradient of Ark/Lib/GradSchemeBasic.h:153-180 with apsi = 4, bpsi = 1).  Either
+// way a walled grid's ghost rows are the ones the last step extrapolated from the
+// phase field it started with, as the reference's shadow cells
+// (Ark/Cpp/Boundary.cpp:38-63, Ark/Cpp/DUGKS2DSolver.cpp:188).
+extern "C" int dugks_gpu_thermo_pressure(dugks_handle_t *h, double *tp) {
+    if (!h || !tp) return fail(h, DUGKS_EINVAL, "null argument");
+    const Params &P = h->P;
+    if (!(P.model == AC || P.model == HCZ)) return fail(h, DUGKS_EINVAL, "the thermodynamic pressure needs an Allen-Cahn case");
+    const int nx = P.nx, ny = P.ny;
+    const size_t n = (size_t)nx * ny;
+    std::vector<double> phi(n), p(n), rx(n), ry(n), gb(nx), gt(nx);
+    int rc = dugks_gpu_get_field(h, F_PHI, phi.data());
+    if (!rc) rc = dugks_gpu_get_field(h, F_P, p.data());
+    if (!rc && !h->fp32) rc = dugks_gpu_get_field(h, F_RHOX, rx.data());
+    if (!rc && !h->fp32) rc = dugks_gpu_get_field(h, F_RHOY, ry.data());
+    if (rc) return rc;
+    if (P.walls && !h->fp32) {
+        cudaError_t e = cudaMemcpy(gb.data(), h->S.gphi + (size_t)(h->gcur * 2 + 0) * P.pitch, nx * sizeof(double),
+                                   cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(gt.data(), h->S.gphi + (size_t)(h->gcur * 2 + 1) * P.pitch, nx * sizeof(double),
+                           cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(h, e, "ghost rows");
+    } else if (P.walls) {
+        // FP32 storage: the ghost rows as (head, tail) pairs
+        if ((rc = sync_last(h))) return rc;
+        for (int side = 0; side < 2; ++side) {
+            const size_t row = f32::gphi_row(h->gcur, side);
+            std::vector<double> &dst = side ? gt : gb;
+            cudaError_t e = cudaSuccess;
+            if (h->fused64) {
+                std::vector<double> hd(2 * (size_t)nx);
+                for (int k = 0; k < 2 && e == cudaSuccess; ++k)
+                    e = cudaMemcpy(hd.data() + (size_t)k * nx, h->S64f.gphi + (row + k) * h->P64f.pitch,
+                                   nx * sizeof(double), cudaMemcpyDeviceToHost);
+                for (int i = 0; i < nx; ++i) dst[i] = hd[i] + hd[(size_t)nx + i];
+            } else {
+                std::vector<float> hf(2 * (size_t)nx);
+                for (int k = 0; k < 2 && e == cudaSuccess; ++k)
+                    e = cudaMemcpy(hf.data() + (size_t)k * nx, h->S32.gphi + (row + k) * h->P32.pitch,
+                                   nx * sizeof(float), cudaMemcpyDeviceToHost);
+                for (int i = 0; i < nx; ++i) dst[i] = (double)hf[i] + (double)hf[(size_t)nx + i];
+            }
+            if (e != cudaSuccess) return cuda_fail(h, e, "ghost rows");
+        }
+    }
+    auto at = [&](int jj, int ii) -> double {
+        ii = ii < 0 ? ii + nx : (ii >= nx ? ii - nx : ii);
+        if (jj < 0) return P.walls ? gb[ii] : phi[(size_t)(ny - 1) * nx + ii];
+        if (jj >= ny) return P.walls ? gt[ii] : phi[ii];
+        return phi[(size_t)jj * nx + ii];
+    };
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            const size_t k = (size_t)j * nx + i;
+            const double ph = phi[k], E = at(j, i + 1), W = at(j, i - 1), N = at(j + 1, i), S = at(j - 1, i);
+            const double NE = at(j + 1, i + 1), NW = at(j + 1, i - 1), SW = at(j - 1, i - 1), SE = at(j - 1, i + 1);
+            if (h->fp32) {
+                double gx = (4 * (E - W) + 1 * (NE - NW + SE - SW)) / (P._2dx * 6);
+                double gy = (4 * (N - S) + 1 * (NE - SE + NW - SW)) / (P._2dy * 6);
+                if (std::fabs(gx) < 1.0e-14) gx = 0.0;  // SetZero (Ark/Header/Mesh_2D.h)
+                if (std::fabs(gy) < 1.0e-14) gy = 0.0;
+                rx[k] = P.aPhi * gx;
+                ry[k] = P.aPhi * gy;
+            }
+            const double lap = (4 * (E + N + W + S) + (NE + NW + SW + SE) - 20 * ph) / (6 * P.MinL * P.MinL);
+            const double sq = (rx[k] * rx[k] + ry[k] * ry[k]) / (P.aPhi * P.aPhi);
+            const double pZero = ph * 2 * P.Beta * (ph - P.PhiL) * (ph - P.PhiV) * (2 * ph - P.PhiL - P.PhiV) -
+                                 P.Beta * (ph - P.PhiL) * (ph - P.PhiL) * (ph - P.PhiV) * (ph - P.PhiV);
+            tp[k] = pZero - P.Kappa * ph * lap + P.Kappa * sq / 2 + p[k];
+        }
     return DUGKS_OK;
 }
 

@@ -57,15 +57,21 @@ constexpr int MAX_DEVICES = 64;
 std::mutex g_addr_mutex;
 double *g_addr[MAX_DEVICES] = {};
 
-// Device address of the scratch on the current device, looked up once per
-// device (the first call on each device does this set-up).
-cudaError_t scratch_address(double **out) {
+// Device address of the scratch on the current device.  Looked up on every call
+// made outside a stream capture (so a re-created context, e.g. after
+// cudaDeviceReset, never sees a stale address); a call whose stream is being
+// captured uses the address the last uncaptured call on this device found, and
+// looks it up only if there is none yet.
+cudaError_t scratch_address(cudaStream_t st, double **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(st, &cap);
+    if (e != cudaSuccess) return e;
     std::lock_guard<std::mutex> lk(g_addr_mutex);
-    if (!g_addr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone || !g_addr[dev]) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return e;
@@ -109,7 +115,7 @@ extern "C" int dugks_gpu_step_noalloc(const dugks_case_t *c, const dugks_grid_t 
     }
     if (nsteps == 0) return DUGKS_OK;
     double *base = nullptr;
-    cudaError_t e = scratch_address(&base);
+    cudaError_t e = scratch_address(static_cast<cudaStream_t>(stream), &base);
     if (e != cudaSuccess) {
         set_global_error(std::string("dugks_gpu_step_noalloc: cudaGetSymbolAddress failed: ") +
                          cudaGetErrorString(e));

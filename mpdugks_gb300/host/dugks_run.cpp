@@ -16,8 +16,18 @@
 //       --checkpoint writes the whole GPU state (dugks_gpu_checkpoint) to FILE
 //       at every FlowField output point and at the end; --resume restores
 //       such a file after the initialisation and continues from its step.
+//       The Allen-Cahn models also write the reference's line profiles into
+//       DIR/Convergence/ (Ark/Cpp/DUGKS2DSolver.cpp:326-333,836-841): Diag and
+//       MidX at every FlowField output point, Diag, MidX and MidY at the end
+//       (Diag only when ny >= nx).  --l2 (the reference's
+//       _OUTPUT_L2NORM_ERROR_FLIP, drop initialisations only) appends
+//       AC_Drop_L2Norm at every residual point to
+//       DIR/Convergence/L2_uvp_mu<Mu0>_Re<Re>_<mesh>.dat (Output_L2Norm,
+//       Ark/Cpp/Output.cpp:239-256) and prints "L2_phi <value>" at the end.
 //   dugks_run rewrite-ark <in> <out>        parse a Case.ark and write it back
 //   dugks_run rewrite-flowfield <in> <out>  parse a FlowField file and write it back
+//   dugks_run rewrite-profile <MidX|MidY|Diag> <nx> <ny> <in> <out>
+//                                           parse a line-profile file and write it back
 //   dugks_run mesh-info <FILE.cas>          nx ny y_walls, then the grid
 //                                           position j*nx+i of every mesh cell
 #include <cstdio>
@@ -32,6 +42,7 @@
 #include "case_ark.hpp"
 #include "flowfield.hpp"
 #include "mesh_cas.hpp"
+#include "profiles.hpp"
 
 using namespace dugks_host;
 
@@ -73,6 +84,46 @@ void output(dugks_handle_t *h, const RunConfig &c, const CartesianMap *mesh, con
     write_flowfield(path, fields(h, c, mesh));
 }
 
+bool allen_cahn(const RunConfig &c) {
+    return c.cs.model == DUGKS_MODEL_AC || c.cs.model == DUGKS_MODEL_HCZ;
+}
+
+// the reference's line profiles at this step (Output_MidX / MidY / Diag)
+void write_profiles(dugks_handle_t *h, const RunConfig &c, const std::string &dir, int64_t step, bool midy) {
+    ProfileFields f;
+    f.nx = c.grid.nx;
+    f.ny = c.grid.ny;
+    f.m_phi = c.cs.M_Phi;
+    const size_t n = (size_t)f.nx * f.ny;
+    for (auto *v : {&f.rho, &f.p, &f.tp, &f.u, &f.v}) v->assign(n, 0.0);
+    check(h, dugks_gpu_download(h, f.rho.data(), f.u.data(), f.v.data(), nullptr, f.p.data()), "download");
+    check(h, dugks_gpu_thermo_pressure(h, f.tp.data()), "thermodynamic pressure");
+    const double ratio = c.cs.RhoL / c.cs.RhoV;
+    auto put = [&](Profile k) {
+        const std::string path = dir + "/Convergence/" + profile_name(k, c.mach, c.mesh_type, c.nl, c.cfl, ratio, step);
+        std::FILE *o = std::fopen(path.c_str(), "wb");
+        if (!o) throw std::runtime_error("cannot write " + path);
+        const std::string text = format_profile(k, f);
+        const size_t w = std::fwrite(text.data(), 1, text.size(), o);
+        if (std::fclose(o) != 0 || w != text.size()) throw std::runtime_error("write failed: " + path);
+    };
+    if (f.ny >= f.nx) put(Profile::Diag);
+    put(Profile::MidX);
+    if (midy) put(Profile::MidY);
+}
+
+// one line t, L2(phi), L2_p = 0 (Output_L2Norm's layout, %.8e)
+void append_l2(dugks_handle_t *h, const RunConfig &c, const CaseArk &ark, const std::string &dir, int64_t step) {
+    double l2 = 0.0;
+    check(h, dugks_gpu_drop_l2(h, &l2), "drop L2 norm");
+    const std::string path = dir + "/Convergence/L2_uvp_mu" + ark.get("dynamic viscosity", "0.1") + "_Re" +
+                             ark.get("Re", "0") + "_" + c.mesh_name + ".dat";
+    std::FILE *o = std::fopen(path.c_str(), "ab");
+    if (!o) throw std::runtime_error("cannot write " + path);
+    std::fprintf(o, "%.8e    %.8e    %.8e\n", (double)step * c.dt, l2, 0.0);
+    if (std::fclose(o) != 0) throw std::runtime_error("write failed: " + path);
+}
+
 // the whole GPU state to a file (written to FILE.tmp, then renamed)
 void checkpoint_file(dugks_handle_t *h, const std::string &path) {
     size_t n = 0;
@@ -107,6 +158,7 @@ int run(int argc, char **argv) {
     CaseArk ark = read_case_ark(argv[2]);
     std::string out = "FlowField", mesh_file, ckpt_file, resume_file;
     int64_t steps_override = -1;
+    bool l2 = false;
     for (int k = 3; k < argc; ++k) {
         const std::string a = argv[k];
         auto next = [&]() -> std::string {
@@ -119,6 +171,7 @@ int run(int argc, char **argv) {
         else if (a == "--mesh") mesh_file = next();
         else if (a == "--checkpoint") ckpt_file = next();
         else if (a == "--resume") resume_file = next();
+        else if (a == "--l2") l2 = true;
         else if (a == "--set") {
             const std::string kv = next();
             const size_t eq = kv.find('=');
@@ -138,6 +191,10 @@ int run(int argc, char **argv) {
     const CartesianMap *pm = mesh_file.empty() ? nullptr : &mesh;
     make_dir(out);
     make_dir(out + "/global");
+    const bool ac = allen_cahn(c);
+    if (ac) make_dir(out + "/Convergence");
+    if (l2 && !(ac && (c.init_kind == 0 || c.init_kind == 1)))
+        throw std::runtime_error("--l2 needs an Allen-Cahn case with a drop initialisation");
     write_case_ark(out + "/Case.ark", ark);
 
     dugks_handle_t *h = nullptr;
@@ -172,13 +229,21 @@ int run(int argc, char **argv) {
                 std::printf("%lld    %.6g    %.12e    %.6e\n", (long long)step, (double)step * c.dt, r.sum_rho,
                             r.residual);
                 std::fflush(stdout);
+                if (l2) append_l2(h, c, ark, out, step);
             }
             if (step % c.write_every == 0 && step < c.end_step) {
                 output(h, c, pm, out, step);
+                if (ac) write_profiles(h, c, out, step, false);
                 if (!ckpt_file.empty()) checkpoint_file(h, ckpt_file);
             }
         }
         output(h, c, pm, out, step);
+        if (ac) write_profiles(h, c, out, step, true);
+        if (l2) {
+            double v = 0.0;
+            check(h, dugks_gpu_drop_l2(h, &v), "drop L2 norm");
+            std::printf("L2_phi %.17e\n", v);
+        }
         if (!ckpt_file.empty()) checkpoint_file(h, ckpt_file);
         std::printf("iteration End    step : %lld\n", (long long)step);
     } catch (...) {
@@ -196,6 +261,14 @@ int main(int argc, char **argv) {
         if (argc >= 2 && std::strcmp(argv[1], "run") == 0) return run(argc, argv);
         if (argc == 4 && std::strcmp(argv[1], "rewrite-ark") == 0) {
             write_case_ark(argv[3], read_case_ark(argv[2]));
+            return 0;
+        }
+        if (argc == 7 && std::strcmp(argv[1], "rewrite-profile") == 0) {
+            const Profile k = profile_kind(argv[2]);
+            const std::string text = format_profile(k, read_profile(k, std::atoi(argv[3]), std::atoi(argv[4]), argv[5]));
+            std::FILE *o = std::fopen(argv[6], "wb");
+            if (!o || std::fwrite(text.data(), 1, text.size(), o) != text.size() || std::fclose(o) != 0)
+                throw std::runtime_error(std::string("cannot write ") + argv[6]);
             return 0;
         }
         if (argc == 4 && std::strcmp(argv[1], "rewrite-flowfield") == 0) {
@@ -224,6 +297,7 @@ int main(int argc, char **argv) {
                      "                     [--checkpoint FILE] [--resume FILE] [--set k=v]...\n"
                      "       dugks_run rewrite-ark <in> <out>\n"
                      "       dugks_run rewrite-flowfield <in> <out>\n"
+                     "       dugks_run rewrite-profile <MidX|MidY|Diag> <nx> <ny> <in> <out>\n"
                      "       dugks_run show-config <Case.ark>\n"
                      "       dugks_run mesh-info <F.cas>\n");
         return 2;

@@ -34,8 +34,15 @@ sys.path.insert(0, str(HERE))
 from mesh_cas import write_cas  # noqa: E402
 from variants import VARIANTS  # noqa: E402
 
-REF = Path(os.environ.get('DUGKS_REFERENCE', '/root/reference')) / 'Ark'
+# the reference tree: DUGKS_REFERENCE, else where the build container mounts it
+REF_ROOT = Path(os.environ.get('DUGKS_REFERENCE', '/root/reference'))
+REF = REF_ROOT / 'Ark'
 OUT = HERE.parent / '_ref'
+
+
+def available() -> bool:
+    """Whether the reference sources are present (they are not on the GPU machines)."""
+    return (REF / 'Cpp').is_dir()
 
 
 def _sub(text: str, old: str, new: str, what: str) -> str:

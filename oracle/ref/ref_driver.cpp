@@ -12,7 +12,11 @@
 //  * fixed step count instead of the residual stop;
 //  * Output_* is called only with REF_FLOWFIELD set in the environment: the
 //    reference's Case.ark and FlowField writers at step 0 and after the
-//    last step (golden files for the host reader and writer tests);
+//    last step, and for the Allen-Cahn models its MidX / MidY / Diag profile
+//    writers after the last step (Diag only when Ny >= Nx: it walks the
+//    anti-diagonal (k, Nx + 1 - k), outside the grid otherwise) and, for the
+//    ac_drop init, AC_Drop_L2Norm printed to stdout (golden files for the host
+//    reader, writer and output tests);
 //  * the pseudopotential face force (Ark/Cpp/PseudoP.cpp:39-46) reads the
 //    face psi of neighbouring faces while the same loop writes them (a data
 //    race at >1 thread, order-dependent at 1 thread).  Here the face loop is
@@ -62,6 +66,12 @@ extern void Update_PseudoForce(Cell_2D &cell);
 extern void Update_PseudoForce(Face_2D &face);
 extern void OutputCase();
 extern void Output_Flowfield(double const &t, int step);
+#ifdef _ARK_ALLENCAHN_FLIP
+extern void Output_MidX(int step);
+extern void Output_MidY(int step);
+extern void Output_Diag(int step);
+extern void AC_Drop_L2Norm(double &L2_Phi);
+#endif
 extern void WallShadowC_fBP(Cell_2D &shadowCell);
 extern void Wall_3_BB(Face_2D &face);
 extern void Wall_3_NEE(Face_2D &face);
@@ -371,6 +381,18 @@ int main(int argc, char **argv) {
     printf("done steps %d cells %d seconds %.6f mlups %.4f sumrho %.15e\n", nsteps, Cells, secs,
            nsteps > 0 ? 1e-6 * Cells * (double)nsteps / secs : 0.0, sum_rho());
     dump(dumpbase.c_str(), nsteps);
-    if (flowfield) Output_Flowfield(nsteps * dt, nsteps);
+    if (flowfield) {
+        Output_Flowfield(nsteps * dt, nsteps);
+#ifdef _ARK_ALLENCAHN_FLIP
+        Output_MidX(nsteps);
+        Output_MidY(nsteps);
+        if (Ny >= Nx) Output_Diag(nsteps);
+        if (init == "ac_drop") {
+            double l2 = 0.0;
+            AC_Drop_L2Norm(l2);
+            printf("L2_phi %.17e\n", l2);
+        }
+#endif
+    }
     return 0;
 }

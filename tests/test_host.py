@@ -1,7 +1,9 @@
-"""Host side of the drop-in: Case.ark reader/writer, FlowField writer and the
-dugks_run driver, against files written by the reference's own OutputCase and
-Output_Flowfield (tests/golden/flowfield, made by make_flowfield_golden.py)."""
+"""Host side of the drop-in: Case.ark reader/writer, FlowField and line-profile
+writers and the dugks_run driver, against files written by the reference's own
+OutputCase, Output_Flowfield, Output_MidX / MidY / Diag and AC_Drop_L2Norm
+(tests/golden/flowfield, made by make_flowfield_golden.py)."""
 import gzip
+import json
 import subprocess
 from pathlib import Path
 
@@ -89,6 +91,32 @@ def test_flowfield_sections_hold_the_reference_fields_in_cell_order():
     assert np.all(ff['T'] == float('3.333333333333e-01'))
 
 
+GRID = {'ac_ff': (32, 24), 'uw_ff': (32, 24), 'hcz_rt': (16, 64), 'nee_rt': (16, 64)}
+
+
+def golden_profiles(case: str) -> list[Path]:
+    return sorted(GOLD.joinpath(case, 'Convergence').glob('*.dat'))
+
+
+def test_golden_profiles_are_present():
+    """Every case has MidX and MidY after the last step; Diag only where ny >= nx."""
+    for case, (nx, ny) in GRID.items():
+        kinds = sorted(f.name.split('_')[0] for f in golden_profiles(case))
+        assert kinds == (['Diag', 'MidX', 'MidY'] if ny >= nx else ['MidX', 'MidY']), case
+
+
+@pytest.mark.parametrize('case', CASES)
+def test_profile_writer_reproduces_the_reference_layout(case, tmp_path):
+    """Parse each golden MidX / MidY / Diag file and write it back: byte-identical
+    (zone headers, the M_Phi title at the file's precision, coordinates, 4-space
+    separators)."""
+    nx, ny = GRID[case]
+    for f in golden_profiles(case):
+        kind = f.name.split('_')[0]
+        subprocess.run([runner(), 'rewrite-profile', kind, str(nx), str(ny), f, tmp_path / f.name], check=True)
+        assert (tmp_path / f.name).read_bytes() == f.read_bytes(), f.name
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize('case,extra', [('ac_ff', []),
                                         ('hcz_rt', ['--set', 'init=ac_rt', '--set', 'gravity=0.0001']),
@@ -96,14 +124,32 @@ def test_flowfield_sections_hold_the_reference_fields_in_cell_order():
                                         ('nee_rt', ['--set', 'init=ac_rt', '--set', 'gravity=0.0001',
                                                     '--set', 'wall scheme=NEE'])])
 def test_driver_output_equals_the_reference_files(case, extra, tmp_path):
-    """dugks_run on the reference's Case.ark, plain FP64 path: Case.ark and the
-    FlowField files at steps 0 and 20 are byte-identical to the reference's."""
+    """dugks_run on the reference's Case.ark, plain FP64 path: Case.ark, the
+    FlowField files at steps 0 and 20 and the MidX / MidY / Diag profiles at step
+    20 (thermoPressure included) are byte-identical to the reference's."""
     out = tmp_path / 'FlowField'
     subprocess.run([runner(), 'run', GOLD / case / 'Case.ark', '--out', out, '--steps', '20'] + extra, check=True,
                    capture_output=True)
     for step in (0, 20):
         name, text = golden_dat(case, step)
         assert (out / 'global' / name).read_bytes() == text, (case, step)
+    for f in golden_profiles(case):
+        assert (out / 'Convergence' / f.name).read_bytes() == f.read_bytes(), (case, f.name)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('case', ['ac_ff', 'uw_ff'])
+def test_driver_drop_l2_equals_the_reference(case, tmp_path):
+    """AC_Drop_L2Norm after 20 steps of the reference's AC_Drop case: the value
+    dugks_run --l2 prints equals the reference's to the last bit."""
+    out = tmp_path / 'FlowField'
+    r = subprocess.run([runner(), 'run', GOLD / case / 'Case.ark', '--out', out, '--steps', '20', '--l2',
+                        '--set', 'residual every=10'], check=True, capture_output=True, text=True)
+    got = [ln.split()[1] for ln in r.stdout.splitlines() if ln.startswith('L2_phi ')]
+    want = json.loads(GOLD.joinpath(case, 'l2.json').read_text())['L2_phi']
+    assert got and float(got[0]) == float(want), (got, want)
+    rows = next(out.joinpath('Convergence').glob('L2_uvp_mu*.dat')).read_text().splitlines()
+    assert len(rows) == 2 and float(rows[-1].split()[1]) == float(f'{float(want):.8e}')
 
 
 @pytest.mark.gpu

@@ -3,17 +3,14 @@
 Runs only where the reference sources are mounted (the build container);
 the committed fixtures cover the same ground everywhere else.
 """
-import os
-from pathlib import Path
-
+import build_ref
 import numpy as np
 import pytest
 
 from oracle.oracle import Oracle, read_dump
 from variants import VARIANTS
 
-REF = Path(os.environ.get('DUGKS_REFERENCE', '/root/reference'))
-pytestmark = pytest.mark.skipif(not (REF / 'Ark' / 'Cpp').is_dir(), reason='reference sources not mounted')
+pytestmark = pytest.mark.skipif(not build_ref.available(), reason='reference sources not mounted')
 
 
 @pytest.mark.parametrize('name', ['ac_small', 'hcz_rt', 'pp_drop'])

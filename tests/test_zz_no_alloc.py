@@ -82,3 +82,41 @@ def test_noalloc_rejects_grids_beyond_the_scratch():
     buf = C.create_string_buffer(256)
     lib.dugks_gpu_last_error(None, buf, 256)
     assert b'4096' in buf.value
+
+
+def test_noalloc_inside_a_captured_graph():
+    """One direct call, then the same call captured into a CUDA graph on a side
+    stream and replayed: the capture reuses the scratch address the direct call
+    looked up, and the replay equals a second direct call bit for bit."""
+    import torch
+    from mpdugks_gb300 import capi
+    v = VARIANTS['ac_small']
+    case, gc = _handle_case(v)
+    f0, h0, a0 = _state(gc)
+    dev = torch.device('cuda', torch.cuda.current_device())
+    df = torch.from_numpy(f0.copy()).to(dev)
+    dh = torch.from_numpy(h0.copy()).to(dev)
+    da = torch.from_numpy(a0.copy()).to(dev)
+    grid = capi.GridT(v['nx'], v['ny'], int(v['walls']))
+    lib = capi.load()
+    n = 11
+    rc = lib.dugks_gpu_step_noalloc(C.byref(case), C.byref(grid), df.data_ptr(), dh.data_ptr(), da.data_ptr(), n,
+                                    torch.cuda.current_stream().cuda_stream)
+    assert rc == capi.DUGKS_OK
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(g, stream=side, capture_error_mode='thread_local'):
+            rc = lib.dugks_gpu_step_noalloc(C.byref(case), C.byref(grid), df.data_ptr(), dh.data_ptr(),
+                                            da.data_ptr(), n, side.cuda_stream)
+    assert rc == capi.DUGKS_OK
+    g.replay()
+    torch.cuda.synchronize()
+    gc.step(2 * n)
+    f1, h1, a1 = _state(gc)
+    assert np.array_equal(df.cpu().numpy(), f1)
+    assert np.array_equal(dh.cpu().numpy(), h1)
+    got = da.cpu().numpy()
+    for k, fld in enumerate(capi.FIELDS):
+        assert np.array_equal(got[k], a1[k]), fld
