@@ -106,8 +106,11 @@ def fp64_pipe(lups: float) -> dict:
     out = {'peak_tflops': round(peak, 4), 'peak_source': 'measured: torch float64 matmul 4096^3 (cuBLAS DGEMM)'}
     if FP64_FLOPS_PER_CELL:
         ach = FP64_FLOPS_PER_CELL * lups / 1e12
+        # a DGEMM issues DFMAs only (2 flops each): its instruction rate is peak / 2
+        instr = FP64_INSTR_PER_CELL * lups / 1e12
         out.update({'flops_per_cell': FP64_FLOPS_PER_CELL, 'achieved_tflops': round(ach, 4),
-                    'frac': round(ach / peak, 4)})
+                    'frac': round(ach / peak, 4), 'instr_per_cell': FP64_INSTR_PER_CELL,
+                    'instr_frac': round(instr / (peak / 2), 4)})
     return out
 
 
@@ -115,7 +118,8 @@ def fp64_pipe(lups: float) -> dict:
 # on the 512x2048 Rayleigh-Taylor case, reference-exact variant): ncu counts of the DADD,
 # DMUL and DFMA thread instructions of one step divided by the cells, a DFMA counted as two
 # (profiles/fp64_step_rt512x2048_fp64_ops.md)
-FP64_FLOPS_PER_CELL = None
+FP64_FLOPS_PER_CELL = 1720
+FP64_INSTR_PER_CELL = 1620
 
 
 class ClockSampler:
@@ -665,6 +669,37 @@ def rt_fronts(phi, nx: int, yc: float) -> dict:
             'mixing_zone': round(float(mix.size) / nx, 5)}
 
 
+def slabs_bench(args, wl, nparts: int) -> dict:
+    """The workload split along y into `nparts` slab partitions on this GPU (dugks_slabs_*,
+    halo rows exchanged by device copies after every step), against the undivided case:
+    the cost of the decomposition's exchange and of the partitions' smaller launches.
+    Host wall time around `steps` steps followed by a synchronising reduction (the
+    partitions run on the library's own stream)."""
+    import time
+    from mpdugks_gb300 import capi
+    nx, ny = wl['nx'], wl['ny']
+    cells = nx * ny
+    steps = max(10, args.steps // 10)
+    out = {'workload': wl['name'], 'partitions': nparts, 'steps': steps, 'precision': 'fp32dev'}
+    for label, n in (('undivided', 0), ('slabs', nparts)):
+        if n:
+            run = capi.Slabs(capi.make_case('HCZ', 'fp32dev', **case_kw(wl)), nx, ny, True, n)
+        else:
+            run = capi.GpuCase(capi.make_case('HCZ', 'fp32dev', **case_kw(wl)), nx, ny, True)
+        run.init('ac_rt', wl['init'])
+        run.step(args.warmup)
+        run.reduce()
+        t0 = time.perf_counter()
+        run.step(steps)
+        r = run.reduce()
+        dt = time.perf_counter() - t0
+        out[label] = {'mlups': round(cells * steps / dt / 1e6, 1), 'ms_per_step': round(dt * 1e3 / steps, 4),
+                      'sum_rho': r.sum_rho}
+        run.close()
+    out['slabs_vs_undivided'] = round(out['slabs']['mlups'] / out['undivided']['mlups'], 4)
+    return out
+
+
 def full_run(args, wl) -> dict:
     """The configuration run to its full step count: time per 1000 steps (CUDA events),
     mass and phase-field drift, density residual, finiteness and the fronts of the
@@ -920,6 +955,9 @@ def main():
                     help='run the workload for its configured step count (10000 at 8192^2, 20000 at 512x2048) '
                          'and print its history (timing, conservation, residual, instability fronts)')
     ap.add_argument('--full-steps', type=int, default=0, help='step count of --full-run (0: the configured one)')
+    ap.add_argument('--slabs', type=int, default=0,
+                    help='run only the slab decomposition of the workload into this many partitions on this GPU '
+                         'against the undivided case (steps / 10 timed steps)')
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -951,6 +989,11 @@ def main():
         import torch
         torch.cuda.set_device(local)
         print(json.dumps({'serving': serving_bench(args)}), flush=True)
+        return 0
+    if args.slabs:
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps({'slabs': slabs_bench(args, wl, args.slabs)}), flush=True)
         return 0
     if args.c3_full:
         import torch

@@ -356,7 +356,21 @@ int dugks_slabs_plan(int ny, int y_walls, int nparts, int *row0, int *nrows, int
 int dugks_slabs_create(const dugks_case_t *c, const dugks_grid_t *g, int nparts, const int *devices,
                        dugks_slabs_t **out);
 int dugks_slabs_init(dugks_slabs_t *s, int kind, const double *params, int nparams, uint64_t seed);
+/* The halo copies issued after every step, in issue order (host-only, the same
+ * list dugks_slabs_step executes): `rows` rows of all state planes from local row
+ * src_row of partition src to local row dst_row of partition dst (local row 0 =
+ * the partition's first owned row; -2, -1 = its lower halo, nrows, nrows + 1 = its
+ * upper halo).  *count = the number of copies; out may be NULL to ask only that,
+ * else it holds max entries. */
+typedef struct dugks_halo_copy {
+    int src, src_row, dst, dst_row, rows;
+} dugks_halo_copy_t;
+int dugks_slabs_schedule(int ny, int y_walls, int nparts, dugks_halo_copy_t *out, int max, int *count);
 int dugks_slabs_step(dugks_slabs_t *s, int nsteps);
+/* Sum of rho, sum of phi and the density residual over the whole grid, as
+ * dugks_gpu_reduce: each partition reduces its rows on its device, the host adds
+ * the partitions in order (equal to the undivided case's sums to rounding). */
+int dugks_slabs_reduce(dugks_slabs_t *s, dugks_reductions_t *r);
 /* the whole grid's fields ([ny][nx] each); any pointer may be NULL */
 int dugks_slabs_download(dugks_slabs_t *s, double *rho, double *u, double *v, double *phi, double *p);
 int64_t dugks_slabs_launch_count(const dugks_slabs_t *s);

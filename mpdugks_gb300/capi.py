@@ -45,6 +45,10 @@ class ReductionsT(C.Structure):
                 ('steps', C.c_int64)]
 
 
+class HaloCopyT(C.Structure):
+    _fields_ = [('src', C.c_int), ('src_row', C.c_int), ('dst', C.c_int), ('dst_row', C.c_int), ('rows', C.c_int)]
+
+
 class SrvConfigT(C.Structure):
     _fields_ = [('max_bytes', C.c_size_t), ('chunk_steps', C.c_int), ('solo_lanes', C.c_int),
                 ('reserved', C.c_int * 5)]
@@ -118,6 +122,9 @@ SIGNATURES = {
                                      C.POINTER(C.c_void_p)]),
     'dugks_slabs_init': (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_int, C.c_uint64]),
     'dugks_slabs_step': (C.c_int, [C.c_void_p, C.c_int]),
+    'dugks_slabs_schedule': (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(HaloCopyT), C.c_int,
+                                       C.POINTER(C.c_int)]),
+    'dugks_slabs_reduce': (C.c_int, [C.c_void_p, C.POINTER(ReductionsT)]),
     'dugks_slabs_download': (C.c_int, [C.c_void_p] + [C.c_void_p] * 5),
     'dugks_slabs_launch_count': (C.c_int64, [C.c_void_p]),
     'dugks_slabs_destroy': (C.c_int, [C.c_void_p]),
@@ -352,6 +359,22 @@ def slab_plan(ny: int, y_walls: bool, nparts: int):
     return tuple([list(a) for a in arrs])
 
 
+def slab_schedule(ny: int, y_walls: bool, nparts: int) -> list[tuple[int, int, int, int, int]]:
+    """Host-only halo exchange schedule: (src, src_row, dst, dst_row, rows) per copy, in
+    the order the device exchange issues them (local rows; negative = lower halo)."""
+    lib = load()
+    n = C.c_int()
+    rc = lib.dugks_slabs_schedule(ny, int(y_walls), nparts, None, 0, C.byref(n))
+    if rc == DUGKS_OK:
+        out = (HaloCopyT * max(1, n.value))()
+        rc = lib.dugks_slabs_schedule(ny, int(y_walls), nparts, out, n.value, C.byref(n))
+    if rc != DUGKS_OK:
+        buf = C.create_string_buffer(512)
+        lib.dugks_gpu_last_error(None, buf, 512)
+        raise DugksError(rc, buf.value.decode())
+    return [(c.src, c.src_row, c.dst, c.dst_row, c.rows) for c in out[:n.value]]
+
+
 class Slabs:
     """One FP32-storage case split along y into partitions with halo exchange (dugks_slabs_*)."""
 
@@ -376,6 +399,11 @@ class Slabs:
 
     def step(self, n: int = 1) -> None:
         self._check(self.lib.dugks_slabs_step(self.h, n))
+
+    def reduce(self) -> ReductionsT:
+        r = ReductionsT()
+        self._check(self.lib.dugks_slabs_reduce(self.h, C.byref(r)))
+        return r
 
     def fields(self) -> dict[str, np.ndarray]:
         out = {k: np.empty((self.ny, self.nx), dtype=np.float64) for k in ('rho', 'u', 'v', 'phi', 'p')}

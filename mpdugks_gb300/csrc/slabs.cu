@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -46,6 +47,10 @@ template <typename R>
 cudaError_t launch_plane_from_f64(R *dst, int dpitch, const double *src, int nx, int ny, double sub,
                                   cudaStream_t st, int64_t *launches);
 }  // namespace f32
+namespace exact {
+void launch_reduce(const Params &P, const double *rho, const double *phi, double *rho_last, double *partial,
+                   int nblocks, double *out4, int has_phi, cudaStream_t st, int64_t *launches);
+}  // namespace exact
 }  // namespace dugks
 
 using namespace dugks;
@@ -54,6 +59,7 @@ namespace {
 
 constexpr int H = f32::SLAB_HALO;
 constexpr int MIN_ROWS = 8;  // rows of a partition (the streaming kernel's window)
+constexpr int RED_BLOCKS = 152;  // blocks of a partition's reduction
 
 struct Part {
     int device = 0, row0 = 0, nrows = 0, lo = -1, hi = -1;  // lo/hi: neighbour partition, -1 = wall
@@ -61,6 +67,7 @@ struct Part {
     f32::S32 S{};          // current orientation (ping-pong swapped after each step)
     float *arena = nullptr;
     double *fields = nullptr;  // rho u v p phi [5][nrows][pitch] (download)
+    double *red = nullptr;     // reductions: rho_last [nrows][pitch], partial sums [RED_BLOCKS][4], totals [4]
     size_t plane = 0;          // floats per plane (nrows + 2H rows)
     cudaStream_t st = nullptr;
     bool own_stream = false;
@@ -82,6 +89,19 @@ bool plan(int ny, int walls, int nparts, std::vector<int> &row0, std::vector<int
     return true;
 }
 
+// The halo copies after every step, in issue order: for each partition, its top H
+// rows into the upper neighbour's lower halo, then its bottom H rows into the lower
+// neighbour's upper halo.  Rows are local (0 = the first owned row).
+std::vector<dugks_halo_copy_t> schedule(const std::vector<int> &nrows, const std::vector<int> &lo,
+                                        const std::vector<int> &hi) {
+    std::vector<dugks_halo_copy_t> out;
+    for (size_t p = 0; p < nrows.size(); ++p) {
+        if (hi[p] >= 0) out.push_back({(int)p, nrows[p] - H, hi[p], -H, H});
+        if (lo[p] >= 0) out.push_back({(int)p, 0, lo[p], nrows[lo[p]], H});
+    }
+    return out;
+}
+
 }  // namespace
 
 struct dugks_slabs {
@@ -89,6 +109,7 @@ struct dugks_slabs {
     dugks_grid_t grid{};
     Params P{};
     std::vector<Part> parts;
+    std::vector<dugks_halo_copy_t> copies;  // the exchange schedule
     int first = 1, gcur = 0;
     int64_t steps = 0, launches = 0;
     bool multi_device = false;
@@ -111,23 +132,16 @@ cudaError_t copy_rows(float *dst, size_t dp, const float *src, size_t sp, int pi
                              f32::PL_N, cudaMemcpyDefault, st);
 }
 
-// halo exchange into the current state of every partition
+// halo exchange into the current state of every partition, as the schedule lists it
 cudaError_t exchange(dugks_slabs *s) {
     const int pitch = s->P.pitch;
-    for (auto &p : s->parts) {
-        if (p.hi >= 0) {  // my top rows -> the upper neighbour's lower halo
-            Part &q = s->parts[p.hi];
-            cudaSetDevice(q.device);
-            cudaError_t e = copy_rows(q.S.df - (size_t)H * pitch, q.plane, p.S.df + (size_t)(p.nrows - H) * pitch,
-                                      p.plane, pitch, H, q.st);
-            if (e != cudaSuccess) return e;
-        }
-        if (p.lo >= 0) {  // my bottom rows -> the lower neighbour's upper halo
-            Part &q = s->parts[p.lo];
-            cudaSetDevice(q.device);
-            cudaError_t e = copy_rows(q.S.df + (size_t)q.nrows * pitch, q.plane, p.S.df, p.plane, pitch, H, q.st);
-            if (e != cudaSuccess) return e;
-        }
+    for (const auto &c : s->copies) {
+        const Part &p = s->parts[c.src];
+        Part &q = s->parts[c.dst];
+        cudaSetDevice(q.device);
+        cudaError_t e = copy_rows(q.S.df + (ptrdiff_t)c.dst_row * pitch, q.plane, p.S.df + (ptrdiff_t)c.src_row * pitch,
+                                  p.plane, pitch, c.rows, q.st);
+        if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
@@ -158,6 +172,19 @@ extern "C" int dugks_slabs_plan(int ny, int y_walls, int nparts, int *row0, int 
     return DUGKS_OK;
 }
 
+extern "C" int dugks_slabs_schedule(int ny, int y_walls, int nparts, dugks_halo_copy_t *out, int max, int *count) {
+    std::vector<int> row0, nrows, lo, hi;
+    if (!count || !plan(ny, y_walls, nparts, row0, nrows, lo, hi))
+        return fail("schedule: needs count and at least " + std::to_string(MIN_ROWS) + " rows per partition");
+    const std::vector<dugks_halo_copy_t> c = schedule(nrows, lo, hi);
+    *count = (int)c.size();
+    if (out) {
+        if (max < (int)c.size()) return fail("schedule: output holds fewer copies than the schedule");
+        std::copy(c.begin(), c.end(), out);
+    }
+    return DUGKS_OK;
+}
+
 extern "C" int dugks_slabs_create(const dugks_case_t *c, const dugks_grid_t *g, int nparts, const int *devices,
                                   dugks_slabs_t **out) {
     if (!c || !g || !out) return fail("null argument");
@@ -176,6 +203,7 @@ extern "C" int dugks_slabs_create(const dugks_case_t *c, const dugks_grid_t *g, 
     s->grid = *g;
     derive_params(*c, *g, s->P);
     s->parts.resize(nparts);
+    s->copies = schedule(nrows, lo, hi);
     int dev0 = 0;
     cudaGetDevice(&dev0);
     for (int p = 0; p < nparts; ++p) {
@@ -207,6 +235,9 @@ extern "C" int dugks_slabs_create(const dugks_case_t *c, const dugks_grid_t *g, 
         }
         if (e == cudaSuccess) e = cudaMalloc(&q.arena, floats * sizeof(float));
         if (e == cudaSuccess) e = cudaMalloc(&q.fields, 5 * (size_t)q.nrows * pitch * sizeof(double));
+        const size_t red = (size_t)q.nrows * pitch + 4 * RED_BLOCKS + 4;
+        if (e == cudaSuccess) e = cudaMalloc(&q.red, red * sizeof(double));
+        if (e == cudaSuccess) e = cudaMemsetAsync(q.red, 0, red * sizeof(double), q.st);
         if (e == cudaSuccess) e = cudaMemsetAsync(q.arena, 0, floats * sizeof(float), q.st);
         if (e != cudaSuccess) {
             dugks_slabs_destroy(s);
@@ -337,6 +368,41 @@ extern "C" int dugks_slabs_download(dugks_slabs_t *s, double *rho, double *u, do
     return DUGKS_OK;
 }
 
+// Each partition reduces its own rows on its device (the handle's reduction kernel);
+// the host adds the partitions' totals in partition order.
+extern "C" int dugks_slabs_reduce(dugks_slabs_t *s, dugks_reductions_t *r) {
+    if (!s || !r) return fail("null argument");
+    const int pitch = s->P.pitch;
+    std::vector<double> tot(4 * s->parts.size());
+    for (size_t k = 0; k < s->parts.size(); ++k) {
+        Part &q = s->parts[k];
+        cudaSetDevice(q.device);
+        const size_t fp = (size_t)q.nrows * pitch;
+        double *F = q.fields;
+        f32::launch_macros32(q.P, q.S, F, F + fp, F + 2 * fp, F + 3 * fp, F + 4 * fp, pitch, q.st, &s->launches);
+        Params P = s->P;
+        P.ny = q.nrows;
+        double *rho_last = q.red, *partial = q.red + fp, *out4 = partial + 4 * RED_BLOCKS;
+        exact::launch_reduce(P, F, F + 4 * fp, rho_last, partial, RED_BLOCKS, out4, 1, q.st, &s->launches);
+        cudaError_t e = cudaMemcpyAsync(&tot[4 * k], out4, 4 * sizeof(double), cudaMemcpyDeviceToHost, q.st);
+        if (e != cudaSuccess) return cuda_fail(e, "reduce");
+    }
+    cudaError_t e = sync_all(s);
+    if (e != cudaSuccess) return cuda_fail(e, "reduce");
+    double a = 0, b = 0, d = 0, r2 = 0;
+    for (size_t k = 0; k < s->parts.size(); ++k) {
+        a += tot[4 * k];
+        b += tot[4 * k + 1];
+        d += tot[4 * k + 2];
+        r2 += tot[4 * k + 3];
+    }
+    r->sum_rho = a;
+    r->sum_phi = b;
+    r->residual = std::sqrt(d / (r2 + 1.0E-30));
+    r->steps = s->steps;
+    return DUGKS_OK;
+}
+
 extern "C" int64_t dugks_slabs_launch_count(const dugks_slabs_t *s) { return s ? s->launches : 0; }
 
 extern "C" int dugks_slabs_destroy(dugks_slabs_t *s) {
@@ -351,6 +417,7 @@ extern "C" int dugks_slabs_destroy(dugks_slabs_t *s) {
         cudaSetDevice(q.device);
         if (q.arena) cudaFree(q.arena);
         if (q.fields) cudaFree(q.fields);
+        if (q.red) cudaFree(q.red);
     }
     for (auto &q : s->parts) {
         cudaSetDevice(q.device);

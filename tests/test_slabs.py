@@ -37,9 +37,11 @@ def test_plan_rejects_too_many_partitions():
     assert e.value.code == capi.DUGKS_EINVAL
 
 
-# ---- the exchange schedule across two processes (gloo): each rank owns a slab
-# of a global array with two halo rows per side and fills its halos from the
-# neighbours' boundary rows, as the device exchange does after every step
+# ---- the exchange schedule across processes (gloo): each rank owns a slab of a
+# global array with two halo rows per side and executes the library's own halo
+# schedule (dugks_slabs_schedule, the list the device exchange runs after every
+# step): it sends the copies whose source it owns and receives those it is the
+# destination of, tagged by their index in the schedule
 
 def _exchange_rank(rank, world, port, ny, walls, fail_rank, q):
     import torch
@@ -50,6 +52,7 @@ def _exchange_rank(rank, world, port, ny, walls, fail_rank, q):
         os.environ.update(MASTER_ADDR='127.0.0.1', MASTER_PORT=str(port))
         dist.init_process_group('gloo', rank=rank, world_size=world, timeout=timedelta(seconds=5))
         row0, nrows, lo, hi = capi.slab_plan(ny, walls, world)
+        copies = capi.slab_schedule(ny, walls, world)
         nx = 5
         glob = np.arange(ny * nx, dtype=np.float64).reshape(ny, nx) + 1.0
         r0, n = row0[rank], nrows[rank]
@@ -58,18 +61,14 @@ def _exchange_rank(rank, world, port, ny, walls, fail_rank, q):
         if rank == fail_rank:
             raise RuntimeError('rank left before the exchange')
         reqs = []
-        if hi[rank] >= 0:
-            reqs.append(dist.isend(torch.from_numpy(mine[n:n + H].copy()), hi[rank], tag=1))
-        if lo[rank] >= 0:
-            reqs.append(dist.isend(torch.from_numpy(mine[H:2 * H].copy()), lo[rank], tag=2))
-        if lo[rank] >= 0:
-            t = torch.empty((H, nx), dtype=torch.float64)
-            dist.recv(t, lo[rank], tag=1)
-            mine[0:H] = t.numpy()
-        if hi[rank] >= 0:
-            t = torch.empty((H, nx), dtype=torch.float64)
-            dist.recv(t, hi[rank], tag=2)
-            mine[n + H:] = t.numpy()
+        for tag, (src, srow, dst, drow, rows) in enumerate(copies):
+            if src == rank:
+                reqs.append(dist.isend(torch.from_numpy(mine[H + srow:H + srow + rows].copy()), dst, tag=tag))
+        for tag, (src, srow, dst, drow, rows) in enumerate(copies):
+            if dst == rank:
+                t = torch.empty((rows, nx), dtype=torch.float64)
+                dist.recv(t, src, tag=tag)
+                mine[H + drow:H + drow + rows] = t.numpy()
         for r in reqs:
             r.wait()
         for k in range(-H, n + H):
@@ -84,12 +83,13 @@ def _exchange_rank(rank, world, port, ny, walls, fail_rank, q):
         q.put((rank, f'error: {type(e).__name__}: {e}'))
 
 
-def _run_exchange(ny, walls, fail_rank=-1):
+def _run_exchange(ny, walls, fail_rank=-1, world=2):
     import multiprocessing as mp
     ctx = mp.get_context('spawn')
     q = ctx.Queue()
     port = free_port()
-    procs = [ctx.Process(target=_exchange_rank, args=(r, 2, port, ny, walls, fail_rank, q)) for r in range(2)]
+    procs = [ctx.Process(target=_exchange_rank, args=(r, world, port, ny, walls, fail_rank, q))
+             for r in range(world)]
     for p in procs:
         p.start()
     out = dict(q.get(timeout=120) for _ in procs)
@@ -100,10 +100,34 @@ def _run_exchange(ny, walls, fail_rank=-1):
     return out
 
 
-@pytest.mark.parametrize('ny,walls', [(40, False), (41, True)])
-def test_halo_exchange_schedule_two_ranks(ny, walls):
-    out = _run_exchange(ny, walls)
-    assert out == {0: 'ok', 1: 'ok'}, out
+@pytest.mark.parametrize('ny,walls,world', [(40, False, 2), (41, True, 2), (50, False, 3), (35, True, 4)])
+def test_halo_exchange_schedule_across_ranks(ny, walls, world):
+    out = _run_exchange(ny, walls, world=world)
+    assert out == {r: 'ok' for r in range(world)}, out
+
+
+@pytest.mark.parametrize('ny,walls,n', [(40, False, 2), (41, True, 2), (64, False, 4), (33, True, 3)])
+def test_schedule_fills_every_halo_row_once(ny, walls, n):
+    """Every halo row next to a neighbour is written by exactly one copy, from the
+    neighbour's matching boundary rows; wall sides get no copy."""
+    from mpdugks_gb300 import capi
+    row0, nrows, lo, hi = capi.slab_plan(ny, walls, n)
+    seen = {}
+    for src, srow, dst, drow, rows in capi.slab_schedule(ny, walls, n):
+        assert rows == H
+        for k in range(rows):
+            key = (dst, drow + k)
+            assert key not in seen
+            seen[key] = (src, srow + k)
+    want = {}
+    for p in range(n):
+        if lo[p] >= 0:
+            for k in range(H):
+                want[(p, -H + k)] = (lo[p], nrows[lo[p]] - H + k)
+        if hi[p] >= 0:
+            for k in range(H):
+                want[(p, nrows[p] + k)] = (hi[p], k)
+    assert seen == want
 
 
 def test_a_rank_that_leaves_is_reported_not_waited_for():
@@ -132,11 +156,20 @@ def test_partitioned_run_equals_the_undivided_case(model, walls, nx, ny, n, init
     steps = 33
     sl = capi.Slabs(capi.make_case(model, 'fp32dev', **kw), nx, ny, walls, n)
     sl.init(init, params, seed=5)
-    sl.step(steps)
-    a = sl.fields()
-    sl.close()
     gc = capi.GpuCase(capi.make_case(model, 'fp32dev', **kw), nx, ny, walls)
     gc.init(init, params, seed=5)
-    gc.step(steps)
+    red = []
+    for _ in range(2):  # the second residual is the change over `steps` steps
+        sl.step(steps)
+        gc.step(steps)
+        red.append((sl.reduce(), gc.reduce()))
+    a = sl.fields()
+    sl.close()
     for k in ('rho', 'u', 'v', 'phi', 'p'):
         assert np.array_equal(a[k], gc.get(k)), k
+    # the same sums as the undivided case, added in another order
+    for rs, rg in red:
+        assert rs.steps == rg.steps
+        assert abs(rs.sum_rho - rg.sum_rho) <= 1e-13 * abs(rg.sum_rho)
+        assert abs(rs.sum_phi - rg.sum_phi) <= 1e-12 * abs(rg.sum_phi)
+        assert abs(rs.residual - rg.residual) <= 1e-9 * rg.residual
