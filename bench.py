@@ -57,7 +57,7 @@ STORED_BYTES = {'fp32dev': 200, 'fp64': 320, 'fp64fma': 320, 'fp64fused': 400}
 # DRAM bytes per cell and step of the fused FP32 kernel: ncu dram__bytes_read.sum +
 # dram__bytes_write.sum of one k_stream32 launch on 3072x3072 cells, divided by the cells
 # (profiles/k_stream32_rt3072x3072_fp32.md); scaled by the cell count to a full launch
-TRAFFIC_BYTES = {'fp32dev': (1014.983e6 + 860.065e6) / (3072 * 3072)}
+TRAFFIC_BYTES = {'fp32dev': (995.413248e6 + 902.451712e6) / (3072 * 3072)}
 
 
 def case_kw(wl: dict) -> dict:

@@ -10,11 +10,11 @@
 // so every warp runs independently of the others and of its block.
 //
 // Per row k the warp does, in order:
-//   the sums of row k+2's staged deviations (sum f, sum g); the load of row k+3's
-//     deviations into the stage ring (the phase field phi and the aux of a row are
-//     read directly into registers one row ahead of their use);
-//   collision of row k+1 (macros, MacroSource on the 3x3 phi stencil from the phi
-//     of rows k..k+2 and the adjacent lanes, f-bar-plus) into the f-bar-plus ring;
+//   the load of row k+3's deviations into the stage ring (the phase field phi and
+//     the aux of a row are read directly into registers one row ahead of their use);
+//   collision of row k+1 (the sums of its deviations, macros, MacroSource on the 3x3
+//     phi stencil from the phi of rows k..k+2 and the adjacent lanes, f-bar-plus)
+//     into the f-bar-plus ring;
 //   the y-face between rows k and k+1 (its flux is row k's north face and,
 //     carried to the next row, row k+1's south face);
 //   the x-faces of row k (west face per lane, east face from the next lane);
@@ -218,11 +218,9 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
     prefetch(y0 - 2);
     // rolling per-lane state: the phi pairs of rows k-1 .. k+2 (ph_m, ph0, ph1, ph2),
     // of row k+3 (ph_n, loaded one row ahead) and of row k-1 in the west lane
-    // (ph_mw); the (sum f, sum g) of the staged rows k+1, k+2; row k's collision
-    // increments and south-face flux
+    // (ph_mw); row k's collision increments and south-face flux
     T ph_m = mk2(0.f, 0.f), ph_mw = mk2(0.f, 0.f), ph0 = mk2(0.f, 0.f), ph1 = mk2(0.f, 0.f);
     T ph2 = mk2(0.f, 0.f), ph_n = load_phi(y0 - 2);
-    float sfz1 = 0.f, sg1 = 0.f;
     float a6c[A_N];  // aux of row k+1 (loaded at the previous row)
     T inc_cur[9], FS[6];
 #pragma unroll
@@ -262,20 +260,7 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
         } else {
             cp_async_wait_all();
         }
-        __syncwarp();
-        // ---- (sum f, sum g) of row k+2
-        float sfz2 = 0.f, sg2 = 0.f;
-        if (row_ok(k + 2)) {
-            const int sl = m4(k + 2);
-            T za[9];
-#pragma unroll
-            for (int q = 0; q < 9; ++q) za[q] = STG(sl, q);
-            if (MODEL == AC) za[0].x = 0.f;
-            const T z = ff_sum9(za);
-            sfz2 = z.x;
-            sg2 = z.y;
-        }
-        __syncwarp();  // every lane has read slot k+2 (slot k+3 = slot k-1 is refilled next)
+        __syncwarp();  // every lane has read slot k-1 (the update of row k-1), refilled next
         prefetch(k + 3);
         // ---- collision of row k+1
         T inc_nx[9];
@@ -292,11 +277,17 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
                 T Pq[9];
 #pragma unroll
                 for (int q = 0; q < 9; ++q) Pq[q] = STG(sl, q);
-                Pq[0].y = -sg1;
+                // (sum f, sum g) of the row's deviations (AC: without f_0); g_0 = -sum g
+                T za[9];
+#pragma unroll
+                for (int q = 0; q < 9; ++q) za[q] = Pq[q];
+                if (MODEL == AC) za[0].x = 0.f;
+                const T z = ff_sum9(za);
+                Pq[0].y = -z.y;
                 const T ph[8] = {E, W, ph2, ph0, NE, NW, SE, SWv};
                 const long long c = cell(j);
                 float src[6], phi, U, V;
-                collide_cell<MODEL, float>(P, S, c, first, Pq, sfz1, a6c, ph1, ph, inc_nx, src, phi, U, V);
+                collide_cell<MODEL, float>(P, S, c, first, Pq, z.x, a6c, ph1, ph, inc_nx, src, phi, U, V);
                 T bp[9];
 #pragma unroll
                 for (int q = 0; q < 9; ++q) bp[q] = add2(Pq[q], inc_nx[q]);
@@ -447,8 +438,6 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
         ph_mw = SWv;
         ph0 = ph1;
         ph1 = ph2;
-        sfz1 = sfz2;
-        sg1 = sg2;
         if (MODEL != AC) {
 #pragma unroll
             for (int a = 0; a < A_N; ++a) a6c[a] = a6n[a];
