@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -47,6 +48,8 @@ cudaError_t stream_tensor_map(void *map_out, float *base, int nx, int ny, int pi
 cudaError_t launch_pp32_step(const PPP &P, const PPS &S, int do_msrc, cudaStream_t st, int64_t *launches,
                              uint32_t step);
 cudaError_t launch_pp32_force(const PPP &P, const PPS &S, cudaStream_t st, int64_t *launches);
+cudaError_t launch_pp32_stream(const PPP &P, const PPV &in, const PPV &out, float *Fx, float *Fy, double *p,
+                               size_t qs, int do_msrc, cudaStream_t st, int64_t *launches);
 cudaError_t launch_pp_g_from_f64(float *g, int pitch, const double *f, const double *rho, int nx, int ny, double e,
                                  cudaStream_t st, int64_t *launches);
 template <typename R>
@@ -127,6 +130,7 @@ struct dugks_handle {
     int init_kind = -1;       // the last dugks_gpu_init's kind and drop radius (drop L2 norm)
     double init_radius = 0.0;
     const double *pp_rho0 = nullptr;  // the density plane the step reads as created (checkpoint orientation)
+    bool pp_stream = false;           // FP32 pseudopotential: the single-pass step (else four passes)
 };
 
 static std::string g_create_err;
@@ -223,8 +227,20 @@ static cudaError_t to_dev(const dugks_handle *h, double *d, const double *src, i
 static size_t pp32_arena_bytes(const Params &P) {
     const size_t cf = align256((size_t)P.pitch * P.ny * sizeof(float));
     const size_t cd = align256((size_t)P.pitch * P.ny * sizeof(double));
-    return (6 * (size_t)P.Q + 21) * cf + 7 * cd + align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 512 +
+    // four-pass state and scratch, plus the single-pass step's second copy (Q + 7 float
+    // planes, U and V)
+    return (7 * (size_t)P.Q + 28) * cf + 9 * cd + align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 512 +
            (P.model == PP16 ? align256(sizeof(float) * 256) : 0);
+}
+
+// after a step of the FP32 pseudopotential path: the density the update wrote (and, for
+// the single-pass step, the whole copy it wrote) becomes the state
+static void pp32_swap(dugks_handle *h) {
+    std::swap(h->PPs.rho, h->PPs.rho_o);
+    if (h->pp_stream) f32::pp_swap_copies(h->PPs);
+    h->S.fld[F_RHO] = h->PPs.rho;
+    h->S.fld[F_U] = h->PPs.U;
+    h->S.fld[F_V] = h->PPs.V;
 }
 
 // a double as the unevaluated float sum hi + lo (about 48 significant bits)
@@ -236,6 +252,10 @@ static void split_ff(double v, float &hi, float &lo) {
 static int create_pp32(dugks_handle *h, dugks_handle_t **out) {
     Params &P = h->P;
     h->pp32 = true;
+    // the single-pass step needs a 32-column window and 8 rows; DUGKS_PP_PASSES=4 in the
+    // environment keeps the four-pass form (the two are compared by the tests)
+    const char *passes = std::getenv("DUGKS_PP_PASSES");
+    h->pp_stream = P.nx >= 32 && P.ny >= 8 && !(passes && std::atoi(passes) == 4);
     h->nblocks = REDUCE_BLOCKS;
     const size_t cf = align256((size_t)P.pitch * P.ny * sizeof(float));
     const size_t cd = align256((size_t)P.pitch * P.ny * sizeof(double));
@@ -264,6 +284,12 @@ static int create_pp32(dugks_handle *h, dugks_handle_t **out) {
                       &S.xFx, &S.xFy, &S.yFx, &S.yFy, &S.psi, &S.scg, &S.Fx, &S.Fy,
                       &S.psil, &S.xpsl, &S.ypsl};
     for (auto p : scal) *p = tf(1);
+    S.alt.g = tf(Q);
+    float **alt[] = {&S.alt.psi, &S.alt.psil, &S.alt.scg, &S.alt.xFx, &S.alt.xFy, &S.alt.yFx, &S.alt.yFy};
+    for (auto p : alt) *p = tf(1);
+    S.alt.U = td();
+    S.alt.V = td();
+    S.alt.rho = nullptr;
     S.rho = td();
     S.rho_o = td();
     h->pp_rho0 = S.rho;
@@ -738,12 +764,18 @@ extern "C" int dugks_gpu_step(dugks_handle_t *h, int nsteps, void *stream) {
     }
     if (h->pp32) {
         for (int s = 0; s < nsteps; ++s) {
-            cudaError_t e = f32::launch_pp32_step(h->PPc, h->PPs, h->pp_pending, st, &h->launches,
-                                                  (uint32_t)(h->steps + s));
+            cudaError_t e;
+            if (h->pp_stream) {
+                f32::PPV out = h->PPs.alt;
+                out.rho = h->PPs.rho_o;
+                e = f32::launch_pp32_stream(h->PPc, f32::pp_current(h->PPs), out, h->PPs.Fx, h->PPs.Fy, h->PPs.p,
+                                            h->PPs.qs, h->pp_pending, st, &h->launches);
+            } else {
+                e = f32::launch_pp32_step(h->PPc, h->PPs, h->pp_pending, st, &h->launches, (uint32_t)(h->steps + s));
+            }
             if (e != cudaSuccess) return cuda_fail(h, e, "fp32 pseudopotential step launch");
             h->pp_pending = 1;
-            std::swap(h->PPs.rho, h->PPs.rho_o);  // the density the update wrote is the state's
-            h->S.fld[F_RHO] = h->PPs.rho;
+            pp32_swap(h);  // the copy the step wrote is the state
         }
         h->steps += nsteps;
         cudaError_t e = cudaGetLastError();
@@ -1257,8 +1289,7 @@ extern "C" int dugks_gpu_restore(dugks_handle_t *h, const void *buf, size_t len)
     if (h->pp32) h->PPc = hd.ppc;
     if (fused_orient(h) != hd.orient) {
         if (h->pp32) {
-            std::swap(h->PPs.rho, h->PPs.rho_o);
-            h->S.fld[F_RHO] = h->PPs.rho;
+            pp32_swap(h);
         } else if (h->fused64) {
             f32::swap_io(h->S64f);
         } else {

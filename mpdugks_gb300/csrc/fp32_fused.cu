@@ -175,10 +175,10 @@ __device__ __forceinline__ void tile_step(const PR<R> &P, const SR<R> &S, int fi
         Pq[0] = mk2(plane(PL_F), R(0.));
 #pragma unroll
         for (int q = 1; q < 9; ++q) Pq[q] = mk2(plane(PL_F + q), plane(PL_G + q - 1));
-        // (sum f, sum g) as a float-float pair; the Allen-Cahn pressure omits f_0
+        // (sum f, sum g); the Allen-Cahn pressure omits f_0
         const T za[9] = {mk2(MODEL == AC ? R(0.) : Pq[0].x, R(0.)), Pq[1], Pq[2], Pq[3], Pq[4],
                          Pq[5], Pq[6], Pq[7], Pq[8]};
-        const T z = ff_sum9(za);
+        const T z = dev_sum9(za);
         sfz = z.x;
         Pq[0].y = -z.y;  // g_0 = -sum_{q>0} g_q
         sphi[r + 1][e + 1] = mk2(plane(PL_PHI), plane(PL_PHI + 1));

@@ -95,6 +95,15 @@ struct PPP {
     // each case holds its own, so cases of different lattice speed run side by side
     const float *iM16;
 };
+// One copy of the state the single-pass pseudopotential step reads or writes (two
+// copies, swapped after each step: a strip segment reads rows its neighbours write)
+struct PPV {
+    float *g;                              // remainders [Q][ny][pitch]
+    double *rho, *U, *V;                   // density and velocity
+    float *psi, *psil, *scg;               // psi pair and its sign
+    float *xFx, *xFy, *yFx, *yFy;          // face forces (read by the next step's face moments)
+};
+
 // State: the remainders g_q = f_q - e_q rho and the step's scratch in FP32, the
 // density (and the pressure for output) in FP64; the density in two planes: the
 // update reads its neighbours' density while it writes its own into rho_o, and the
@@ -107,8 +116,21 @@ struct PPS {
     double *rho, *rho_o, *p, *U, *V; // cell density (read / written by the update), pressure, velocity
     float *psi, *scg, *Fx, *Fy;
     float *psil, *xpsl, *ypsl;       // the tails of psi (cell, x faces, y faces) as float-float pairs
+    PPV alt;                         // the single-pass step's second copy (its rho is rho_o)
     size_t qs;
 };
+// the copy of the state a step reads
+inline PPV pp_current(const PPS &S) {
+    return {S.df, S.rho, S.U, S.V, S.psi, S.psil, S.scg, S.xFx, S.xFy, S.yFx, S.yFy};
+}
+// after a single-pass step the written copy becomes the state
+inline void pp_swap_copies(PPS &S) {
+    PPV c = pp_current(S), a = S.alt;
+    S.df = a.g, S.U = a.U, S.V = a.V, S.psi = a.psi, S.psil = a.psil, S.scg = a.scg;
+    S.xFx = a.xFx, S.xFy = a.xFy, S.yFx = a.yFx, S.yFy = a.yFy;
+    S.alt = c;
+    S.alt.rho = nullptr;
+}
 
 // halo rows of a slab partition on each side
 constexpr int SLAB_HALO = 2;

@@ -17,6 +17,7 @@ import argparse
 import json
 import os
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -42,9 +43,11 @@ def main() -> int:
     kw = bench.case_kw(wl)
     VARIANTS[NAME] = dict(model='D2Q9HCZ', nx=wl['nx'], ny=wl['ny'], walls=True, init='ac_rt', consts=kw)
     build_ref.build(NAME)
-    # the reference: 1 + steps steps; its printed loop time covers all of them
-    _, log1 = build_ref.run(NAME, 1, threads=a.threads)
-    out, log = build_ref.run(NAME, 1 + a.steps, threads=a.threads)
+    # the reference: 1 + steps steps; its printed loop time covers all of them (dumps in a
+    # temporary directory: ~300 MB each)
+    tmp = tempfile.TemporaryDirectory()
+    _, log1 = build_ref.run(NAME, 1, threads=a.threads, dump=f'{tmp.name}/d1.bin')
+    out, log = build_ref.run(NAME, 1 + a.steps, threads=a.threads, dump=f'{tmp.name}/d.bin')
     secs = lambda text: float(next(ln for ln in text.splitlines() if ln.startswith('done')).split()[6])
     ref_s = secs(log) - secs(log1)
     o = Oracle('HCZ', wl['nx'], wl['ny'], True, 'ac_rt', **kw)
@@ -53,6 +56,7 @@ def main() -> int:
     o.step(a.steps, a.threads)
     port_s = time.perf_counter() - t0
     _, ref = read_dump(out)
+    tmp.cleanup()
     same = all(bool((o.get(k) == v).all()) for k, v in ref.items() if k in ('rho', 'u', 'v', 'p', 'phi'))
     cells = wl['nx'] * wl['ny']
     print(json.dumps({'workload': wl['name'], 'threads': a.threads, 'steps': a.steps,

@@ -109,3 +109,40 @@ def test_d2v16_cases_of_different_lattice_speed_side_by_side(precision):
     for c, g in ((0.5, a), (0.6, b)):
         for k in ('rho', 'u', 'v'):
             assert np.array_equal(g.get(k), alone[c][k]), (c, k)
+
+
+def _handle(model, nx, ny, init, params, passes=None, **kw):
+    """A FP32 pseudopotential handle; passes=4 keeps the four-pass step form."""
+    import os
+    from mpdugks_gb300 import capi
+    old = os.environ.pop('DUGKS_PP_PASSES', None)
+    if passes:
+        os.environ['DUGKS_PP_PASSES'] = str(passes)
+    try:
+        g = capi.GpuCase(capi.make_case(model, 'fp32dev', **kw), nx, ny, False)
+    finally:
+        os.environ.pop('DUGKS_PP_PASSES', None)
+        if old is not None:
+            os.environ['DUGKS_PP_PASSES'] = old
+    g.init(init, params, seed=11)
+    return g
+
+
+@pytest.mark.parametrize('model,kw', [('PP9', {}), ('PP16', dict(d2v16_c=0.5))])
+@pytest.mark.parametrize('nx,ny,init,params', [(64, 40, 'pp_noise', [0.2, 0.01]), (33, 8, 'pp_noise', [0.2, 0.01]),
+                                               (96, 160, 'scmp_drop', []), (300, 270, 'pp_noise', [0.13044, 0.01])])
+def test_single_pass_step_equals_four_passes(model, kw, nx, ny, init, params):
+    """The single-pass streaming step against the four-pass step on grids of one or
+    several strips and segments (26-column strips, ragged last strip, 8 rows = the
+    smallest grid it takes): the same arithmetic, so the same fields and remainders."""
+    if model == 'PP16' and init == 'pp_noise':
+        params = [0.13044, 0.01]
+    a = _handle(model, nx, ny, init, params, **kw)
+    b = _handle(model, nx, ny, init, params, passes=4, **kw)
+    for steps in (1, 7):
+        a.step(steps)
+        b.step(steps)
+        for k in ('rho', 'u', 'v', 'p', 'psi', 'fx', 'fy'):
+            x, y = a.get(k), b.get(k)
+            assert np.array_equal(x, y), (k, float(np.max(np.abs(x - y))))
+        assert np.array_equal(a.dist('f'), b.dist('f'))
