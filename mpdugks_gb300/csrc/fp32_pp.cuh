@@ -23,8 +23,7 @@ __device__ __forceinline__ void pp_deq(const PPP &P, float rho, float u, float v
     if (MODEL == PP16) {
         // Macro16 (Ark/Lib/D2V16.cpp:125-145) at T = T0, p = rho RT, minus its value at
         // (rho, 0, 0) (at rest the moments are linear in rho); times the case's inverse
-        // moment matrix (Ark/Lib/D2V16.cpp:34-52), read through the read-only path (every
-        // lane of a warp reads the same entry)
+        // moment matrix (Ark/Lib/D2V16.cpp:34-52), a kernel parameter
         const float RT = P.RT, u2 = u * u, v2 = v * v, s2 = u2 + v2;
         float M[16];
         M[0] = 0.f;
@@ -47,16 +46,18 @@ __device__ __forceinline__ void pp_deq(const PPP &P, float rho, float u, float v
         for (int j = 0; j < 16; ++j) {
             float s = 0.f;
 #pragma unroll
-            for (int k = 1; k < 16; ++k) s = fmaf(__ldg(P.iM16 + j * 16 + k), M[k], s);
+            for (int k = 1; k < 16; ++k) s = fmaf(P.iM16[j][k], M[k], s);
             de[j] = s;
         }
     } else {
-        // D2Q9PP (Ark/Lib/D2Q9PP.cpp:51-62): w rho (1 + u1 + u1^2/2 - |u|^2 lambda) - w rho
-        const float uu = u * u + v * v;
+        // D2Q9PP (Ark/Lib/D2Q9PP.cpp:51-62): w rho (1 + u1 + u1^2/2 - |u|^2 lambda) - w rho;
+        // every rounding written out, so that each kernel including this evaluates it alike
+        const float uu = fmaf(u, u, __fmul_rn(v, v));
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
-            const float u1 = (sxf(d2q9_xu(q), u) + sxf(d2q9_xv(q), v)) * P.invRT;
-            de[q] = P.w9[q] * (rho * (u1 + 0.5f * u1 * u1 - uu * P.Lambda0));
+            const float u1 = __fmul_rn(__fadd_rn(sxf(d2q9_xu(q), u), sxf(d2q9_xv(q), v)), P.invRT);
+            const float t = fmaf(__fmul_rn(0.5f, u1), u1, u1);
+            de[q] = __fmul_rn(P.w9[q], __fmul_rn(rho, fmaf(-uu, P.Lambda0, t)));
         }
     }
 }

@@ -91,9 +91,10 @@ struct PPP {
     // R0 T_CS, aCS, RT
     float rtcs_hi, rtcs_lo, acs_hi, acs_lo, rt_hi, rt_lo;
     float xi_u[16], xi_v[16], w9[9], erest[16];
-    // D2V16 inverse moment matrix of this case ([16][16], in the case's device memory):
-    // each case holds its own, so cases of different lattice speed run side by side
-    const float *iM16;
+    // D2V16 inverse moment matrix of this case, by value: the kernels read its entries as
+    // constant-bank operands (no loads), and cases of different lattice speed run side by
+    // side with their own
+    float iM16[16][16];
 };
 // One copy of the state the single-pass pseudopotential step reads or writes (two
 // copies, swapped after each step: a strip segment reads rows its neighbours write)
