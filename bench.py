@@ -905,7 +905,7 @@ def run_ours(args, wl, rank, world, local):
             'metric': 'MLUPS', 'value': round(mlups_total, 3), 'unit': 'MLUPS', 'n_gpus': world,
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_max / args.steps, 5),
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
-            'dtype': 'f32 storage, f32 arithmetic, float-float/f64 moment sums' if prec == 'fp32dev' else 'f64',
+            'dtype': 'f32 storage and arithmetic (the phase field a float-float pair), f64 domain sums' if prec == 'fp32dev' else 'f64',
             'data': 'synthetic (seeded Rayleigh-Taylor initial condition, no dataset)',
             'config': {'workload': wl['name'], 'cells': cells, 'precision': prec,
                        'l2_flush': 'none needed: the state read and written each step is larger than the 129 MB L2',

@@ -40,12 +40,12 @@ namespace f32 {
 
 constexpr int SW = 28;   // interior columns of a strip
 constexpr int SEG_MAX = 128;  // longest first-choice segment (rows)
-constexpr int WPB = 2;   // warps per block
+constexpr int WPB = 1;   // warps per block (one warp a block: 4.6 % faster than 2 on 8192^2)
 constexpr int NSTG = 4;  // stage ring: rows k .. k+3
-// resident blocks per SM the streaming kernels are compiled for: 5 blocks of 2 warps
-// (up to 204 registers a thread) ran 1.9 % faster on the 8192^2 step than 6 blocks at
-// 168 registers (the compiler keeps the packed constant pairs in registers)
-constexpr int STREAM_MIN_BLOCKS = 5;
+// resident blocks per SM the streaming kernels are compiled for: 10 one-warp blocks (up to
+// 204 registers a thread; the kernel takes 168 and 12 blocks fit) ran 1.9 % faster on the
+// 8192^2 step than a bound of 12 warps at 168 registers
+constexpr int STREAM_MIN_BLOCKS = 10;
 // per-warp shared memory, in floats:
 //   stage ring [NSTG][17][32]: the raw planes (9 f, then g_1 .. g_8) of rows
 //     k .. k+3, 32 columns each -- the box one TMA load writes;
@@ -406,9 +406,21 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
                 av, fp, 0, FW);
         }
         T FE[6];
+        {   // the east face's flux is the next lane's west face, through row k-1's f-bar-plus
+            // slot (no longer read in this row): three 16-byte stores and loads instead of
+            // twelve shuffles (lane 31 reads past its slot row, in bounds, unused)
+            float4 *fq = reinterpret_cast<float4 *>(Bm.base);
 #pragma unroll
-        for (int s = 0; s < 6; ++s)
-            FE[s] = mk2(__shfl_down_sync(0xffffffffu, FW[s].x, 1), __shfl_down_sync(0xffffffffu, FW[s].y, 1));
+            for (int g = 0; g < 3; ++g)
+                fq[g * 32 + lane] = make_float4(FW[2 * g].x, FW[2 * g].y, FW[2 * g + 1].x, FW[2 * g + 1].y);
+            __syncwarp();
+#pragma unroll
+            for (int g = 0; g < 3; ++g) {
+                const float4 v = fq[g * 32 + lane + 1];
+                FE[2 * g] = mk2(v.x, v.y);
+                FE[2 * g + 1] = mk2(v.z, v.w);
+            }
+        }
         // ---- update of row k
         if (upd && interior) {
             const int sl = m4(k);
