@@ -253,8 +253,8 @@ static int create_pp32(dugks_handle *h, dugks_handle_t **out) {
     h->pp32 = true;
     // the four-pass step; DUGKS_PP_PASSES=1 in the environment selects the single-pass
     // streaming step (grids of at least 32 columns and 8 rows).  The two give the same
-    // results; on the GB300 the four-pass form is 2x faster (the single pass holds a row
-    // pipeline of 16 distributions per lane in 215 registers: 8 warps per SM, latency-bound)
+    // results; on the GB300 the four-pass form is 1.7x faster (the single pass holds a row
+    // pipeline of 16 distributions per lane: ~10 warps per SM, latency-bound)
     const char *passes = std::getenv("DUGKS_PP_PASSES");
     h->pp_stream = P.nx >= 32 && P.ny >= 8 && passes && std::atoi(passes) == 1;
     h->nblocks = REDUCE_BLOCKS;

@@ -22,13 +22,14 @@
 // from one copy and written to the other (a segment reads rows its neighbours write).
 // Periodic in x and y (the pseudopotential models have no walls).
 //
-// Measured on the GB300 (D2V16, 1024^2): 1.69 G cell-updates/s against 3.50 for the four
+// Measured on the GB300 (D2V16, 1024^2): 2.02 G cell-updates/s against 3.51 for the four
 // passes, with the same results bit for bit.  A lane holds the row pipeline of 16
-// distributions (215 registers: 4 blocks of 2 warps per SM) and the face moments and the
-// equation of state are serial float-float chains, so the 8 resident warps cannot hide
-// their latency; the four passes run 40-64 registers a thread at full occupancy and, for
-// all their ~1 KB of traffic per cell-update, stay ahead.  The handle therefore takes the
-// four-pass step; DUGKS_PP_PASSES=1 selects this one.
+// distributions (168 registers when compiled for 5 blocks of 2 warps per SM -- 1.69 G at
+// the 215 the compiler takes unbounded, 2.00 G at 128 with spills) and the face moments
+// and the equation of state are serial float-float chains, so the ~10 resident warps
+// cannot hide their latency; the four passes run 40-64 registers a thread at full
+// occupancy and, for all their ~1 KB of traffic per cell-update, stay ahead.  The handle
+// therefore takes the four-pass step; DUGKS_PP_PASSES=1 selects this one.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -69,7 +70,7 @@ struct PsiG {
 };
 
 template <int MODEL>
-__global__ void __launch_bounds__(PWPB * 32, 4)
+__global__ void __launch_bounds__(PWPB * 32, 5)
     k_pp32_stream(PPP P, PPV in, PPV out, float *__restrict__ Fxo, float *__restrict__ Fyo, double *__restrict__ pout,
                   size_t qs, int do_msrc, int nstrips, int nsegs, int seg_rows) {
     using L = PPLayout<MODEL>;

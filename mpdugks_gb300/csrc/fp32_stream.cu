@@ -116,10 +116,13 @@ static cudaError_t launch_stream_t(const P32 &P, const S32 &S, int first, int gi
     // the longest segment that still gives every resident warp about 4 segments
     // (a long segment costs fewer warm-up rows, a short one less idle tail)
     const int nstrips = (P.nx + SW - 1) / SW, warps = g_stream_nsm * g_stream_blocks * WPB;
-    // a grid with fewer 32-row strip segments than resident warps leaves most of the
-    // GPU idle in this form: the tile kernel (same arithmetic, same results) runs it
-    // (a slab partition reads halo rows, which only this form does: it always runs here)
-    if (!(P.halo_lo || P.halo_hi) && (long long)nstrips * ((P.ny + 31) / 32) < warps) {
+    // a grid with fewer 32-row strip segments than a third of the resident warps leaves
+    // most of the GPU idle in this form: the tile kernel (same arithmetic, same results)
+    // runs it.  Measured (Rayleigh-Taylor, G cell-updates/s, streaming / tile): 256x1024
+    // 5.1 / 7.5 (320 segments), 768^2 9.2 / 8.5 (672), 512x2048 11.9 / 8.5 (1216), 1024^2
+    // 12.5 / 8.8 (1184), against 1824 resident warps.  (A slab partition reads halo rows,
+    // which only this form does: it always runs here.)
+    if (!(P.halo_lo || P.halo_hi) && 3LL * nstrips * ((P.ny + 31) / 32) < warps) {
         *fallback = true;
         return cudaSuccess;
     }
