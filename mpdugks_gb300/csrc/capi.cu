@@ -130,7 +130,7 @@ struct dugks_handle {
     int init_kind = -1;       // the last dugks_gpu_init's kind and drop radius (drop L2 norm)
     double init_radius = 0.0;
     const double *pp_rho0 = nullptr;  // the density plane the step reads as created (checkpoint orientation)
-    bool pp_stream = false;           // FP32 pseudopotential: the single-pass step (else four passes)
+    bool pp_stream = false;           // FP32 pseudopotential: the single-pass step (else three passes)
 };
 
 static std::string g_create_err;
@@ -227,7 +227,7 @@ static cudaError_t to_dev(const dugks_handle *h, double *d, const double *src, i
 static size_t pp32_arena_bytes(const Params &P) {
     const size_t cf = align256((size_t)P.pitch * P.ny * sizeof(float));
     const size_t cd = align256((size_t)P.pitch * P.ny * sizeof(double));
-    // four-pass state and scratch, plus the single-pass step's second copy (Q + 7 float
+    // multi-pass state and scratch, plus the single-pass step's second copy (Q + 7 float
     // planes, U and V)
     return (7 * (size_t)P.Q + 28) * cf + 9 * cd + align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 512;
 }
@@ -251,9 +251,9 @@ static void split_ff(double v, float &hi, float &lo) {
 static int create_pp32(dugks_handle *h, dugks_handle_t **out) {
     Params &P = h->P;
     h->pp32 = true;
-    // the four-pass step; DUGKS_PP_PASSES=1 in the environment selects the single-pass
+    // the three-pass step; DUGKS_PP_PASSES=1 in the environment selects the single-pass
     // streaming step (grids of at least 32 columns and 8 rows).  The two give the same
-    // results; on the GB300 the four-pass form is 1.7x faster (the single pass holds a row
+    // results; on the GB300 the three-pass form is 1.7x faster (the single pass holds a row
     // pipeline of 16 distributions per lane: ~10 warps per SM, latency-bound)
     const char *passes = std::getenv("DUGKS_PP_PASSES");
     h->pp_stream = P.nx >= 32 && P.ny >= 8 && passes && std::atoi(passes) == 1;

@@ -2,11 +2,11 @@
 //
 // The reference's face force reads the face psi of the neighbouring faces of
 // the same step (Ark/Cpp/PseudoP.cpp:39-46, Jacobi semantics: all face psi
-// first, then the face forces), so the step keeps four passes like the FP64
-// path: collision (with the cell force from the psi of the previous update),
-// face pass 1 (reconstruction, face moments, face psi), face pass 2 (face
-// force, equilibrium, He-Shan-Doolen source, flux) and the update (with the
-// cell macros, pressure and psi).
+// first, then the face forces), so face pass 1 (reconstruction, face moments, face
+// psi) of every face precedes face pass 2 (face force, equilibrium, He-Shan-Doolen
+// source, flux) of any.  Three launches: the collision (with the cell force from the
+// psi of the previous update), face pass 1, and face pass 2 fused with the update (the
+// fluxes of a tile in shared memory; with the cell macros, pressure and psi).
 //
 // Storage: the density rho in FP64 and f as the FP32 remainders g_q = f_q - e_q rho,
 // e_q = eq_q(1, 0, 0) the rest equilibrium per unit density.  At rest f = e rho, so
@@ -18,9 +18,10 @@
 // sum of the small face fluxes (the e_q avg(rho) parts cancel: sum_q e_q xi_q = 0)
 // and each g_q by small increments.  Moment sums and the equation of state are
 // float-float (below).
-// (Fusing face pass 2 with the update, the fluxes of a tile in shared memory and the
-// face reconstruction recomputed instead of stored, ran slower: 0.55 against 0.46 ms
-// per D2V16 step at 1024^2, 128 registers and two blocks per SM.)
+// (Fusing face pass 2 with the update saved the fluxes' round trip through DRAM, ~0.2 KB
+// per cell-update, for 0.8 % of the D2V16 step: the passes are latency- as much as
+// bandwidth-bound.  An earlier fusion that recomputed the face reconstruction instead of
+// reading it ran slower.)
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -129,39 +130,41 @@ __global__ void __launch_bounds__(256) k_pp32_faces1(PPP P, PPS S) {
     (xf ? S.xps : S.yps)[c] = f.psi;
 }
 
-// Face pass 2: face force from the face-psi stencil (Ark/Cpp/PseudoP.cpp:39-46,
-// Ark/Lib/GradSchemeBasic.h:181-208), equilibrium, source and flux xi.n.
-template <int MODEL>
-__global__ void __launch_bounds__(256) k_pp32_faces2(PPP P, PPS S) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-    const bool xf = blockIdx.z == 0;
-    if (i >= P.nx || j >= P.ny) return;
+// Face pass 2 of the x face (XF) or y face at (i, j): face force from the face-psi
+// stencil (Ark/Cpp/PseudoP.cpp:39-46, Ark/Lib/GradSchemeBasic.h:181-208), stored for the
+// next step's face moments when own; equilibrium, source and the fluxes xi.n into out.
+template <int MODEL, bool XF>
+__device__ __forceinline__ void pp_face2_at(const PPP &P, const PPS &S, int i, int j, bool own,
+                                            float (&out)[PPQ<MODEL>::Q]) {
     constexpr int Q = PPQ<MODEL>::Q;
     const size_t c = (size_t)j * P.pitch + i;
     float gx, gy;
-    iso_grad(P, xf ? S.xps : S.yps, xf ? S.xpsl : S.ypsl, i, j, gx, gy);
-    const float k = -(xf ? S.xg : S.yg)[c] * (xf ? S.xps : S.yps)[c];
+    iso_grad(P, XF ? S.xps : S.yps, XF ? S.xpsl : S.ypsl, i, j, gx, gy);
+    const float k = -(XF ? S.xg : S.yg)[c] * (XF ? S.xps : S.yps)[c];
     const float Fx = gx * k, Fy = gy * k;
-    (xf ? S.xFx : S.yFx)[c] = Fx;
-    (xf ? S.xFy : S.yFy)[c] = Fy;
+    if (own) {
+        (XF ? S.xFx : S.yFx)[c] = Fx;
+        (XF ? S.xFy : S.yFy)[c] = Fy;
+    }
     PPFace f;
-    f.dr = (xf ? S.xr : S.yr)[c];
-    f.U = (xf ? S.xu : S.yu)[c];
-    f.V = (xf ? S.xv : S.yv)[c];
-    const size_t co = xf ? (size_t)j * P.pitch + wrapi(i - 1, P.nx) : (size_t)wrapi(j - 1, P.ny) * P.pitch + i;
+    f.dr = (XF ? S.xr : S.yr)[c];
+    f.U = (XF ? S.xu : S.yu)[c];
+    f.V = (XF ? S.xv : S.yv)[c];
+    const size_t co = XF ? (size_t)j * P.pitch + wrapi(i - 1, P.nx) : (size_t)wrapi(j - 1, P.ny) * P.pitch + i;
     const float R = (float)(0.5 * (S.rho[co] + S.rho[c]) + (double)f.dr);
-    const float *__restrict__ B = xf ? S.xb : S.yb;
-    float b[Q], out[Q];
+    const float *__restrict__ B = XF ? S.xb : S.yb;
+    float b[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) b[q] = B[(size_t)q * S.qs + c];
-    if (xf) pp_face2<MODEL, true>(P, b, R, f, Fx, Fy, out);
-    else pp_face2<MODEL, false>(P, b, R, f, Fx, Fy, out);
-    float *O = xf ? S.xfl : S.yfl;
-#pragma unroll
-    for (int q = 0; q < Q; ++q) O[(size_t)q * S.qs + c] = out[q];
+    pp_face2<MODEL, XF>(P, b, R, f, Fx, Fy, out);
 }
 
-// Update (Ark/Cpp/DUGKS2DSolver.cpp:748-792) and cell macros (Ark/Lib/D2Q9PP.cpp:89-109):
+// Face pass 2 and the update (Ark/Cpp/DUGKS2DSolver.cpp:748-792) with the cell macros
+// (Ark/Lib/D2Q9PP.cpp:89-109) in one launch: a block of 32x8 threads owns a 32x8-cell tile;
+// each thread computes the fluxes of its cell's west and south faces into shared memory,
+// 40 threads those of the tile's east column and north row (the next tiles' own faces,
+// whose forces those tiles store), and after a block barrier each thread updates its cell
+// from the four faces' fluxes, which never reach DRAM:
 //   rho_new = rho + drho, drho = dt/V sum_q (net face flux of q),
 //   g_q,new = g_q + 4/3 (b_q - g_q) + dt/V (net flux of q)
 //             + e_q (xi_q,x px + xi_q,y py) - e_q drho,
@@ -169,25 +172,50 @@ __global__ void __launch_bounds__(256) k_pp32_faces2(PPP P, PPS S) {
 // divergence on unit cells, from the FP64 density); U, V, p, psi from float-float
 // sums, rho in FP64.
 template <int MODEL>
-__global__ void __launch_bounds__(256) k_pp32_update(PPP P, PPS S, uint32_t step) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= P.nx || j >= P.ny) return;
+__global__ void __launch_bounds__(256) k_pp32_faces2u(PPP P, PPS S) {
     constexpr int Q = PPQ<MODEL>::Q;
+    __shared__ float xs[Q][8][33];  // x-face fluxes of the tile's rows, columns 0 .. 32
+    __shared__ float ys[Q][9][32];  // y-face fluxes of the tile's columns, rows 0 .. 8
+    const int tx = threadIdx.x, ty = threadIdx.y, t = ty * 32 + tx;
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 8;
+    const int w = min(32, P.nx - x0), h = min(8, P.ny - y0);
+    const int i = x0 + tx, j = y0 + ty;
+    const bool in = tx < w && ty < h;
+    float out[Q];
+    if (in) {
+        pp_face2_at<MODEL, true>(P, S, i, j, true, out);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) xs[q][ty][tx] = out[q];
+        pp_face2_at<MODEL, false>(P, S, i, j, true, out);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) ys[q][ty][tx] = out[q];
+    }
+    if (t < h) {  // x faces east of the tile (column x0 + w, periodic)
+        pp_face2_at<MODEL, true>(P, S, wrapi(x0 + w, P.nx), y0 + t, false, out);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) xs[q][t][w] = out[q];
+    } else if (t >= 32 && t < 32 + w) {  // y faces north of the tile (row y0 + h, periodic)
+        pp_face2_at<MODEL, false>(P, S, x0 + t - 32, wrapi(y0 + h, P.ny), false, out);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) ys[q][h][t - 32] = out[q];
+    }
+    __syncthreads();
+    if (!in) return;
     const int pitch = P.pitch;
     const int ip = wrapi(i + 1, P.nx), im = wrapi(i - 1, P.nx), jn = wrapi(j + 1, P.ny), js = wrapi(j - 1, P.ny);
-    const size_t c = (size_t)j * pitch + i, cE = (size_t)j * pitch + ip, cN = (size_t)jn * pitch + i;
-    const float px = (float)(0.5 * (double)P.dtV * (S.rho[(size_t)j * pitch + im] - S.rho[cE]));
-    const float py = (float)(0.5 * (double)P.dtV * (S.rho[(size_t)js * pitch + i] - S.rho[cN]));
+    const size_t c = (size_t)j * pitch + i;
+    const float px = (float)(0.5 * (double)P.dtV * (S.rho[(size_t)j * pitch + im] - S.rho[(size_t)j * pitch + ip]));
+    const float py = (float)(0.5 * (double)P.dtV * (S.rho[(size_t)js * pitch + i] - S.rho[(size_t)jn * pitch + i]));
     float g[Q], bf[Q], fw[Q], fe[Q], fs[Q], fn[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         const size_t o = (size_t)q * S.qs;
         g[q] = S.df[o + c];
         bf[q] = S.bf[o + c];
-        fw[q] = S.xfl[o + c];
-        fe[q] = S.xfl[o + cE];
-        fs[q] = S.yfl[o + c];
-        fn[q] = S.yfl[o + cN];
+        fw[q] = xs[q][ty][tx];
+        fe[q] = xs[q][ty][tx + 1];
+        fs[q] = ys[q][ty][tx];
+        fn[q] = ys[q][ty + 1][tx];
     }
     const PPCell n = pp_update<MODEL>(P, g, bf, fw, fe, fs, fn, S.rho[c], px, py, S.Fx[c], S.Fy[c]);
 #pragma unroll
@@ -236,11 +264,11 @@ static cudaError_t launch_pp_t(const PPP &P, const PPS &S, int do_msrc, cudaStre
                                uint32_t step) {
     const dim3 blk(32, 8);
     const dim3 grd((P.nx + 31) / 32, (P.ny + 7) / 8), grf(grd.x, grd.y, 2);
+    (void)step;
     k_pp32_collide<MODEL><<<grd, blk, 0, st>>>(P, S, do_msrc);
     k_pp32_faces1<MODEL><<<grf, blk, 0, st>>>(P, S);
-    k_pp32_faces2<MODEL><<<grf, blk, 0, st>>>(P, S);
-    k_pp32_update<MODEL><<<grd, blk, 0, st>>>(P, S, step);
-    *launches += 4;
+    k_pp32_faces2u<MODEL><<<grd, blk, 0, st>>>(P, S);
+    *launches += 3;
     return cudaGetLastError();
 }
 

@@ -1,5 +1,5 @@
 // Per-cell and per-face arithmetic of the FP32 pseudopotential step (D2Q9PP, D2V16),
-// shared by the four-pass kernels (fp32_pp.cu) and the single-pass streaming kernel
+// shared by the three-pass kernels (fp32_pp.cu) and the single-pass streaming kernel
 // (fp32_pp_stream.cu), so both evaluate the same expressions.  Storage: the density in
 // FP64, f as the FP32 remainders g_q = f_q - e_q rho (fp32_pp.cu has the derivation).
 #pragma once

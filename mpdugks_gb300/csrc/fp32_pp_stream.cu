@@ -1,6 +1,6 @@
 // FP32 pseudopotential step (D2Q9PP, D2V16) in one streaming pass: k_pp32_stream.
 //
-// The four-pass form (fp32_pp.cu) moves ~1 KB per cell-update through device memory
+// The multi-pass form (fp32_pp.cu) moves ~0.9 KB per cell-update through device memory
 // (f-bar-plus, face reconstructions, face psi, fluxes).  Here each warp marches a strip of
 // 26 columns (a 32-column window: three halo columns on each side) along y through a
 // segment of rows and keeps everything a row needs from its neighbours on the chip:
@@ -18,18 +18,18 @@
 //     flux);
 //   the update of row k.
 // A segment starts four rows early; those rows' results are not written.  The per-cell
-// and per-face arithmetic is the four-pass kernels' (fp32_pp.cuh).  The state is read
+// and per-face arithmetic is the multi-pass kernels' (fp32_pp.cuh).  The state is read
 // from one copy and written to the other (a segment reads rows its neighbours write).
 // Periodic in x and y (the pseudopotential models have no walls).
 //
-// Measured on the GB300 (D2V16, 1024^2): 2.02 G cell-updates/s against 3.51 for the four
+// Measured on the GB300 (D2V16, 1024^2): 2.03 G cell-updates/s against 3.54 for the three
 // passes, with the same results bit for bit.  A lane holds the row pipeline of 16
 // distributions (168 registers when compiled for 5 blocks of 2 warps per SM -- 1.69 G at
 // the 215 the compiler takes unbounded, 2.00 G at 128 with spills) and the face moments
 // and the equation of state are serial float-float chains, so the ~10 resident warps
-// cannot hide their latency; the four passes run 40-64 registers a thread at full
-// occupancy and, for all their ~1 KB of traffic per cell-update, stay ahead.  The handle
-// therefore takes the four-pass step; DUGKS_PP_PASSES=1 selects this one.
+// cannot hide their latency; the three passes run 40-80 registers a thread at high
+// occupancy and, for all their ~0.9 KB of traffic per cell-update, stay ahead.  The handle
+// therefore takes the three-pass step; DUGKS_PP_PASSES=1 selects this one.
 #include <cuda_runtime.h>
 
 #include <cstdint>

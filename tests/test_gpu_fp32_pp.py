@@ -131,8 +131,8 @@ def _handle(model, nx, ny, init, params, passes=None, **kw):
 @pytest.mark.parametrize('model,kw', [('PP9', {}), ('PP16', dict(d2v16_c=0.5))])
 @pytest.mark.parametrize('nx,ny,init,params', [(64, 40, 'pp_noise', [0.2, 0.01]), (33, 8, 'pp_noise', [0.2, 0.01]),
                                                (96, 160, 'scmp_drop', []), (300, 270, 'pp_noise', [0.13044, 0.01])])
-def test_single_pass_step_equals_four_passes(model, kw, nx, ny, init, params):
-    """The single-pass streaming step against the four-pass step on grids of one or
+def test_single_pass_step_equals_three_passes(model, kw, nx, ny, init, params):
+    """The single-pass streaming step against the three-pass step on grids of one or
     several strips and segments (26-column strips, ragged last strip, 8 rows = the
     smallest grid it takes): the same arithmetic, so the same fields and remainders."""
     if model == 'PP16' and init == 'pp_noise':
