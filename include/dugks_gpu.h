@@ -44,7 +44,11 @@ typedef enum dugks_model {
 typedef enum dugks_precision {
     DUGKS_FP64 = 0,       /* plain FP64 drop-in: every operation rounded like the
                              reference (no FMA contraction), bit-identical results */
-    DUGKS_FP32_DEV = 1,   /* FP32 storage of deviations from rest equilibrium */
+    DUGKS_FP32_DEV = 1,   /* FP32 storage of small deviations and remainders (the
+                             phase field as a float-float pair; the pseudopotential
+                             density in FP64).  Pseudopotential models: the multi-pass
+                             step, or with DUGKS_PP_PASSES=1 in the environment at
+                             create time the single-pass streaming step (same results) */
     DUGKS_FP64_FMA = 2,   /* FP64 with FMA contraction and reciprocal multiplies:
                              equal to the reference to rounding, fewer FP64 ops */
     DUGKS_FP64_FUSED = 3  /* the fused one-kernel deviation-form step of

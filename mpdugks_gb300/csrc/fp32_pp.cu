@@ -21,7 +21,9 @@
 // (Fusing face pass 2 with the update saved the fluxes' round trip through DRAM, ~0.2 KB
 // per cell-update, for 0.8 % of the D2V16 step: the passes are latency- as much as
 // bandwidth-bound.  An earlier fusion that recomputed the face reconstruction instead of
-// reading it ran slower.)
+// reading it ran slower, and so did fusing the collision with face pass 1 (f-bar-plus of
+// a 34x10-cell tile ring in shared memory: 127 registers, two blocks per SM, the ring's
+// collisions computed twice; 3.09 against 3.54 G cell-updates/s on D2V16 1024^2).)
 #include <cuda_runtime.h>
 
 #include <cstdint>
