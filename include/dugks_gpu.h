@@ -83,7 +83,8 @@ typedef struct dugks_case {
  * extrapolated phi and rho, its pressure and zero velocity, plus the owner's
  * non-equilibrium part, then bounce-back (Wall_3_NEE,
  * Ark/Cpp/Boundary.cpp:140-184).  NEE runs with DUGKS_FP64 / DUGKS_FP64_FMA
- * and the Allen-Cahn models. */
+ * (bit-identical to the reference) and DUGKS_FP32_DEV (grids of at least 8
+ * rows; within 1e-5 of FP64) for the Allen-Cahn models. */
 typedef enum dugks_wall_scheme {
     DUGKS_WALL_BB = 0,
     DUGKS_WALL_NEE = 1

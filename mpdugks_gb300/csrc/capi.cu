@@ -179,6 +179,8 @@ static void derive_p32(const Params &P, f32::PR<R> &Q) {
     Q.h_ah = (R)P.h_ah; Q.h_bh = (R)P.h_bh; Q.h_ch = (R)P.h_ch;
     Q.r_2dy = (R)P.r_2dy; Q.r_ndx = (R)P.r_ndx; Q.r_n2dx = (R)P.r_n2dx; Q.r_ndy = (R)P.r_ndy;
     Q.aTP = (R)P.aTP; Q.bTP = (R)P.bTP; Q.dtV = (R)P.dtV;
+    Q.nee = P.nee;
+    Q.hneq = (R)(2.0 * P.TauMass / (2.0 * P.TauMass + P.dt));
 }
 
 // rest equilibria the deviations are taken from
@@ -576,10 +578,12 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
     if (c->wall_scheme != DUGKS_WALL_BB && c->wall_scheme != DUGKS_WALL_NEE)
         return fail(nullptr, DUGKS_EINVAL, "unknown wall scheme");
     if (c->wall_scheme == DUGKS_WALL_NEE &&
-        (!(c->precision == DUGKS_FP64 || c->precision == DUGKS_FP64_FMA) ||
+        (!(c->precision == DUGKS_FP64 || c->precision == DUGKS_FP64_FMA || c->precision == DUGKS_FP32_DEV) ||
          !(c->model == DUGKS_MODEL_AC || c->model == DUGKS_MODEL_HCZ)))
         return fail(nullptr, DUGKS_EINVAL,
-                    "NEE walls run with DUGKS_FP64 / DUGKS_FP64_FMA and the Allen-Cahn models");
+                    "NEE walls run with DUGKS_FP64 / DUGKS_FP64_FMA / DUGKS_FP32_DEV and the Allen-Cahn models");
+    if (c->wall_scheme == DUGKS_WALL_NEE && c->precision == DUGKS_FP32_DEV && g->y_walls && g->ny < 8)
+        return fail(nullptr, DUGKS_EINVAL, "NEE walls in FP32 storage need at least 8 rows (the streaming step)");
     if (c->flux_scheme == DUGKS_FLUX_UW &&
         (!(c->precision == DUGKS_FP64 || c->precision == DUGKS_FP64_FMA) ||
          !(c->model == DUGKS_MODEL_AC || c->model == DUGKS_MODEL_HCZ) || g->y_walls))

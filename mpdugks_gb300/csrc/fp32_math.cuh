@@ -302,16 +302,23 @@ __device__ __forceinline__ void eq_pair(const PR<R> &P, const EqSite<R> &e, type
 // collision increment inc = B - T of every direction.  Pq and inc are (f, h) pairs
 // whose h part is relative to w_q phi of this cell: Pq[q].y = g_q, and the h
 // equilibrium enters as h_eq - w_q phi = w_q phi u1.  src = {srcx, srcy, rhox, rhoy,
-// fx, fy}; phi_o, U_o, V_o for the caller's outputs.
-template <int MODEL, typename R>
+// fx, fy}; phi_o, U_o, V_o for the caller's outputs.  EQOUT: also the equilibria,
+// sources and macroscopic state the NEE wall faces need, into *eo.
+template <typename R>
+struct CellEq {
+    typename Pair<R>::T Eq[9], So[9];
+    R phi, dp, srcy, tau;
+};
+template <int MODEL, typename R, bool EQOUT = false>
 __device__ __forceinline__ void collide_cell(const PR<R> &P, const SR<R> &S, long long c, int first,
                                              const typename Pair<R>::T (&Pq)[9], R sfz, const R (&a6)[A_N],
                                              typename Pair<R>::T pc, const typename Pair<R>::T (&ph)[8],
-                                             typename Pair<R>::T (&inc)[9], R (&src)[6], R &phi_o, R &U_o, R &V_o) {
+                                             typename Pair<R>::T (&inc)[9], R (&src)[6], R &phi_o, R &U_o, R &V_o,
+                                             CellEq<R> *eo = nullptr) {
     using T = typename Pair<R>::T;
     R phi = pc.x + pc.y, rho = R(0.), U = R(0.), V = R(0.), dp = R(0.);
     R srcx = R(0.), srcy = R(0.), rhox = R(0.), rhoy = R(0.), fx = R(0.), fy = R(0.);
-    R aBP, cBP, rxo = R(0.), ryo = R(0.);
+    R aBP, cBP, rxo = R(0.), ryo = R(0.), tau_c = P.tauf;
     if (first) {
         // first step after an initialisation: the reference uses the state the
         // initialisation left (p0, zero forces, tau from Mu0), as uploaded
@@ -328,6 +335,7 @@ __device__ __forceinline__ void collide_cell(const PR<R> &P, const SR<R> &S, lon
         fx = I[I_FX * ps + c];
         fy = I[I_FY * ps + c];
         const R tau = I[I_TAU * ps + c];
+        tau_c = tau;
         aBP = (R(2.) * tau - P.hDt) / (R(2.) * tau + P.dt);
         cBP = tau * (R(1.) - aBP);
     } else {
@@ -395,6 +403,52 @@ __device__ __forceinline__ void collide_cell(const PR<R> &P, const SR<R> &S, lon
     phi_o = phi;
     U_o = U;
     V_o = V;
+    if (EQOUT) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            eo->Eq[q] = Eq[q];
+            eo->So[q] = So[q];
+        }
+        eo->phi = phi;
+        eo->dp = dp;
+        eo->srcy = srcy;
+        eo->tau = tau_c;
+    }
+}
+
+// NEE wall face (Wall_3_NEE, Ark/Cpp/Boundary.cpp:140-184, then Wall_3_BB) of a wall row's
+// cell from its collision state ce and stored deviations Pq: the equilibrium at the wall
+// (the face velocity stays 0, phi extrapolated to the face with the MacroSource vector,
+// Phi_y, the reference's choice) plus the cell's non-equilibrium part f - Eq + hDt S times
+// 2 tau / (2 tau + dt) (h: 2 TauMass / (2 TauMass + dt)), the directions entering the fluid
+// bounced back; fluxes xi.n of the six directions crossing the face, the f parts as
+// deviations and the h parts relative to w_q avg (the face phi the update's flux
+// divergence takes for it).  side: 0 the bottom wall (below the cell), 1 the top.
+template <int MODEL, typename R>
+__device__ __forceinline__ void nee_wall_flux(const PR<R> &P, const CellEq<R> &ce,
+                                              const typename Pair<R>::T (&Pq)[9], R avg, int side,
+                                              typename Pair<R>::T (&F)[6]) {
+    using T = typename Pair<R>::T;
+    const R dyw = side ? R(0.5) : R(-0.5);
+    const R Phi_w = ce.phi + ce.srcy * dyw;
+    const R fneq = R(2.) * ce.tau / (R(2.) * ce.tau + P.dt);
+    T v[9];
+#pragma unroll
+    for (int q = 1; q < 9; ++q) {
+        const R wq = (R)d2q9_w(q);
+        // the wall equilibrium at u = 0 as a deviation: w (p - p0) (HCZ), w (p - p0) / RT (AC)
+        const R feq = MODEL == AC ? wq * ce.dp * P.invRT : wq * ce.dp;
+        const T ne = fma2(mk2(P.hDt, P.hDt), ce.So[q], sub2(Pq[q], ce.Eq[q]));
+        v[q] = mk2(fma(fneq, ne.x, feq), fma(P.hneq, ne.y, wq * (Phi_w - avg)));
+    }
+#pragma unroll
+    for (int q = 1; q < 9; ++q) {
+        const int xv = d2q9_xv(q);
+        if (side ? xv < 0 : xv > 0) v[q] = v[d2q9_bb(q)];
+    }
+#pragma unroll
+    for (int q = 1; q < 9; ++q)
+        if (d2q9_xv(q) != 0) F[yslot(q)] = d2q9_xv(q) > 0 ? v[q] : neg2(v[q]);
 }
 
 // Phase-field inputs of one face: avg = (phi_o + phi_n)/2 (the face's h reference is

@@ -22,6 +22,7 @@ namespace f32 {
 template <typename R>
 struct PR {
     int nx, ny, pitch, walls, model, gravity;
+    int nee;  // NEE walls (Ark/Cpp/Boundary.cpp:140-184) instead of bounce-back
     // slab partitions: global row of local row 0, and whether the rows below 0 /
     // from ny up are a neighbour's halo (2 rows of device memory) instead of a
     // wall or the periodic wrap; 0 for a whole grid
@@ -33,6 +34,7 @@ struct PR {
     R h_aBP, h_bBP, h_cBP, h_ah, h_bh, h_ch;  // phase-field relaxation
     R r_2dy, r_ndx, r_n2dx, r_ndy;             // reconstruction multipliers
     R aTP, bTP, dtV;
+    R hneq;  // NEE: 2 TauMass / (2 TauMass + dt), the phase field's non-equilibrium factor
 };
 using P32 = PR<float>;
 

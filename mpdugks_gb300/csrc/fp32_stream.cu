@@ -26,7 +26,7 @@ namespace f32 {
 // TMA_WAIT_LIMIT polls sets *err and ends the warp.
 // The per-item work is stream_item (fp32_stream.cuh), the same function the batched
 // serving kernel runs, so a change to the steps lands in both.
-template <int MODEL, bool WALLS, bool TMA>
+template <int MODEL, bool WALLS, bool TMA, bool NEE>
 __global__ void __launch_bounds__(WPB * 32, STREAM_MIN_BLOCKS)
     k_stream32(P32 P, S32 S, int first, int gin, int gout, uint32_t step, int nstrips, int nsegs, int seg_rows,
                const __grid_constant__ CUtensorMap tmap, int zin, int *err) {
@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(WPB * 32, STREAM_MIN_BLOCKS)
     for (int item = gw; item < nstrips * nsegs; item += nw) {
         const int strip = item % nstrips, seg = item / nstrips;
         const int y0 = seg * seg_rows, y1 = min(y0 + seg_rows, ny);
-        if (!stream_item<MODEL, WALLS, TMA>(P, S, first, gin, gout, step, strip, y0, y1, tma_ok, &tmap, zin, err, stg,
+        if (!stream_item<MODEL, WALLS, TMA, NEE>(P, S, first, gin, gout, step, strip, y0, y1, tma_ok, &tmap, zin, err, stg,
                                             bring, aring, bar0, phases, lane))
             return;
     }
@@ -87,27 +87,28 @@ int stream_segment_rows(int nstrips, int ny, int warps) {
     return best;
 }
 
-template <int MODEL, bool WALLS, bool TMA>
+template <int MODEL, bool WALLS, bool TMA, bool NEE>
 static cudaError_t stream_prepare() {
-    cudaError_t e = cudaFuncSetAttribute(k_stream32<MODEL, WALLS, TMA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)STREAM_SMEM);
+    cudaError_t e = cudaFuncSetAttribute(k_stream32<MODEL, WALLS, TMA, NEE>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)STREAM_SMEM);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stream32<MODEL, WALLS, TMA>, WPB * 32, STREAM_SMEM);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stream32<MODEL, WALLS, TMA, NEE>, WPB * 32,
+                                                      STREAM_SMEM);
     if (e != cudaSuccess) return e;
     if (per_sm <= 0) return cudaErrorInvalidConfiguration;
     g_stream_blocks = g_stream_blocks ? min(g_stream_blocks, per_sm) : per_sm;
     return cudaSuccess;
 }
 
-template <int MODEL, bool WALLS>
+template <int MODEL, bool WALLS, bool NEE>
 static cudaError_t launch_stream_t(const P32 &P, const S32 &S, int first, int gin, int gout, cudaStream_t st,
                                    uint32_t step, const CUtensorMap *tmap, int zin, int *err, bool *fallback) {
     static bool ready = false;
     if (!ready) {
-        cudaError_t e = stream_prepare<MODEL, WALLS, false>();
+        cudaError_t e = stream_prepare<MODEL, WALLS, false, NEE>();
         if (e != cudaSuccess) return e;
-        if ((e = stream_prepare<MODEL, WALLS, true>()) != cudaSuccess) return e;
+        if ((e = stream_prepare<MODEL, WALLS, true, NEE>()) != cudaSuccess) return e;
         int dev = 0;
         if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
         if ((e = cudaDeviceGetAttribute(&g_stream_nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
@@ -121,8 +122,8 @@ static cudaError_t launch_stream_t(const P32 &P, const S32 &S, int first, int gi
     // runs it.  Measured (Rayleigh-Taylor, G cell-updates/s, streaming / tile): 256x1024
     // 5.1 / 7.5 (320 segments), 768^2 9.2 / 8.5 (672), 512x2048 11.9 / 8.5 (1216), 1024^2
     // 12.5 / 8.8 (1184), against 1824 resident warps.  (A slab partition reads halo rows,
-    // which only this form does: it always runs here.)
-    if (!(P.halo_lo || P.halo_hi) && 3LL * nstrips * ((P.ny + 31) / 32) < warps) {
+    // which only this form does, and so do NEE walls: it always runs those.)
+    if (!NEE && !(P.halo_lo || P.halo_hi) && 3LL * nstrips * ((P.ny + 31) / 32) < warps) {
         *fallback = true;
         return cudaSuccess;
     }
@@ -131,13 +132,13 @@ static cudaError_t launch_stream_t(const P32 &P, const S32 &S, int first, int gi
     const int items = nstrips * nsegs;
     const int blocks = min((items + WPB - 1) / WPB, g_stream_nsm * g_stream_blocks);
     if (tmap) {
-        k_stream32<MODEL, WALLS, true><<<blocks, WPB * 32, STREAM_SMEM, st>>>(P, S, first, gin, gout, step, nstrips,
-                                                                            nsegs, seg, *tmap, zin, err);
+        k_stream32<MODEL, WALLS, true, NEE><<<blocks, WPB * 32, STREAM_SMEM, st>>>(P, S, first, gin, gout, step,
+                                                                                 nstrips, nsegs, seg, *tmap, zin, err);
     } else {
         CUtensorMap none;
         memset(&none, 0, sizeof none);
-        k_stream32<MODEL, WALLS, false><<<blocks, WPB * 32, STREAM_SMEM, st>>>(P, S, first, gin, gout, step, nstrips,
-                                                                             nsegs, seg, none, 0, err);
+        k_stream32<MODEL, WALLS, false, NEE><<<blocks, WPB * 32, STREAM_SMEM, st>>>(P, S, first, gin, gout, step,
+                                                                                  nstrips, nsegs, seg, none, 0, err);
     }
     return cudaGetLastError();
 }
@@ -156,14 +157,25 @@ cudaError_t launch_stream32(const P32 &P, const S32 &S, int first, int gin, int 
     const CUtensorMap *tm = static_cast<const CUtensorMap *>(tmap);
     cudaError_t e = cudaErrorInvalidValue;
     bool fallback = false;
-    switch (P.model * 2 + (P.walls ? 1 : 0)) {
-        case AC * 2 + 0: e = launch_stream_t<AC, false>(P, S, first, gin, gout, st, step, tm, zin, err, &fallback); break;
-        case AC * 2 + 1: e = launch_stream_t<AC, true>(P, S, first, gin, gout, st, step, tm, zin, err, &fallback); break;
-        case HCZ * 2 + 0:
-            e = launch_stream_t<HCZ, false>(P, S, first, gin, gout, st, step, tm, zin, err, &fallback);
+    // NEE walls run the streaming form (the tile kernel has bounce-back walls only)
+    switch (P.model * 4 + (P.walls ? 2 : 0) + (P.walls && P.nee ? 1 : 0)) {
+        case AC * 4 + 0:
+            e = launch_stream_t<AC, false, false>(P, S, first, gin, gout, st, step, tm, zin, err, &fallback);
             break;
-        case HCZ * 2 + 1:
-            e = launch_stream_t<HCZ, true>(P, S, first, gin, gout, st, step, tm, zin, err, &fallback);
+        case AC * 4 + 2:
+            e = launch_stream_t<AC, true, false>(P, S, first, gin, gout, st, step, tm, zin, err, &fallback);
+            break;
+        case AC * 4 + 3:
+            e = launch_stream_t<AC, true, true>(P, S, first, gin, gout, st, step, tm, zin, err, &fallback);
+            break;
+        case HCZ * 4 + 0:
+            e = launch_stream_t<HCZ, false, false>(P, S, first, gin, gout, st, step, tm, zin, err, &fallback);
+            break;
+        case HCZ * 4 + 2:
+            e = launch_stream_t<HCZ, true, false>(P, S, first, gin, gout, st, step, tm, zin, err, &fallback);
+            break;
+        case HCZ * 4 + 3:
+            e = launch_stream_t<HCZ, true, true>(P, S, first, gin, gout, st, step, tm, zin, err, &fallback);
             break;
         default: break;
     }

@@ -141,8 +141,9 @@ struct ARow {
 // One (strip, rows y0 .. y1-1) item of a step of one case.  stg, bring, aring: the
 // warp's shared-memory rings; bar0, phases: its stage-slot mbarriers and their phase
 // parities (TMA instances).  use of TMA for the item: tma_ok and a window that does not
-// wrap around x.  Returns false when a TMA load did not complete (the warp must end).
-template <int MODEL, bool WALLS, bool TMA>
+// wrap around x.  NEE: the wall faces by non-equilibrium extrapolation (P.nee cases) instead
+// of bounce-back.  Returns false when a TMA load did not complete (the warp must end).
+template <int MODEL, bool WALLS, bool TMA, bool NEE = false>
 __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int first, int gin, int gout, uint32_t step,
                                             int strip, int y0, int y1, bool tma_ok, const CUtensorMap *tmap_p,
                                             int zin, int *err, float *stg, float *bring, float *aring,
@@ -349,8 +350,35 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
             up_w = ghost_pair(SWv, ph_mw);
             up_e = ghost_pair(SE, mE);
         }
+        // NEE wall face of row k (side 0: below, 1: above) into F: the row's collision state
+        // again (the collision ran a row earlier and kept only f-bar-plus), from its staged
+        // deviations, its aux and the 3x3 phi stencil around it -- the wall rows only
+        auto nee_face = [&](int side, T (&F)[6]) {
+            const T mE = from_east(ph_m);  // every lane (shuffle)
+            if (!interior) return;
+            const int sl = m4(k);
+            T Pq[9], za[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) za[q] = Pq[q] = STG(sl, q);
+            if (MODEL == AC) za[0].x = 0.f;
+            const T z = dev_sum9(za);
+            Pq[0].y = -z.y;
+            const long long c = cell(k);
+            float a6[A_N];
+#pragma unroll
+            for (int a = 0; a < A_N; ++a) a6[a] = (MODEL != AC && !first) ? __ldg(S.aux + (size_t)a * S.qs + c) : 0.f;
+            const T ph[8] = {SE, SWv, ph1, ph_m, E, W, mE, ph_mw};
+            T inc[9];
+            float src[6], phi, U, V;
+            CellEq<float> ce;
+            collide_cell<MODEL, float, true>(P, S, c, first, Pq, z.x, a6, ph0, ph, inc, src, phi, U, V, &ce);
+            const float avg = side ? 0.5f * (ph0.x + up_c.x) : 0.5f * (dn_c.x + ph0.x);
+            nee_wall_flux<MODEL, float>(P, ce, Pq, avg, side, F);
+        };
         // ---- y-face between rows k-1 and k at the bottom wall (row 0's south face)
-        if (bot && interior) {
+        if (NEE && bot) {
+            nee_face(0, FS);
+        } else if (bot && interior) {
             float av[6], am[6], a0[6];
             Am.get(am, lane);
             A0.get(a0, lane);
@@ -370,7 +398,9 @@ __device__ __forceinline__ bool stream_item(const P32 &P, const S32 &S, int firs
 #pragma unroll
         for (int s = 0; s < 6; ++s) FN[s] = mk2(0.f, 0.f);
         const bool yface = k >= y0 - 1 && ((row_ok(k) && row_ok(k + 1)) || top);
-        if (yface && interior) {
+        if (NEE && top) {
+            nee_face(1, FN);
+        } else if (yface && interior) {
             float av[6], a0[6], ap[6];
             A0.get(a0, lane);
             Ap.get(ap, lane);

@@ -104,13 +104,15 @@ def test_uw_flux_scheme_rejected_where_not_supported(model, precision, walls):
     assert b'UW' in buf.value
 
 
-@pytest.mark.parametrize('model,precision,walls', [('AC', 'fp32dev', 1), ('PP9', 'fp64', 0), ('HCZ', 'fp64fused', 1)])
-def test_nee_walls_rejected_where_not_supported(model, precision, walls):
+# FP32 storage takes NEE walls on grids of at least 8 rows (its streaming step)
+@pytest.mark.parametrize('model,precision,walls,ny', [('AC', 'fp32dev', 1, 6), ('PP9', 'fp64', 0, 16),
+                                                      ('HCZ', 'fp64fused', 1, 16)])
+def test_nee_walls_rejected_where_not_supported(model, precision, walls, ny):
     import ctypes
     from mpdugks_gb300 import capi
     lib = capi.load(build_if_missing=True)
     case = capi.make_case(model, precision, wall='NEE')
-    grid = capi.GridT(16, 16, walls)
+    grid = capi.GridT(16, ny, walls)
     h = ctypes.c_void_p()
     rc = lib.dugks_gpu_create(ctypes.byref(case), ctypes.byref(grid), ctypes.byref(h))
     assert rc == capi.DUGKS_EINVAL and not h.value

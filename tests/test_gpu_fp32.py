@@ -18,7 +18,8 @@ TARGET = 1e-5
 def make(v, precision):
     from mpdugks_gb300 import capi
     c = v['consts']
-    gc = capi.GpuCase(capi.make_case(MODEL[v['model']], precision, **{k: c[k] for k in KEYS if k in c}),
+    gc = capi.GpuCase(capi.make_case(MODEL[v['model']], precision, wall=v.get('wall', 'BB'),
+                                     **{k: c[k] for k in KEYS if k in c}),
                       v['nx'], v['ny'], v['walls'])
     if v['init'] == 'ac_rt':
         gc.init('ac_rt')
@@ -60,7 +61,8 @@ def test_fp32_first_step_matches_fp64():
 # the field's largest value.  The static drop's velocity is its spurious current
 # (max |u| ~5e-4): the phase field is stored as phi (float-float) plus small
 # remainders, so its rounding no longer moves the interface that drives that current.
-@pytest.mark.parametrize('name,steps', [('ac_c1', 2000), ('hcz_drop', 1000), ('hcz_drop', 2000), ('hcz_rt', 50)])
+@pytest.mark.parametrize('name,steps', [('ac_c1', 2000), ('hcz_drop', 1000), ('hcz_drop', 2000), ('hcz_rt', 50),
+                                        ('nee_rt', 50), ('nee_ac', 1000)])
 def test_fp32_error_vs_fp64(name, steps):
     v = VARIANTS[name]
     a, b = make(v, 'fp32dev'), make(v, 'fp64')

@@ -153,13 +153,19 @@ def test_driver_drop_l2_equals_the_reference(case, tmp_path):
 
 
 @pytest.mark.gpu
-def test_driver_fp32_run_is_close_to_the_reference_files(tmp_path):
+@pytest.mark.parametrize('case,extra', [('ac_ff', []),
+                                        ('nee_rt', ['--set', 'init=ac_rt', '--set', 'gravity=0.0001',
+                                                    '--set', 'wall scheme=NEE'])])
+def test_driver_fp32_run_is_close_to_the_reference_files(case, extra, tmp_path):
+    """FP32 storage through dugks_run against the reference's FlowField files at step 20
+    (the AC_Drop case, and the Rayleigh-Taylor box with NEE walls)."""
     out = tmp_path / 'FlowField'
-    subprocess.run([runner(), 'run', GOLD / 'ac_ff' / 'Case.ark', '--out', out, '--steps', '20', '--precision',
-                    'fp32dev'], check=True, capture_output=True)
-    name, text = golden_dat('ac_ff', 20)
-    a = parse_flowfield((out / 'global' / name).read_bytes(), 32 * 24)
-    b = parse_flowfield(text, 32 * 24)
+    subprocess.run([runner(), 'run', GOLD / case / 'Case.ark', '--out', out, '--steps', '20', '--precision',
+                    'fp32dev'] + extra, check=True, capture_output=True)
+    name, text = golden_dat(case, 20)
+    nx, ny = GRID[case]
+    a = parse_flowfield((out / 'global' / name).read_bytes(), nx * ny)
+    b = parse_flowfield(text, nx * ny)
     for k in ('rho', 'p', 'phi', 'tau', 'T'):
         assert np.max(np.abs(a[k] - b[k])) <= 1e-5 * np.max(np.abs(b[k])), k
     for k in ('fx', 'fy'):
