@@ -181,18 +181,6 @@ static void derive_p32(const Params &P, f32::PR<R> &Q) {
     Q.aTP = (R)P.aTP; Q.bTP = (R)P.bTP; Q.dtV = (R)P.dtV;
     Q.nee = P.nee;
     Q.hneq = (R)(2.0 * P.TauMass / (2.0 * P.TauMass + P.dt));
-    // face reconstruction weights in R arithmetic (one rounding per operation, as on the device)
-    const R half = R(0.5);
-    Q.cnx = Q.hDt * (R(1) * Q.r_ndx);
-    Q.cny = Q.hDt * (R(1) * Q.r_ndy);
-    Q.ktx = -(Q.hDt * (half * R(1) * Q.r_2dy));
-    Q.kty = -(Q.hDt * (half * R(1) * Q.r_n2dx));
-    Q.wpx = {half + Q.cnx, half + Q.cnx};
-    Q.wmx = {half - Q.cnx, half - Q.cnx};
-    Q.wpy = {half + Q.cny, half + Q.cny};
-    Q.wmy = {half - Q.cny, half - Q.cny};
-    Q.ktx2 = {Q.ktx, Q.ktx};
-    Q.kty2 = {Q.kty, Q.kty};
 }
 
 // rest equilibria the deviations are taken from

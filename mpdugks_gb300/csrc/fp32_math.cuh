@@ -505,21 +505,19 @@ __device__ __forceinline__ void face_flux(const PR<R> &P, FO &&O, FN &&N, FD &&D
         // the tangential central difference, averaged over the two cells of the
         // face, enters with the weight -hDt st/(4 d_t); the phase field's w_q phi
         // part takes the same weights on phi: w_q (cn (phi_n - phi_o) + k dt)
-        // (the weights are case constants, PR::cnx .. kty2; a velocity of -1 negates cn and
-        // k exactly and swaps the two weight pairs)
         T b = avg;
         R wphi = R(0.);
         if (sn != 0) {
-            const R cn = sn > 0 ? (XF ? P.cnx : P.cny) : -(XF ? P.cnx : P.cny);
-            const T wp = XF ? P.wpx : P.wpy, wm = XF ? P.wmx : P.wmy;
-            b = fma2(n, sn > 0 ? wp : wm, mul2(o, sn > 0 ? wm : wp));
+            const R rn = XF ? P.r_ndx : P.r_ndy;
+            const R cn = P.hDt * ((R)sn * rn);
+            b = fma2(n, mk2(R(0.5) + cn, R(0.5) + cn), mul2(o, mk2(R(0.5) - cn, R(0.5) - cn)));
             wphi = cn * fp.dn;
         }
         if (st != 0) {
             const T d = D(q);
-            const R k = st > 0 ? (XF ? P.ktx : P.kty) : -(XF ? P.ktx : P.kty);
-            const T k2 = st > 0 ? (XF ? P.ktx2 : P.kty2) : neg2(XF ? P.ktx2 : P.kty2);
-            b = fma2(d, k2, b);
+            const R rt = XF ? P.r_2dy : P.r_n2dx;
+            const R k = -(P.hDt * (R(0.5) * (R)st * rt));
+            b = fma2(d, mk2(k, k), b);
             wphi = fma(k, fp.dt, wphi);
         }
         b.y = fma((R)d2q9_w(q), wphi, b.y);

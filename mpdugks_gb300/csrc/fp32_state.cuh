@@ -15,11 +15,6 @@
 namespace dugks {
 namespace f32 {
 
-// a pair of R (float2 / double2): packed constants the packed instructions take whole
-template <typename R> struct V2;
-template <> struct V2<float> { using T = float2; };
-template <> struct V2<double> { using T = double2; };
-
 // Case constants of the fused deviation-form step in the storage type R
 // (derived in FP64 on the host with the reference's expressions, then
 // rounded once).  R = float is the FP32 storage path; R = double runs the
@@ -40,12 +35,6 @@ struct PR {
     R r_2dy, r_ndx, r_n2dx, r_ndy;             // reconstruction multipliers
     R aTP, bTP, dtV;
     R hneq;  // NEE: 2 TauMass / (2 TauMass + dt), the phase field's non-equilibrium factor
-    // face reconstruction weights, evaluated on the host in R exactly as the device formed
-    // them before (so the results do not change): cn = hDt r_n (normal velocity +1; x faces
-    // r_ndx, y faces r_ndy), the pairs (1/2 + cn, 1/2 + cn) and (1/2 - cn, 1/2 - cn);
-    // kt = -(hDt (1/2 r_t)) (tangential velocity +1; x faces r_2dy, y faces r_n2dx) and (kt, kt)
-    R cnx, cny, ktx, kty;
-    typename V2<R>::T wpx, wmx, wpy, wmy, ktx2, kty2;
 };
 using P32 = PR<float>;
 
