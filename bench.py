@@ -202,9 +202,15 @@ def cpu_baseline(wl: dict, seconds: float, fixed_steps: int = 0):
     _, one, _ = cpu_sample(wl, 1, thr)
     nsteps = fixed_steps or max(2, int(seconds / max(one, 1e-3)))
     mlups, secs, (nx, ny) = cpu_sample(wl, nsteps, thr)
-    return {'value': round(mlups, 4), 'unit': 'MLUPS', 'cores': thr, 'kind': 'port',
-            'sample': f'{nsteps} steps of a {nx}x{ny} Rayleigh-Taylor grid with the case constants of '
-                      f'{wl["name"]} on the CPU restatement (OpenMP, {thr} threads, {secs:.1f} s)'}, nsteps, secs
+    out = {'value': round(mlups, 4), 'unit': 'MLUPS', 'cores': thr, 'kind': 'port',
+           'sample': f'{nsteps} steps of a {nx}x{ny} Rayleigh-Taylor grid with the case constants of '
+                     f'{wl["name"]} on the CPU restatement (OpenMP, {thr} threads, {secs:.1f} s)'}
+    # the unmodified reference against the restatement on the same cores, where the reference
+    # builds (oracle/ref/time_reference.py): the restatement's speed over the reference's
+    cal = ROOT / 'oracle' / 'ref' / 'reference_timing.json'
+    if cal.exists():
+        out['reference_calibration'] = json.loads(cal.read_text())
+    return out, nsteps, secs
 
 
 def run_reference(args, wl, rank, world):

@@ -9,7 +9,9 @@ one untimed step; the reference reports its own loop time (ref_driver's
 "done ... seconds"), the restatement is timed around Oracle.step.  The two final
 states are compared bit for bit.  Prints one JSON line.
 
-Usage: python oracle/ref/time_reference.py [--steps N] [--threads T]
+Usage: python oracle/ref/time_reference.py [--steps N] [--threads T] [--out FILE]
+(the committed oracle/ref/reference_timing.json is its output; bench.py reports it beside the
+CPU baseline)
 """
 from __future__ import annotations
 
@@ -36,6 +38,7 @@ def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument('--steps', type=int, default=20)
     ap.add_argument('--threads', type=int, default=os.cpu_count() or 1)
+    ap.add_argument('--out', default=None)
     a = ap.parse_args()
     import bench
     from oracle.oracle import Oracle, read_dump
@@ -59,10 +62,16 @@ def main() -> int:
     tmp.cleanup()
     same = all(bool((o.get(k) == v).all()) for k, v in ref.items() if k in ('rho', 'u', 'v', 'p', 'phi'))
     cells = wl['nx'] * wl['ny']
-    print(json.dumps({'workload': wl['name'], 'threads': a.threads, 'steps': a.steps,
-                      'reference_mlups': round(cells * a.steps / ref_s / 1e6, 3),
-                      'port_mlups': round(cells * a.steps / port_s / 1e6, 3),
-                      'port_over_reference': round(ref_s / port_s, 3), 'final_states_bit_identical': same}))
+    res = {'workload': wl['name'], 'threads': a.threads, 'steps': a.steps,
+           'reference_mlups': round(cells * a.steps / ref_s / 1e6, 3),
+           'port_mlups': round(cells * a.steps / port_s / 1e6, 3),
+           'port_over_reference': round(ref_s / port_s, 3), 'final_states_bit_identical': same}
+    print(json.dumps(res))
+    if a.out:
+        res['where'] = ('the x86-64 build container (the reference cannot be built on the aarch64 GPU host: '
+                        'its sources are not there and there is no cross compiler)')
+        res['recipe'] = f'python oracle/ref/time_reference.py --steps {a.steps} --out {a.out}'
+        Path(a.out).write_text(json.dumps(res, indent=1) + '\n')
     return 0
 
 
