@@ -604,11 +604,12 @@ def c3_full(args) -> dict:
 
 # ---------------------------------------------------------------- scheme variants
 
-def scheme_variants_bench(steps: int = 20) -> dict:
+def scheme_variants_bench(steps: int = 20, precision: str = 'fp64') -> dict:
     """The reference's alternative face reconstruction (UW) and wall treatment (NEE)
-    on the plain FP64 path, beside the defaults (CD, bounce-back) on the same grid:
-    a 1024x1024 periodic HCZ droplet (CD / UW) and the 512x2048 Rayleigh-Taylor box
-    with walls (BB / NEE); MLUPS over `steps` steps after 3 warm-up steps."""
+    beside the defaults (CD, bounce-back) on the same grid, in one precision (the plain
+    FP64 path or FP32 storage): a 1024x1024 periodic HCZ droplet (CD / UW) and the
+    512x2048 Rayleigh-Taylor box with walls (BB / NEE); MLUPS over `steps` steps after 3
+    warm-up steps."""
     import torch
     from mpdugks_gb300 import capi
     st = torch.cuda.Stream()
@@ -620,14 +621,14 @@ def scheme_variants_bench(steps: int = 20) -> dict:
             ('bb', 'HCZ', case_kw(rt), rt['nx'], rt['ny'], True, 'ac_rt', rt['init'], {}),
             ('nee', 'HCZ', case_kw(rt), rt['nx'], rt['ny'], True, 'ac_rt', rt['init'], dict(wall='NEE'))]
     for tag, model, kw, nx, ny, walls, init, params, extra in runs:
-        g = capi.GpuCase(capi.make_case(model, 'fp64', **kw, **extra), nx, ny, walls)
+        g = capi.GpuCase(capi.make_case(model, precision, **kw, **extra), nx, ny, walls)
         g.init(init, params)
         g.step(3, st.cuda_stream)
         ms, launches, _ = timed_steps(g, steps, st)
         out[tag] = {'grid': f'{nx}x{ny}', 'mlups': round(nx * ny * steps / (ms * 1e-3) / 1e6, 2),
                     'ms_per_step': round(ms / steps, 4), 'launches_per_step': launches // steps}
         del g
-    return {'precision': 'fp64 (reference-exact rounding)', 'steps': steps,
+    return {'precision': 'fp64 (reference-exact rounding)' if precision == 'fp64' else precision, 'steps': steps,
             'droplet_1024x1024': {'cd': out['cd'], 'uw': out['uw']},
             'rayleigh_taylor_512x2048': {'bounce_back': out['bb'], 'nee': out['nee']}}
 
@@ -899,9 +900,10 @@ def run_ours(args, wl, rank, world, local):
     pseudo = None
     if rank == 0 and not args.no_pseudopotential:
         pseudo = pseudopotential_bench(args.pp_steps)
-    variants = None
-    if rank == 0 and not args.no_fp64:
+    variants = variants32 = None
+    if rank == 0 and not args.no_fp64:  # the scheme variants in FP64 and in FP32 storage
         variants = scheme_variants_bench()
+        variants32 = scheme_variants_bench(precision='fp32dev')
 
     if rank == 0:
         cpu = None
@@ -926,6 +928,7 @@ def run_ours(args, wl, rank, world, local):
             'serving': serving,
             'pseudopotential_d2v16': pseudo,
             'fp64_scheme_variants': variants,
+            'fp32_scheme_variants': variants32,
             'gpu_launches': int(launches),
             'clocks': clocks,
             'state_finite': finite,

@@ -97,9 +97,11 @@ typedef enum dugks_wall_scheme {
  * (Grad_VS_6points, Ark/Lib/GradSchemeBasic.h:95-126; UW_Interior_phi_Bh,
  * Ark/Cpp/DUGKS2DSolver.cpp:558-603,689-706), both cells averaged for
  * velocities along the face.  UW runs with the plain FP64 precisions
- * (DUGKS_FP64, DUGKS_FP64_FMA), the Allen-Cahn models and periodic y: the
- * reference's UW with walls reads the gradients of its wall shadow cells,
- * which it never writes (uninitialised memory). */
+ * (DUGKS_FP64, DUGKS_FP64_FMA) and with DUGKS_FP32_DEV (four launches a step:
+ * collision, gradients, faces, update), the Allen-Cahn models and periodic y:
+ * the reference's UW with walls reads the gradients of its wall shadow cells,
+ * which it never writes (uninitialised memory).  Serving runs UW cases in solo
+ * lanes. */
 typedef enum dugks_flux_scheme {
     DUGKS_FLUX_CD = 0,
     DUGKS_FLUX_UW = 1

@@ -45,6 +45,7 @@ void launch_macros64f(const PR<double> &P, const SR<double> &S, double *rho, dou
 cudaError_t launch_stream32(const P32 &P, const S32 &S, int first, int gin, int gout, cudaStream_t st,
                             int64_t *launches, uint32_t step, const void *tmap, int zin, int *err);
 cudaError_t stream_tensor_map(void *map_out, float *base, int nx, int ny, int pitch, size_t qs);
+cudaError_t launch_uw32(const P32 &P, const S32 &S, float *U, int first, cudaStream_t st, int64_t *launches);
 cudaError_t launch_pp32_step(const PPP &P, const PPS &S, int do_msrc, cudaStream_t st, int64_t *launches,
                              uint32_t step);
 cudaError_t launch_pp32_force(const PPP &P, const PPS &S, cudaStream_t st, int64_t *launches);
@@ -120,6 +121,7 @@ struct dugks_handle {
     bool has_tmap = false;
     const float *tmap_base = nullptr;
     int *kerr = nullptr;
+    float *uw32 = nullptr;    // scratch planes of the FP32 UW step (f32::UW_PLANES)
     bool macros_fresh = false;
     double *out3 = nullptr;   // tau, Fx, Fy for output (allocated on first request)
     // FP32 storage of the pseudopotential models
@@ -198,7 +200,8 @@ static size_t fused_arena_bytes(const Params &P, size_t rsize) {
     const size_t cellf = align256(rowf * P.ny);
     const size_t celld = align256((size_t)P.pitch * sizeof(double) * P.ny);
     return 2 * f32::PL_N * cellf + f32::I_N * cellf + align256(f32::GPHI_ROWS * rowf) +
-           6 * celld /* rho u v p phi + rho_last */ + align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 512;
+           6 * celld /* rho u v p phi + rho_last */ + align256(sizeof(double) * 4 * REDUCE_BLOCKS) + 512 +
+           (P.uw ? f32::UW_PLANES * cellf : 0) /* the UW step's scratch */;
 }
 
 // device bytes of one case of the multi-kernel FP64 step
@@ -453,6 +456,7 @@ static int create_fused(dugks_handle *h, dugks_handle_t **out, f32::PR<R> &PQ, f
     h->partial = taked(align256(sizeof(double) * 4 * h->nblocks));
     h->out4 = taked(256);
     h->flag = reinterpret_cast<int *>(taked(256));
+    if (P.uw) h->uw32 = reinterpret_cast<float *>(takef(f32::UW_PLANES * cellf));
     e = cudaStreamSynchronize(nullptr);  // the clear above (legacy stream; leaves non-blocking streams running)
     if (e != cudaSuccess) {
         cudaFree(h->arena);
@@ -585,11 +589,11 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
     if (c->wall_scheme == DUGKS_WALL_NEE && c->precision == DUGKS_FP32_DEV && g->y_walls && g->ny < 8)
         return fail(nullptr, DUGKS_EINVAL, "NEE walls in FP32 storage need at least 8 rows (the streaming step)");
     if (c->flux_scheme == DUGKS_FLUX_UW &&
-        (!(c->precision == DUGKS_FP64 || c->precision == DUGKS_FP64_FMA) ||
+        (!(c->precision == DUGKS_FP64 || c->precision == DUGKS_FP64_FMA || c->precision == DUGKS_FP32_DEV) ||
          !(c->model == DUGKS_MODEL_AC || c->model == DUGKS_MODEL_HCZ) || g->y_walls))
         return fail(nullptr, DUGKS_EINVAL,
-                    "the UW flux scheme runs with DUGKS_FP64 / DUGKS_FP64_FMA, the Allen-Cahn models and periodic y "
-                    "(the reference's UW reads unwritten gradients of its wall shadow cells)");
+                    "the UW flux scheme runs with DUGKS_FP64 / DUGKS_FP64_FMA / DUGKS_FP32_DEV, the Allen-Cahn models "
+                    "and periodic y (the reference's UW reads unwritten gradients of its wall shadow cells)");
     dugks_handle *h = new (std::nothrow) dugks_handle();
     if (!h) return fail(nullptr, DUGKS_ENOMEM, "host allocation failed");
     h->cs = *c;
@@ -779,12 +783,17 @@ extern "C" int dugks_gpu_step(dugks_handle_t *h, int nsteps, void *stream) {
     if (h->fp32) {
         for (int s = 0; s < nsteps; ++s) {
             const uint32_t sn = (uint32_t)(h->steps + s);
-            // FP32 storage: the streaming kernel; the FP64 instance of the fused step: the tile kernel
-            cudaError_t e = h->fused64 ? f32::launch_stepX(h->P64f, h->S64f, h->first, h->gcur, h->gcur ^ 1, st,
-                                                           &h->launches, sn)
-                                       : f32::launch_stream32(h->P32, h->S32, h->first, h->gcur, h->gcur ^ 1, st,
-                                                              &h->launches, sn, h->has_tmap ? &h->tmap : nullptr,
-                                                              h->S32.df == h->tmap_base ? 0 : f32::PL_N, h->kerr);
+            // FP32 storage: the streaming kernel (UW: the four-launch upwind step); the FP64
+            // instance of the fused step: the tile kernel
+            cudaError_t e;
+            if (h->fused64)
+                e = f32::launch_stepX(h->P64f, h->S64f, h->first, h->gcur, h->gcur ^ 1, st, &h->launches, sn);
+            else if (h->uw32)
+                e = f32::launch_uw32(h->P32, h->S32, h->uw32, h->first, st, &h->launches);
+            else
+                e = f32::launch_stream32(h->P32, h->S32, h->first, h->gcur, h->gcur ^ 1, st, &h->launches, sn,
+                                         h->has_tmap ? &h->tmap : nullptr, h->S32.df == h->tmap_base ? 0 : f32::PL_N,
+                                         h->kerr);
             if (e != cudaSuccess) return cuda_fail(h, e, "fp32 step launch");
             if (h->fused64) f32::swap_io(h->S64f);
             else f32::swap_io(h->S32);
@@ -1317,7 +1326,7 @@ size_t footprint(const dugks_case_t &c, const dugks_grid_t &g) {
 }
 
 bool batchable(const dugks_handle_t *h) {
-    return h && h->fp32 && !h->fused64 && (h->P.model == AC || h->P.model == HCZ);
+    return h && h->fp32 && !h->fused64 && !h->P.uw && (h->P.model == AC || h->P.model == HCZ);
 }
 
 void fp32_views(const dugks_handle_t *h, f32::P32 *P, f32::S32 *S) {

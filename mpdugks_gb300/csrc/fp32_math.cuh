@@ -471,6 +471,10 @@ __device__ __forceinline__ FacePhi<decltype(T::x)> face_phi_y(T o, T n, T nw, T 
     return {R(0.5) * (o.x + n.x), pdiff(n, o), pdiff(nw, ne) + pdiff(ow, oe)};
 }
 
+template <int MODEL, bool XF, typename R>
+__device__ __forceinline__ void face_state_flux(const PR<R> &P, const typename Pair<R>::T (&bh)[9], const R (&av)[6],
+                                                R avg, int wall, typename Pair<R>::T (&F)[6]);
+
 // Stage 2 of one face: half-step reconstruction at the face midpoint, face
 // moments, equilibria of the six directions crossing the face and their
 // fluxes xi.n (f, h pairs, slot order xslot / yslot).  XF: an x-face (normal
@@ -523,13 +527,24 @@ __device__ __forceinline__ void face_flux(const PR<R> &P, FO &&O, FN &&N, FD &&D
         b.y = fma((R)d2q9_w(q), wphi, b.y);
         bh[q] = b;
     }
+    face_state_flux<MODEL, XF, R>(P, bh, av, fp.avg, wall, F);
+}
+
+// The rest of a face from its reconstructed half-step state bh (f deviations, h relative
+// to w_q avg, avg the face's phi reference): face moments, equilibria of the six
+// directions crossing the face, bounce-back at a wall face, fluxes xi.n (slot order
+// xslot / yslot).  Shared by the central (face_flux) and upwind reconstructions.
+template <int MODEL, bool XF, typename R>
+__device__ __forceinline__ void face_state_flux(const PR<R> &P, const typename Pair<R>::T (&bh)[9], const R (&av)[6],
+                                                R avg, int wall, typename Pair<R>::T (&F)[6]) {
+    using T = typename Pair<R>::T;
     // face moments (sum f, sum h) with the mirror-symmetric association
     const T z = add2(mk2(MODEL == AC ? R(0.) : bh[0].x, bh[0].y), sym8p(bh));
     // dphif: the face phi relative to fp.avg
     const R sf = z.x, dphif = z.y;
     const R su = (bh[1].x - bh[5].x) + ((bh[2].x - bh[6].x) + (bh[8].x - bh[4].x));
     const R sv = (bh[3].x - bh[7].x) + ((bh[2].x - bh[6].x) + (bh[4].x - bh[8].x));
-    const R phif = fp.avg + dphif;
+    const R phif = avg + dphif;
     const R rhof = P.aPhi * phif + P.bPhi;
     R Uf, Vf, dpf;
     if (MODEL == AC) {

@@ -54,6 +54,15 @@ enum { A_FX = 0, A_FY, A_RHOX, A_RHOY, A_PPU, A_PPV, A_N };
 // and the remainders g_q are small, so what FP32 rounds is small.
 constexpr int PL_F = 0, PL_G = 9, PL_PHI = 17, PL_AUX = 19, PL_N = PL_AUX + A_N;
 
+// Scratch planes of the upwind (UW) step (fp32_uw.cu), one every qs floats:
+//   B:   f-bar-plus pairs, 9 f planes then 9 h-relative (g) planes;
+//   A:   the averaged-field inputs {srcx, srcy, rhox, rhoy, fx, fy};
+//   INC: the collision increments B - T, laid out as B;
+//   GX, GY: the 6-point gradients of the 18 B planes;  GP: the gradient of phi (x, y);
+//   XF, YF: the six (f, h) flux pairs of each cell's west x-face / south y-face.
+constexpr int UW_B = 0, UW_A = 18, UW_INC = 24, UW_GX = 42, UW_GY = 60, UW_GP = 78, UW_XF = 80, UW_YF = 92,
+              UW_PLANES = 104;
+
 template <typename R>
 struct SR {
     R *df, *dg, *phi, *aux;      // the copy a step reads: planes PL_F, PL_G, PL_PHI, PL_AUX

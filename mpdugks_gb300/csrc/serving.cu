@@ -837,10 +837,11 @@ extern "C" int dugks_srv_submit_request(dugks_srv_t *s, const dugks_srv_request_
     k->snapshot_every = rq->snapshot_every;
     if (rq->out_dir) k->out_dir = rq->out_dir;
     k->bytes = internal::footprint(rq->cs, rq->grid);
-    // NEE walls take a solo lane (the batched kernels have bounce-back walls only)
+    // NEE walls and the UW flux scheme take a solo lane (the batched kernels have the
+    // central scheme and bounce-back walls only)
     k->batched = rq->cs.precision == DUGKS_FP32_DEV &&
                  (rq->cs.model == DUGKS_MODEL_AC || rq->cs.model == DUGKS_MODEL_HCZ) &&
-                 !(rq->grid.y_walls && rq->cs.wall_scheme == DUGKS_WALL_NEE);
+                 rq->cs.flux_scheme == DUGKS_FLUX_CD && !(rq->grid.y_walls && rq->cs.wall_scheme == DUGKS_WALL_NEE);
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->stopping) return DUGKS_EINVAL;
     if (k->bytes > s->max_bytes) {

@@ -86,11 +86,12 @@ def test_struct_layouts_match_the_header(tmp_path):
     assert got == want
 
 
-@pytest.mark.parametrize('model,precision,walls', [('AC', 'fp32dev', False), ('HCZ', 'fp64', True),
-                                                   ('PP9', 'fp64', False), ('AC', 'fp64fused', False)])
+@pytest.mark.parametrize('model,precision,walls', [('AC', 'fp32dev', True), ('HCZ', 'fp64', True),
+                                                   ('PP9', 'fp64', False), ('PP16', 'fp32dev', False),
+                                                   ('AC', 'fp64fused', False)])
 def test_uw_flux_scheme_rejected_where_not_supported(model, precision, walls):
-    """UW runs with the plain FP64 precisions, the Allen-Cahn models and periodic y; other
-    combinations are refused before any device work, with the reason."""
+    """UW runs with the plain FP64 precisions and FP32 storage, the Allen-Cahn models and
+    periodic y; other combinations are refused before any device work, with the reason."""
     import ctypes
     from mpdugks_gb300 import capi
     lib = capi.load(build_if_missing=True)

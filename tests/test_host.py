@@ -153,12 +153,13 @@ def test_driver_drop_l2_equals_the_reference(case, tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize('case,extra', [('ac_ff', []),
+@pytest.mark.parametrize('case,extra', [('ac_ff', []), ('uw_ff', []),
                                         ('nee_rt', ['--set', 'init=ac_rt', '--set', 'gravity=0.0001',
                                                     '--set', 'wall scheme=NEE'])])
 def test_driver_fp32_run_is_close_to_the_reference_files(case, extra, tmp_path):
     """FP32 storage through dugks_run against the reference's FlowField files at step 20
-    (the AC_Drop case, and the Rayleigh-Taylor box with NEE walls)."""
+    (the AC_Drop case with the central and the upwind scheme, and the Rayleigh-Taylor box
+    with NEE walls)."""
     out = tmp_path / 'FlowField'
     subprocess.run([runner(), 'run', GOLD / case / 'Case.ark', '--out', out, '--steps', '20', '--precision',
                     'fp32dev'] + extra, check=True, capture_output=True)
