@@ -159,6 +159,18 @@ static int cuda_fail(dugks_handle *h, cudaError_t e, const char *what) {
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
+// The device address of host memory the device can access in place (pinned and mapped:
+// cudaHostAlloc, or registered with the mapped flag), else null.  On the GB300 such memory
+// is read and written by kernels over NVLink-C2C, with no copy-engine staging.
+static void *mapped_host(const void *p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 // constants of the fused step: FP64 reference expressions, rounded once to R.
 template <typename R>
 static void derive_p32(const Params &P, f32::PR<R> &Q) {
@@ -485,47 +497,111 @@ static int create_fp32(dugks_handle *h, dugks_handle_t **out) {
 }
 
 // FP64 [Q][ny][nx] state -> deviations and first-step planes on the device.
-// Each FP64 plane is copied as-is into a device staging plane (one of the
-// FP64 output fields, which an upload invalidates anyway) and converted there.
+// Each FP64 plane is copied as-is into a device staging plane and converted there.  The
+// host-to-device copies run on a stream of their own through two staging planes (two of
+// the FP64 output fields, which an upload invalidates anyway), so the copy of a plane
+// overlaps the conversion of the one before on the handle's stream; a host plane that
+// feeds several device planes (the forces and density gradients: first-step inputs and
+// the previous MacroSource) is copied once.
 template <typename R>
 static int upload_fused(dugks_handle *h, f32::SR<R> &S, const double *f, const double *hd, const double *aux) {
     const Params &P = h->P;
     const int nx = P.nx, ny = P.ny;
-    const size_t n = (size_t)nx * ny;
-    cudaStream_t st = h->last_stream;
-    double *stage = h->S.fld[F_RHO];
-    cudaError_t e;
-    auto put = [&](R *dst, const double *src, double sub) -> cudaError_t {
-        cudaError_t r = cudaMemcpyAsync(stage, src, n * sizeof(double), cudaMemcpyHostToDevice, st);
-        if (r != cudaSuccess) return r;
-        return f32::launch_plane_from_f64<R>(dst, P.pitch, stage, nx, ny, sub, st, &h->launches);
+    const size_t n = (size_t)nx * ny, bytes = n * sizeof(double);
+    cudaStream_t st = h->last_stream, cs = nullptr;
+    cudaEvent_t ev[5] = {};  // staging plane copied (2), staging plane consumed (2), h copied
+    struct Cleanup {
+        cudaStream_t &cs;
+        cudaEvent_t (&ev)[5];
+        ~Cleanup() {
+            if (cs) cudaStreamSynchronize(cs);
+            for (auto &x : ev)
+                if (x) cudaEventDestroy(x);
+            if (cs) cudaStreamDestroy(cs);
+        }
+    } cleanup{cs, ev};
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    for (auto &x : ev)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(h, e, "upload streams");
+    double *stage[2] = {h->S.fld[F_RHO], h->S.fld[F_U]};
+    // host arrays the device can read in place (pinned and mapped): the conversions read
+    // them directly (measured on the 8192^2 state, 18 GB: 92 ms against 82 ms through the
+    // copy engines on an idle GPU, but 138-166 ms against 210-861 ms right after a run of
+    // steps, when the copy-engine path slowed down and this one much less)
+    const double *fm = static_cast<const double *>(mapped_host(f));
+    const double *hm = hd ? static_cast<const double *>(mapped_host(hd)) : nullptr;
+    const double *am = static_cast<const double *>(mapped_host(aux));
+    struct Dst {
+        R *p;
+        double sub;
     };
-    for (int q = 0; q < 9; ++q)
-        if ((e = put(S.df + q * S.qs, f + q * n, f_rest(P, q))) != cudaSuccess) return cuda_fail(h, e, "upload f");
+    int job = 0;
+    auto put = [&](const double *src, const Dst *dsts, int nd, const double *dsrc) -> cudaError_t {
+        if (dsrc) {
+            cudaError_t r = cudaSuccess;
+            for (int k = 0; k < nd && r == cudaSuccess; ++k)
+                r = f32::launch_plane_from_f64<R>(dsts[k].p, P.pitch, dsrc, nx, ny, dsts[k].sub, st, &h->launches);
+            return r;
+        }
+        const int b = job++ & 1;
+        cudaError_t r = job > 2 ? cudaStreamWaitEvent(cs, ev[2 + b], 0) : cudaSuccess;
+        if (r == cudaSuccess) r = cudaMemcpyAsync(stage[b], src, bytes, cudaMemcpyHostToDevice, cs);
+        if (r == cudaSuccess) r = cudaEventRecord(ev[b], cs);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(st, ev[b], 0);
+        for (int k = 0; k < nd && r == cudaSuccess; ++k)
+            r = f32::launch_plane_from_f64<R>(dsts[k].p, P.pitch, stage[b], nx, ny, dsts[k].sub, st, &h->launches);
+        if (r == cudaSuccess) r = cudaEventRecord(ev[2 + b], st);
+        return r;
+    };
+    for (int q = 0; q < 9; ++q) {
+        const Dst d = {S.df + q * S.qs, f_rest(P, q)};
+        if ((e = put(f + q * n, &d, 1, fm ? fm + q * n : nullptr)) != cudaSuccess) return cuda_fail(h, e, "upload f");
+    }
     // the phase field: the nine FP64 h planes go to the copy the next step writes (free
     // until then: 9 n doubles fit in its PL_N planes), then phi = sum_q h_q as a pair and
     // g_q = h_q - w_q phi into the copy it reads
     {
-        double *hst = reinterpret_cast<double *>(S.odf);
-        if ((e = cudaMemcpyAsync(hst, hd, 9 * n * sizeof(double), cudaMemcpyHostToDevice, st)) != cudaSuccess)
-            return cuda_fail(h, e, "upload h");
-        if ((e = f32::launch_phase_from_f64<R>(S.dg, S.phi, S.qs, P.pitch, hst, nx, ny, st, &h->launches)) !=
-            cudaSuccess)
-            return cuda_fail(h, e, "upload h");
+        const double *hst = hm;
+        if (!hst) {
+            double *hs = reinterpret_cast<double *>(S.odf);
+            e = cudaMemcpyAsync(hs, hd, 9 * bytes, cudaMemcpyHostToDevice, cs);
+            if (e == cudaSuccess) e = cudaEventRecord(ev[4], cs);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev[4], 0);
+            hst = hs;
+        }
+        if (e == cudaSuccess) e = f32::launch_phase_from_f64<R>(S.dg, S.phi, S.qs, P.pitch, hst, nx, ny, st, &h->launches);
+        if (e != cudaSuccess) return cuda_fail(h, e, "upload h");
     }
-    const int src[f32::I_N] = {F_PHI, F_RHO, F_U, F_V, F_P, F_TAU, F_PHIX, F_PHIY, F_RHOX, F_RHOY, F_FX, F_FY};
-    for (int k = 0; k < f32::I_N; ++k) {
-        const double sub = k == f32::I_DPHI ? DUGKS_F32_PHI0 : (k == f32::I_DP ? 1.0 : 0.0);
-        if ((e = put(S.init + k * S.qs, aux + (size_t)src[k] * n, sub)) != cudaSuccess)
+    // first-step inputs (init planes) and the previous MacroSource outputs (aux planes)
+    const size_t qs = S.qs;
+    R *I = S.init, *A = S.aux;
+    struct Plane {
+        int field, nd;
+        Dst d[2];
+    };
+    const Plane planes[] = {
+        {F_PHI, 1, {{I + f32::I_DPHI * qs, DUGKS_F32_PHI0}, {}}},
+        {F_RHO, 1, {{I + f32::I_RHO * qs, 0.0}, {}}},
+        {F_U, 1, {{I + f32::I_U * qs, 0.0}, {}}},
+        {F_V, 1, {{I + f32::I_V * qs, 0.0}, {}}},
+        {F_P, 1, {{I + f32::I_DP * qs, 1.0}, {}}},
+        {F_TAU, 1, {{I + f32::I_TAU * qs, 0.0}, {}}},
+        {F_PHIX, 1, {{I + f32::I_SRCX * qs, 0.0}, {}}},
+        {F_PHIY, 1, {{I + f32::I_SRCY * qs, 0.0}, {}}},
+        {F_RHOX, 2, {{I + f32::I_RHOX * qs, 0.0}, {A + f32::A_RHOX * qs, 0.0}}},
+        {F_RHOY, 2, {{I + f32::I_RHOY * qs, 0.0}, {A + f32::A_RHOY * qs, 0.0}}},
+        {F_FX, 2, {{I + f32::I_FX * qs, 0.0}, {A + f32::A_FX * qs, 0.0}}},
+        {F_FY, 2, {{I + f32::I_FY * qs, 0.0}, {A + f32::A_FY * qs, 0.0}}},
+        {F_PPU, 1, {{A + f32::A_PPU * qs, 0.0}, {}}},
+        {F_PPV, 1, {{A + f32::A_PPV * qs, 0.0}, {}}},
+    };
+    for (const Plane &pl : planes)
+        if ((e = put(aux + (size_t)pl.field * n, pl.d, pl.nd, am ? am + (size_t)pl.field * n : nullptr)) != cudaSuccess)
             return cuda_fail(h, e, "upload init");
-    }
-    // previous MacroSource outputs as the first step's successor will read them
-    const int asrc[f32::A_N] = {F_FX, F_FY, F_RHOX, F_RHOY, F_PPU, F_PPV};
-    for (int k = 0; k < f32::A_N; ++k)
-        if ((e = put(S.aux + k * S.qs, aux + (size_t)asrc[k] * n, 0.0)) != cudaSuccess)
-            return cuda_fail(h, e, "upload aux");
     if ((e = cudaMemsetAsync(h->rho_last, 0, (size_t)P.pitch * ny * sizeof(double), st)) != cudaSuccess)
         return cuda_fail(h, e, "upload");
+    // the handle's stream waited for every copy before converting it
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(h, e, "upload");
     h->first = 1;
@@ -690,8 +766,21 @@ static cudaError_t to_dev(const dugks_handle *h, double *d, const double *src, i
     return cudaMemcpy2D(d, (size_t)P.pitch * sizeof(double), src, (size_t)P.nx * sizeof(double),
                         (size_t)P.nx * sizeof(double), rows < 0 ? P.ny : rows, cudaMemcpyHostToDevice);
 }
+__global__ void k_plane_to_dense(double *dst, const double *__restrict__ src, int nx, int ny, int pitch) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nx) return;
+    for (int j = blockIdx.y; j < ny; j += gridDim.y) dst[(size_t)j * nx + i] = src[(size_t)j * pitch + i];
+}
+// a device plane [ny][pitch] to host [ny][nx]; pinned, mapped host memory is written in
+// place by a kernel on the handle's stream (the callers have synchronised it)
 static cudaError_t to_host(const dugks_handle *h, double *dst, const double *d) {
     const Params &P = h->P;
+    if (double *m = static_cast<double *>(mapped_host(dst))) {
+        k_plane_to_dense<<<dim3((P.nx + 255) / 256, P.ny < 65535 ? P.ny : 65535), 256, 0, h->last_stream>>>(
+            m, d, P.nx, P.ny, P.pitch);
+        const cudaError_t e = cudaGetLastError();
+        return e == cudaSuccess ? cudaStreamSynchronize(h->last_stream) : e;
+    }
     return cudaMemcpy2D(dst, (size_t)P.nx * sizeof(double), d, (size_t)P.pitch * sizeof(double),
                         (size_t)P.nx * sizeof(double), P.ny, cudaMemcpyDeviceToHost);
 }
