@@ -143,7 +143,10 @@ int dugks_gpu_nq(const dugks_handle_t *h);
 /* Upload a full state: f and hdist are [Q][ny][nx] (hdist ignored for the
  * pseudopotential models, may be NULL); aux is [DUGKS_F_NFIELDS][ny][nx] in
  * dugks_field order.  The next step uses aux as-is (like the reference's
- * first step after an initialisation function). */
+ * first step after an initialisation function).  Host arrays in pinned, mapped
+ * memory (cudaHostAlloc) are read in place by the DUGKS_FP32_DEV and
+ * DUGKS_FP64_FUSED conversion kernels; other memory is copied through staging
+ * planes.  The results are the same either way. */
 int dugks_gpu_upload(dugks_handle_t *h, const double *f, const double *hdist, const double *aux);
 
 /* Initialise on the host like the reference initialisation functions and
@@ -172,7 +175,8 @@ int dugks_gpu_step_profiled(dugks_handle_t *h, int nsteps, void *stream, double 
  * not complete within its bounded wait (the state is then not valid). */
 int dugks_gpu_reduce(dugks_handle_t *h, dugks_reductions_t *r);
 
-/* Download the macroscopic fields (any pointer may be NULL): [ny][nx] each. */
+/* Download the macroscopic fields (any pointer may be NULL): [ny][nx] each.
+ * Pinned, mapped host arrays are written in place by a copy kernel. */
 int dugks_gpu_download(dugks_handle_t *h, double *rho, double *u, double *v, double *phi, double *p);
 
 /* Single field / distribution access.  which: 0 = f, 1 = h. */
