@@ -108,7 +108,10 @@ __global__ void __launch_bounds__(UBX *UBY) k_uw32_collide(P32 P, S32 S, float *
 }
 
 // 6-point gradients (axis neighbours 4, diagonals 1, over 12 dx) of the 18 f-bar-plus
-// planes and of phi (from pair differences)
+// planes and of phi (from pair differences).  blockIdx.z: a third of the planes each (one
+// thread over all 18 took 4x as long: its dependent neighbour loads, not the bandwidth,
+// set the pace); the first third also the phase field's.
+constexpr int UW_GRAD_SLICES = 3;
 __global__ void __launch_bounds__(UBX *UBY) k_uw32_grad(P32 P, S32 S, float *U) {
     Cells k;
     if (!cell_of(P, k)) return;
@@ -117,13 +120,15 @@ __global__ void __launch_bounds__(UBX *UBY) k_uw32_grad(P32 P, S32 S, float *U) 
     const size_t cNE = at(P, k.jp, k.ip), cNW = at(P, k.jp, k.im), cSE = at(P, k.jm, k.ip), cSW = at(P, k.jm, k.im);
     auto gx = [&](float s) { return s * P.inv_12dx; };
     auto gy = [&](float s) { return s * P.inv_12dy; };
-#pragma unroll 6
-    for (int p = 0; p < 18; ++p) {
+    constexpr int PER = 18 / UW_GRAD_SLICES;
+#pragma unroll
+    for (int p = blockIdx.z * PER; p < (int)(blockIdx.z + 1) * PER; ++p) {
         const float *B = U + (size_t)(UW_B + p) * qs;
         const float E = B[cE], W = B[cW], N = B[cN], Sv = B[cS], NE = B[cNE], NW = B[cNW], SE = B[cSE], SW = B[cSW];
         U[(size_t)(UW_GX + p) * qs + c] = gx(fmaf(4.f, E - W, (NE - NW) + (SE - SW)));
         U[(size_t)(UW_GY + p) * qs + c] = gy(fmaf(4.f, N - Sv, (NE - SE) + (NW - SW)));
     }
+    if (blockIdx.z != 0) return;
     const float2 E = phi_at(S, cE), W = phi_at(S, cW), N = phi_at(S, cN), Sv = phi_at(S, cS);
     const float2 NE = phi_at(S, cNE), NW = phi_at(S, cNW), SE = phi_at(S, cSE), SW = phi_at(S, cSW);
     U[(size_t)UW_GP * qs + c] = gx(fmaf(4.f, pdiff(E, W), pdiff(NE, NW) + pdiff(SE, SW)));
@@ -179,13 +184,15 @@ __device__ __forceinline__ void uw_face(const P32 &P, const S32 &S, float *U, si
     }
 }
 
-// blockIdx.z 0: the west x-face of every cell; 1: its south y-face
+// the west x-face and the south y-face of every cell, one thread both (the cell's own
+// values, read by both, come from the cache the second time: half the DRAM reads of one
+// launch slice per face direction)
 template <int MODEL>
 __global__ void __launch_bounds__(UBX *UBY) k_uw32_faces(P32 P, S32 S, float *U) {
     Cells k;
     if (!cell_of(P, k)) return;
-    if (blockIdx.z == 0) uw_face<MODEL, true>(P, S, U, at(P, k.j, k.im), k.c);
-    else uw_face<MODEL, false>(P, S, U, at(P, k.jm, k.i), k.c);
+    uw_face<MODEL, true>(P, S, U, at(P, k.j, k.im), k.c);
+    uw_face<MODEL, false>(P, S, U, at(P, k.jm, k.i), k.c);
 }
 
 // finite-volume update of every cell from its four faces' fluxes
@@ -225,10 +232,10 @@ __global__ void __launch_bounds__(UBX *UBY) k_uw32_update(P32 P, S32 S, const fl
 
 template <int MODEL>
 static cudaError_t launch_uw32_t(const P32 &P, const S32 &S, float *U, int first, cudaStream_t st) {
-    const dim3 blk(UBX, UBY), grd((P.nx + UBX - 1) / UBX, (P.ny + UBY - 1) / UBY), grd2(grd.x, grd.y, 2);
+    const dim3 blk(UBX, UBY), grd((P.nx + UBX - 1) / UBX, (P.ny + UBY - 1) / UBY);
     k_uw32_collide<MODEL><<<grd, blk, 0, st>>>(P, S, U, first);
-    k_uw32_grad<<<grd, blk, 0, st>>>(P, S, U);
-    k_uw32_faces<MODEL><<<grd2, blk, 0, st>>>(P, S, U);
+    k_uw32_grad<<<dim3(grd.x, grd.y, UW_GRAD_SLICES), blk, 0, st>>>(P, S, U);
+    k_uw32_faces<MODEL><<<grd, blk, 0, st>>>(P, S, U);
     k_uw32_update<MODEL><<<grd, blk, 0, st>>>(P, S, U);
     return cudaGetLastError();
 }

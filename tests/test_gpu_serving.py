@@ -33,7 +33,16 @@ MIX = [
     # pseudopotential FP32 cases: solo lanes, concurrently
     (lambda: pp_case('PP16'), 40, 40, False, 'scmp_drop', [], 80),
     (lambda: pp_case('PP9'), 48, 48, False, 'pp_noise', [0.2, 0.01], 90),
+    # FP32 storage with the UW flux scheme and with NEE walls: solo lanes
+    (lambda: ac_case(scheme='UW'), 64, 48, False, 'ac_drop_inside', [10.0], 70),
+    (lambda: nee_case(), 32, 64, True, 'ac_rt', [1.0, 0.1, 1e-4], 55),
 ]
+
+
+def nee_case():
+    from mpdugks_gb300 import capi
+    return capi.make_case('HCZ', 'fp32dev', Mu0=0.01, M_Phi=0.05, W=4.0, Sigma=1e-4, RhoL=3.0, RhoV=1.0,
+                          Gy=1e-4, wall='NEE')
 
 
 def pp_case(model, precision='fp32dev'):
@@ -88,6 +97,22 @@ def test_solo_lane_fp64_matches_the_plain_path():
     f, nx, ny, w, init, params, n = MIX[3]
     srv = capi.Server(chunk_steps=16)
     r = run(srv, [MIX[3], MIX[0]])[0]
+    srv.close()
+    gc = capi.GpuCase(f(), nx, ny, w)
+    gc.init(init, params, seed=7)
+    gc.step(n)
+    for k in FIELDS:
+        assert np.array_equal(r[k], gc.get(k)), k
+
+
+@pytest.mark.parametrize('item', [-2, -1], ids=['fp32_uw', 'fp32_nee'])
+def test_solo_lane_fp32_variants_match_the_plain_path(item):
+    """FP32 cases the batched kernels do not take (UW flux scheme, NEE walls) run in a solo
+    lane and equal the same case stepped through its own handle."""
+    from mpdugks_gb300 import capi
+    f, nx, ny, w, init, params, n = MIX[item]
+    srv = capi.Server(chunk_steps=16)
+    r = run(srv, [MIX[item], MIX[0]])[0]
     srv.close()
     gc = capi.GpuCase(f(), nx, ny, w)
     gc.init(init, params, seed=7)
