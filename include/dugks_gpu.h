@@ -101,10 +101,17 @@ typedef enum dugks_wall_scheme {
  * collision, gradients, faces, update), the Allen-Cahn models and periodic y:
  * the reference's UW with walls reads the gradients of its wall shadow cells,
  * which it never writes (uninitialised memory).  Serving runs UW cases in solo
- * lanes. */
+ * lanes.  UW_LS and UW_4P are UW with the reference's other cell gradients, the
+ * least-squares one (Grad_VS_LS, Ark/Cpp/GradScheme.cpp:219-231 ->
+ * Ark/Lib/GradSchemeBasic.h:127-152, weights from Grad_LSMatrix :49-75) and the
+ * 4-point central one (Grad_VS_4points :191-204 -> GradSchemeBasic.h:76-94), which
+ * the reference selects by editing the gradient call at
+ * Ark/Cpp/DUGKS2DSolver.cpp:201-203; same precisions and restrictions as UW. */
 typedef enum dugks_flux_scheme {
     DUGKS_FLUX_CD = 0,
-    DUGKS_FLUX_UW = 1
+    DUGKS_FLUX_UW = 1,
+    DUGKS_FLUX_UW_LS = 2,
+    DUGKS_FLUX_UW_4P = 3
 } dugks_flux_scheme;
 
 typedef struct dugks_grid {

@@ -157,7 +157,7 @@ def load(build_if_missing: bool = False):
     return lib
 
 
-FLUX_SCHEMES = {'CD': 0, 'UW': 1}
+FLUX_SCHEMES = {'CD': 0, 'UW': 1, 'UW_LS': 2, 'UW_4P': 3}  # dugks_flux_scheme
 WALL_SCHEMES = {'BB': 0, 'NEE': 1}
 
 

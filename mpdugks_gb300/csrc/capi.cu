@@ -194,6 +194,7 @@ static void derive_p32(const Params &P, f32::PR<R> &Q) {
     Q.r_2dy = (R)P.r_2dy; Q.r_ndx = (R)P.r_ndx; Q.r_n2dx = (R)P.r_n2dx; Q.r_ndy = (R)P.r_ndy;
     Q.aTP = (R)P.aTP; Q.bTP = (R)P.bTP; Q.dtV = (R)P.dtV;
     Q.nee = P.nee;
+    Q.uw_grad = P.uw_grad;
     Q.hneq = (R)(2.0 * P.TauMass / (2.0 * P.TauMass + P.dt));
 }
 
@@ -653,7 +654,7 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
         return fail(nullptr, DUGKS_EINVAL, "unknown precision");
     if (c->precision == DUGKS_FP64_FUSED && !(c->model == DUGKS_MODEL_AC || c->model == DUGKS_MODEL_HCZ))
         return fail(nullptr, DUGKS_EINVAL, "the fused deviation-form step supports the Allen-Cahn models (AC, HCZ)");
-    if (c->flux_scheme != DUGKS_FLUX_CD && c->flux_scheme != DUGKS_FLUX_UW)
+    if (c->flux_scheme < DUGKS_FLUX_CD || c->flux_scheme > DUGKS_FLUX_UW_4P)
         return fail(nullptr, DUGKS_EINVAL, "unknown flux scheme");
     if (c->wall_scheme != DUGKS_WALL_BB && c->wall_scheme != DUGKS_WALL_NEE)
         return fail(nullptr, DUGKS_EINVAL, "unknown wall scheme");
@@ -664,7 +665,7 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
                     "NEE walls run with DUGKS_FP64 / DUGKS_FP64_FMA / DUGKS_FP32_DEV and the Allen-Cahn models");
     if (c->wall_scheme == DUGKS_WALL_NEE && c->precision == DUGKS_FP32_DEV && g->y_walls && g->ny < 8)
         return fail(nullptr, DUGKS_EINVAL, "NEE walls in FP32 storage need at least 8 rows (the streaming step)");
-    if (c->flux_scheme == DUGKS_FLUX_UW &&
+    if (c->flux_scheme != DUGKS_FLUX_CD &&
         (!(c->precision == DUGKS_FP64 || c->precision == DUGKS_FP64_FMA || c->precision == DUGKS_FP32_DEV) ||
          !(c->model == DUGKS_MODEL_AC || c->model == DUGKS_MODEL_HCZ) || g->y_walls))
         return fail(nullptr, DUGKS_EINVAL,

@@ -42,7 +42,8 @@ struct Params {
     // reciprocals RN(1/d) of divisors fixed per case, for the correctly rounded quotient
     // qdiv_rn: 1/RT, 1/(6 2dx), 1/(6 2dy), 1/(6 MinL MinL), 1/(W (PhiL - PhiV)), 1/(RT dt)
     double r_RT, r_g6x, r_g6y, r_lap, r_wI, r_RTdt;
-    int grad_mul, uw;                              // uw: upwind face reconstruction (DUGKS_FLUX_UW)
+    int grad_mul, uw;                              // uw: upwind face reconstruction (DUGKS_FLUX_UW*)
+    int uw_grad;                                   // its cell gradient: 0 6-point, 1 least squares, 2 4-point
     double c16;                                    // D2V16 lattice speed
     // D2V16 inverse moment matrix of this case, [16][16] in the case's device memory
     // (Ark/Lib/D2V16.cpp:34-52): each case holds its own

@@ -23,6 +23,7 @@ template <typename R>
 struct PR {
     int nx, ny, pitch, walls, model, gravity;
     int nee;  // NEE walls (Ark/Cpp/Boundary.cpp:140-184) instead of bounce-back
+    int uw_grad;  // UW cell gradient: 0 6-point, 1 least squares, 2 4-point
     // slab partitions: global row of local row 0, and whether the rows below 0 /
     // from ny up are a neighbour's halo (2 rows of device memory) instead of a
     // wall or the periodic wrap; 0 for a whole grid

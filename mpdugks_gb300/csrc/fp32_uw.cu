@@ -108,7 +108,9 @@ __global__ void __launch_bounds__(UBX *UBY) k_uw32_collide(P32 P, S32 S, float *
 }
 
 // 6-point gradients (axis neighbours 4, diagonals 1, over 12 dx) of the 18 f-bar-plus
-// planes and of phi (from pair differences).  blockIdx.z: a third of the planes each (one
+// planes and of phi (from pair differences), or with uw_grad the least-squares and the
+// 4-point gradients, which on unit cells are both (E - W) / 2 and (N - S) / 2 (their
+// different FP64 roundings are below FP32's).  blockIdx.z: a third of the planes each (one
 // thread over all 18 took 4x as long: its dependent neighbour loads, not the bandwidth,
 // set the pace); the first third also the phase field's.
 constexpr int UW_GRAD_SLICES = 3;
@@ -120,19 +122,37 @@ __global__ void __launch_bounds__(UBX *UBY) k_uw32_grad(P32 P, S32 S, float *U) 
     const size_t cNE = at(P, k.jp, k.ip), cNW = at(P, k.jp, k.im), cSE = at(P, k.jm, k.ip), cSW = at(P, k.jm, k.im);
     auto gx = [&](float s) { return s * P.inv_12dx; };
     auto gy = [&](float s) { return s * P.inv_12dy; };
+    const bool six = P.uw_grad == 0;
     constexpr int PER = 18 / UW_GRAD_SLICES;
 #pragma unroll
     for (int p = blockIdx.z * PER; p < (int)(blockIdx.z + 1) * PER; ++p) {
         const float *B = U + (size_t)(UW_B + p) * qs;
-        const float E = B[cE], W = B[cW], N = B[cN], Sv = B[cS], NE = B[cNE], NW = B[cNW], SE = B[cSE], SW = B[cSW];
-        U[(size_t)(UW_GX + p) * qs + c] = gx(fmaf(4.f, E - W, (NE - NW) + (SE - SW)));
-        U[(size_t)(UW_GY + p) * qs + c] = gy(fmaf(4.f, N - Sv, (NE - SE) + (NW - SW)));
+        const float E = B[cE], W = B[cW], N = B[cN], Sv = B[cS];
+        float x, y;
+        if (six) {
+            const float NE = B[cNE], NW = B[cNW], SE = B[cSE], SW = B[cSW];
+            x = gx(fmaf(4.f, E - W, (NE - NW) + (SE - SW)));
+            y = gy(fmaf(4.f, N - Sv, (NE - SE) + (NW - SW)));
+        } else {
+            x = 0.5f * (E - W);
+            y = 0.5f * (N - Sv);
+        }
+        U[(size_t)(UW_GX + p) * qs + c] = x;
+        U[(size_t)(UW_GY + p) * qs + c] = y;
     }
     if (blockIdx.z != 0) return;
     const float2 E = phi_at(S, cE), W = phi_at(S, cW), N = phi_at(S, cN), Sv = phi_at(S, cS);
-    const float2 NE = phi_at(S, cNE), NW = phi_at(S, cNW), SE = phi_at(S, cSE), SW = phi_at(S, cSW);
-    U[(size_t)UW_GP * qs + c] = gx(fmaf(4.f, pdiff(E, W), pdiff(NE, NW) + pdiff(SE, SW)));
-    U[(size_t)(UW_GP + 1) * qs + c] = gy(fmaf(4.f, pdiff(N, Sv), pdiff(NE, SE) + pdiff(NW, SW)));
+    float x, y;
+    if (six) {
+        const float2 NE = phi_at(S, cNE), NW = phi_at(S, cNW), SE = phi_at(S, cSE), SW = phi_at(S, cSW);
+        x = gx(fmaf(4.f, pdiff(E, W), pdiff(NE, NW) + pdiff(SE, SW)));
+        y = gy(fmaf(4.f, pdiff(N, Sv), pdiff(NE, SE) + pdiff(NW, SW)));
+    } else {
+        x = 0.5f * pdiff(E, W);
+        y = 0.5f * pdiff(N, Sv);
+    }
+    U[(size_t)UW_GP * qs + c] = x;
+    U[(size_t)(UW_GP + 1) * qs + c] = y;
 }
 
 // Upwind reconstruction and fluxes of the west x-face (XF) or the south y-face of every

@@ -428,9 +428,35 @@ __global__ void __launch_bounds__(256) k_grad6(Params P, State S) {
         for (int w = 0; w < 2; ++w) {
             const double *B = (w ? S.bh : S.bf) + (size_t)q * S.qs;
             const double E = B[cE], W = B[cW], N = B[cN], Sv = B[cS];
-            const double NE = B[cNE], NW = B[cNW], SW = B[cSW], SE = B[cSE];
-            const double gx = QDIV(4.0 * (E - W) + (((NE - NW) + SE) - SW), dxd, rdx);
-            const double gy = QDIV(4.0 * (N - Sv) + (((NE - SE) + NW) - SW), dyd, rdy);
+            double gx, gy;
+            if (P.uw_grad == 1) {
+                // Grad_VS_LS (Ark/Lib/GradSchemeBasic.h:127-152): sum over the neighbours
+                // E, N, W, S of w_k (B_k - B_c), then the inverse 2x2 matrix.  On this
+                // mesh of unit cells the weights of Grad_LSMatrix (:13-75) are exact: the
+                // cell centres (two-triangle centroids, Ark/Cpp/Mesh/Cell_2D.cpp:157-179)
+                // are i + 1/2, j + 1/2 and the periodic shadows' are offset by exactly
+                // Lx / Ly, so wdx = {1, 0, -1, 0}, wdy = {0, 1, 0, -1} and the inverse
+                // matrix is {{0.5, -0}, {-0, 0.5}}; every product and sum of the reference
+                // is kept (the zero terms included), so the result is the same bits.
+                const double C = B[c];
+                const double nb[4] = {E, N, W, Sv}, wx[4] = {1.0, 0.0, -1.0, 0.0}, wy[4] = {0.0, 1.0, 0.0, -1.0};
+                double sx = 0.0, sy = 0.0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    sx = sx + wx[k] * (nb[k] - C);
+                    sy = sy + wy[k] * (nb[k] - C);
+                }
+                gx = 0.5 * sx + -0.0 * sy;
+                gy = -0.0 * sx + 0.5 * sy;
+            } else if (P.uw_grad == 2) {
+                // Grad_VS_4points (Ark/Lib/GradSchemeBasic.h:76-94): (C0 - C2) / (2 dx)
+                gx = QDIV(E - W, P._2dx, 0.5 / P.dx);
+                gy = QDIV(N - Sv, P._2dy, 0.5 / P.dy);
+            } else {
+                const double NE = B[cNE], NW = B[cNW], SW = B[cSW], SE = B[cSE];
+                gx = QDIV(4.0 * (E - W) + (((NE - NW) + SE) - SW), dxd, rdx);
+                gy = QDIV(4.0 * (N - Sv) + (((NE - SE) + NW) - SW), dyd, rdy);
+            }
             (w ? S.ghx : S.gfx)[(size_t)q * S.qs + c] = gx;
             (w ? S.ghy : S.gfy)[(size_t)q * S.qs + c] = gy;
         }

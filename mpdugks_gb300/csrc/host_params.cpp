@@ -98,7 +98,8 @@ void derive_params(const dugks_case_t &cs, const dugks_grid_t &g, Params &P) {
         P.r_wI = 1.0 / (P.wI * (P.PhiL - P.PhiV));
         P.r_RTdt = 1.0 / (P.RT * P.dt);
     }
-    P.uw = cs.flux_scheme == DUGKS_FLUX_UW ? 1 : 0;
+    P.uw = cs.flux_scheme != DUGKS_FLUX_CD ? 1 : 0;
+    P.uw_grad = cs.flux_scheme == DUGKS_FLUX_UW_LS ? 1 : (cs.flux_scheme == DUGKS_FLUX_UW_4P ? 2 : 0);
     P.nee = (cs.wall_scheme == DUGKS_WALL_NEE && g.y_walls) ? 1 : 0;
     P.T_CS = cs.Tr * cs.Tc_CS;
     P.aCS = cs.aCS;

@@ -148,6 +148,13 @@ RunConfig config_from_case_ark(const CaseArk &ark) {
     if (fs == "CD") c.cs.flux_scheme = DUGKS_FLUX_CD;
     else if (fs == "UW") c.cs.flux_scheme = DUGKS_FLUX_UW;
     else throw std::runtime_error("Case.ark: unknown flux scheme '" + fs + "'");
+    // the UW cell gradient (which Grad_VS_* call Ark/Cpp/DUGKS2DSolver.cpp:201-203 keeps;
+    // not in OutputCase): 6points (the reference's), LS or 4points
+    const std::string gs = ark.get("cell gradient", "6points");
+    if (gs == "LS" && c.cs.flux_scheme == DUGKS_FLUX_UW) c.cs.flux_scheme = DUGKS_FLUX_UW_LS;
+    else if (gs == "4points" && c.cs.flux_scheme == DUGKS_FLUX_UW) c.cs.flux_scheme = DUGKS_FLUX_UW_4P;
+    else if (gs != "6points" && gs != "LS" && gs != "4points")
+        throw std::runtime_error("Case.ark: unknown cell gradient '" + gs + "'");
     // the wall treatment (_Wall_3_BCs_BB / _NEE of Ark/Constant/ZeroFlip.h; not in OutputCase)
     const std::string ws = ark.get("wall scheme", "BB");
     if (ws == "BB") c.cs.wall_scheme = DUGKS_WALL_BB;

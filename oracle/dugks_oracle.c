@@ -477,6 +477,45 @@ static void cell_grad6(orc_state *s, const double *B, double *GX, double *GY, in
     }
 }
 
+/* Grad_VS_LS (Ark/Cpp/GradScheme.cpp:219-231 -> Ark/Lib/GradSchemeBasic.h:127-152): the
+ * least-squares gradient, sum over C0..C3 = E,N,W,S of w_k (B_k - B_c), then the inverse
+ * 2x2 matrix of Grad_LSMatrix (:13-75).  On unit cells the cell centres are exact
+ * (i + 1/2, j + 1/2; periodic shadows offset by exactly Lx, Ly), so wdx = {1,0,-1,0},
+ * wdy = {0,1,0,-1} and the inverse is {{0.5,-0},{-0,0.5}}; the reference's products and
+ * sums are all kept, zero terms included. */
+static void cell_grad_ls(orc_state *s, const double *B, double *GX, double *GY, int i, int j) {
+    int im = wrapx(s, i - 1), ip = wrapx(s, i + 1);
+    static const double wdx[4] = {1.0, 0.0, -1.0, 0.0}, wdy[4] = {0.0, 1.0, 0.0, -1.0};
+    for (int q = 0; q < s->Q; ++q) {
+        double c = BQ(s, B, q, j, i);
+        double nb[4] = {BQ(s, B, q, j, ip), BQ(s, B, q, j + 1, i), BQ(s, B, q, j, im), BQ(s, B, q, j - 1, i)};
+        double sx = 0.0, sy = 0.0;
+        for (int k = 0; k < 4; ++k) {
+            sx += wdx[k] * (nb[k] - c);
+            sy += wdy[k] * (nb[k] - c);
+        }
+        BQ(s, GX, q, j, i) = 0.5 * sx + -0.0 * sy;
+        BQ(s, GY, q, j, i) = -0.0 * sx + 0.5 * sy;
+    }
+}
+
+/* Grad_VS_4points (Ark/Cpp/GradScheme.cpp:191-204 -> Ark/Lib/GradSchemeBasic.h:76-94):
+ * (C0 - C2) / _2dx and (C1 - C3) / _2dy */
+static void cell_grad4(orc_state *s, const double *B, double *GX, double *GY, int i, int j) {
+    int im = wrapx(s, i - 1), ip = wrapx(s, i + 1);
+    for (int q = 0; q < s->Q; ++q) {
+        BQ(s, GX, q, j, i) = (BQ(s, B, q, j, ip) - BQ(s, B, q, j, im)) / s->_2dx;
+        BQ(s, GY, q, j, i) = (BQ(s, B, q, j + 1, i) - BQ(s, B, q, j - 1, i)) / s->_2dy;
+    }
+}
+
+/* the cell gradient of the UW scheme: in->uw 1 6-point, 2 least squares, 3 4-point */
+static void cell_grad(orc_state *s, const double *B, double *GX, double *GY, int i, int j) {
+    if (s->in.uw == 2) cell_grad_ls(s, B, GX, GY, i, j);
+    else if (s->in.uw == 3) cell_grad4(s, B, GX, GY, i, j);
+    else cell_grad6(s, B, GX, GY, i, j);
+}
+
 /* UW_Interior_phi_Bh (Ark/Cpp/DUGKS2DSolver.cpp:558-603), chosen by the sign of
  * xi.n dS (:689-706): the upwind cell's BarP + (dx BarP_x + dy BarP_y) with
  * (dx, dy) = x_f - hDt xi - x_c, the two cells averaged (owner first) along the
@@ -695,8 +734,8 @@ static void one_step(orc_state *s) {
 #pragma omp parallel for schedule(static)
         for (int j = 0; j < ny; ++j)
             for (int i = 0; i < nx; ++i) {
-                cell_grad6(s, s->bf, s->gfx, s->gfy, i, j);
-                cell_grad6(s, s->bh, s->ghx, s->ghy, i, j);
+                cell_grad(s, s->bf, s->gfx, s->gfy, i, j);
+                cell_grad(s, s->bh, s->ghx, s->ghy, i, j);
             }
         for (int q = 0; q < Q; ++q) {
             double *g[] = {s->gfx, s->gfy, s->ghx, s->ghy};

@@ -32,7 +32,9 @@ typedef struct orc_inputs {
     double noise_rho0, noise_amp;                          /* pp_noise init */
     uint64_t seed;
     double d2v16_c;                                        /* D2V16 lattice speed (1.2) */
-    int uw;                                                /* 1: the UW flux scheme (Allen-Cahn, periodic) */
+    int uw;                                                /* the UW flux scheme (Allen-Cahn, periodic) with the
+                                                              6-point (1), least-squares (2) or 4-point (3)
+                                                              cell gradient; 0: CD */
     int nee;                                               /* 1: NEE walls instead of bounce-back */
 } orc_inputs;
 

@@ -64,6 +64,10 @@ DEFAULTS = dict(Mu0=0.1, M_Phi=0.1, W=5.0, Sigma=1e-2, RhoL=10.0, RhoV=1.0, Gy=0
                 noise_rho0=0.2, noise_amp=0.01, seed=12345, d2v16_c=1.2, uw=0, nee=0)
 
 
+# flux scheme of a variant -> orc_inputs.uw (the C ABI's dugks_flux_scheme values)
+UW_CODE = {'CD': 0, 'UW': 1, 'UW_LS': 2, 'UW_4P': 3}
+
+
 class Oracle:
     """One CPU-restatement solver instance."""
 
@@ -86,7 +90,7 @@ class Oracle:
     @classmethod
     def from_variant(cls, v: dict) -> 'Oracle':
         return cls(REF_MODEL[v['model']], v['nx'], v['ny'], v['walls'], v['init'], **v['consts'],
-                   uw=int(v.get('scheme', 'CD') == 'UW'), nee=int(v.get('wall', 'BB') == 'NEE'))
+                   uw=UW_CODE[v.get('scheme', 'CD')], nee=int(v.get('wall', 'BB') == 'NEE'))
 
     def __del__(self):
         h = getattr(self, '_h', None)

@@ -96,10 +96,15 @@ def gen_headers(name: str, v: dict, inc: Path) -> None:
     t = (REF / 'Constant/ZeroFlip.h').read_text()
     t = _sub(t, '"128_128_Car_Periodic_Square_LBM"', f'"{mesh_name(v)}"', 'mesh name')
     extra = []
-    if v.get('scheme') == 'UW':
+    if v.get('scheme', 'CD').startswith('UW'):
         t = _sub(t, '#ifndef _FLUX_SCHEME_CD_ARK\n#define _FLUX_SCHEME_CD_ARK "CD"\n'
                     '#define _FLUX_SCHEME_ARK _FLUX_SCHEME_CD_ARK\n#endif',
                  '#define _FLUX_SCHEME_UW_ARK "UW"\n#define _FLUX_SCHEME_ARK _FLUX_SCHEME_UW_ARK', 'flux scheme')
+        # the cell gradient of the UW reconstruction (read by ref_driver.cpp)
+        if v['scheme'] == 'UW_LS':
+            extra.append('#define REF_UW_GRAD_LS')
+        elif v['scheme'] == 'UW_4P':
+            extra.append('#define REF_UW_GRAD_4P')
     if v['model'] == 'D2Q9PP':
         t = _sub(t, '#ifndef _ARK_ALLENCAHN_FLIP\n#define _ARK_ALLENCAHN_FLIP\n#endif', '', 'AC flip')
         extra.append('#define _ARK_PSEUDOPSI_FLIP')

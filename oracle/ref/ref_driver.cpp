@@ -76,6 +76,8 @@ extern void WallShadowC_fBP(Cell_2D &shadowCell);
 extern void Wall_3_BB(Face_2D &face);
 extern void Wall_3_NEE(Face_2D &face);
 extern void Grad_VS_6points(Cell_2D *center);
+extern void Grad_VS_LS(Cell_2D *center);
+extern void Grad_VS_4points(Cell_2D *center);
 
 
 namespace {
@@ -175,9 +177,19 @@ void run_step() {
     for (int n = 0; n < WallFaceNum; ++n) WallShadowC_fBP(WallShadowCA[n]);
 #endif
 #ifdef _FLUX_SCHEME_UW_ARK
-    // cell gradients of BarP for the UW reconstruction (Ark/Cpp/DUGKS2DSolver.cpp:196-205)
+    // cell gradients of BarP for the UW reconstruction (Ark/Cpp/DUGKS2DSolver.cpp:196-205);
+    // REF_UW_GRAD_LS / REF_UW_GRAD_4P select the gradient calls the reference keeps
+    // commented out beside Grad_VS_6points (:201-203)
 #pragma omp parallel for schedule(static)
-    for (int n = 0; n < Cells; ++n) Grad_VS_6points(&CellArray[n]);
+    for (int n = 0; n < Cells; ++n) {
+#if defined REF_UW_GRAD_LS
+        Grad_VS_LS(&CellArray[n]);
+#elif defined REF_UW_GRAD_4P
+        Grad_VS_4points(&CellArray[n]);
+#else
+        Grad_VS_6points(&CellArray[n]);
+#endif
+    }
 #endif
 #if defined _ARK_PSEUDOPSI_FLIP && defined _ARK_FORCE_FLIP
     // pass 1: face distributions, moments and psi of every face

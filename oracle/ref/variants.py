@@ -53,6 +53,16 @@ VARIANTS = {
                      consts=dict(Mu0=0.01, W=4.0, Sigma=1e-3, RhoL=1.0, RhoV=0.1, radius=6.0)),
     'uw_hcz': dict(model='D2Q9HCZ', nx=32, ny=32, walls=False, init='ac_drop_inside', scheme='UW',
                    consts=dict(Mu0=0.02, W=4.0, Sigma=1e-2, RhoL=10.0, RhoV=1.0, radius=8.0)),
+    # UW with the reference's other cell gradients: least squares (Grad_VS_LS,
+    # Ark/Lib/GradSchemeBasic.h:127-152, weights of Grad_LSMatrix :13-75) and the 4-point
+    # central one (Grad_VS_4points, :76-94), the calls Ark/Cpp/DUGKS2DSolver.cpp:201-203
+    # keeps commented out beside the 6-point one.
+    'uwls_small': dict(model='D2Q9AC', nx=24, ny=20, walls=False, init='ac_drop_inside', scheme='UW_LS',
+                       consts=dict(Mu0=0.01, W=4.0, Sigma=1e-3, RhoL=1.0, RhoV=0.1, radius=6.0)),
+    'uwls_hcz': dict(model='D2Q9HCZ', nx=32, ny=32, walls=False, init='ac_drop_inside', scheme='UW_LS',
+                     consts=dict(Mu0=0.02, W=4.0, Sigma=1e-2, RhoL=10.0, RhoV=1.0, radius=8.0)),
+    'uw4p_hcz': dict(model='D2Q9HCZ', nx=32, ny=32, walls=False, init='ac_drop_inside', scheme='UW_4P',
+                     consts=dict(Mu0=0.02, W=4.0, Sigma=1e-2, RhoL=10.0, RhoV=1.0, radius=8.0)),
     # Non-equilibrium extrapolation walls (_Wall_3_BCs_NEE, Ark/Cpp/Boundary.cpp:140-184)
     # instead of bounce-back: the Rayleigh-Taylor box and a droplet between walls.
     'nee_rt': dict(model='D2Q9HCZ', nx=16, ny=64, walls=True, init='ac_rt', wall='NEE',

@@ -32,6 +32,9 @@ PLAN = {
     'ac_default': (2000, 0, ['rho', 'p', 'phi']),
     'uw_small': (500, 500, 'all'),
     'uw_hcz': (200, 200, 'all'),
+    'uwls_small': (500, 500, 'all'),
+    'uwls_hcz': (200, 200, 'all'),
+    'uw4p_hcz': (200, 200, 'all'),
     'nee_rt': (300, 300, 'all'),
     'nee_ac': (300, 300, 'all'),
 }

@@ -82,7 +82,8 @@ def test_fp32_error_vs_fp64(name, steps):
 # the reconstruction computed in FP64, i.e. from the FP32 state storage the central scheme
 # shares, which UW amplifies about twice as much (its FP64-FMA spread is twice the
 # central scheme's too).
-@pytest.mark.parametrize('name,steps', [('uw_small', 2000), ('uw_hcz', 1000), ('uw_ff', 500)])
+@pytest.mark.parametrize('name,steps', [('uw_small', 2000), ('uw_hcz', 1000), ('uw_ff', 500), ('uwls_small', 2000),
+                                        ('uwls_hcz', 1000), ('uw4p_hcz', 1000)])
 def test_fp32_uw_error_vs_fp64(name, steps):
     v = VARIANTS[name]
     a, b = make(v, 'fp32dev'), make(v, 'fp64')

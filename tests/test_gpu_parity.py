@@ -20,7 +20,8 @@ pytestmark = pytest.mark.gpu
 
 TOL = 1e-12
 UV_ABS = 1e-13
-SMALL = ['ac_small', 'hcz_drop', 'hcz_rt', 'pp_drop', 'uw_small', 'uw_hcz', 'nee_rt', 'nee_ac']
+SMALL = ['ac_small', 'hcz_drop', 'hcz_rt', 'pp_drop', 'uw_small', 'uw_hcz', 'uwls_small', 'uwls_hcz', 'uw4p_hcz',
+         'nee_rt', 'nee_ac']
 PRECISIONS = ['fp64', 'fp64fma']
 MODEL = {'D2Q9AC': 'AC', 'D2Q9HCZ': 'HCZ', 'D2Q9PP': 'PP9'}
 CASE_KEYS = ('Mu0', 'M_Phi', 'W', 'Sigma', 'RhoL', 'RhoV', 'Gy', 'Tr', 'aCS', 'Tc_CS')

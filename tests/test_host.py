@@ -68,6 +68,16 @@ def test_case_ark_decodes_the_reference_constants():
     out = subprocess.run([runner(), 'show-config', GOLD / 'uw_ff' / 'Case.ark'], check=True, capture_output=True,
                          text=True).stdout.split()
     assert dict(zip(out[0::2], out[1::2]))['flux'] == '1'  # "UW = Flux Scheme"
+
+
+@pytest.mark.parametrize('grad,flux', [('6points', '1'), ('LS', '2'), ('4points', '3')])
+def test_case_ark_selects_the_uw_cell_gradient(tmp_path, grad, flux):
+    """A 'cell gradient' entry picks the UW gradient the reference selects in its source
+    (Grad_VS_6points / Grad_VS_LS / Grad_VS_4points)."""
+    ark = tmp_path / 'Case.ark'
+    ark.write_text((GOLD / 'uw_ff' / 'Case.ark').read_text() + f'{grad}    =    cell gradient\n')
+    out = subprocess.run([runner(), 'show-config', ark], check=True, capture_output=True, text=True).stdout.split()
+    assert dict(zip(out[0::2], out[1::2]))['flux'] == flux
     # the Rayleigh-Taylor box: walls from the mesh name; no case name, so an init entry is required
     r = subprocess.run([runner(), 'show-config', GOLD / 'hcz_rt' / 'Case.ark'], capture_output=True, text=True)
     assert r.returncode == 1 and "give an 'init' entry" in r.stderr

@@ -9,7 +9,8 @@ import pytest
 from oracle.oracle import Oracle
 from variants import VARIANTS
 
-SMALL = ['ac_small', 'hcz_drop', 'hcz_rt', 'pp_drop', 'uw_small', 'uw_hcz', 'nee_rt', 'nee_ac']
+SMALL = ['ac_small', 'hcz_drop', 'hcz_rt', 'pp_drop', 'uw_small', 'uw_hcz', 'uwls_small', 'uwls_hcz', 'uw4p_hcz',
+         'nee_rt', 'nee_ac']
 
 
 def _fields(o, names):
