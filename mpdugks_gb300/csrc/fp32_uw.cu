@@ -8,7 +8,9 @@
 // face).  The gradient needs f-bar-plus of a cell's eight neighbours, so this form runs
 // four launches over scratch planes (UW_PLANES, one every qs floats from U):
 //   collision  -> f-bar-plus pairs, collision increments, averaged-field inputs;
-//   gradients  -> 6-point gradients of the f-bar-plus pairs and of the phase field;
+//   gradients  -> cell gradients of the f-bar-plus pairs and of the phase field (the
+//                 6-point one, or the least-squares / 4-point ones of DUGKS_FLUX_UW_LS /
+//                 DUGKS_FLUX_UW_4P);
 //   faces      -> upwind reconstruction, then the same face moments, equilibria and
 //                 fluxes as the central scheme (face_state_flux);
 //   update     -> the same finite-volume update (update_cell).
