@@ -182,8 +182,7 @@ int dugks_gpu_step_profiled(dugks_handle_t *h, int nsteps, void *stream, double 
  * not complete within its bounded wait (the state is then not valid). */
 int dugks_gpu_reduce(dugks_handle_t *h, dugks_reductions_t *r);
 
-/* Download the macroscopic fields (any pointer may be NULL): [ny][nx] each.
- * Pinned, mapped host arrays are written in place by a copy kernel. */
+/* Download the macroscopic fields (any pointer may be NULL): [ny][nx] each. */
 int dugks_gpu_download(dugks_handle_t *h, double *rho, double *u, double *v, double *phi, double *p);
 
 /* Single field / distribution access.  which: 0 = f, 1 = h. */

@@ -767,21 +767,8 @@ static cudaError_t to_dev(const dugks_handle *h, double *d, const double *src, i
     return cudaMemcpy2D(d, (size_t)P.pitch * sizeof(double), src, (size_t)P.nx * sizeof(double),
                         (size_t)P.nx * sizeof(double), rows < 0 ? P.ny : rows, cudaMemcpyHostToDevice);
 }
-__global__ void k_plane_to_dense(double *dst, const double *__restrict__ src, int nx, int ny, int pitch) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nx) return;
-    for (int j = blockIdx.y; j < ny; j += gridDim.y) dst[(size_t)j * nx + i] = src[(size_t)j * pitch + i];
-}
-// a device plane [ny][pitch] to host [ny][nx]; pinned, mapped host memory is written in
-// place by a kernel on the handle's stream (the callers have synchronised it)
 static cudaError_t to_host(const dugks_handle *h, double *dst, const double *d) {
     const Params &P = h->P;
-    if (double *m = static_cast<double *>(mapped_host(dst))) {
-        k_plane_to_dense<<<dim3((P.nx + 255) / 256, P.ny < 65535 ? P.ny : 65535), 256, 0, h->last_stream>>>(
-            m, d, P.nx, P.ny, P.pitch);
-        const cudaError_t e = cudaGetLastError();
-        return e == cudaSuccess ? cudaStreamSynchronize(h->last_stream) : e;
-    }
     return cudaMemcpy2D(dst, (size_t)P.nx * sizeof(double), d, (size_t)P.pitch * sizeof(double),
                         (size_t)P.nx * sizeof(double), P.ny, cudaMemcpyDeviceToHost);
 }
