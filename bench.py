@@ -923,8 +923,8 @@ def run_ours(args, wl, rank, world, local):
             'cpu_baseline': cpu,
             'e2e': {'value': round(e2e_mlups, 3), 'unit': 'MLUPS', 'h2d_bytes_per_step': int(h2d),
                     'd2h_bytes_per_step': int(d2h),
-                    'how': 'C ABI with pinned host buffers (read and written in place by the library\'s '
-                           'conversion and copy kernels over NVLink-C2C): upload the FP64 initial state, K steps, '
+                    'how': 'C ABI with pinned host buffers (the upload read in place by the library\'s '
+                           'conversion kernels over NVLink-C2C): upload the FP64 initial state, K steps, '
                            'reductions, download 5 fields'},
             'serving': serving,
             'pseudopotential_d2v16': pseudo,
