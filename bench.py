@@ -388,6 +388,8 @@ def serving_bench(args) -> dict:
     pp_cases = [c for c in stream if c['model'] == 'PP16']
     samples = {'AC': strata(ac, args.serving_sample), 'PP16': strata(pp_cases, max(1, args.serving_sample // 2))}
 
+    one_stream = torch.cuda.Stream()
+
     def one_at_a_time(precision):
         rates, out = {}, {}
         for model, sample in samples.items():
@@ -395,11 +397,11 @@ def serving_bench(args) -> dict:
             for c in sample:
                 gc = capi.GpuCase(serving_case(c, precision), c['n'], c['n'], False)
                 gc.init(c['init'], c['params'])
-                gc.step(2)
+                gc.step(2, one_stream.cuda_stream)
                 torch.cuda.synchronize()
                 nst = max(20, min(1000, c['steps']) // args.serving_fraction)
                 ta = time.perf_counter()
-                gc.step(nst)
+                gc.step(nst, one_stream.cuda_stream)  # a caller's stream, as the server's lanes
                 gc.get('rho')
                 el = time.perf_counter() - ta
                 rates[model].append((c['n'], el / (c['n'] * c['n'] * nst)))  # seconds per cell update
