@@ -18,6 +18,10 @@ CASES = [
     ('HCZ', 'fp32dev', 1120, 1664, True, 'ac_rt', [1.0, 0.1, 1e-4], dict(Gy=1e-4, RhoL=3.0, RhoV=1.0)),
     ('HCZ', 'fp64fused', 48, 48, False, 'ac_drop_inside', [12.0], {}),
     ('PP16', 'fp32dev', 32, 32, False, 'scmp_drop', [], {}),
+    # the upwind scheme in FP32 storage (its scratch is rebuilt every step) and the
+    # least-squares cell gradient in FP64
+    ('HCZ', 'fp32dev', 40, 36, False, 'ac_drop_inside', [9.0], dict(scheme='UW')),
+    ('AC', 'fp64', 24, 20, False, 'ac_drop_inside', [6.0], dict(scheme='UW_LS')),
     ('PP9', 'fp64', 32, 32, False, 'scmp_drop', [], {}),
 ]
 

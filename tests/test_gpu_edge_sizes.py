@@ -43,6 +43,44 @@ def test_fp64_equals_the_oracle(nx, ny, model, walls):
         assert np.array_equal(gc.get(k), o.get(k)), (nx, ny, k)
 
 
+UW_CODE = {'UW': 1, 'UW_LS': 2, 'UW_4P': 3}
+
+
+@pytest.mark.parametrize('nx,ny', SIZES)
+@pytest.mark.parametrize('scheme', ['UW', 'UW_LS', 'UW_4P'])
+def test_fp64_uw_equals_the_oracle(nx, ny, scheme):
+    """The upwind scheme with each cell gradient (periodic grids only) on the edge sizes:
+    the plain FP64 path equals the oracle bit for bit."""
+    from mpdugks_gb300 import capi
+    from oracle.oracle import Oracle
+    kw = case_kw('HCZ')
+    init, params = init_of(nx, ny, False)
+    gc = capi.GpuCase(capi.make_case('HCZ', 'fp64', scheme=scheme, **kw), nx, ny, False)
+    gc.init(init, params)
+    o = Oracle('HCZ', nx, ny, False, init, radius=params[0], uw=UW_CODE[scheme], **kw)
+    gc.step(30)
+    o.step(30)
+    for k in FIELDS:
+        assert np.array_equal(gc.get(k), o.get(k)), (nx, ny, k)
+
+
+@pytest.mark.parametrize('nx,ny', SIZES)
+def test_fp32_uw_close_to_fp64(nx, ny):
+    """The FP32 upwind step (four launches, any grid size) against FP64 UW from a seeded
+    noisy interface, as the central-scheme test below."""
+    from mpdugks_gb300 import capi
+    kw = case_kw('HCZ')
+    out = {}
+    for prec in ('fp32dev', 'fp64'):
+        g = capi.GpuCase(capi.make_case('HCZ', prec, scheme='UW', **kw), nx, ny, False)
+        g.init('ac_rt', [0.5 * ny / nx, 0.1, 1e-3], seed=5)
+        g.step(30)
+        assert g.check_finite() == 0
+        out[prec] = {k: g.get(k) for k in FIELDS}
+    for k in ('rho', 'p', 'phi'):
+        assert rel_err(out['fp32dev'][k], out['fp64'][k]) <= 2e-5, (nx, ny, k)
+
+
 @pytest.mark.parametrize('nx,ny', SIZES)
 @pytest.mark.parametrize('model,walls', [('AC', False), ('HCZ', True)])
 def test_fused_kernel_equals_fp64_to_rounding(nx, ny, model, walls):
