@@ -355,6 +355,7 @@ static int create_pp32(dugks_handle *h, dugks_handle_t **out) {
     split_ff(P.R0 * P.T_CS, C.rtcs_hi, C.rtcs_lo);
     split_ff(P.aCS, C.acs_hi, C.acs_lo);
     split_ff(P.RT, C.rt_hi, C.rt_lo);
+    split_ff(P.c16, C.lat_hi, C.lat_lo);
     for (int q = 0; q < Q; ++q) {
         C.xi_u[q] = (float)P.xi_u[q];
         C.xi_v[q] = (float)P.xi_v[q];

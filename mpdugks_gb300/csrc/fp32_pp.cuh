@@ -68,8 +68,7 @@ __device__ __forceinline__ void pp_deq(const PPP &P, float rho, float u, float v
 // two-step long division as in Bailey's double-double arithmetic: about 44
 // significant bits, for the moment sums and the equation of state that the FP64
 // path evaluates in double (the FP64 units of this GPU are ~1/60 of its FP32
-// rate, and these were most of this path's time).  Products that feed a TwoSum
-// use __fmul_rn so that no fma contraction changes them.
+// rate, and these were most of this path's time).
 struct FF {
     float hi, lo;
 };
@@ -85,11 +84,6 @@ __device__ __forceinline__ void ff_acc(FF &s, float x) {  // Sum2 step: s += x
     const FF t = two_sum(s.hi, x);
     s.hi = t.hi;
     s.lo = __fadd_rn(s.lo, t.lo);
-}
-__device__ __forceinline__ void ff_acc_prod(FF &s, float a, float b) {  // s += a b, the product exactly
-    const float p = __fmul_rn(a, b);
-    ff_acc(s, p);
-    s.lo = __fadd_rn(s.lo, fmaf(a, b, -p));
 }
 __device__ __forceinline__ FF ff_neg(FF a) { return {-a.hi, -a.lo}; }
 __device__ __forceinline__ FF ff_add(FF a, FF b) {
@@ -135,6 +129,48 @@ __device__ __forceinline__ void cs_psi(const PPP &P, FF rho, FF p, float &scg, f
     psil = psi > 0.f ? __fdiv_rn(fmaf(-psi, psi, xh) + xl, 2.f * psi) : 0.f;
 }
 __device__ __forceinline__ double ff_to_double(FF a) { return (double)a.hi + (double)a.lo; }
+
+// The velocity set as integers times the lattice speed (D2V16: Ark/Lib/D2V16.cpp:53-66,
+// D2Q9: Ark/Lib/D2Q9.h:86-88) and each direction's opposite
+template <int MODEL>
+__host__ __device__ constexpr int lat_u(int q) {
+    return MODEL == PP16 ? (q == 0 || q == 4 || q == 7 ? 1 : q == 2 || q == 5 || q == 6 ? -1 : q == 8 || q == 12 || q == 15 ? 2
+                                                                                        : q == 10 || q == 13 || q == 14 ? -2 : 0)
+                         : d2q9_xu(q);
+}
+template <int MODEL>
+__host__ __device__ constexpr int lat_v(int q) {
+    return MODEL == PP16 ? (q == 1 || q == 4 || q == 5 ? 1 : q == 3 || q == 6 || q == 7 ? -1 : q == 9 || q == 12 || q == 13 ? 2
+                                                                                        : q == 11 || q == 14 || q == 15 ? -2 : 0)
+                         : d2q9_xv(q);
+}
+template <int MODEL>
+__host__ __device__ constexpr int lat_opp(int q) {
+    return MODEL == PP16 ? (q & ~3) | ((q + 2) & 3) : d2q9_bb(q);
+}
+// n b as an exact float for the integer n in {-2, ..., 2}
+__device__ __forceinline__ float times_small(int n, float b) { return n == 1 ? b : n == -1 ? -b : n == 2 ? 2.f * b : -2.f * b; }
+
+// First moments sum_q xi_q b_q (x, y) as float-float: over the opposite pairs (q, q') of
+// n_q (b_q - b_q'), n_q = xi_q / speed an integer (each term exact scaling of one rounded
+// difference, zero components skipped), then times the lattice speed as a pair
+template <int MODEL>
+__device__ __forceinline__ void pp_first_moments(const PPP &P, const float (&b)[PPQ<MODEL>::Q], FF &su, FF &sv) {
+    constexpr int Q = PPQ<MODEL>::Q;
+    FF ax{0.f, 0.f}, ay{0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const int qo = lat_opp<MODEL>(q);
+        if (qo <= q) continue;  // each pair once, from its lower index; the rest direction has none
+        const float d = __fsub_rn(b[q], b[qo]);
+        const int nu = lat_u<MODEL>(q), nv = lat_v<MODEL>(q);
+        if (nu != 0) ff_acc(ax, times_small(nu, d));
+        if (nv != 0) ff_acc(ay, times_small(nv, d));
+    }
+    const FF c{P.lat_hi, P.lat_lo};
+    su = ff_mul(ff_norm(ax), c);
+    sv = ff_mul(ff_norm(ay), c);
+}
 
 
 
@@ -198,9 +234,8 @@ __device__ __forceinline__ PPFace pp_face1(const PPP &P, const float (&o)[PPQ<MO
         bq = fmaf(-P.erest[q], hgxf * P.xi_u[q] + hgyf * P.xi_v[q], bq);
         b[q] = bq;
         ff_acc(sR, bq);
-        ff_acc_prod(su, bq, P.xi_u[q]);
-        ff_acc_prod(sv, bq, P.xi_v[q]);
     }
+    pp_first_moments<MODEL>(P, b, su, sv);
     sR = ff_norm(sR);
     const float rah = (float)ravg;
     const FF R = ff_add(FF{rah, (float)(ravg - (double)rah)}, sR);
@@ -274,9 +309,8 @@ __device__ __forceinline__ PPCell pp_update(const PPP &P, float (&g)[PPQ<MODEL>:
         float inc = fmaf(P.aTP, bf[q] - g[q], P.dtV * sq[q]);
         inc = fmaf(P.erest[q], (P.xi_u[q] * px + P.xi_v[q] * py) - drf, inc);
         g[q] = g[q] + inc;
-        ff_acc_prod(su, g[q], P.xi_u[q]);
-        ff_acc_prod(sv, g[q], P.xi_v[q]);
     }
+    pp_first_moments<MODEL>(P, g, su, sv);
     const float rh = (float)c.rho;
     const FF R{rh, (float)(c.rho - (double)rh)};
     c.U = __fadd_rn(su.hi, su.lo) / rh;

@@ -102,6 +102,7 @@ struct PPP {
     // the same constants as float-float pairs (hi + lo) for the device arithmetic:
     // R0 T_CS, aCS, RT
     float rtcs_hi, rtcs_lo, acs_hi, acs_lo, rt_hi, rt_lo;
+    float lat_hi, lat_lo;  // the lattice speed (velocities = lat times small integers) as hi + lo
     float xi_u[16], xi_v[16], w9[9], erest[16];
     // D2V16 inverse moment matrix of this case, by value: the kernels read its entries as
     // constant-bank operands (no loads), and cases of different lattice speed run side by
