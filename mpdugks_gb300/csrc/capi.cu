@@ -31,6 +31,7 @@ DUGKS_DECLARE_FP64(exact)
 DUGKS_DECLARE_FP64(fast)
 }  // namespace dugks
 #include "fp32_state.cuh"
+#include "fp32_pp.cuh"
 #include "trace.hpp"
 namespace dugks {
 namespace f32 {
@@ -266,12 +267,31 @@ static void split_ff(double v, float &hi, float &lo) {
     lo = (float)(v - (double)hi);
 }
 
+// The FP32 D2V16 equilibrium (pp_deq, fp32_pp.cuh) evaluates the inverse moment matrix by
+// opposite-direction pairs and skips its structural zeros: check that this case's matrix
+// has that form (opposite rows equal in the even moments' entries, negated in the odd
+// ones; zeros where d2v16_entry says), so a change of the table cannot go unnoticed.
+static bool d2v16_matrix_has_pair_form(const double (&iM)[16][16]) {
+    for (int j = 0; j < 16; ++j) {
+        const int jo = f32::lat_opp<PP16>(j);
+        for (int k = 1; k < 16; ++k) {
+            if (!f32::d2v16_entry(j, k) && (iM[j][k] != 0.0 || iM[jo][k] != 0.0)) return false;
+            if (iM[jo][k] != (f32::d2v16_odd_moment(k) ? -iM[j][k] : iM[j][k])) return false;
+        }
+    }
+    return true;
+}
+
 static int create_pp32(dugks_handle *h, dugks_handle_t **out) {
     Params &P = h->P;
+    if (P.model == PP16 && !d2v16_matrix_has_pair_form(h->iM)) {
+        delete h;
+        return fail(nullptr, DUGKS_EINVAL, "D2V16 inverse moment matrix without the pair form the FP32 step assumes");
+    }
     h->pp32 = true;
     // the three-pass step; DUGKS_PP_PASSES=1 in the environment selects the single-pass
     // streaming step (grids of at least 32 columns and 8 rows).  The two give the same
-    // results; on the GB300 the three-pass form is 1.7x faster (the single pass holds a row
+    // results; on the GB300 the three-pass form is 1.75x faster (the single pass holds a row
     // pipeline of 16 distributions per lane: ~10 warps per SM, latency-bound)
     const char *passes = std::getenv("DUGKS_PP_PASSES");
     h->pp_stream = P.nx >= 32 && P.ny >= 8 && passes && std::atoi(passes) == 1;

@@ -17,6 +17,35 @@ struct PPQ {
     static constexpr int Q = MODEL == PP16 ? 16 : 9;
 };
 
+// The velocity set as integers times the lattice speed (D2V16: Ark/Lib/D2V16.cpp:53-66,
+// D2Q9: Ark/Lib/D2Q9.h:86-88) and each direction's opposite
+template <int MODEL>
+__host__ __device__ constexpr int lat_u(int q) {
+    return MODEL == PP16 ? (q == 0 || q == 4 || q == 7 ? 1 : q == 2 || q == 5 || q == 6 ? -1 : q == 8 || q == 12 || q == 15 ? 2
+                                                                                        : q == 10 || q == 13 || q == 14 ? -2 : 0)
+                         : d2q9_xu(q);
+}
+template <int MODEL>
+__host__ __device__ constexpr int lat_v(int q) {
+    return MODEL == PP16 ? (q == 1 || q == 4 || q == 5 ? 1 : q == 3 || q == 6 || q == 7 ? -1 : q == 9 || q == 12 || q == 13 ? 2
+                                                                                        : q == 11 || q == 14 || q == 15 ? -2 : 0)
+                         : d2q9_xv(q);
+}
+template <int MODEL>
+__host__ __device__ constexpr int lat_opp(int q) {
+    return MODEL == PP16 ? (q & ~3) | ((q + 2) & 3) : d2q9_bb(q);
+}
+// The D2V16 moments (Macro16, Ark/Lib/D2V16.cpp:125-145) odd in xi, and the entries of the
+// inverse moment matrix (Ark/Lib/D2V16.cpp:14-52) that are not identically zero: the axis
+// rings' rows (directions 0-3, 8-11) have none at the moments 1, 2, 4, 13 and, for the
+// directions along x, 8, 10, 11 (along y: 7, 9, 12)
+__host__ __device__ constexpr bool d2v16_odd_moment(int k) { return k == 1 || k == 2 || (k >= 7 && k <= 12); }
+__host__ __device__ constexpr bool d2v16_entry(int j, int k) {
+    return (j & 4) ? true
+                   : !(k == 1 || k == 2 || k == 4 || k == 13 ||
+                       ((j & 1) ? (k == 7 || k == 9 || k == 12) : (k == 8 || k == 10 || k == 11)));
+}
+
 // Equilibrium parts de_q = eq_q(rho, u, v) - e_q rho (zero at rest).
 template <int MODEL>
 __device__ __forceinline__ void pp_deq(const PPP &P, float rho, float u, float v, float *de) {
@@ -42,12 +71,23 @@ __device__ __forceinline__ void pp_deq(const PPP &P, float rho, float u, float v
         M[13] = (7.f * RT + s2) * M[4];
         M[14] = rho * RT * (8.f * u2 + v2) + rho * u2 * s2;
         M[15] = rho * RT * (8.f * v2 + u2) + rho * v2 * s2;
+        // row j' (the opposite direction of j) holds row j's entries of the even moments and
+        // the negated entries of the odd ones, and the axis rings' rows have fixed zeros
+        // (d2v16_odd_moment, d2v16_entry): per opposite pair the even and odd partial sums,
+        // de_j = E + O, de_j' = E - O
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-            float s = 0.f;
+            const int jo = lat_opp<PP16>(j);
+            if (jo < j) continue;
+            float E = 0.f, O = 0.f;
 #pragma unroll
-            for (int k = 1; k < 16; ++k) s = fmaf(P.iM16[j][k], M[k], s);
-            de[j] = s;
+            for (int k = 1; k < 16; ++k) {
+                if (!d2v16_entry(j, k)) continue;
+                if (d2v16_odd_moment(k)) O = fmaf(P.iM16[j][k], M[k], O);
+                else E = fmaf(P.iM16[j][k], M[k], E);
+            }
+            de[j] = E + O;
+            de[jo] = E - O;
         }
     } else {
         // D2Q9PP (Ark/Lib/D2Q9PP.cpp:51-62): w rho (1 + u1 + u1^2/2 - |u|^2 lambda) - w rho;
@@ -130,24 +170,6 @@ __device__ __forceinline__ void cs_psi(const PPP &P, FF rho, FF p, float &scg, f
 }
 __device__ __forceinline__ double ff_to_double(FF a) { return (double)a.hi + (double)a.lo; }
 
-// The velocity set as integers times the lattice speed (D2V16: Ark/Lib/D2V16.cpp:53-66,
-// D2Q9: Ark/Lib/D2Q9.h:86-88) and each direction's opposite
-template <int MODEL>
-__host__ __device__ constexpr int lat_u(int q) {
-    return MODEL == PP16 ? (q == 0 || q == 4 || q == 7 ? 1 : q == 2 || q == 5 || q == 6 ? -1 : q == 8 || q == 12 || q == 15 ? 2
-                                                                                        : q == 10 || q == 13 || q == 14 ? -2 : 0)
-                         : d2q9_xu(q);
-}
-template <int MODEL>
-__host__ __device__ constexpr int lat_v(int q) {
-    return MODEL == PP16 ? (q == 1 || q == 4 || q == 5 ? 1 : q == 3 || q == 6 || q == 7 ? -1 : q == 9 || q == 12 || q == 13 ? 2
-                                                                                        : q == 11 || q == 14 || q == 15 ? -2 : 0)
-                         : d2q9_xv(q);
-}
-template <int MODEL>
-__host__ __device__ constexpr int lat_opp(int q) {
-    return MODEL == PP16 ? (q & ~3) | ((q + 2) & 3) : d2q9_bb(q);
-}
 // n b as an exact float for the integer n in {-2, ..., 2}
 __device__ __forceinline__ float times_small(int n, float b) { return n == 1 ? b : n == -1 ? -b : n == 2 ? 2.f * b : -2.f * b; }
 

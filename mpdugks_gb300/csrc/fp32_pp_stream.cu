@@ -22,10 +22,9 @@
 // from one copy and written to the other (a segment reads rows its neighbours write).
 // Periodic in x and y (the pseudopotential models have no walls).
 //
-// Measured on the GB300 (D2V16, 1024^2): 1.86 G cell-updates/s against 3.72 for the three
-// passes, with the same results bit for bit (2.03 against 3.54 before the first moments
-// were formed from opposite-direction differences, which the two forms share: the three
-// passes gained, this form, at its register limit, spills more).  A lane holds the row pipeline of 16
+// Measured on the GB300 (D2V16, 1024^2): 2.35 G cell-updates/s against 4.10 for the three
+// passes, with the same results bit for bit (the equilibrium by opposite-direction pairs,
+// which the two forms share, took both up from 1.86 and 3.72).  A lane holds the row pipeline of 16
 // distributions (168 registers when compiled for 5 blocks of 2 warps per SM -- 1.69 G at
 // the 215 the compiler takes unbounded, 2.00 G at 128 with spills) and the face moments
 // and the equation of state are serial float-float chains, so the ~10 resident warps
