@@ -267,16 +267,17 @@ static void split_ff(double v, float &hi, float &lo) {
     lo = (float)(v - (double)hi);
 }
 
-// The FP32 D2V16 equilibrium (pp_deq, fp32_pp.cuh) evaluates the inverse moment matrix by
-// opposite-direction pairs and skips its structural zeros: check that this case's matrix
-// has that form (opposite rows equal in the even moments' entries, negated in the odd
-// ones; zeros where d2v16_entry says), so a change of the table cannot go unnoticed.
+// The FP32 D2V16 equilibrium (pp_deq, fp32_pp.cuh) and the FP64-FMA one (d2v16_eq,
+// fp64_step.cuh) evaluate the inverse moment matrix by opposite-direction pairs and skip its
+// structural zeros: check that this case's matrix has that form (opposite rows equal in the
+// even moments' entries, negated in the odd ones; zeros where d2v16_entry says), so a change
+// of the table cannot go unnoticed.
 static bool d2v16_matrix_has_pair_form(const double (&iM)[16][16]) {
     for (int j = 0; j < 16; ++j) {
-        const int jo = f32::lat_opp<PP16>(j);
-        for (int k = 1; k < 16; ++k) {
-            if (!f32::d2v16_entry(j, k) && (iM[j][k] != 0.0 || iM[jo][k] != 0.0)) return false;
-            if (iM[jo][k] != (f32::d2v16_odd_moment(k) ? -iM[j][k] : iM[j][k])) return false;
+        const int jo = d2v16_opp(j);
+        for (int k = 0; k < 16; ++k) {
+            if (!d2v16_entry(j, k) && (iM[j][k] != 0.0 || iM[jo][k] != 0.0)) return false;
+            if (iM[jo][k] != (d2v16_odd_moment(k) ? -iM[j][k] : iM[j][k])) return false;
         }
     }
     return true;
@@ -284,10 +285,6 @@ static bool d2v16_matrix_has_pair_form(const double (&iM)[16][16]) {
 
 static int create_pp32(dugks_handle *h, dugks_handle_t **out) {
     Params &P = h->P;
-    if (P.model == PP16 && !d2v16_matrix_has_pair_form(h->iM)) {
-        delete h;
-        return fail(nullptr, DUGKS_EINVAL, "D2V16 inverse moment matrix without the pair form the FP32 step assumes");
-    }
     h->pp32 = true;
     // the three-pass step; DUGKS_PP_PASSES=1 in the environment selects the single-pass
     // streaming step (grids of at least 32 columns and 8 rows).  The two give the same
@@ -699,6 +696,10 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
     derive_params(*c, *g, h->P);
     Params &P = h->P;
     if (P.model == PP16) build_d2v16_matrix(P.c16, h->iM);
+    if (P.model == PP16 && c->precision != DUGKS_FP64 && !d2v16_matrix_has_pair_form(h->iM)) {
+        delete h;
+        return fail(nullptr, DUGKS_EINVAL, "D2V16 inverse moment matrix without the opposite-pair form the step assumes");
+    }
     if (c->precision == DUGKS_FP32_DEV && (P.model == PP9 || P.model == PP16)) return create_pp32(h, out);
     if (c->precision == DUGKS_FP32_DEV || c->precision == DUGKS_FP64_FUSED) return create_fp32(h, out);
     // ---- carve the arena

@@ -81,6 +81,20 @@ __host__ __device__ constexpr double d2q9_w(int q) {
 }
 __host__ __device__ constexpr int d2q9_bb(int q) { return q == 0 ? 0 : (q <= 4 ? q + 4 : q - 4); }
 
+// D2V16 velocity set (Ark/Lib/D2V16.cpp:53-66): four rings of four directions, q = 4r + i,
+// the opposite of q being 4r + (i + 2) mod 4.  The moments (Macro16, Ark/Lib/D2V16.cpp:125-145)
+// odd in xi, and the entries of the inverse moment matrix (Ark/Lib/D2V16.cpp:14-52) that are
+// not identically zero: the axis rings' rows (directions 0-3, 8-11) have none at the moments
+// 1, 2, 4, 13 and, for the directions along x, 8, 10, 11 (along y: 7, 9, 12).  Row q' of the
+// matrix holds row q's entries of the even moments and the negated entries of the odd ones.
+__host__ __device__ constexpr int d2v16_opp(int q) { return (q & ~3) | ((q + 2) & 3); }
+__host__ __device__ constexpr bool d2v16_odd_moment(int k) { return k == 1 || k == 2 || (k >= 7 && k <= 12); }
+__host__ __device__ constexpr bool d2v16_entry(int j, int k) {
+    return (j & 4) ? true
+                   : !(k == 1 || k == 2 || k == 4 || k == 13 ||
+                       ((j & 1) ? (k == 7 || k == 9 || k == 12) : (k == 8 || k == 10 || k == 11)));
+}
+
 // x * s for s in {-1, 0, 1}: exact, no multiply issued.
 __device__ __forceinline__ double sx(int s, double x) { return s > 0 ? x : (s < 0 ? -x : 0.0); }
 

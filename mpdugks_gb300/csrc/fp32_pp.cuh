@@ -33,17 +33,7 @@ __host__ __device__ constexpr int lat_v(int q) {
 }
 template <int MODEL>
 __host__ __device__ constexpr int lat_opp(int q) {
-    return MODEL == PP16 ? (q & ~3) | ((q + 2) & 3) : d2q9_bb(q);
-}
-// The D2V16 moments (Macro16, Ark/Lib/D2V16.cpp:125-145) odd in xi, and the entries of the
-// inverse moment matrix (Ark/Lib/D2V16.cpp:14-52) that are not identically zero: the axis
-// rings' rows (directions 0-3, 8-11) have none at the moments 1, 2, 4, 13 and, for the
-// directions along x, 8, 10, 11 (along y: 7, 9, 12)
-__host__ __device__ constexpr bool d2v16_odd_moment(int k) { return k == 1 || k == 2 || (k >= 7 && k <= 12); }
-__host__ __device__ constexpr bool d2v16_entry(int j, int k) {
-    return (j & 4) ? true
-                   : !(k == 1 || k == 2 || k == 4 || k == 13 ||
-                       ((j & 1) ? (k == 7 || k == 9 || k == 12) : (k == 8 || k == 10 || k == 11)));
+    return MODEL == PP16 ? d2v16_opp(q) : d2q9_bb(q);
 }
 
 // Equilibrium parts de_q = eq_q(rho, u, v) - e_q rho (zero at rest).

@@ -95,7 +95,8 @@ __device__ __forceinline__ Xi4 xi4(double a, double b, double RT, double invRT) 
 
 // ---------------------------------------------------------------------------
 // D2V16 equilibrium: Macro16 (Ark/Lib/D2V16.cpp:125-145) at T = T0, p = rho R0 T0,
-// then the inverse moment matrix.
+// then the inverse moment matrix: row by row in the exact variant, by opposite pairs in
+// the FMA variant (the handle checks the matrix's pair form when it is made).
 __device__ __forceinline__ void d2v16_eq(const Params &P, double rho, double u, double v, double *eq) {
     const double degrees = 3.0, degPlus2 = degrees + 2.0;
     const double T = P.T0, p = rho * P.R0 * T;
@@ -117,6 +118,7 @@ __device__ __forceinline__ void d2v16_eq(const Params &P, double rho, double u, 
     M[13] = ((degrees + 4.0) * RT + u2 + v2) * M[4];
     M[14] = degPlus2 * rho * RT * RT + p * ((degrees + 5.0) * u2 + v2) + rho * u2 * (u2 + v2);
     M[15] = degPlus2 * rho * RT * RT + p * ((degrees + 5.0) * v2 + u2) + rho * v2 * (u2 + v2);
+#if DUGKS_EXACT
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
         double s = 0;
@@ -124,6 +126,25 @@ __device__ __forceinline__ void d2v16_eq(const Params &P, double rho, double u, 
         for (int k = 0; k < 16; ++k) s += __ldg(P.iM16 + j * 16 + k) * M[k];
         eq[j] = s;
     }
+#else
+    // per opposite pair the even and odd partial sums over the matrix entries that are not
+    // identically zero (d2v16_entry, d2v16_odd_moment): eq_j = E + O, eq_j' = E - O; 100
+    // multiply-adds and loads instead of 256
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        const int jo = d2v16_opp(j);
+        if (jo < j) continue;
+        double E = 0, O = 0;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            if (!d2v16_entry(j, k)) continue;
+            if (d2v16_odd_moment(k)) O += __ldg(P.iM16 + j * 16 + k) * M[k];
+            else E += __ldg(P.iM16 + j * 16 + k) * M[k];
+        }
+        eq[j] = E + O;
+        eq[jo] = E - O;
+    }
+#endif
 }
 
 // D2Q9PP equilibrium (Ark/Lib/D2Q9PP.cpp:51-62).
