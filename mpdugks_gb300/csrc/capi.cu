@@ -267,11 +267,11 @@ static void split_ff(double v, float &hi, float &lo) {
     lo = (float)(v - (double)hi);
 }
 
-// The FP32 D2V16 equilibrium (pp_deq, fp32_pp.cuh) and the FP64-FMA one (d2v16_eq,
-// fp64_step.cuh) evaluate the inverse moment matrix by opposite-direction pairs and skip its
-// structural zeros: check that this case's matrix has that form (opposite rows equal in the
-// even moments' entries, negated in the odd ones; zeros where d2v16_entry says), so a change
-// of the table cannot go unnoticed.
+// The D2V16 equilibria (pp_deq, fp32_pp.cuh; d2v16_eq, fp64_step.cuh) skip the inverse
+// moment matrix's structural zeros, and the FP32 and FP64-FMA ones evaluate it by
+// opposite-direction pairs: check that this case's matrix has that form (opposite rows
+// equal in the even moments' entries, negated in the odd ones; zeros where d2v16_entry
+// says), so a change of the table cannot go unnoticed.
 static bool d2v16_matrix_has_pair_form(const double (&iM)[16][16]) {
     for (int j = 0; j < 16; ++j) {
         const int jo = d2v16_opp(j);
@@ -696,7 +696,7 @@ extern "C" int dugks_gpu_create(const dugks_case_t *c, const dugks_grid_t *g, du
     derive_params(*c, *g, h->P);
     Params &P = h->P;
     if (P.model == PP16) build_d2v16_matrix(P.c16, h->iM);
-    if (P.model == PP16 && c->precision != DUGKS_FP64 && !d2v16_matrix_has_pair_form(h->iM)) {
+    if (P.model == PP16 && !d2v16_matrix_has_pair_form(h->iM)) {
         delete h;
         return fail(nullptr, DUGKS_EINVAL, "D2V16 inverse moment matrix without the opposite-pair form the step assumes");
     }

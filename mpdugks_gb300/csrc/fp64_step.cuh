@@ -96,7 +96,8 @@ __device__ __forceinline__ Xi4 xi4(double a, double b, double RT, double invRT) 
 // ---------------------------------------------------------------------------
 // D2V16 equilibrium: Macro16 (Ark/Lib/D2V16.cpp:125-145) at T = T0, p = rho R0 T0,
 // then the inverse moment matrix: row by row in the exact variant, by opposite pairs in
-// the FMA variant (the handle checks the matrix's pair form when it is made).
+// the FMA variant, both without the structural zeros (the handle checks the matrix's form
+// when it is made).
 __device__ __forceinline__ void d2v16_eq(const Params &P, double rho, double u, double v, double *eq) {
     const double degrees = 3.0, degPlus2 = degrees + 2.0;
     const double T = P.T0, p = rho * P.R0 * T;
@@ -119,11 +120,15 @@ __device__ __forceinline__ void d2v16_eq(const Params &P, double rho, double u, 
     M[14] = degPlus2 * rho * RT * RT + p * ((degrees + 5.0) * u2 + v2) + rho * u2 * (u2 + v2);
     M[15] = degPlus2 * rho * RT * RT + p * ((degrees + 5.0) * v2 + u2) + rho * v2 * (u2 + v2);
 #if DUGKS_EXACT
+    // the reference's row sums in its order, less the terms of the matrix's structural zeros:
+    // a sum that starts at +0 never becomes -0, so adding 0 * M[k] leaves it unchanged for
+    // finite moments (a non-finite moment gives a non-finite sum either way)
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
         double s = 0;
 #pragma unroll
-        for (int k = 0; k < 16; ++k) s += __ldg(P.iM16 + j * 16 + k) * M[k];
+        for (int k = 0; k < 16; ++k)
+            if (d2v16_entry(j, k)) s += __ldg(P.iM16 + j * 16 + k) * M[k];
         eq[j] = s;
     }
 #else
