@@ -73,3 +73,53 @@ def test_periodic_run_conserves_mass():
     o.step(60)
     m1 = o.get('rho').sum()
     assert abs(m1 - m0) <= 1e-12 * m0
+
+
+def opposite(q):
+    return (q & ~3) | ((q + 2) & 3)
+
+
+def entry(j, k):
+    """Entries of the inverse moment matrix that are not identically zero (the axis rings'
+    rows, directions 0-3 and 8-11, have none at the moments 1, 2, 4, 13 and, along x,
+    8, 10, 11; along y, 7, 9, 12): the structure the GPU equilibria skip."""
+    if j & 4:
+        return True
+    return k not in ((1, 2, 4, 13) + ((7, 9, 12) if j & 1 else (8, 10, 11)))
+
+
+ODD = (1, 2, 7, 8, 9, 10, 11, 12)
+
+
+@pytest.mark.parametrize('c', [1.2, 0.5])
+def test_inverse_moment_matrix_has_the_pair_form(c):
+    """Row q' (the opposite direction) of the inverse moment matrix equals row q in the
+    moments even in xi and is its negation in the odd ones; the zeros sit where entry()
+    says.  The FP32 and FP64-FMA equilibria evaluate the matrix by these pairs, and every
+    handle checks its own table for this form when it is made."""
+    o = Oracle('PP16', 8, 8, init='pp_noise', d2v16_c=c)
+    xu, xv, x2 = o.velocities()
+    for q in range(16):
+        assert xu[opposite(q)] == -xu[q] and xv[opposite(q)] == -xv[q]
+    iM = np.linalg.inv(basis(xu, xv, x2))  # iM[q, k]
+    scale = np.abs(iM).max(axis=0)
+    for j in range(16):
+        jo = opposite(j)
+        for k in range(16):
+            if not entry(j, k):
+                assert abs(iM[j, k]) <= 1e-12 * scale[k], (j, k)
+            sign = -1.0 if k in ODD else 1.0
+            assert abs(iM[jo, k] - sign * iM[j, k]) <= 1e-12 * scale[k], (j, k)
+
+
+def test_equilibrium_reverses_with_the_velocity():
+    """eq_q(rho, -u, -v) == eq_q'(rho, u, v) bit for bit: the moments change sign exactly
+    with (u, v) and the oracle's table has the pair form."""
+    o = Oracle('PP16', 8, 8, init='pp_noise', d2v16_c=0.5)
+    rng = np.random.default_rng(11)
+    opp = [opposite(q) for q in range(16)]
+    for _ in range(50):
+        rho, u, v = rng.uniform(0.01, 0.4), rng.uniform(-0.2, 0.2), rng.uniform(-0.2, 0.2)
+        a = o.d2v16_equilibrium(rho, u, v)
+        b = o.d2v16_equilibrium(rho, -u, -v)
+        assert np.array_equal(b, a[opp])
