@@ -120,16 +120,24 @@ __device__ __forceinline__ void d2v16_eq(const Params &P, double rho, double u, 
     M[14] = degPlus2 * rho * RT * RT + p * ((degrees + 5.0) * u2 + v2) + rho * u2 * (u2 + v2);
     M[15] = degPlus2 * rho * RT * RT + p * ((degrees + 5.0) * v2 + u2) + rho * v2 * (u2 + v2);
 #if DUGKS_EXACT
-    // the reference's row sums in its order, less the terms of the matrix's structural zeros:
-    // a sum that starts at +0 never becomes -0, so adding 0 * M[k] leaves it unchanged for
-    // finite moments (a non-finite moment gives a non-finite sum either way)
+    // the reference's row sums in its order, less the terms of the matrix's structural zeros
+    // (a sum that starts at +0 never becomes -0, so adding 0 * M[k] leaves it unchanged for
+    // finite moments; a non-finite moment gives a non-finite sum either way), rows j and j'
+    // together: the opposite row's product is t or -t exactly, (-a) m = -(a m)
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-        double s = 0;
+        const int jo = d2v16_opp(j);
+        if (jo < j) continue;
+        double s = 0, so = 0;
 #pragma unroll
-        for (int k = 0; k < 16; ++k)
-            if (d2v16_entry(j, k)) s += __ldg(P.iM16 + j * 16 + k) * M[k];
+        for (int k = 0; k < 16; ++k) {
+            if (!d2v16_entry(j, k)) continue;
+            const double t = __ldg(P.iM16 + j * 16 + k) * M[k];
+            s += t;
+            so += d2v16_odd_moment(k) ? -t : t;
+        }
         eq[j] = s;
+        eq[jo] = so;
     }
 #else
     // per opposite pair the even and odd partial sums over the matrix entries that are not
