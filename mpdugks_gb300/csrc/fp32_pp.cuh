@@ -194,6 +194,28 @@ __device__ __forceinline__ void pp_iso_grad(const PPP &P, float2 E, float2 W, fl
     gy = (4.f * pdiff(N, S) + (pdiff(NE, SE) + pdiff(NW, SW))) * P.inv_6_2dy;
 }
 
+// The He-Shan-Doolen projections (xi_q - u).F of the directions, by opposite pairs: with
+// d = xi_q.F and w = u.F, (xi_q - u).F = d - w and (xi_q' - u).F = -d - w (xi_q' = -xi_q);
+// a rest direction (D2Q9PP's 0) has -w.
+template <int MODEL>
+__device__ __forceinline__ void pp_src_proj(const PPP &P, float fx, float fy, float U, float V,
+                                            float (&pr)[PPQ<MODEL>::Q]) {
+    constexpr int Q = PPQ<MODEL>::Q;
+    const float w = fmaf(fx, U, fy * V);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const int qo = lat_opp<MODEL>(q);
+        if (qo < q) continue;
+        if (qo == q) {
+            pr[q] = -w;
+            continue;
+        }
+        const float d = fmaf(fx, P.xi_u[q], fy * P.xi_v[q]);
+        pr[q] = d - w;
+        pr[qo] = -d - w;
+    }
+}
+
 // Collision pre-step of one cell: f-bar-plus as the remainder
 // B_q - e_q rho = g_q + (1 - a)(de_q - g_q) + c S_q, S the He-Shan-Doolen source of the
 // cell force (fx, fy).
@@ -206,10 +228,12 @@ __device__ __forceinline__ void pp_collide(const PPP &P, const float (&g)[PPQ<MO
     const float tau = P.Tau0;
     const float aBP = (2.f * tau - P.hDt) / (2.f * tau + P.dt), bBP = 1.f - aBP, cBP = tau * bBP;
     const float inv = 1.f / (rho * P.RT);
+    float pr[Q];
+    pp_src_proj<MODEL>(P, fx, fy, U, V, pr);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         const float eq = fmaf(P.erest[q], rho, de[q]);
-        const float So = (fx * (P.xi_u[q] - U) + fy * (P.xi_v[q] - V)) * eq * inv;
+        const float So = pr[q] * eq * inv;
         bf[q] = g[q] + (bBP * (de[q] - g[q]) + cBP * So);
     }
 }
@@ -274,10 +298,12 @@ __device__ __forceinline__ void pp_face2(const PPP &P, const float (&b)[PPQ<MODE
     const float tauh = P.Tau0;
     const float ah = 2.f * tauh / (2.f * tauh + P.hDt), bh = 1.f - ah, ch = tauh * bh;
     const float inv = 1.f / (R * P.RT);
+    float pr[Q];
+    pp_src_proj<MODEL>(P, fx, fy, f.U, f.V, pr);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         const float eq = fmaf(P.erest[q], R, de[q]);
-        const float So = (fx * (P.xi_u[q] - f.U) + fy * (P.xi_v[q] - f.V)) * eq * inv;
+        const float So = pr[q] * eq * inv;
         const float heq = fmaf(P.erest[q], f.dr, de[q]);  // eq - e_q avg(rho)
         const float t = heq + ah * (b[q] - heq) + ch * So;
         out[q] = t * (XF ? P.xi_u[q] : P.xi_v[q]);
