@@ -178,6 +178,29 @@ __device__ __forceinline__ void pp_eq(const Params &P, double rho, double U, dou
     else d2q9pp_eq(P, rho, U, V, eq);
 }
 
+#if !DUGKS_EXACT
+// FMA variant: the He-Shan-Doolen projections (xi_q - u).F by opposite pairs, d - w and
+// -d - w with d = xi_q.F, w = u.F (xi_q' = -xi_q); a rest direction has -w.  The exact
+// variant keeps the reference's fx (xi_u - U) + fy (xi_v - V).
+template <int MODEL>
+__device__ __forceinline__ void pp_src_proj(const Params &P, double fx, double fy, double U, double V, double *pr) {
+    constexpr int Q = MODEL == PP16 ? 16 : 9;
+    const double w = fx * U + fy * V;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const int qo = MODEL == PP16 ? d2v16_opp(q) : d2q9_bb(q);
+        if (qo < q) continue;
+        if (qo == q) {
+            pr[q] = -w;
+            continue;
+        }
+        const double d = fx * P.xi_u[q] + fy * P.xi_v[q];
+        pr[q] = d - w;
+        pr[qo] = -d - w;
+    }
+}
+#endif
+
 // Carnahan-Starling, b = 4 (Ark/Lib/nonidealEoS.h:114-118) and calcPsi
 // (Ark/Header/Macroscopic.h:64-68).
 __device__ __forceinline__ double cs_pressure(const Params &P, double rho) {
@@ -345,9 +368,17 @@ __global__ void __launch_bounds__(256) k_collide(Params P, State S, int do_msrc,
         double eq[Q];
         pp_eq<MODEL>(P, rho, U, V, eq);
         const double inv = 1.0 / (rho * P.RT);
+#if !DUGKS_EXACT
+        double pr[Q];
+        pp_src_proj<MODEL>(P, fx, fy, U, V, pr);
+#endif
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
+#if DUGKS_EXACT
             const double So = QDIV((fx * (P.xi_u[q] - U) + fy * (P.xi_v[q] - V)) * eq[q], rho * P.RT, inv);
+#else
+            const double So = pr[q] * eq[q] * inv;
+#endif
             const size_t o = (size_t)q * S.qs + c;
             S.bf[o] = aBP * S.f[o] + bBP * eq[q] + cBP * So;
         }
@@ -795,9 +826,17 @@ __global__ void __launch_bounds__(256) k_faces_pp2(Params P, State S) {
     const double *__restrict__ BB = xf ? S.xbf : S.ybf;
     double *out = xf ? S.xff : S.yff;
     const size_t qs = xf ? S.qs : S.qsy;
+#if !DUGKS_EXACT
+    double pr[Q];
+    pp_src_proj<MODEL>(P, Fx, Fy, U, V, pr);
+#endif
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
+#if DUGKS_EXACT
         const double So = QDIV((Fx * (P.xi_u[q] - U) + Fy * (P.xi_v[q] - V)) * eq[q], R * P.RT, inv);
+#else
+        const double So = pr[q] * eq[q] * inv;
+#endif
         const double t = ah * BB[(size_t)q * S.qs + c] + bh * eq[q] + ch * So;
         out[(size_t)q * qs + c] = t * (xf ? P.xi_u[q] : P.xi_v[q]);
     }
